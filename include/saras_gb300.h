@@ -1,0 +1,208 @@
+/*
+ * saras_gb300.h -- C ABI of the GB300 (sm_103a) implementation of SARAS-CC's
+ * data-parallel hot path: the cell-centred geometric-multigrid pressure-Poisson
+ * solve and the low-storage RK3 sub-step stencils around it.
+ *
+ * Every entry point takes plain pointers and sizes.  Field pointers address
+ * element (0,0,0) of a padded, row-major (i,j,k) array with k fastest -- the
+ * layout of a Blitz++ plainsf/field array indexed from -pad -- and `strides`
+ * gives the element strides of i, j and k.  Host ("_host" or no suffix) and
+ * device ("_dev") variants exist where the reference caller may hold either.
+ *
+ * Reference interfaces replaced (paths relative to the SARAS-CC source tree):
+ *   saras_mg_create   <- multigrid_d3::multigrid_d3 / multigrid_d2::multigrid_d2
+ *                        (lib/poisson/poisson.h:168,202; poisson.cc:66-92)
+ *   saras_mg_solve    <- void poisson::mgSolve(plainsf &outLHS, const plainsf &inpRHS)
+ *                        (lib/poisson/poisson.h:128; poisson.cc:109-189)
+ *   saras_rk3_create  <- lsRK3_d3::lsRK3_d3 / lsRK3_d2::lsRK3_d2
+ *                        (lib/timestep/lsRK3_d3.cc:58-79; timestep.cc:58-121)
+ *   saras_rk3_step    <- lsRK3_d3::timeAdvance(vfield&, sfield&, sfield&) and
+ *                        timeAdvance(vfield&, sfield&) (lsRK3_d3.cc:94-177,190-305)
+ *   saras_grid_metrics<- grid::mgGridMetrics / createTanHypGrid / setVCDepth
+ *                        (lib/grid/grid.cc:411-742), as copied by
+ *                        poisson::copyDerivs (lib/poisson/poisson.cc:501-622)
+ *
+ * Errors are returned, never raised: no entry point calls exit().  A handle
+ * is used by one host thread at a time; its work is ordered on the CUDA
+ * stream given at creation.
+ */
+#ifndef SARAS_GB300_H
+#define SARAS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum saras_status {
+    SARAS_OK = 0,
+    SARAS_NOT_CONVERGED = 1, /* vcCount / outer-iteration cap reached above tolerance */
+    SARAS_BAD_ARG = 2,
+    SARAS_OOM = 3,           /* device allocation failed */
+    SARAS_BUDGET = 4,        /* serving: request does not fit the HBM budget */
+    SARAS_TIMEOUT = 5,       /* a bounded device wait gave up */
+    SARAS_CUDA_ERR = 6,
+    SARAS_NO_DEVICE = 7,
+    SARAS_DIVERGED = 8,      /* CN Jacobi hit maxIterations (reference aborts here) */
+    SARAS_NAN = 9            /* non-finite value met in an input or a residual */
+} saras_status;
+
+/* "Mesh Type" characters U/S/D (lib/io/parser.cc:413-452) */
+enum { SARAS_MESH_UNIFORM = 0, SARAS_MESH_SINGLE_TANH = 1, SARAS_MESH_DOUBLE_TANH = 2 };
+
+/* Poisson ghost-cell kinds per non-periodic face (lib/poisson/poisson_d3.cc:876-952):
+ * NEUMANN        ghost = interior              (allNeumann, the reference default)
+ * DIRICHLET      ghost = -interior             (homogeneous Dirichlet branch)
+ * DIRICHLET_TEST ghost = 2*wall - interior at the finest level outside the
+ *                error equation, -interior otherwise, wall = r^2/6 (3D) or
+ *                r^2/4 (2D)                    (TEST_POISSON branch) */
+enum { SARAS_BC_NEUMANN = 0, SARAS_BC_DIRICHLET = 1, SARAS_BC_DIRICHLET_TEST = 2 };
+
+/* Arithmetic of the multigrid solve.
+ * FP64_EXACT  reference operation order, no FMA contraction, IEEE division:
+ *             bitwise equal to the CPU restatement of mgSolve.
+ * FP64        FP64 throughout, coefficients pre-folded, FMA allowed.
+ * MIXED       FP32 V-cycle (smoothing, restriction, prolongation) inside an
+ *             FP64 defect-correction loop; residual, update, null-space
+ *             projection and coarsest solve in FP64. */
+enum { SARAS_PREC_FP64_EXACT = 0, SARAS_PREC_FP64 = 1, SARAS_PREC_MIXED = 2 };
+
+/* Field boundary kinds of the RK3 fields (lib/boundary/dirichlet.cc, neumann.cc) */
+enum { SARAS_FBC_DIRICHLET = 0, SARAS_FBC_NEUMANN = 1 };
+
+typedef struct saras_grid_desc {
+    int32_t dims;         /* 3, or 2 for the PLANAR (x,z) build */
+    int32_t n[3];         /* "X Size", "Y Size", "Z Size"; n[1] is forced to 1 when dims==2 */
+    double  len[3];       /* "X Length", "Y Length", "Z Length" */
+    int32_t mesh_type[3]; /* SARAS_MESH_* from "Mesh Type" */
+    double  beta[3];      /* "X Beta", "Y Beta", "Z Beta" */
+    int32_t periodic[3];  /* "Domain Type": 'P' -> 1, 'N' -> 0 */
+    int32_t pad;          /* pad width of caller fields: 1 ("Differentiation Scheme" 1) or 2 */
+} saras_grid_desc;
+
+typedef struct saras_mg_params {
+    int32_t vc_count;      /* "V-Cycle Count" (mixed form: outer iterations) */
+    double  vc_tolerance;  /* "Residual Tolerance" */
+    int32_t solve_flag;    /* "Solve Coarsest" */
+    double  mg_tolerance;  /* Multigrid "Solve Tolerance" (absolute, coarsest level) */
+    double  sor_param;     /* "SOR Parameter" */
+    int32_t pre_smooth;    /* "Pre-Smoothing Count" */
+    int32_t post_smooth;   /* "Post-Smoothing Count" */
+    int32_t res_type;      /* "Residual Type": 0 Linf, 1 L1, 2 L2 (relative to the RHS) */
+    int32_t print_residual;/* "Print Residual" */
+    int32_t bc_kind[6];    /* SARAS_BC_* for faces x-, x+, y-, y+, z-, z+ */
+    int32_t test_poisson;  /* TEST_POISSON build semantics: no early exit */
+    int32_t precision;     /* SARAS_PREC_* */
+    int32_t levels;        /* 0: reference depth from setVCDepth; >0: that many levels */
+} saras_mg_params;
+
+typedef struct saras_mg saras_mg;
+
+/* Fills the parameters with the reference defaults of input/parameters.yaml's
+ * Multigrid section and Neumann walls. */
+void saras_mg_default_params(saras_mg_params *p);
+
+/* Builds the level hierarchy, metric tables and device arrays.  `stream` is
+ * a cudaStream_t (NULL: the legacy default stream). */
+saras_status saras_mg_create(const saras_grid_desc *grid, const saras_mg_params *prm,
+                             void *stream, saras_mg **out);
+
+/* mgSolve with HOST fields: reads the core of rhs and of lhs (initial guess),
+ * writes the core plus one ghost layer of lhs.  res_hist (may be NULL)
+ * receives the residual after each V-cycle, up to hist_cap entries;
+ * *n_cycles the number of V-cycles (outer iterations) run. */
+saras_status saras_mg_solve(saras_mg *h, double *lhs, const double *rhs, const int64_t strides[3],
+                            double *res_hist, int32_t hist_cap, int32_t *n_cycles);
+
+/* Same with DEVICE pointers (same layout rules); no host copies. */
+saras_status saras_mg_solve_dev(saras_mg *h, double *lhs, const double *rhs, const int64_t strides[3],
+                                double *res_hist, int32_t hist_cap, int32_t *n_cycles);
+
+saras_status saras_mg_destroy(saras_mg *h);
+
+int32_t saras_mg_num_levels(const saras_mg *h);
+
+/* Bytes of device memory the handle holds. */
+int64_t saras_mg_device_bytes(const saras_mg *h);
+
+/* Kernel timing: when enabled, launches of each kernel class are bracketed
+ * with CUDA events on the solve stream.  Class ids: 0 smoothing sweep at the
+ * finest level, 1 residual+restriction, 2 prolongation+correction,
+ * 3 residual norm, 4 coarsest solve. */
+saras_status saras_mg_set_kernel_timing(saras_mg *h, int32_t enable);
+saras_status saras_mg_kernel_stats(saras_mg *h, int32_t kclass, int64_t *launches,
+                                   double *total_ms, double *bytes_per_launch);
+/* Total kernel launches issued by the last solve. */
+int64_t saras_mg_last_launches(const saras_mg *h);
+
+/* Host restatement of the per-level grid metrics the multigrid uses:
+ * x (cell centres), xixx and xix2 for `axis` at `level`, each over indices
+ * -1..n_l (n_l + 2 values).  *n_out receives n_l. */
+saras_status saras_grid_metrics(const saras_grid_desc *grid, int32_t levels, int32_t level,
+                                int32_t axis, double *x, double *xixx, double *xix2,
+                                int32_t *n_out);
+
+/* Number of levels setVCDepth gives for this grid (vcdGlo + 1), or -1. */
+int32_t saras_reference_levels(const saras_grid_desc *grid);
+
+/* Left null vector w of the 1-D all-Neumann finest-level operator along
+ * `axis` (n values, normalised to max |w| = 1).  The 3-D operator's left null
+ * vector is w_x (x) w_y (x) w_z; a right-hand side f is compatible iff
+ * sum w f = 0. */
+saras_status saras_neumann_null_vector(const saras_grid_desc *grid, int32_t axis, double *w);
+
+/* ---------------------------------------------------------------- RK3 ---- */
+
+typedef struct saras_field_bc {
+    int32_t type[6];   /* SARAS_FBC_* for faces x-, x+, y-, y+, z-, z+ */
+    double  value[6];
+} saras_field_bc;
+
+typedef struct saras_rk3_params {
+    double  nu, kappa;      /* from timestep::timestep (see saras_rbc_coefficients) */
+    double  dt;             /* "Time-Step" */
+    double  cn_tolerance;   /* Solver "Solve Tolerance" */
+    int32_t max_iterations; /* 0: int(pow(log(Nx*Ny*Nz), 3)) as timestep.cc:115 */
+    double  g_terms[3];     /* buoyancy Fb*g/|g|; all zero for zeroForcing */
+    int32_t with_scalar;    /* 1: timeAdvance(V,P,T); 0: timeAdvance(V,P) */
+    int32_t nl_scheme;      /* "Non-Linear Term": 1 (central) */
+    saras_field_bc bc_vx, bc_vy, bc_vz, bc_t;
+    saras_field_bc bc_p;    /* pressure field walls */
+    saras_mg_params mg;     /* pressure-correction solve */
+} saras_rk3_params;
+
+typedef struct saras_rk3 saras_rk3;
+
+/* nu, kappa and buoyancy strength Fb for "RBC Type" 1-4 (timestep.cc:74-99,
+ * buoyantForce.cc:45-57). */
+saras_status saras_rbc_coefficients(int32_t rbc_type, double ra, double pr,
+                                    double *nu, double *kappa, double *fb);
+
+saras_status saras_rk3_create(const saras_grid_desc *grid, const saras_rk3_params *prm,
+                              void *stream, saras_rk3 **out);
+/* Copies full padded fields (pad from the grid descriptor) host -> device.
+ * vy is ignored for dims==2, t when with_scalar==0.  pp is the pressure
+ * correction, the multigrid initial guess that persists between calls. */
+saras_status saras_rk3_upload(saras_rk3 *h, const double *vx, const double *vy, const double *vz,
+                              const double *p, const double *t, const double *pp,
+                              const int64_t strides[3]);
+saras_status saras_rk3_download(saras_rk3 *h, double *vx, double *vy, double *vz,
+                                double *p, double *t, double *pp, const int64_t strides[3]);
+/* Runs nsteps calls of timeAdvance.  *mg_cycles (may be NULL) receives the
+ * total V-cycles of the pressure solves, *cn_iters the total Jacobi sweeps. */
+saras_status saras_rk3_step(saras_rk3 *h, int32_t nsteps, int32_t *mg_cycles, int32_t *cn_iters);
+saras_status saras_rk3_destroy(saras_rk3 *h);
+int64_t saras_rk3_last_launches(const saras_rk3 *h);
+
+/* ------------------------------------------------------------- common ---- */
+
+const char *saras_status_string(saras_status s);
+/* Text of the last error on the calling thread ("" if none). */
+const char *saras_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SARAS_GB300_H */

@@ -1,0 +1,125 @@
+"""ctypes binding of oracle/liboracle.so -- TEST INFRASTRUCTURE ONLY.
+
+The oracle is the CPU restatement of SARAS-CC's hot path (oracle/saras_oracle.cpp).
+It is loaded by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg
+to check and time the reference algorithm; the product never imports it.
+The ABI structs are the ones declared in include/saras_gb300.h (shared with
+the product binding, which defines them for ctypes).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import pathlib
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = pathlib.Path(__file__).resolve().parent
+LIB_PATH = HERE / "liboracle.so"
+sys.path.insert(0, str(HERE.parent / "saras-cc_gb300"))
+import saras_gb300 as abi  # noqa: E402  (ctypes struct layouts only)
+
+_lib = None
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        build()
+    lib = C.CDLL(str(LIB_PATH))
+    vp, i32, i64, dp = C.c_void_p, C.c_int, C.c_int64, C.POINTER(C.c_double)
+    lib.oracle_set_threads.argtypes = [i32]
+    lib.oracle_max_threads.restype = i32
+    lib.oracle_num_levels.argtypes = [C.POINTER(abi.GridDesc), i32]
+    lib.oracle_num_levels.restype = i32
+    lib.oracle_grid_metrics.argtypes = [C.POINTER(abi.GridDesc), i32, i32, i32, dp, dp, dp,
+                                        C.POINTER(i32)]
+    lib.oracle_field_metrics.argtypes = [C.POINTER(abi.GridDesc), i32, dp, dp, dp, dp]
+    lib.oracle_mg_solve.argtypes = [C.POINTER(abi.GridDesc), C.POINTER(abi.MgParams), vp, vp,
+                                    C.POINTER(i64), dp, i32, C.POINTER(i32), C.POINTER(i32), dp]
+    lib.oracle_rk3_run.argtypes = [C.POINTER(abi.GridDesc), C.POINTER(abi.Rk3Params), vp, vp, vp, vp,
+                                   vp, vp, C.POINTER(i64), i32, C.POINTER(i32), C.POINTER(i32), dp]
+    _lib = lib
+    return lib
+
+
+def set_threads(n: int):
+    load().oracle_set_threads(n)
+
+
+def max_threads() -> int:
+    return load().oracle_max_threads()
+
+
+def num_levels(grid, levels=0) -> int:
+    return load().oracle_num_levels(C.byref(grid), levels)
+
+
+def grid_metrics(grid, level, axis, levels=0):
+    lib = load()
+    cap = grid.n[axis] + 2
+    x, a, b = (np.zeros(cap) for _ in range(3))
+    n = C.c_int()
+    dp = C.POINTER(C.c_double)
+    s = lib.oracle_grid_metrics(C.byref(grid), levels, level, axis, x.ctypes.data_as(dp),
+                                a.ctypes.data_as(dp), b.ctypes.data_as(dp), C.byref(n))
+    if s:
+        raise RuntimeError(f"oracle_grid_metrics status {s}")
+    m = n.value + 2
+    return x[:m].copy(), a[:m].copy(), b[:m].copy()
+
+
+def field_metrics(grid, axis):
+    lib = load()
+    m = grid.n[axis] + 2 * grid.pad
+    arrs = [np.zeros(m) for _ in range(4)]
+    dp = C.POINTER(C.c_double)
+    s = lib.oracle_field_metrics(C.byref(grid), axis, *[a.ctypes.data_as(dp) for a in arrs])
+    if s:
+        raise RuntimeError(f"oracle_field_metrics status {s}")
+    return arrs  # x, xi_x, xixx, xix2
+
+
+class Result:
+    pass
+
+
+def mg_solve(grid, params, out_lhs: np.ndarray, inp_rhs: np.ndarray, hist_cap: int = 512):
+    """poisson::mgSolve on numpy padded fields (out_lhs updated in place)."""
+    lib = load()
+    po, st = abi.field_origin(out_lhs, grid)
+    pi, _ = abi.field_origin(inp_rhs, grid)
+    hist = np.zeros(hist_cap)
+    n, cs, sec = C.c_int(), C.c_int(), C.c_double()
+    s = lib.oracle_mg_solve(C.byref(grid), C.byref(params), po, pi, st,
+                            hist.ctypes.data_as(C.POINTER(C.c_double)), hist_cap, C.byref(n),
+                            C.byref(cs), C.byref(sec))
+    r = Result()
+    r.status, r.cycles, r.coarse_sweeps, r.seconds = s, n.value, cs.value, sec.value
+    r.history = hist[:min(n.value, hist_cap)].copy()
+    return r
+
+
+def rk3_run(grid, params, vx, vy, vz, p, t, pp, nsteps=1):
+    lib = load()
+    ptrs = []
+    st = None
+    for f in (vx, vy, vz, p, t, pp):
+        if f is None:
+            ptrs.append(C.c_void_p(0))
+            continue
+        ptr, st = abi.field_origin(f, grid)
+        ptrs.append(ptr)
+    mgc, cni, sec = C.c_int(), C.c_int(), C.c_double()
+    s = lib.oracle_rk3_run(C.byref(grid), C.byref(params), *ptrs, st, nsteps, C.byref(mgc),
+                           C.byref(cni), C.byref(sec))
+    r = Result()
+    r.status, r.mg_cycles, r.cn_iters, r.seconds = s, mgc.value, cni.value, sec.value
+    return r

@@ -1,0 +1,67 @@
+// Shared helpers of the GB300 SARAS hot-path library: error reporting,
+// padded device array layout and FP64 arithmetic with explicit rounding.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+
+#include "../../include/saras_gb300.h"
+
+namespace saras {
+
+// Records a message for saras_last_error() on the calling thread.
+void set_error(const char *fmt, ...);
+saras_status cuda_fail(cudaError_t e, const char *what, const char *file, int line);
+
+#define SARAS_CUDA(call)                                                          \
+    do {                                                                          \
+        cudaError_t e_ = (call);                                                  \
+        if (e_ != cudaSuccess) return ::saras::cuda_fail(e_, #call, __FILE__, __LINE__); \
+    } while (0)
+
+#define SARAS_TRY(call)                               \
+    do {                                              \
+        saras_status s_ = (call);                     \
+        if (s_ != SARAS_OK) return s_;                \
+    } while (0)
+
+// Padded level array: core (0..n-1 per axis) plus one ghost layer.  Element
+// (i,j,k) sits at (i+1)*s0 + (j+1)*s1 + (k+KOFF): each k-row starts its core
+// on a 32-byte boundary (KOFF = 4 elements) so rows load with aligned
+// vector accesses; the ghost k=-1 sits at KOFF-1.
+constexpr int KOFF = 4;
+
+struct Lay {
+    int n0, n1, n2;  // core extents (n1 == 1 for the planar case)
+    int64_t s0, s1;  // element strides of i and j (k stride 1)
+    int64_t size;    // elements including alignment padding
+
+    __host__ __device__ __forceinline__ int64_t at(int i, int j, int k) const {
+        return (int64_t)(i + 1) * s0 + (int64_t)(j + 1) * s1 + (int64_t)(k + KOFF);
+    }
+};
+
+inline Lay make_lay(int n0, int n1, int n2) {
+    Lay l;
+    l.n0 = n0;
+    l.n1 = n1;
+    l.n2 = n2;
+    l.s1 = ((int64_t)n2 + KOFF + 1 + 3) / 4 * 4;
+    l.s0 = l.s1 * (n1 + 2);
+    l.size = l.s0 * (n0 + 2);
+    return l;
+}
+
+// FP64 with explicit rounding: these never contract into fused
+// multiply-adds, which keeps the exact kernels' results bit-identical to the
+// reference's separately rounded operations.
+__device__ __forceinline__ double radd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double rsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double rmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double rdiv(double a, double b) { return __ddiv_rn(a, b); }
+
+inline unsigned cdiv(int64_t a, int64_t b) { return (unsigned)((a + b - 1) / b); }
+
+}  // namespace saras

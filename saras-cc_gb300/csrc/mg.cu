@@ -1,0 +1,982 @@
+// Cell-centred geometric multigrid for the SARAS pressure-Poisson equation on
+// GB300 (sm_103a): hierarchy set-up, the FP64_EXACT kernels, the solve loop
+// and the saras_mg_* C entry points.  The FP64 and MIXED forms live in
+// mg_fast.cu and share this handle.
+//
+// Reference: lib/poisson/poisson.cc (mgSolve 109-189, vCycle 203-279,
+// setStagBounds 358-441, setCoefficients 453-483, copyDerivs 501-622) and
+// poisson_d3.cc / poisson_d2.cc (computeResidual, smooth, solve, coarsen,
+// prolong, computeError, imposeBC, updateFace), single-rank semantics.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "mg_handle.cuh"
+#include "mg_fast.cuh"
+
+using namespace saras;
+
+namespace {
+
+constexpr int BX = 128;
+
+inline dim3 cell_grid(const Lay &L, bool d3, int kcount, int bx) {
+    return dim3(cdiv(kcount, bx), d3 ? (unsigned)L.n1 : 1u, (unsigned)L.n0);
+}
+
+// ------------------------------------------------------------ kernels ----
+
+// One colour of the SOR red-black sweep: cells with (i+j+k) even are red,
+// odd are black (the parity loops of poisson_d3.cc:104-242).
+template <bool D3>
+__global__ void k_rbgs_exact(double *u, const double *__restrict__ f, Lay L, Coef C, int colour,
+                             double w, double omc) {
+    const int kk = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = D3 ? (int)blockIdx.y : 0;
+    const int i = blockIdx.z;
+    const int k = 2 * kk + ((i + j + colour) & 1);
+    if (k >= L.n2) return;
+    u[L.at(i, j, k)] = rbgs_exact<D3>(u, f, L, C, i, j, k, w, omc);
+}
+
+template <bool D3>
+__global__ void k_resid_exact(const double *__restrict__ u, const double *__restrict__ f,
+                              double *__restrict__ t, Lay L, Coef C) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = D3 ? (int)blockIdx.y : 0;
+    const int i = blockIdx.z;
+    if (k >= L.n2) return;
+    t[L.at(i, j, k)] = resid_exact<D3>(u, f, L, C, i, j, k);
+}
+
+// Restriction (multigrid_d3::coarsen regular branch, poisson_d3.cc:483-511;
+// multigrid_d2::coarsen: mean of four).
+template <bool D3>
+__global__ void k_restrict_exact(const double *__restrict__ t, double *__restrict__ r, Lay Lf, Lay Lc,
+                                 RTab R) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = D3 ? (int)blockIdx.y : 0;
+    const int i = blockIdx.z;
+    if (k >= Lc.n2) return;
+    const int i2 = 2 * i, j2 = 2 * j, k2 = 2 * k;
+    if (D3) {
+        const double x0 = R.r0x[i], x1 = R.r1x[i], y0 = R.r0y[j], y1 = R.r1y[j], z0 = R.r0z[k],
+                     z1 = R.r1z[k];
+        const double v000 = rmul(rmul(x0, y0), z0);
+        const double v100 = rmul(rmul(x1, y0), z0);
+        const double v010 = rmul(rmul(x0, y1), z0);
+        const double v001 = rmul(rmul(x0, y0), z1);
+        const double v011 = rmul(rmul(x0, y1), z1);
+        const double v101 = rmul(rmul(x1, y0), z1);
+        const double v110 = rmul(rmul(x1, y1), z0);
+        const double v111 = rmul(rmul(x1, y1), z1);
+        const double vt = rmul(rmul(R.rtx[i], R.rty[j]), R.rtz[k]);
+        double s = rmul(v111, t[Lf.at(i2 + 1, j2 + 1, k2 + 1)]);
+        s = radd(s, rmul(v000, t[Lf.at(i2, j2, k2)]));
+        s = radd(s, rmul(v110, t[Lf.at(i2 + 1, j2 + 1, k2)]));
+        s = radd(s, rmul(v001, t[Lf.at(i2, j2, k2 + 1)]));
+        s = radd(s, rmul(v101, t[Lf.at(i2 + 1, j2, k2 + 1)]));
+        s = radd(s, rmul(v010, t[Lf.at(i2, j2 + 1, k2)]));
+        s = radd(s, rmul(v011, t[Lf.at(i2, j2 + 1, k2 + 1)]));
+        s = radd(s, rmul(v100, t[Lf.at(i2 + 1, j2, k2)]));
+        r[Lc.at(i, j, k)] = rdiv(s, vt);
+    } else {
+        double s = radd(t[Lf.at(i2 + 1, 0, k2 + 1)], t[Lf.at(i2, 0, k2)]);
+        s = radd(s, t[Lf.at(i2 + 1, 0, k2)]);
+        s = radd(s, t[Lf.at(i2, 0, k2 + 1)]);
+        r[Lc.at(i, 0, k)] = rdiv(s, 4.0);
+    }
+}
+
+// Injection prolongation into a zeroed fine array followed by lhs += smd
+// over the full padded array (poisson_d3.cc:516-560, poisson.cc:263-266).
+__global__ void k_prolong_exact(const double *__restrict__ c, const double *__restrict__ smd,
+                                double *__restrict__ f, Lay Lf, Lay Lc, int d3) {
+    const int k = (int)(blockIdx.x * blockDim.x + threadIdx.x) - 1;
+    const int j = (int)blockIdx.y - 1;
+    const int i = (int)blockIdx.z - 1;
+    if (k > Lf.n2) return;
+    const bool core = i >= 0 && i < Lf.n0 && j >= 0 && j < Lf.n1 && k >= 0 && k < Lf.n2;
+    const double v = core ? c[Lc.at(i / 2, d3 ? j / 2 : 0, k / 2)] : 0.0;
+    const int64_t q = Lf.at(i, j, k);
+    f[q] = radd(v, smd[q]);
+}
+
+// One axis of the ghost refresh over a plane range.
+__global__ void k_ghost(double *u, Lay L, Ghost G, int axis, int wall_pass, int zeroBC, int lvl0,
+                        int a_lo, int b_lo, int b_cnt) {
+    const int b = b_lo + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int a = a_lo + (int)blockIdx.y;
+    if (b >= b_lo + b_cnt) return;
+    ghost_axis_cell(u, L, G, axis, a, b, wall_pass != 0, zeroBC != 0, lvl0 != 0);
+}
+
+__device__ __forceinline__ double warp_max(double v) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const double w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    return v;
+}
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v = radd(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Residual norms of the finest level (multigrid_d3::computeError,
+// poisson_d3.cc:563-663): per-block partials of max|r|, max|f|, and the
+// sums of |r|,|f| (L1) or r^2, f^2 (L2).
+template <bool D3>
+__global__ void k_norm_exact(const double *__restrict__ u, const double *__restrict__ f, Lay L, Coef C,
+                             int rtype, double *__restrict__ part) {
+    const int64_t total = (int64_t)L.n0 * L.n1 * L.n2;
+    double mr = 0.0, mf = 0.0, sr = 0.0, sf = 0.0;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int k = (int)(q % L.n2);
+        const int64_t rest = q / L.n2;
+        const int j = (int)(rest % L.n1);
+        const int i = (int)(rest / L.n1);
+        const double r = resid_exact<D3>(u, f, L, C, i, j, k);
+        const double fv = f[L.at(i, j, k)];
+        if (rtype == 0) {
+            const double ar = fabs(r), af = fabs(fv);
+            if (ar > mr) mr = ar;
+            if (af > mf) mf = af;
+        } else if (rtype == 1) {
+            sr = radd(sr, fabs(r));
+            sf = radd(sf, fabs(fv));
+        } else {
+            sr = radd(sr, rmul(r, r));
+            sf = radd(sf, rmul(fv, fv));
+        }
+    }
+    __shared__ double sh[4][32];
+    mr = warp_max(mr);
+    mf = warp_max(mf);
+    sr = warp_sum(sr);
+    sf = warp_sum(sf);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (lane == 0) {
+        sh[0][wid] = mr;
+        sh[1][wid] = mf;
+        sh[2][wid] = sr;
+        sh[3][wid] = sf;
+    }
+    __syncthreads();
+    if (wid == 0) {
+        mr = lane < nw ? sh[0][lane] : 0.0;
+        mf = lane < nw ? sh[1][lane] : 0.0;
+        sr = lane < nw ? sh[2][lane] : 0.0;
+        sf = lane < nw ? sh[3][lane] : 0.0;
+        mr = warp_max(mr);
+        mf = warp_max(mf);
+        sr = warp_sum(sr);
+        sf = warp_sum(sf);
+        if (lane == 0) {
+            part[4 * blockIdx.x + 0] = mr;
+            part[4 * blockIdx.x + 1] = mf;
+            part[4 * blockIdx.x + 2] = sr;
+            part[4 * blockIdx.x + 3] = sf;
+        }
+    }
+}
+
+// Combines the partials in a fixed order and forms residualVal.
+__global__ void k_norm_final(const double *__restrict__ part, int nb, int rtype, double point_count,
+                             double *__restrict__ out) {
+    double mr = 0.0, mf = 0.0, sr = 0.0, sf = 0.0;
+    for (int b = threadIdx.x; b < nb; b += 32) {
+        const double a = part[4 * b], c = part[4 * b + 1];
+        if (a > mr) mr = a;
+        if (c > mf) mf = c;
+        sr = radd(sr, part[4 * b + 2]);
+        sf = radd(sf, part[4 * b + 3]);
+    }
+    mr = warp_max(mr);
+    mf = warp_max(mf);
+    sr = warp_sum(sr);
+    sf = warp_sum(sf);
+    if (threadIdx.x == 0) {
+        double num, den, res;
+        if (rtype == 0) {
+            num = mr;
+            den = mf;
+            res = den != 0.0 ? rdiv(num, den) : num;
+        } else if (rtype == 1) {
+            num = sr;
+            den = sf;
+            res = den != 0.0 ? rdiv(num, den) : rdiv(num, point_count);
+        } else {
+            num = sr;
+            den = sf;
+            res = den != 0.0 ? rdiv(__dsqrt_rn(rdiv(num, point_count)), __dsqrt_rn(rdiv(den, point_count)))
+                             : __dsqrt_rn(rdiv(num, point_count));
+        }
+        out[0] = res;
+        out[1] = num;
+        out[2] = den;
+    }
+}
+
+// ---- coarsest-level solve (multigrid_d3::solve, poisson_d3.cc:249-432) ----
+
+__device__ void block_ghost_pass(double *u, const Lay &L, const Ghost &G, bool d3, bool wall_pass) {
+    for (int axis = 0; axis < 3; axis++) {
+        if (!d3 && axis == 1) continue;
+        const int n[3] = {L.n0, L.n1, L.n2};
+        const int o0 = axis == 0 ? 1 : 0, o1 = axis == 2 ? 1 : 2;
+        int alo = -1, acnt = n[o0] + 2, blo = -1, bcnt = n[o1] + 2;
+        if (!d3) {
+            if (o0 == 1) { alo = 0; acnt = 1; }
+            if (o1 == 1) { blo = 0; bcnt = 1; }
+        }
+        const int total = acnt * bcnt;
+        for (int q = threadIdx.x; q < total; q += blockDim.x)
+            ghost_axis_cell(u, L, G, axis, alo + q / bcnt, blo + q % bcnt, wall_pass, true, false);
+        __syncthreads();
+    }
+}
+
+template <bool D3>
+__device__ void block_colour(double *u, const double *f, const Lay &L, const Coef &C, int colour, double w,
+                             double omc) {
+    const int half = (L.n2 + 1) / 2;
+    const int total = L.n0 * L.n1 * half;
+    for (int q = threadIdx.x; q < total; q += blockDim.x) {
+        const int kk = q % half;
+        const int rest = q / half;
+        const int j = rest % L.n1;
+        const int i = rest / L.n1;
+        const int k = 2 * kk + ((i + j + colour) & 1);
+        if (k < L.n2) u[L.at(i, j, k)] = rbgs_exact<D3>(u, f, L, C, i, j, k, w, omc);
+    }
+    __syncthreads();
+}
+
+template <bool D3>
+__global__ void k_coarsest_exact(double *u, const double *__restrict__ f, Lay L, Coef C, Ghost G, double w,
+                                 double omc, double tol, int max_count, int *sweeps_out) {
+    __shared__ double sh[32];
+    int iter = 0, sweeps = 0;
+    for (;;) {
+        block_ghost_pass(u, L, G, D3, false);
+        block_ghost_pass(u, L, G, D3, true);
+        block_colour<D3>(u, f, L, C, 0, w, omc);
+        block_ghost_pass(u, L, G, D3, false);
+        block_colour<D3>(u, f, L, C, 1, w, omc);
+        double m = -1.0e-10;
+        const int total = L.n0 * L.n1 * L.n2;
+        for (int q = threadIdx.x; q < total; q += blockDim.x) {
+            const int k = q % L.n2;
+            const int rest = q / L.n2;
+            const int j = rest % L.n1;
+            const int i = rest / L.n1;
+            const double t = fabs(resid_exact<D3>(u, f, L, C, i, j, k));
+            if (t > m) m = t;
+        }
+        m = warp_max(m);
+        if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            double v = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : -1.0e-10;
+            v = warp_max(v);
+            if (threadIdx.x == 0) sh[0] = v;
+        }
+        __syncthreads();
+        m = sh[0];
+        __syncthreads();
+        sweeps++;
+        if (m < tol) break;
+        iter++;
+        if (iter > max_count) break;  // the reference warns and moves on
+    }
+    block_ghost_pass(u, L, G, D3, false);
+    block_ghost_pass(u, L, G, D3, true);
+    if (threadIdx.x == 0) *sweeps_out += sweeps;
+}
+
+// ---- caller arrays ----
+
+__global__ void k_scatter(const double *__restrict__ lhs_src, const double *__restrict__ rhs_src, int64_t s0,
+                          int64_t s1, int64_t s2, double *__restrict__ lhs, double *__restrict__ rhs, Lay L) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y, i = blockIdx.z;
+    if (k >= L.n2) return;
+    const int64_t q = (int64_t)i * s0 + (int64_t)j * s1 + (int64_t)k * s2;
+    const int64_t d = L.at(i, j, k);
+    lhs[d] = lhs_src[q];
+    rhs[d] = rhs_src[q];
+}
+
+__global__ void k_gather(const double *__restrict__ lhs, Lay L, double *__restrict__ dst, int64_t s0, int64_t s1,
+                         int64_t s2) {
+    const int k = (int)(blockIdx.x * blockDim.x + threadIdx.x) - 1;
+    const int j = (int)blockIdx.y - 1, i = (int)blockIdx.z - 1;
+    if (k > L.n2) return;
+    dst[(int64_t)i * s0 + (int64_t)j * s1 + (int64_t)k * s2] = lhs[L.at(i, j, k)];
+}
+
+}  // namespace
+
+// ------------------------------------------------------- host helpers ----
+
+namespace saras {
+
+void kbegin(saras_mg *h, cudaStream_t s, int kc) {
+    h->issued++;
+    if (!h->timing || kc < 0) return;
+    if (h->ev_used + 2 > h->ev_pool.size()) {
+        for (int q = 0; q < 64; q++) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            h->ev_pool.push_back(e);
+        }
+    }
+    h->ev_marks.push_back({kc, h->ev_used});
+    cudaEventRecord(h->ev_pool[h->ev_used], s);
+    h->ev_used += 2;
+}
+
+void kend(saras_mg *h, cudaStream_t s, int kc) {
+    if (!h->timing || kc < 0) return;
+    cudaEventRecord(h->ev_pool[h->ev_marks.back().second + 1], s);
+}
+
+void harvest_timing(saras_mg *h) {
+    if (!h->timing) return;
+    for (auto &m : h->ev_marks) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, h->ev_pool[m.second], h->ev_pool[m.second + 1]);
+        h->kc_ms[m.first] += ms;
+        h->kc_launches[m.first] += 1;
+    }
+    h->ev_marks.clear();
+    h->ev_used = 0;
+}
+
+static void ghost_axis_launch(saras_mg *h, cudaStream_t s, double *u, const Lay &L, int axis, bool wall_pass,
+                              bool zeroBC, bool lvl0) {
+    if (!h->d3 && axis == 1) return;
+    if (wall_pass == (bool)h->ghost.per[axis]) return;  // nothing to do on this axis in this pass
+    const int n[3] = {L.n0, L.n1, L.n2};
+    const int o0 = axis == 0 ? 1 : 0, o1 = axis == 2 ? 1 : 2;
+    int alo = -1, acnt = n[o0] + 2, blo = -1, bcnt = n[o1] + 2;
+    if (!h->d3) {
+        if (o0 == 1) { alo = 0; acnt = 1; }
+        if (o1 == 1) { blo = 0; bcnt = 1; }
+    }
+    const int bx = std::min(128, (bcnt + 31) / 32 * 32);
+    kbegin(h, s, -1);
+    k_ghost<<<dim3(cdiv(bcnt, bx), (unsigned)acnt), bx, 0, s>>>(u, L, h->ghost, axis, wall_pass, zeroBC, lvl0,
+                                                               alo, blo, bcnt);
+}
+
+// imposeBC: wrap pass over x, y, z, then wall pass over x, y, z.
+static void ghost_all(saras_mg *h, cudaStream_t s, int l, bool zeroBC) {
+    Level &v = h->lv[(size_t)l];
+    for (int a = 0; a < 3; a++) ghost_axis_launch(h, s, v.lhs, v.lay, a, false, zeroBC, l == 0);
+    for (int a = 0; a < 3; a++) ghost_axis_launch(h, s, v.lhs, v.lay, a, true, zeroBC, l == 0);
+}
+
+static void ghost_wrap(saras_mg *h, cudaStream_t s, int l) {
+    Level &v = h->lv[(size_t)l];
+    for (int a = 0; a < 3; a++) ghost_axis_launch(h, s, v.lhs, v.lay, a, false, true, l == 0);
+}
+
+static void colour_exact(saras_mg *h, cudaStream_t s, int l, int colour) {
+    Level &v = h->lv[(size_t)l];
+    const Lay &L = v.lay;
+    const int half = (L.n2 + 1) / 2;
+    const int bx = std::min(BX, (half + 31) / 32 * 32);
+    const double w = h->prm.sor_param, omc = 1.0 - h->prm.sor_param;
+    kbegin(h, s, l == 0 ? KC_SMOOTH0 : -1);
+    if (h->d3)
+        k_rbgs_exact<true><<<cell_grid(L, true, half, bx), bx, 0, s>>>(v.lhs, v.rhs, L, v.coef, colour, w, omc);
+    else
+        k_rbgs_exact<false><<<cell_grid(L, false, half, bx), bx, 0, s>>>(v.lhs, v.rhs, L, v.coef, colour, w, omc);
+    kend(h, s, l == 0 ? KC_SMOOTH0 : -1);
+}
+
+// multigrid_d*::smooth
+static void smooth_exact(saras_mg *h, cudaStream_t s, int l, int count, bool zeroBC) {
+    for (int n = 0; n < count; n++) {
+        ghost_all(h, s, l, zeroBC);
+        colour_exact(h, s, l, 0);
+        ghost_wrap(h, s, l);
+        colour_exact(h, s, l, 1);
+    }
+    ghost_all(h, s, l, zeroBC);
+}
+
+static void norm_exact(saras_mg *h, cudaStream_t s) {
+    Level &v = h->lv[0];
+    const double pc = h->d3 ? (double)h->grid.N[0] * h->grid.N[1] * h->grid.N[2]
+                            : (double)h->grid.N[0] * h->grid.N[2];
+    kbegin(h, s, KC_NORM);
+    if (h->d3)
+        k_norm_exact<true><<<h->norm_blocks, 256, 0, s>>>(v.lhs, v.rhs, v.lay, v.coef, h->prm.res_type,
+                                                           h->norm_part);
+    else
+        k_norm_exact<false><<<h->norm_blocks, 256, 0, s>>>(v.lhs, v.rhs, v.lay, v.coef, h->prm.res_type,
+                                                            h->norm_part);
+    kend(h, s, KC_NORM);
+    kbegin(h, s, -1);
+    k_norm_final<<<1, 32, 0, s>>>(h->norm_part, h->norm_blocks, h->prm.res_type, pc, h->norm_out);
+}
+
+// poisson::vCycle in the FP64_EXACT form.
+static void vcycle_exact(saras_mg *h, cudaStream_t s) {
+    const int top = h->nl - 1;
+    const double w = h->prm.sor_param, omc = 1.0 - h->prm.sor_param;
+    smooth_exact(h, s, 0, h->prm.pre_smooth, false);
+    for (int l = 0; l < top; l++) {
+        Level &f = h->lv[(size_t)l];
+        Level &c = h->lv[(size_t)l + 1];
+        const Lay &L = f.lay;
+        const int bx = std::min(BX, (L.n2 + 31) / 32 * 32);
+        kbegin(h, s, l == 0 ? KC_RESTRICT : -1);
+        if (h->d3)
+            k_resid_exact<true><<<cell_grid(L, true, L.n2, bx), bx, 0, s>>>(f.lhs, f.rhs, f.tmp, L, f.coef);
+        else
+            k_resid_exact<false><<<cell_grid(L, false, L.n2, bx), bx, 0, s>>>(f.lhs, f.rhs, f.tmp, L, f.coef);
+        kend(h, s, l == 0 ? KC_RESTRICT : -1);
+        cudaMemcpyAsync(f.smd, f.lhs, (size_t)L.size * sizeof(double), cudaMemcpyDeviceToDevice, s);
+        const Lay &C = c.lay;
+        const int cbx = std::min(BX, (C.n2 + 31) / 32 * 32);
+        kbegin(h, s, -1);
+        if (h->d3)
+            k_restrict_exact<true><<<cell_grid(C, true, C.n2, cbx), cbx, 0, s>>>(f.tmp, c.rhs, L, C, c.rt);
+        else
+            k_restrict_exact<false><<<cell_grid(C, false, C.n2, cbx), cbx, 0, s>>>(f.tmp, c.rhs, L, C, c.rt);
+        cudaMemsetAsync(c.lhs, 0, (size_t)C.size * sizeof(double), s);
+        if (l + 1 == top && h->prm.solve_flag) {
+            kbegin(h, s, KC_COARSE);
+            if (h->d3)
+                k_coarsest_exact<true><<<1, 256, 0, s>>>(c.lhs, c.rhs, C, c.coef, h->ghost, w, omc,
+                                                          h->prm.mg_tolerance, h->maxCount(), h->coarse_sweeps);
+            else
+                k_coarsest_exact<false><<<1, 256, 0, s>>>(c.lhs, c.rhs, C, c.coef, h->ghost, w, omc,
+                                                           h->prm.mg_tolerance, h->maxCount(), h->coarse_sweeps);
+            kend(h, s, KC_COARSE);
+        } else {
+            smooth_exact(h, s, l + 1, h->prm.pre_smooth, true);
+        }
+    }
+    for (int l = top; l > 0; l--) {
+        Level &c = h->lv[(size_t)l];
+        Level &f = h->lv[(size_t)l - 1];
+        const Lay &L = f.lay;
+        const int bx = std::min(BX, (L.n2 + 2 + 31) / 32 * 32);
+        kbegin(h, s, l == 1 ? KC_PROLONG : -1);
+        k_prolong_exact<<<dim3(cdiv(L.n2 + 2, bx), (unsigned)L.n1 + 2, (unsigned)L.n0 + 2), bx, 0, s>>>(
+            c.lhs, f.smd, f.lhs, L, c.lay, h->d3 ? 1 : 0);
+        kend(h, s, l == 1 ? KC_PROLONG : -1);
+        smooth_exact(h, s, l - 1, h->prm.post_smooth, l - 1 != 0);
+    }
+    norm_exact(h, s);
+}
+
+// Hooks used by the FP64 and MIXED forms (mg_fast.cu).
+void coarsest_level(saras_mg *h, cudaStream_t s) {
+    const int top = h->nl - 1;
+    Level &c = h->lv[(size_t)top];
+    if (h->prm.solve_flag) {
+        const double w = h->prm.sor_param, omc = 1.0 - h->prm.sor_param;
+        kbegin(h, s, KC_COARSE);
+        if (h->d3)
+            k_coarsest_exact<true><<<1, 256, 0, s>>>(c.lhs, c.rhs, c.lay, c.coef, h->ghost, w, omc,
+                                                      h->prm.mg_tolerance, h->maxCount(), h->coarse_sweeps);
+        else
+            k_coarsest_exact<false><<<1, 256, 0, s>>>(c.lhs, c.rhs, c.lay, c.coef, h->ghost, w, omc,
+                                                       h->prm.mg_tolerance, h->maxCount(), h->coarse_sweeps);
+        kend(h, s, KC_COARSE);
+    } else {
+        smooth_exact(h, s, top, h->prm.pre_smooth, true);
+    }
+}
+
+void norm_final(saras_mg *h, cudaStream_t s) {
+    const double pc = h->d3 ? (double)h->grid.N[0] * h->grid.N[1] * h->grid.N[2]
+                            : (double)h->grid.N[0] * h->grid.N[2];
+    kbegin(h, s, -1);
+    k_norm_final<<<1, 32, 0, s>>>(h->norm_part, h->norm_blocks, h->prm.res_type, pc, h->norm_out);
+}
+
+void ghost_all_level(saras_mg *h, cudaStream_t s, int l, bool zeroBC) { ghost_all(h, s, l, zeroBC); }
+
+}  // namespace saras
+
+int saras_mg::maxCount() const {
+    // poisson::setStagBounds (poisson.cc:430-436)
+    int cg[3];
+    for (int d = 0; d < 3; d++) cg[d] = grid.N[d] / int(std::pow(2, nl - 1));
+    return d3 ? int(2.5 * cg[0] * cg[1] * cg[2]) : int(2.5 * cg[0] * cg[2]);
+}
+
+// ------------------------------------------------------------ set-up ----
+
+namespace {
+
+template <class T>
+saras_status dalloc(saras_mg *h, T **p, int64_t count) {
+    const size_t bytes = (size_t)std::max<int64_t>(count, 1) * sizeof(T);
+    cudaError_t e = cudaMalloc((void **)p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_error("cudaMalloc of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? SARAS_OOM : SARAS_CUDA_ERR;
+    }
+    h->dev_bytes += (int64_t)bytes;
+    return SARAS_OK;
+}
+
+saras_status build_tables(saras_mg *h) {
+    const HostGrid &g = h->grid;
+    for (int l = 0; l < h->nl; l++) {
+        Level &v = h->lv[(size_t)l];
+        // Per axis: A2, A1 (exact form), cm, cp, dg (FP64 form), r0, r1, rt, w
+        // (restriction), each sized to the axis extent.
+        int n[3] = {v.lay.n0, v.lay.n1, v.lay.n2};
+        const int per_axis = 10;
+        int64_t total = 0;
+        for (int d = 0; d < 3; d++) total += (int64_t)per_axis * n[d];
+        std::vector<double> host((size_t)total, 0.0);
+        SARAS_TRY(dalloc(h, &v.tab, total));
+        std::vector<float> host32((size_t)total, 0.f);
+        SARAS_TRY(dalloc(h, &v.tab32, total));
+        int64_t off = 0;
+        const double *dp[3][per_axis];
+        const float *fp[3][per_axis];
+        for (int d = 0; d < 3; d++) {
+            const AxisLevel &a = g.lv[(size_t)l][(size_t)d];
+            const int hInc = 1 << l;
+            double ih2 = 0.0, i2h = 0.0;
+            if (g.active(d)) {
+                // poisson::setCoefficients (poisson.cc:463-482)
+                const double hx = hInc * g.dxi[d];
+                const double hx2 = std::pow(hx, 2);
+                i2h = 0.5 / hx;
+                ih2 = 1.0 / hx2;
+            }
+            for (int q = 0; q < per_axis; q++) {
+                dp[d][q] = v.tab + off + (int64_t)q * n[d];
+                fp[d][q] = v.tab32 + off + (int64_t)q * n[d];
+            }
+            for (int i = 0; i < n[d]; i++) {
+                const double xix2 = a.at(a.xix2, i), xixx = a.at(a.xixx, i);
+                const double A2 = xix2 * ih2, A1 = xixx * i2h;
+                double vals[per_axis] = {A2, A1, A2 - A1, A2 + A1, A2, 0, 0, 0, 0.5, 0.5};
+                if (l > 0 && g.active(d)) {
+                    const AxisLevel &f = g.lv[(size_t)l - 1][(size_t)d];
+                    const double xc = a.at(a.x, i), xf0 = f.at(f.x, 2 * i), xf1 = f.at(f.x, 2 * i + 1);
+                    vals[5] = xc - xf0;
+                    vals[6] = xf1 - xc;
+                    vals[7] = xf1 - xf0;
+                    vals[8] = vals[5] / vals[7];
+                    vals[9] = vals[6] / vals[7];
+                }
+                for (int q = 0; q < per_axis; q++) {
+                    host[(size_t)(off + (int64_t)q * n[d] + i)] = vals[q];
+                    host32[(size_t)(off + (int64_t)q * n[d] + i)] = (float)vals[q];
+                }
+            }
+            off += (int64_t)per_axis * n[d];
+        }
+        SARAS_CUDA(cudaMemcpy(v.tab, host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice));
+        SARAS_CUDA(cudaMemcpy(v.tab32, host32.data(), host32.size() * sizeof(float), cudaMemcpyHostToDevice));
+        v.coef = Coef{dp[0][0], dp[0][1], dp[1][0], dp[1][1], dp[2][0], dp[2][1]};
+        v.rt = RTab{dp[0][5], dp[0][6], dp[0][7], dp[1][5], dp[1][6], dp[1][7], dp[2][5], dp[2][6], dp[2][7]};
+        for (int d = 0; d < 3; d++) {
+            v.cm[d] = dp[d][2];
+            v.cp[d] = dp[d][3];
+            v.dg[d] = dp[d][4];
+            v.cm32[d] = fp[d][2];
+            v.cp32[d] = fp[d][3];
+            v.dg32[d] = fp[d][4];
+            v.w0[d] = dp[d][8];
+            v.w1[d] = dp[d][9];
+            v.w032[d] = fp[d][8];
+            v.w132[d] = fp[d][9];
+        }
+    }
+    return SARAS_OK;
+}
+
+saras_status build_walls(saras_mg *h) {
+    // multigrid_d3::initDirichlet / multigrid_d2::initDirichlet
+    // (poisson_d3.cc:824-873): analytic r^2/6 (3D) or r^2/4 (2D) on the walls.
+    const HostGrid &g = h->grid;
+    bool any = false;
+    for (int f = 0; f < 6; f++) any = any || h->prm.bc_kind[f] == SARAS_BC_DIRICHLET_TEST;
+    if (!any) return SARAS_OK;
+    const Lay &L = h->lv[0].lay;
+    const int64_t nx = (int64_t)(L.n1 + 2) * (L.n2 + 2), ny = (int64_t)(L.n0 + 2) * (L.n2 + 2),
+                  nz = (int64_t)(L.n0 + 2) * (L.n1 + 2);
+    std::vector<double> w((size_t)(nx + ny + nz), 0.0);
+    const AxisLevel &ax = g.lv[0][0], &ay = g.lv[0][1], &az = g.lv[0][2];
+    if (h->d3) {
+        const double xd = g.L[0] / 2.0, yd = g.L[1] / 2.0, zd = g.L[2] / 2.0;
+        for (int j = 0; j < L.n1; j++)
+            for (int k = 0; k < L.n2; k++) {
+                const double y = ay.at(ay.x, j) - 0.5, z = az.at(az.x, k) - 0.5;
+                w[(size_t)((j + 1) * (L.n2 + 2) + k + 1)] = (xd * xd + y * y + z * z) / 6.0;
+            }
+        for (int i = 0; i < L.n0; i++)
+            for (int k = 0; k < L.n2; k++) {
+                const double x = ax.at(ax.x, i) - 0.5, z = az.at(az.x, k) - 0.5;
+                w[(size_t)(nx + (i + 1) * (L.n2 + 2) + k + 1)] = (x * x + yd * yd + z * z) / 6.0;
+            }
+        for (int i = 0; i < L.n0; i++)
+            for (int j = 0; j < L.n1; j++) {
+                const double x = ax.at(ax.x, i) - 0.5, y = ay.at(ay.x, j) - 0.5;
+                w[(size_t)(nx + ny + (i + 1) * (L.n1 + 2) + j + 1)] = (x * x + y * y + zd * zd) / 6.0;
+            }
+    } else {
+        const double xd = g.L[0] / 2.0, zd = g.L[2] / 2.0;
+        for (int k = 0; k < L.n2; k++) {
+            const double z = az.at(az.x, k) - 0.5;
+            w[(size_t)((0 + 1) * (L.n2 + 2) + k + 1)] = (xd * xd + z * z) / 4.0;
+        }
+        for (int i = 0; i < L.n0; i++) {
+            const double x = ax.at(ax.x, i) - 0.5;
+            w[(size_t)(nx + ny + (i + 1) * (L.n1 + 2) + 0 + 1)] = (x * x + zd * zd) / 4.0;
+        }
+    }
+    SARAS_TRY(dalloc(h, &h->walls, (int64_t)w.size()));
+    SARAS_CUDA(cudaMemcpy(h->walls, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice));
+    h->ghost.wallx = h->walls;
+    h->ghost.wally = h->walls + nx;
+    h->ghost.wallz = h->walls + nx + ny;
+    return SARAS_OK;
+}
+
+saras_status check_params(const saras_mg_params &p) {
+    if (p.vc_count < 1 || p.pre_smooth < 0 || p.post_smooth < 0 || p.res_type < 0 || p.res_type > 2 ||
+        p.precision < 0 || p.precision > 2 || p.levels < 0 || !(p.sor_param > 0.0 && p.sor_param < 2.0)) {
+        set_error("invalid multigrid parameters");
+        return SARAS_BAD_ARG;
+    }
+    for (int f = 0; f < 6; f++)
+        if (p.bc_kind[f] < 0 || p.bc_kind[f] > 2) {
+            set_error("invalid boundary kind on face %d", f);
+            return SARAS_BAD_ARG;
+        }
+    return SARAS_OK;
+}
+
+void free_all(saras_mg *h) {
+    for (Level &v : h->lv) {
+        cudaFree(v.lhs);
+        cudaFree(v.rhs);
+        cudaFree(v.tmp);
+        cudaFree(v.smd);
+        cudaFree(v.e32);
+        cudaFree(v.r32);
+        cudaFree(v.t32);
+        cudaFree(v.s32);
+        cudaFree(v.tab);
+        cudaFree(v.tab32);
+        cudaFree(v.inv_diag);
+        cudaFree(v.inv_diag32);
+    }
+    cudaFree(h->walls);
+    cudaFree(h->norm_part);
+    cudaFree(h->norm_out);
+    cudaFree(h->coarse_sweeps);
+    cudaFree(h->stage_lhs);
+    cudaFree(h->stage_rhs);
+    cudaFree(h->mix_scalar);
+    if (h->norm_host) cudaFreeHost(h->norm_host);
+    if (h->graph) cudaGraphExecDestroy(h->graph);
+    for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
+    if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
+}
+
+saras_status create(const saras_grid_desc *gd, const saras_mg_params *prm, void *stream, saras_mg *h) {
+    SARAS_TRY(check_params(*prm));
+    h->prm = *prm;
+    SARAS_TRY(h->grid.build(*gd, prm->levels));
+    h->d3 = h->grid.dims == 3;
+    h->nl = h->grid.levels;
+    h->stream = (cudaStream_t)stream;
+    int dev_count = 0;
+    if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0) {
+        cudaGetLastError();
+        set_error("no CUDA device");
+        return SARAS_NO_DEVICE;
+    }
+    for (int d = 0; d < 3; d++) h->ghost.per[d] = h->grid.per[d] ? 1 : 0;
+    for (int f = 0; f < 6; f++) h->ghost.kind[f] = prm->bc_kind[f];
+    h->lv.resize((size_t)h->nl);
+    const bool mixed = prm->precision == SARAS_PREC_MIXED;
+    if (mixed && h->nl < 2) {
+        set_error("the MIXED form needs at least two levels");
+        return SARAS_BAD_ARG;
+    }
+    const bool fast = prm->precision == SARAS_PREC_FP64;
+    for (int l = 0; l < h->nl; l++) {
+        Level &v = h->lv[(size_t)l];
+        const AxisLevel *a = h->grid.lv[(size_t)l].data();
+        v.lay = make_lay(a[0].n, h->d3 ? a[1].n : 1, a[2].n);
+        const int64_t sz = v.lay.size;
+        const bool coarsest = l == h->nl - 1;
+        if (!mixed || l == 0 || coarsest) {
+            SARAS_TRY(dalloc(h, &v.lhs, sz));
+            SARAS_TRY(dalloc(h, &v.rhs, sz));
+            SARAS_CUDA(cudaMemset(v.lhs, 0, (size_t)sz * sizeof(double)));
+            SARAS_CUDA(cudaMemset(v.rhs, 0, (size_t)sz * sizeof(double)));
+        }
+        if (!mixed) {
+            SARAS_TRY(dalloc(h, &v.tmp, sz));
+            SARAS_TRY(dalloc(h, &v.smd, sz));
+        }
+        if (mixed && !coarsest) {
+            SARAS_TRY(dalloc(h, &v.e32, sz));
+            SARAS_TRY(dalloc(h, &v.r32, sz));
+            SARAS_TRY(dalloc(h, &v.s32, sz));
+            SARAS_CUDA(cudaMemset(v.e32, 0, (size_t)sz * sizeof(float)));
+            SARAS_CUDA(cudaMemset(v.r32, 0, (size_t)sz * sizeof(float)));
+        }
+        if (mixed && coarsest) {
+            SARAS_TRY(dalloc(h, &v.tmp, sz));  // FP64 coarse residual scratch
+        }
+        if (fast) SARAS_TRY(dalloc(h, &v.inv_diag, sz));
+        if (mixed && !coarsest) SARAS_TRY(dalloc(h, &v.inv_diag32, sz));
+    }
+    SARAS_TRY(build_tables(h));
+    SARAS_TRY(build_walls(h));
+    const Lay &L0 = h->lv[0].lay;
+    const int64_t cells = (int64_t)L0.n0 * L0.n1 * L0.n2;
+    h->norm_blocks = (int)std::max<int64_t>(1, std::min<int64_t>(1216, (cells + 255) / 256));
+    SARAS_TRY(dalloc(h, &h->norm_part, 4 * (int64_t)h->norm_blocks));
+    SARAS_TRY(dalloc(h, &h->norm_out, 8));
+    SARAS_TRY(dalloc(h, &h->coarse_sweeps, 4));
+    SARAS_TRY(dalloc(h, &h->mix_scalar, 16));
+    SARAS_CUDA(cudaMemset(h->coarse_sweeps, 0, 4 * sizeof(int)));
+    SARAS_CUDA(cudaMemset(h->norm_out, 0, 8 * sizeof(double)));
+    SARAS_CUDA(cudaMallocHost((void **)&h->norm_host, 8 * sizeof(double)));
+    // Dense padded box of a caller field for the host entry point.
+    const int p = h->grid.pad, py = h->d3 ? p : 1;
+    h->stage_st[2] = 1;
+    h->stage_st[1] = L0.n2 + 2 * p;
+    h->stage_st[0] = h->stage_st[1] * (L0.n1 + 2 * py);
+    h->stage_elems = h->stage_st[0] * (L0.n0 + 2 * p);
+    SARAS_TRY(dalloc(h, &h->stage_lhs, h->stage_elems));
+    SARAS_TRY(dalloc(h, &h->stage_rhs, h->stage_elems));
+    SARAS_CUDA(cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking));
+    if (fast || mixed) SARAS_TRY(fast_setup(h));
+    SARAS_CUDA(cudaDeviceSynchronize());
+    return SARAS_OK;
+}
+
+// Issues one V-cycle (with its norm and the host copy of the norm).
+void issue_cycle(saras_mg *h, cudaStream_t s) {
+    h->issued = 0;
+    if (h->prm.precision == SARAS_PREC_FP64_EXACT)
+        vcycle_exact(h, s);
+    else
+        fast_cycle(h, s);
+    cudaMemcpyAsync(h->norm_host, h->norm_out, 8 * sizeof(double), cudaMemcpyDeviceToHost, s);
+}
+
+saras_status ensure_graph(saras_mg *h) {
+    if (h->graph || !h->use_graph || h->timing) return SARAS_OK;
+    cudaGraph_t g = nullptr;
+    SARAS_CUDA(cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeThreadLocal));
+    issue_cycle(h, h->cap_stream);
+    cudaError_t e = cudaStreamEndCapture(h->cap_stream, &g);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        h->use_graph = false;  // fall back to direct launches
+        return SARAS_OK;
+    }
+    h->launches_cycle = h->issued;
+    e = cudaGraphInstantiate(&h->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        h->graph = nullptr;
+        h->use_graph = false;
+    }
+    return SARAS_OK;
+}
+
+// poisson::mgSolve on level-0 arrays already filled by the caller path.
+saras_status solve_loop(saras_mg *h, double *res_hist, int32_t hist_cap, int32_t *n_cycles) {
+    cudaStream_t s = h->stream;
+    SARAS_TRY(ensure_graph(h));
+    int cyc = 0;
+    double r = 0.0;
+    for (int c = 0; c < h->prm.vc_count; c++) {
+        if (h->prm.precision == SARAS_PREC_MIXED && c == 0) {
+            // the defect-correction loop starts from the residual of the guess
+            mixed_prepare(h, s);
+        }
+        if (h->graph) {
+            SARAS_CUDA(cudaGraphLaunch(h->graph, s));
+            h->last_launches += h->launches_cycle;
+        } else {
+            issue_cycle(h, s);
+            h->last_launches += h->issued;
+        }
+        SARAS_CUDA(cudaStreamSynchronize(s));
+        harvest_timing(h);
+        r = h->norm_host[0];
+        cyc++;
+        if (res_hist && c < hist_cap) res_hist[c] = r;
+        if (h->prm.print_residual) std::printf("\nResidual after V Cycle %d is %.3e\n", c, r);
+        if (!std::isfinite(r)) {
+            if (n_cycles) *n_cycles = cyc;
+            set_error("non-finite residual after V-cycle %d", c);
+            return SARAS_NAN;
+        }
+        if (!h->prm.test_poisson && r < h->prm.vc_tolerance) break;
+    }
+    if (h->prm.precision == SARAS_PREC_MIXED)
+        mixed_finish(h, s);
+    else if (h->prm.precision == SARAS_PREC_FP64)
+        final_ghosts(h, s);
+    if (n_cycles) *n_cycles = cyc;
+    if (h->prm.test_poisson) return SARAS_OK;
+    return r < h->prm.vc_tolerance ? SARAS_OK : SARAS_NOT_CONVERGED;
+}
+
+saras_status solve_common(saras_mg *h, double *lhs, const double *rhs, const int64_t st[3], double *res_hist,
+                          int32_t hist_cap, int32_t *n_cycles) {
+    cudaStream_t s = h->stream;
+    Level &v0 = h->lv[0];
+    const Lay &L = v0.lay;
+    h->last_launches = 0;
+    double *u0 = v0.lhs;
+    double *f0 = v0.rhs;
+    // mgSolve zeroes the finest arrays before copying the caller's core in
+    SARAS_CUDA(cudaMemsetAsync(u0, 0, (size_t)L.size * sizeof(double), s));
+    SARAS_CUDA(cudaMemsetAsync(f0, 0, (size_t)L.size * sizeof(double), s));
+    const int bx = std::min(BX, (L.n2 + 31) / 32 * 32);
+    k_scatter<<<dim3(cdiv(L.n2, bx), (unsigned)L.n1, (unsigned)L.n0), bx, 0, s>>>(lhs, rhs, st[0], st[1], st[2],
+                                                                                u0, f0, L);
+    h->last_launches += 1;
+    saras_status status = solve_loop(h, res_hist, hist_cap, n_cycles);
+    if (status != SARAS_OK && status != SARAS_NOT_CONVERGED) return status;
+    const int gbx = std::min(BX, (L.n2 + 2 + 31) / 32 * 32);
+    k_gather<<<dim3(cdiv(L.n2 + 2, gbx), (unsigned)L.n1 + 2, (unsigned)L.n0 + 2), gbx, 0, s>>>(u0, L, lhs, st[0],
+                                                                                            st[1], st[2]);
+    h->last_launches += 1;
+    SARAS_CUDA(cudaGetLastError());
+    return status;
+}
+
+}  // namespace
+
+// ------------------------------------------------------- C entry points ----
+
+extern "C" {
+
+void saras_mg_default_params(saras_mg_params *p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    // Multigrid section of input/parameters.yaml
+    p->vc_count = 20;
+    p->vc_tolerance = 1.0e-6;
+    p->solve_flag = 1;
+    p->mg_tolerance = 1.0e-2;
+    p->sor_param = 1.0;
+    p->pre_smooth = 3;
+    p->post_smooth = 6;
+    p->res_type = 0;
+    p->print_residual = 0;
+    for (int f = 0; f < 6; f++) p->bc_kind[f] = SARAS_BC_NEUMANN;
+    p->test_poisson = 0;
+    p->precision = SARAS_PREC_FP64_EXACT;
+    p->levels = 0;
+}
+
+saras_status saras_mg_create(const saras_grid_desc *grid, const saras_mg_params *prm, void *stream,
+                             saras_mg **out) {
+    if (!grid || !prm || !out) {
+        set_error("null argument");
+        return SARAS_BAD_ARG;
+    }
+    *out = nullptr;
+    saras_mg *h = new saras_mg();
+    saras_status s = create(grid, prm, stream, h);
+    if (s != SARAS_OK) {
+        free_all(h);
+        delete h;
+        return s;
+    }
+    *out = h;
+    return SARAS_OK;
+}
+
+saras_status saras_mg_solve_dev(saras_mg *h, double *lhs, const double *rhs, const int64_t strides[3],
+                                double *res_hist, int32_t hist_cap, int32_t *n_cycles) {
+    if (!h || !lhs || !rhs || !strides) {
+        set_error("null argument");
+        return SARAS_BAD_ARG;
+    }
+    return solve_common(h, lhs, rhs, strides, res_hist, hist_cap, n_cycles);
+}
+
+saras_status saras_mg_solve(saras_mg *h, double *lhs, const double *rhs, const int64_t strides[3],
+                            double *res_hist, int32_t hist_cap, int32_t *n_cycles) {
+    if (!h || !lhs || !rhs || !strides) {
+        set_error("null argument");
+        return SARAS_BAD_ARG;
+    }
+    // Host fields must be dense padded boxes (the plainsf layout).
+    for (int d = 0; d < 3; d++)
+        if (strides[d] != h->stage_st[d]) {
+            set_error("host fields must be C-contiguous padded arrays (stride %d is %lld, expected %lld)", d,
+                      (long long)strides[d], (long long)h->stage_st[d]);
+            return SARAS_BAD_ARG;
+        }
+    const int p = h->grid.pad, py = h->d3 ? p : 1;
+    const int64_t origin = p * h->stage_st[0] + py * h->stage_st[1] + p;
+    const size_t bytes = (size_t)h->stage_elems * sizeof(double);
+    cudaStream_t s = h->stream;
+    SARAS_CUDA(cudaMemcpyAsync(h->stage_lhs, lhs - origin, bytes, cudaMemcpyHostToDevice, s));
+    SARAS_CUDA(cudaMemcpyAsync(h->stage_rhs, rhs - origin, bytes, cudaMemcpyHostToDevice, s));
+    saras_status st = solve_common(h, h->stage_lhs + origin, h->stage_rhs + origin, h->stage_st, res_hist,
+                                   hist_cap, n_cycles);
+    if (st != SARAS_OK && st != SARAS_NOT_CONVERGED) return st;
+    SARAS_CUDA(cudaMemcpyAsync(lhs - origin, h->stage_lhs, bytes, cudaMemcpyDeviceToHost, s));
+    SARAS_CUDA(cudaStreamSynchronize(s));
+    return st;
+}
+
+saras_status saras_mg_destroy(saras_mg *h) {
+    if (!h) return SARAS_OK;
+    cudaStreamSynchronize(h->stream);
+    free_all(h);
+    delete h;
+    return SARAS_OK;
+}
+
+int32_t saras_mg_num_levels(const saras_mg *h) { return h ? h->nl : -1; }
+
+int64_t saras_mg_device_bytes(const saras_mg *h) { return h ? h->dev_bytes : -1; }
+
+saras_status saras_mg_set_kernel_timing(saras_mg *h, int32_t enable) {
+    if (!h) return SARAS_BAD_ARG;
+    h->timing = enable != 0;
+    for (int c = 0; c < KC_COUNT; c++) {
+        h->kc_launches[c] = 0;
+        h->kc_ms[c] = 0.0;
+    }
+    return SARAS_OK;
+}
+
+saras_status saras_mg_kernel_stats(saras_mg *h, int32_t kclass, int64_t *launches, double *total_ms,
+                                   double *bytes_per_launch) {
+    if (!h || kclass < 0 || kclass >= KC_COUNT) return SARAS_BAD_ARG;
+    if (launches) *launches = h->kc_launches[kclass];
+    if (total_ms) *total_ms = h->kc_ms[kclass];
+    if (bytes_per_launch) *bytes_per_launch = kernel_bytes(h, kclass);
+    return SARAS_OK;
+}
+
+int64_t saras_mg_last_launches(const saras_mg *h) { return h ? h->last_launches : -1; }
+
+}  // extern "C"

@@ -1,0 +1,615 @@
+// FP64 and MIXED forms of the SARAS multigrid solve on GB300.
+//
+// FP64 form: the reference V-cycle (poisson.cc:203-279) with the stencil
+// coefficients folded per axis (c- = xix2*ihx2 - xixx*i2hx, c+ = ... +,
+// stored once per level), omega/D stored per cell, ghost cells folded into
+// the stencil (Neumann: ghost = own value, Dirichlet: minus it, periodic:
+// the wrapped neighbour), residual and restriction fused into one pass and
+// the saved copy smd replaced by an in-place correction.  Results agree with
+// the FP64_EXACT form to rounding.
+//
+// MIXED form: FP32 V-cycle (smoothing, restriction, prolongation) on the
+// error equation A e = r inside an FP64 defect-correction loop; the finest
+// residual r = f - A u, the update u += e, the coarsest solve and the
+// null-space projection (compensated sums) are FP64.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "mg_fast.cuh"
+
+using namespace saras;
+
+namespace {
+
+constexpr int BX = 128;
+
+// Ghost rule folded into the stencil: per axis periodic flag and the sign
+// of the mirrored value on the low and high faces (+1 Neumann, -1 Dirichlet).
+struct Bnd {
+    int per[3];
+    int sg_lo[3], sg_hi[3];
+};
+
+template <class T>
+struct Tab3 {
+    const T *cm[3], *cp[3], *dg[3];
+};
+
+template <class T>
+struct WTab {
+    const T *w0[3], *w1[3];
+};
+
+__device__ __forceinline__ float fmat(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fmat(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+template <class T>
+__device__ __forceinline__ T nb_lo(const T *u, int64_t c, int i, int n, int64_t s, int per, int sg, T uc) {
+    if (i > 0) return u[c - s];
+    if (per) return u[c + (int64_t)(n - 1) * s];
+    return sg > 0 ? uc : -uc;
+}
+template <class T>
+__device__ __forceinline__ T nb_hi(const T *u, int64_t c, int i, int n, int64_t s, int per, int sg, T uc) {
+    if (i < n - 1) return u[c + s];
+    if (per) return u[c - (int64_t)(n - 1) * s];
+    return sg > 0 ? uc : -uc;
+}
+
+// Off-diagonal part of the stretched 7-point operator at cell (i,j,k).
+template <class T, bool D3>
+__device__ __forceinline__ T offdiag(const T *u, const Lay &L, const Tab3<T> &t, const Bnd &b, int i, int j,
+                                     int k, int64_t c, T uc) {
+    const T xm = nb_lo(u, c, i, L.n0, L.s0, b.per[0], b.sg_lo[0], uc);
+    const T xp = nb_hi(u, c, i, L.n0, L.s0, b.per[0], b.sg_hi[0], uc);
+    const T zm = nb_lo(u, c, k, L.n2, (int64_t)1, b.per[2], b.sg_lo[2], uc);
+    const T zp = nb_hi(u, c, k, L.n2, (int64_t)1, b.per[2], b.sg_hi[2], uc);
+    T s = t.cm[0][i] * xm;
+    s = fmat(t.cp[0][i], xp, s);
+    if (D3) {
+        const T ym = nb_lo(u, c, j, L.n1, L.s1, b.per[1], b.sg_lo[1], uc);
+        const T yp = nb_hi(u, c, j, L.n1, L.s1, b.per[1], b.sg_hi[1], uc);
+        s = fmat(t.cm[1][j], ym, s);
+        s = fmat(t.cp[1][j], yp, s);
+    }
+    s = fmat(t.cm[2][k], zm, s);
+    s = fmat(t.cp[2][k], zp, s);
+    return s;
+}
+
+template <class T, bool D3>
+__device__ __forceinline__ T diag(const Tab3<T> &t, int i, int j, int k) {
+    T d = t.dg[0][i] + t.dg[2][k];
+    if (D3) d += t.dg[1][j];
+    return d + d;
+}
+
+// f - A u
+template <class T, bool D3>
+__device__ __forceinline__ T resid(const T *u, const T *f, const Lay &L, const Tab3<T> &t, const Bnd &b, int i,
+                                   int j, int k) {
+    const int64_t c = L.at(i, j, k);
+    const T uc = u[c];
+    const T s = offdiag<T, D3>(u, L, t, b, i, j, k, c, uc);
+    return f[c] - fmat(-diag<T, D3>(t, i, j, k), uc, s);
+}
+
+// ------------------------------------------------------------ kernels ----
+
+// FP64 colour sweep with omega/D stored per cell.
+template <bool D3, bool W1>
+__global__ void k_rbgs64(double *u, const double *__restrict__ f, const double *__restrict__ wd, Lay L,
+                         Tab3<double> t, Bnd b, int colour, double omc) {
+    const int kk = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = D3 ? (int)blockIdx.y : 0;
+    const int i = blockIdx.z;
+    const int k = 2 * kk + ((i + j + colour) & 1);
+    if (k >= L.n2) return;
+    const int64_t c = L.at(i, j, k);
+    const double uc = u[c];
+    const double s = offdiag<double, D3>(u, L, t, b, i, j, k, c, uc) - f[c];
+    u[c] = W1 ? s * wd[c] : fmat(s, wd[c], omc * uc);
+}
+
+// FP32 colour sweep; the diagonal is rebuilt from the 1-D tables.
+template <bool D3>
+__global__ void k_rbgs32(float *e, const float *__restrict__ r, Lay L, Tab3<float> t, Bnd b, int colour, float w,
+                         float omc) {
+    const int kk = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = D3 ? (int)blockIdx.y : 0;
+    const int i = blockIdx.z;
+    const int k = 2 * kk + ((i + j + colour) & 1);
+    if (k >= L.n2) return;
+    const int64_t c = L.at(i, j, k);
+    const float uc = e[c];
+    const float s = offdiag<float, D3>(e, L, t, b, i, j, k, c, uc) - r[c];
+    e[c] = fmat(omc, uc, __fdiv_rn(w * s, diag<float, D3>(t, i, j, k)));
+}
+
+// Fused residual and restriction: one thread per coarse cell forms the
+// residuals of its 2x2x2 children and their weighted sum (the coarsen
+// weights v_abc / vTot of poisson_d3.cc:494-508, factorised per axis).
+template <class T, class TO, bool D3>
+__global__ void k_resid_restrict(const T *__restrict__ u, const T *__restrict__ f, Lay Lf, Tab3<T> t, Bnd b,
+                                 WTab<T> w, TO *__restrict__ rc, Lay Lc) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = D3 ? (int)blockIdx.y : 0;
+    const int i = blockIdx.z;
+    if (k >= Lc.n2) return;
+    const int i2 = 2 * i, j2 = 2 * j, k2 = 2 * k;
+    T out;
+    if (D3) {
+        T sy[2];
+        for (int a = 0; a < 2; a++) {
+            T sz[2];
+            for (int bb = 0; bb < 2; bb++) {
+                const T r0 = resid<T, true>(u, f, Lf, t, b, i2 + a, j2 + bb, k2);
+                const T r1 = resid<T, true>(u, f, Lf, t, b, i2 + a, j2 + bb, k2 + 1);
+                sz[bb] = fmat(w.w1[2][k], r1, w.w0[2][k] * r0);
+            }
+            sy[a] = fmat(w.w1[1][j], sz[1], w.w0[1][j] * sz[0]);
+        }
+        out = fmat(w.w1[0][i], sy[1], w.w0[0][i] * sy[0]);
+    } else {
+        const T r00 = resid<T, false>(u, f, Lf, t, b, i2, 0, k2);
+        const T r01 = resid<T, false>(u, f, Lf, t, b, i2, 0, k2 + 1);
+        const T r10 = resid<T, false>(u, f, Lf, t, b, i2 + 1, 0, k2);
+        const T r11 = resid<T, false>(u, f, Lf, t, b, i2 + 1, 0, k2 + 1);
+        out = ((r00 + r01) + (r10 + r11)) * T(0.25);
+    }
+    rc[Lc.at(i, j, k)] = (TO)out;
+}
+
+// Injection prolongation and correction in place: fine += coarse(i/2,..).
+template <class TF, class TC>
+__global__ void k_prolong_add(TF *__restrict__ f, const TC *__restrict__ c, Lay Lf, Lay Lc, int d3) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y, i = blockIdx.z;
+    if (k >= Lf.n2) return;
+    const int64_t q = Lf.at(i, j, k);
+    f[q] = f[q] + (TF)c[Lc.at(i >> 1, d3 ? (j >> 1) : 0, k >> 1)];
+}
+
+__device__ __forceinline__ double warp_max(double v) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const double w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    return v;
+}
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <int NV>
+__device__ __forceinline__ void block_store(double (&v)[NV], const bool (&is_max)[NV], double *part) {
+    __shared__ double sh[NV][32];
+    for (int q = 0; q < NV; q++) v[q] = is_max[q] ? warp_max(v[q]) : warp_sum(v[q]);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (lane == 0)
+        for (int q = 0; q < NV; q++) sh[q][wid] = v[q];
+    __syncthreads();
+    if (wid == 0) {
+        for (int q = 0; q < NV; q++) {
+            double x = lane < nw ? sh[q][lane] : 0.0;
+            x = is_max[q] ? warp_max(x) : warp_sum(x);
+            if (lane == 0) part[NV * blockIdx.x + q] = x;
+        }
+    }
+}
+
+// FP64 residual of the finest level with norm partials; optionally writes
+// the residual in FP32 (MIXED form) and first applies u += e.
+template <bool D3, bool MIX>
+__global__ void k_resid_norm64(const double *__restrict__ u, const double *__restrict__ f, Lay L, Tab3<double> t,
+                               Bnd b, int rtype, double *__restrict__ part, float *__restrict__ r32) {
+    const int64_t total = (int64_t)L.n0 * L.n1 * L.n2;
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int k = (int)(q % L.n2);
+        const int64_t rest = q / L.n2;
+        const int j = (int)(rest % L.n1);
+        const int i = (int)(rest / L.n1);
+        const double r = resid<double, D3>(u, f, L, t, b, i, j, k);
+        const double fv = f[L.at(i, j, k)];
+        if (MIX) r32[L.at(i, j, k)] = (float)r;
+        if (rtype == 0) {
+            const double ar = fabs(r), af = fabs(fv);
+            if (ar > v[0]) v[0] = ar;
+            if (af > v[1]) v[1] = af;
+        } else if (rtype == 1) {
+            v[2] += fabs(r);
+            v[3] += fabs(fv);
+        } else {
+            v[2] = fmat(r, r, v[2]);
+            v[3] = fmat(fv, fv, v[3]);
+        }
+    }
+    const bool mx[4] = {true, true, false, false};
+    block_store<4>(v, mx, part);
+}
+
+// u += e over the core (MIXED form update, FP64 accumulate).
+__global__ void k_update64(double *__restrict__ u, const float *__restrict__ e, Lay L) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y, i = blockIdx.z;
+    if (k >= L.n2) return;
+    const int64_t q = L.at(i, j, k);
+    u[q] = u[q] + (double)e[q];
+}
+
+__device__ __forceinline__ void two_sum(double a, double b, double &s, double &c) {
+    s = a + b;
+    const double bb = s - a;
+    c = (a - (s - bb)) + (b - bb);
+}
+
+// Compensated (Neumaier) sum of the core of u: per-block (sum, error) pairs.
+__global__ void k_csum(const double *__restrict__ u, Lay L, double *__restrict__ part) {
+    const int64_t total = (int64_t)L.n0 * L.n1 * L.n2;
+    double s = 0.0, c = 0.0;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int k = (int)(q % L.n2);
+        const int64_t rest = q / L.n2;
+        const int j = (int)(rest % L.n1);
+        const int i = (int)(rest / L.n1);
+        double t, e;
+        two_sum(s, u[L.at(i, j, k)], t, e);
+        s = t;
+        c += e;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const double s2 = __shfl_xor_sync(0xffffffffu, s, o), c2 = __shfl_xor_sync(0xffffffffu, c, o);
+        double t, e;
+        two_sum(s, s2, t, e);
+        s = t;
+        c += c2 + e;
+    }
+    __shared__ double sh[2][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (lane == 0) {
+        sh[0][wid] = s;
+        sh[1][wid] = c;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double S = 0.0, Cc = 0.0;
+        for (int w = 0; w < nw; w++) {
+            double t, e;
+            two_sum(S, sh[0][w], t, e);
+            S = t;
+            Cc += sh[1][w] + e;
+        }
+        part[2 * blockIdx.x] = S;
+        part[2 * blockIdx.x + 1] = Cc;
+    }
+}
+
+// Mean of u from the (sum, error) partials, in a fixed order; slot 0 of
+// `out` receives the mean; with `sub` set, out[0] becomes mean - out[1].
+__global__ void k_csum_final(const double *__restrict__ part, int nb, double count, double *out, int slot) {
+    if (threadIdx.x != 0) return;
+    double S = 0.0, Cc = 0.0;
+    for (int q = 0; q < nb; q++) {
+        double t, e;
+        two_sum(S, part[2 * q], t, e);
+        S = t;
+        Cc += part[2 * q + 1] + e;
+    }
+    out[slot] = (S + Cc) / count;
+}
+
+__global__ void k_shift(double *__restrict__ u, Lay L, const double *__restrict__ m) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y, i = blockIdx.z;
+    if (k >= L.n2) return;
+    const int64_t q = L.at(i, j, k);
+    u[q] = u[q] - (m[0] - m[1]);
+}
+
+// omega / D per cell for the FP64 form.
+template <bool D3>
+__global__ void k_inv_diag(double *__restrict__ wd, Lay L, Tab3<double> t, double w) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = D3 ? (int)blockIdx.y : 0;
+    const int i = blockIdx.z;
+    if (k >= L.n2) return;
+    wd[L.at(i, j, k)] = w / diag<double, D3>(t, i, j, k);
+}
+
+// ------------------------------------------------------- host side ----
+
+Tab3<double> tab64(const Level &v) {
+    return Tab3<double>{{v.cm[0], v.cm[1], v.cm[2]}, {v.cp[0], v.cp[1], v.cp[2]}, {v.dg[0], v.dg[1], v.dg[2]}};
+}
+Tab3<float> tab32(const Level &v) {
+    return Tab3<float>{{v.cm32[0], v.cm32[1], v.cm32[2]},
+                       {v.cp32[0], v.cp32[1], v.cp32[2]},
+                       {v.dg32[0], v.dg32[1], v.dg32[2]}};
+}
+WTab<double> wt64(const Level &v) { return WTab<double>{{v.w0[0], v.w0[1], v.w0[2]}, {v.w1[0], v.w1[1], v.w1[2]}}; }
+WTab<float> wt32(const Level &v) {
+    return WTab<float>{{v.w032[0], v.w032[1], v.w032[2]}, {v.w132[0], v.w132[1], v.w132[2]}};
+}
+
+Bnd bnd(const saras_mg *h) {
+    Bnd b;
+    for (int d = 0; d < 3; d++) {
+        b.per[d] = h->ghost.per[d];
+        b.sg_lo[d] = h->ghost.kind[2 * d] == SARAS_BC_NEUMANN ? 1 : -1;
+        b.sg_hi[d] = h->ghost.kind[2 * d + 1] == SARAS_BC_NEUMANN ? 1 : -1;
+    }
+    return b;
+}
+
+inline dim3 cgrid(const Lay &L, bool d3, int kcount, int bx) {
+    return dim3(cdiv(kcount, bx), d3 ? (unsigned)L.n1 : 1u, (unsigned)L.n0);
+}
+inline int bxfor(int n) { return std::min(BX, (n + 31) / 32 * 32); }
+
+void colour64(saras_mg *h, cudaStream_t s, int l, int colour) {
+    Level &v = h->lv[(size_t)l];
+    const Lay &L = v.lay;
+    const int half = (L.n2 + 1) / 2, bx = bxfor(half);
+    const double omc = 1.0 - h->prm.sor_param;
+    const bool w1 = h->prm.sor_param == 1.0;
+    const Bnd b = bnd(h);
+    kbegin(h, s, l == 0 ? KC_SMOOTH0 : -1);
+    if (h->d3) {
+        if (w1)
+            k_rbgs64<true, true><<<cgrid(L, true, half, bx), bx, 0, s>>>(v.lhs, v.rhs, v.inv_diag, L, tab64(v), b,
+                                                                         colour, omc);
+        else
+            k_rbgs64<true, false><<<cgrid(L, true, half, bx), bx, 0, s>>>(v.lhs, v.rhs, v.inv_diag, L, tab64(v), b,
+                                                                          colour, omc);
+    } else {
+        if (w1)
+            k_rbgs64<false, true><<<cgrid(L, false, half, bx), bx, 0, s>>>(v.lhs, v.rhs, v.inv_diag, L, tab64(v),
+                                                                           b, colour, omc);
+        else
+            k_rbgs64<false, false><<<cgrid(L, false, half, bx), bx, 0, s>>>(v.lhs, v.rhs, v.inv_diag, L, tab64(v),
+                                                                            b, colour, omc);
+    }
+    kend(h, s, l == 0 ? KC_SMOOTH0 : -1);
+}
+
+void colour32(saras_mg *h, cudaStream_t s, int l, int colour) {
+    Level &v = h->lv[(size_t)l];
+    const Lay &L = v.lay;
+    const int half = (L.n2 + 1) / 2, bx = bxfor(half);
+    const float w = (float)h->prm.sor_param, omc = (float)(1.0 - h->prm.sor_param);
+    const Bnd b = bnd(h);
+    kbegin(h, s, l == 0 ? KC_SMOOTH0 : -1);
+    if (h->d3)
+        k_rbgs32<true><<<cgrid(L, true, half, bx), bx, 0, s>>>(v.e32, v.r32, L, tab32(v), b, colour, w, omc);
+    else
+        k_rbgs32<false><<<cgrid(L, false, half, bx), bx, 0, s>>>(v.e32, v.r32, L, tab32(v), b, colour, w, omc);
+    kend(h, s, l == 0 ? KC_SMOOTH0 : -1);
+}
+
+// Coarsest level: the FP64_EXACT single-block solve (or smoothing), shared
+// by all forms; declared in mg.cu.
+}  // namespace
+
+namespace saras {
+void coarsest_level(saras_mg *h, cudaStream_t s);
+void norm_final(saras_mg *h, cudaStream_t s);
+void ghost_all_level(saras_mg *h, cudaStream_t s, int l, bool zeroBC);
+}  // namespace saras
+
+namespace {
+
+void residual_restrict(saras_mg *h, cudaStream_t s, int l, bool mixed) {
+    Level &f = h->lv[(size_t)l];
+    Level &c = h->lv[(size_t)l + 1];
+    const Lay &Lc = c.lay;
+    const int bx = bxfor(Lc.n2);
+    const Bnd b = bnd(h);
+    const bool to64 = l + 1 == h->nl - 1;  // the coarsest level is FP64 in every form
+    kbegin(h, s, l == 0 ? KC_RESTRICT : -1);
+    if (!mixed) {
+        if (h->d3)
+            k_resid_restrict<double, double, true><<<cgrid(Lc, true, Lc.n2, bx), bx, 0, s>>>(
+                f.lhs, f.rhs, f.lay, tab64(f), b, wt64(c), c.rhs, Lc);
+        else
+            k_resid_restrict<double, double, false><<<cgrid(Lc, false, Lc.n2, bx), bx, 0, s>>>(
+                f.lhs, f.rhs, f.lay, tab64(f), b, wt64(c), c.rhs, Lc);
+    } else if (to64) {
+        if (h->d3)
+            k_resid_restrict<float, double, true><<<cgrid(Lc, true, Lc.n2, bx), bx, 0, s>>>(
+                f.e32, f.r32, f.lay, tab32(f), b, wt32(c), c.rhs, Lc);
+        else
+            k_resid_restrict<float, double, false><<<cgrid(Lc, false, Lc.n2, bx), bx, 0, s>>>(
+                f.e32, f.r32, f.lay, tab32(f), b, wt32(c), c.rhs, Lc);
+    } else {
+        if (h->d3)
+            k_resid_restrict<float, float, true><<<cgrid(Lc, true, Lc.n2, bx), bx, 0, s>>>(
+                f.e32, f.r32, f.lay, tab32(f), b, wt32(c), c.r32, Lc);
+        else
+            k_resid_restrict<float, float, false><<<cgrid(Lc, false, Lc.n2, bx), bx, 0, s>>>(
+                f.e32, f.r32, f.lay, tab32(f), b, wt32(c), c.r32, Lc);
+    }
+    kend(h, s, l == 0 ? KC_RESTRICT : -1);
+}
+
+void prolong_add(saras_mg *h, cudaStream_t s, int l, bool mixed) {
+    Level &c = h->lv[(size_t)l];
+    Level &f = h->lv[(size_t)l - 1];
+    const Lay &L = f.lay;
+    const int bx = bxfor(L.n2);
+    const dim3 g(cdiv(L.n2, bx), (unsigned)L.n1, (unsigned)L.n0);
+    kbegin(h, s, l == 1 ? KC_PROLONG : -1);
+    if (!mixed)
+        k_prolong_add<double, double><<<g, bx, 0, s>>>(f.lhs, c.lhs, L, c.lay, h->d3 ? 1 : 0);
+    else if (l == h->nl - 1)
+        k_prolong_add<float, double><<<g, bx, 0, s>>>(f.e32, c.lhs, L, c.lay, h->d3 ? 1 : 0);
+    else
+        k_prolong_add<float, float><<<g, bx, 0, s>>>(f.e32, c.e32, L, c.lay, h->d3 ? 1 : 0);
+    kend(h, s, l == 1 ? KC_PROLONG : -1);
+}
+
+void smooth(saras_mg *h, cudaStream_t s, int l, int count, bool mixed) {
+    for (int n = 0; n < count; n++) {
+        if (mixed) {
+            colour32(h, s, l, 0);
+            colour32(h, s, l, 1);
+        } else {
+            colour64(h, s, l, 0);
+            colour64(h, s, l, 1);
+        }
+    }
+}
+
+void resid_norm(saras_mg *h, cudaStream_t s, bool mixed) {
+    Level &v = h->lv[0];
+    const Bnd b = bnd(h);
+    kbegin(h, s, KC_NORM);
+    if (h->d3) {
+        if (mixed)
+            k_resid_norm64<true, true><<<h->norm_blocks, 256, 0, s>>>(v.lhs, v.rhs, v.lay, tab64(v), b,
+                                                                      h->prm.res_type, h->norm_part, v.r32);
+        else
+            k_resid_norm64<true, false><<<h->norm_blocks, 256, 0, s>>>(v.lhs, v.rhs, v.lay, tab64(v), b,
+                                                                       h->prm.res_type, h->norm_part, nullptr);
+    } else {
+        if (mixed)
+            k_resid_norm64<false, true><<<h->norm_blocks, 256, 0, s>>>(v.lhs, v.rhs, v.lay, tab64(v), b,
+                                                                       h->prm.res_type, h->norm_part, v.r32);
+        else
+            k_resid_norm64<false, false><<<h->norm_blocks, 256, 0, s>>>(v.lhs, v.rhs, v.lay, tab64(v), b,
+                                                                        h->prm.res_type, h->norm_part, nullptr);
+    }
+    kend(h, s, KC_NORM);
+    norm_final(h, s);
+}
+
+bool singular(const saras_mg *h) {
+    for (int d = 0; d < 3; d++) {
+        if (!h->grid.active(d) || h->ghost.per[d]) continue;
+        if (h->ghost.kind[2 * d] != SARAS_BC_NEUMANN || h->ghost.kind[2 * d + 1] != SARAS_BC_NEUMANN) return false;
+    }
+    return true;
+}
+
+void csum(saras_mg *h, cudaStream_t s, const double *u, int slot) {
+    const Lay &L = h->lv[0].lay;
+    const double count = (double)L.n0 * L.n1 * L.n2;
+    kbegin(h, s, -1);
+    k_csum<<<h->norm_blocks, 256, 0, s>>>(u, L, h->norm_part);
+    kbegin(h, s, -1);
+    k_csum_final<<<1, 32, 0, s>>>(h->norm_part, h->norm_blocks, count, h->mix_scalar, slot);
+}
+
+}  // namespace
+
+namespace saras {
+
+saras_status fast_setup(saras_mg *h) {
+    for (int f = 0; f < 6; f++)
+        if (h->prm.bc_kind[f] == SARAS_BC_DIRICHLET_TEST) {
+            set_error("the TEST_POISSON wall kind is available in the FP64_EXACT form only");
+            return SARAS_BAD_ARG;
+        }
+    if (h->prm.precision == SARAS_PREC_FP64) {
+        for (int l = 0; l < h->nl; l++) {
+            Level &v = h->lv[(size_t)l];
+            const Lay &L = v.lay;
+            const int bx = bxfor(L.n2);
+            if (h->d3)
+                k_inv_diag<true><<<cgrid(L, true, L.n2, bx), bx>>>(v.inv_diag, L, tab64(v), h->prm.sor_param);
+            else
+                k_inv_diag<false><<<cgrid(L, false, L.n2, bx), bx>>>(v.inv_diag, L, tab64(v), h->prm.sor_param);
+        }
+    }
+    SARAS_CUDA(cudaGetLastError());
+    return SARAS_OK;
+}
+
+// One V-cycle of the FP64 form, or one outer iteration of the MIXED form.
+void fast_cycle(saras_mg *h, cudaStream_t s) {
+    const bool mixed = h->prm.precision == SARAS_PREC_MIXED;
+    const int top = h->nl - 1;
+    if (mixed) {
+        // error equation at the finest level starts from zero
+        Level &v0 = h->lv[0];
+        cudaMemsetAsync(v0.e32, 0, (size_t)v0.lay.size * sizeof(float), s);
+    }
+    if (top == 0) {
+        smooth(h, s, 0, h->prm.pre_smooth, mixed);
+    } else {
+        smooth(h, s, 0, h->prm.pre_smooth, mixed);
+        for (int l = 0; l < top; l++) {
+            residual_restrict(h, s, l, mixed);
+            Level &c = h->lv[(size_t)l + 1];
+            if (l + 1 == top) {
+                cudaMemsetAsync(c.lhs, 0, (size_t)c.lay.size * sizeof(double), s);
+                coarsest_level(h, s);
+            } else {
+                if (mixed)
+                    cudaMemsetAsync(c.e32, 0, (size_t)c.lay.size * sizeof(float), s);
+                else
+                    cudaMemsetAsync(c.lhs, 0, (size_t)c.lay.size * sizeof(double), s);
+                smooth(h, s, l + 1, h->prm.pre_smooth, mixed);
+            }
+        }
+        for (int l = top; l > 0; l--) {
+            prolong_add(h, s, l, mixed);
+            smooth(h, s, l - 1, h->prm.post_smooth, mixed);
+        }
+    }
+    if (mixed) {
+        Level &v0 = h->lv[0];
+        const Lay &L = v0.lay;
+        const int bx = bxfor(L.n2);
+        kbegin(h, s, -1);
+        k_update64<<<dim3(cdiv(L.n2, bx), (unsigned)L.n1, (unsigned)L.n0), bx, 0, s>>>(v0.lhs, v0.e32, L);
+    }
+    resid_norm(h, s, mixed);
+}
+
+void mixed_prepare(saras_mg *h, cudaStream_t s) {
+    // residual of the initial guess feeds the first FP32 V-cycle; the mean
+    // of the guess is kept for the null-space projection
+    resid_norm(h, s, true);
+    if (singular(h)) csum(h, s, h->lv[0].lhs, 1);
+}
+
+void final_ghosts(saras_mg *h, cudaStream_t s) { ghost_all_level(h, s, 0, false); }
+
+void mixed_finish(saras_mg *h, cudaStream_t s) {
+    if (singular(h)) {
+        // remove the drift of the constant null-space component: the mean of
+        // the result returns to the mean of the initial guess
+        csum(h, s, h->lv[0].lhs, 0);
+        const Lay &L = h->lv[0].lay;
+        const int bx = bxfor(L.n2);
+        kbegin(h, s, -1);
+        k_shift<<<dim3(cdiv(L.n2, bx), (unsigned)L.n1, (unsigned)L.n0), bx, 0, s>>>(h->lv[0].lhs, L, h->mix_scalar);
+    }
+    final_ghosts(h, s);
+}
+
+double kernel_bytes(const saras_mg *h, int kclass) {
+    const Lay &L = h->lv[0].lay;
+    const double n = (double)L.n0 * L.n1 * L.n2;
+    const bool mixed = h->prm.precision == SARAS_PREC_MIXED;
+    const double sz = mixed ? 4.0 : 8.0;
+    switch (kclass) {
+    case KC_SMOOTH0:  // one colour = half of an RBGS iteration's 3 N s
+        return 1.5 * n * sz;
+    case KC_RESTRICT:  // read u, f; write the coarse rhs
+        return (2.0 + 0.125) * n * sz;
+    case KC_PROLONG:  // read coarse, read and write fine
+        return (0.125 + 2.0) * n * sz;
+    case KC_NORM:  // read u, f (FP64); MIXED also writes r in FP32
+        return mixed ? 20.0 * n : 16.0 * n;
+    default:
+        return 0.0;
+    }
+}
+
+}  // namespace saras

@@ -1,0 +1,22 @@
+// FP64 and MIXED forms of the multigrid solve (mg_fast.cu) and the host
+// helpers the translation units share.
+#pragma once
+
+#include "mg_handle.cuh"
+
+namespace saras {
+
+// Kernel-class event timing (mg.cu)
+void kbegin(saras_mg *h, cudaStream_t s, int kc);
+void kend(saras_mg *h, cudaStream_t s, int kc);
+void harvest_timing(saras_mg *h);
+
+// mg_fast.cu
+saras_status fast_setup(saras_mg *h);          // per-cell inverse diagonals, checks
+void fast_cycle(saras_mg *h, cudaStream_t s);  // one V-cycle / outer iteration + norm
+void mixed_prepare(saras_mg *h, cudaStream_t s);
+void mixed_finish(saras_mg *h, cudaStream_t s);
+void final_ghosts(saras_mg *h, cudaStream_t s);
+double kernel_bytes(const saras_mg *h, int kclass);
+
+}  // namespace saras

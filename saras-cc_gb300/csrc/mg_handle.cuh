@@ -1,0 +1,80 @@
+// Device-resident multigrid hierarchy behind the saras_mg_* entry points.
+#pragma once
+
+#include <vector>
+
+#include "common.cuh"
+#include "grid_host.h"
+#include "mg_exact.cuh"
+
+namespace saras {
+
+// Per-level device state.  FP64 arrays serve the FP64_EXACT and FP64 forms
+// and the finest level of the MIXED form; FP32 arrays hold the MIXED form's
+// error hierarchy.
+struct Level {
+    Lay lay;
+    double *lhs = nullptr, *rhs = nullptr, *tmp = nullptr, *smd = nullptr;
+    float *e32 = nullptr, *r32 = nullptr, *t32 = nullptr, *s32 = nullptr;
+    double *tab = nullptr;  // all 1-D tables of the level in one allocation
+    Coef coef{};
+    RTab rt{};
+    // FP64 form: folded stencil coefficients per axis, c_minus/c_plus
+    // (xix2*ihx2 -/+ xixx*i2hx) and the diagonal half-sum d = xix2*ihx2.
+    const double *cm[3] = {nullptr, nullptr, nullptr}, *cp[3] = {nullptr, nullptr, nullptr};
+    const double *dg[3] = {nullptr, nullptr, nullptr};
+    // restriction weights of the two children normalised by the parent
+    // extent: w0 = r0/rt, w1 = r1/rt (so that v_abc/vTot = wx_a wy_b wz_c)
+    const double *w0[3] = {nullptr, nullptr, nullptr}, *w1[3] = {nullptr, nullptr, nullptr};
+    // FP32 copies of the folded tables for the MIXED form
+    float *tab32 = nullptr;
+    const float *cm32[3] = {nullptr, nullptr, nullptr}, *cp32[3] = {nullptr, nullptr, nullptr};
+    const float *dg32[3] = {nullptr, nullptr, nullptr};
+    const float *w032[3] = {nullptr, nullptr, nullptr}, *w132[3] = {nullptr, nullptr, nullptr};
+    double *inv_diag = nullptr;  // FP64 form: omega / D per cell
+    float *inv_diag32 = nullptr; // MIXED form: omega / D per cell
+};
+
+enum KClass { KC_SMOOTH0 = 0, KC_RESTRICT = 1, KC_PROLONG = 2, KC_NORM = 3, KC_COARSE = 4, KC_COUNT = 5 };
+
+}  // namespace saras
+
+struct saras_mg {
+    saras::HostGrid grid;
+    saras_mg_params prm{};
+    bool d3 = true;
+    int nl = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t cap_stream = nullptr;
+    std::vector<saras::Level> lv;
+    saras::Ghost ghost{};
+    double *walls = nullptr;
+    // residual-norm scratch
+    double *norm_part = nullptr;
+    double *norm_out = nullptr;   // device: [0] residualVal, [1] numerator, [2] denominator
+    double *norm_host = nullptr;  // pinned mirror of norm_out
+    int norm_blocks = 0;
+    int *coarse_sweeps = nullptr;
+    // staging of caller host fields (dense padded boxes)
+    double *stage_lhs = nullptr, *stage_rhs = nullptr;
+    int64_t stage_elems = 0;
+    int64_t stage_st[3] = {0, 0, 0};
+    // mixed form scratch
+    double *mix_scalar = nullptr;
+    // graph of one V-cycle (plus the norm and its host copy)
+    cudaGraphExec_t graph = nullptr;
+    bool use_graph = true;
+    int64_t launches_cycle = 0;
+    int64_t last_launches = 0;
+    int64_t dev_bytes = 0;
+    // kernel timing
+    bool timing = false;
+    std::vector<cudaEvent_t> ev_pool;
+    size_t ev_used = 0;
+    std::vector<std::pair<int, size_t>> ev_marks;  // (class, index of start event)
+    int64_t kc_launches[saras::KC_COUNT] = {0, 0, 0, 0, 0};
+    double kc_ms[saras::KC_COUNT] = {0, 0, 0, 0, 0};
+    double kc_bytes[saras::KC_COUNT] = {0, 0, 0, 0, 0};
+    int64_t issued = 0;  // launches issued while recording the current sequence
+    int maxCount() const;  // coarsest-level iteration limit (poisson.cc:430-436)
+};
