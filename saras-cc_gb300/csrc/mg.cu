@@ -326,7 +326,11 @@ namespace saras {
 void kbegin(saras_mg *h, cudaStream_t s, int kc) {
     h->issued++;
     if (!h->timing || kc < 0) return;
+    if (h->graph && !h->capturing) return;  // only the graph's launches are timed in graph mode
     if (h->ev_used + 2 > h->ev_pool.size()) {
+        if (h->capturing) {  // no event creation inside a capture: stop timing this class
+            return;
+        }
         for (int q = 0; q < 64; q++) {
             cudaEvent_t e;
             cudaEventCreate(&e);
@@ -336,23 +340,32 @@ void kbegin(saras_mg *h, cudaStream_t s, int kc) {
     h->ev_marks.push_back({kc, h->ev_used});
     cudaEventRecord(h->ev_pool[h->ev_used], s);
     h->ev_used += 2;
+    h->mark_open = true;
 }
 
 void kend(saras_mg *h, cudaStream_t s, int kc) {
-    if (!h->timing || kc < 0) return;
+    if (!h->timing || kc < 0 || !h->mark_open) return;
     cudaEventRecord(h->ev_pool[h->ev_marks.back().second + 1], s);
+    h->mark_open = false;
 }
 
+// Adds the elapsed times of the bracketed launches of the last sequence.
+// With a captured graph the event-record nodes are part of the graph and the
+// marks stay valid for every replay.
 void harvest_timing(saras_mg *h) {
     if (!h->timing) return;
-    for (auto &m : h->ev_marks) {
+    const bool from_graph = h->graph != nullptr;
+    auto &marks = from_graph ? h->graph_marks : h->ev_marks;
+    for (auto &m : marks) {
         float ms = 0.f;
         cudaEventElapsedTime(&ms, h->ev_pool[m.second], h->ev_pool[m.second + 1]);
         h->kc_ms[m.first] += ms;
         h->kc_launches[m.first] += 1;
     }
-    h->ev_marks.clear();
-    h->ev_used = 0;
+    if (!from_graph) {
+        h->ev_marks.clear();
+        h->ev_used = 0;
+    }
 }
 
 static void ghost_axis_launch(saras_mg *h, cudaStream_t s, double *u, const Lay &L, int axis, bool wall_pass,
@@ -781,10 +794,29 @@ void issue_cycle(saras_mg *h, cudaStream_t s) {
 }
 
 saras_status ensure_graph(saras_mg *h) {
-    if (h->graph || !h->use_graph || h->timing) return SARAS_OK;
+    if (h->graph && h->graph_timing != h->timing) {
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+    }
+    if (h->graph || !h->use_graph) return SARAS_OK;
+    if (h->timing) {
+        // events are created before capture; the marks recorded while
+        // capturing become the graph's event-record nodes
+        h->ev_marks.clear();
+        h->ev_used = 0;
+        if (h->ev_pool.size() < 4096) {
+            while (h->ev_pool.size() < 4096) {
+                cudaEvent_t e;
+                SARAS_CUDA(cudaEventCreate(&e));
+                h->ev_pool.push_back(e);
+            }
+        }
+    }
     cudaGraph_t g = nullptr;
     SARAS_CUDA(cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeThreadLocal));
+    h->capturing = true;
     issue_cycle(h, h->cap_stream);
+    h->capturing = false;
     cudaError_t e = cudaStreamEndCapture(h->cap_stream, &g);
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -792,6 +824,9 @@ saras_status ensure_graph(saras_mg *h) {
         return SARAS_OK;
     }
     h->launches_cycle = h->issued;
+    h->graph_marks = h->ev_marks;
+    h->ev_marks.clear();
+    h->graph_timing = h->timing;
     e = cudaGraphInstantiate(&h->graph, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) {

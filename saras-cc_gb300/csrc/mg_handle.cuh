@@ -72,6 +72,10 @@ struct saras_mg {
     std::vector<cudaEvent_t> ev_pool;
     size_t ev_used = 0;
     std::vector<std::pair<int, size_t>> ev_marks;  // (class, index of start event)
+    std::vector<std::pair<int, size_t>> graph_marks;  // marks baked into the graph
+    bool graph_timing = false;
+    bool capturing = false;
+    bool mark_open = false;
     int64_t kc_launches[saras::KC_COUNT] = {0, 0, 0, 0, 0};
     double kc_ms[saras::KC_COUNT] = {0, 0, 0, 0, 0};
     double kc_bytes[saras::KC_COUNT] = {0, 0, 0, 0, 0};
