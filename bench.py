@@ -58,7 +58,7 @@ def workload(S):
     return g, rhs
 
 
-def mg_kw(S, precision, cycles=200):
+def mg_kw(S, precision, cycles=2000):
     return dict(vc_count=cycles, vc_tolerance=TOL, solve_flag=1, mg_tolerance=1e-12, sor_param=1.0,
                 pre_smooth=2, post_smooth=2, res_type=0, precision=precision)
 

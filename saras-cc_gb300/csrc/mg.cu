@@ -11,6 +11,8 @@
 #include <cmath>
 #include <cstring>
 
+#include <math_constants.h>
+
 #include "mg_handle.cuh"
 #include "mg_fast.cuh"
 
@@ -143,6 +145,7 @@ __global__ void k_norm_exact(const double *__restrict__ u, const double *__restr
             const double ar = fabs(r), af = fabs(fv);
             if (ar > mr) mr = ar;
             if (af > mf) mf = af;
+            if (!isfinite(r)) mr = CUDART_INF;  // reported as SARAS_NAN by the host
         } else if (rtype == 1) {
             sr = radd(sr, fabs(r));
             sf = radd(sf, fabs(fv));
@@ -338,14 +341,16 @@ void kbegin(saras_mg *h, cudaStream_t s, int kc) {
         }
     }
     h->ev_marks.push_back({kc, h->ev_used});
-    cudaEventRecord(h->ev_pool[h->ev_used], s);
+    // inside a capture only an "external" record becomes an event-record node
+    cudaEventRecordWithFlags(h->ev_pool[h->ev_used], s, h->capturing ? cudaEventRecordExternal : 0);
     h->ev_used += 2;
     h->mark_open = true;
 }
 
 void kend(saras_mg *h, cudaStream_t s, int kc) {
     if (!h->timing || kc < 0 || !h->mark_open) return;
-    cudaEventRecord(h->ev_pool[h->ev_marks.back().second + 1], s);
+    cudaEventRecordWithFlags(h->ev_pool[h->ev_marks.back().second + 1], s,
+                             h->capturing ? cudaEventRecordExternal : 0);
     h->mark_open = false;
 }
 
@@ -366,6 +371,7 @@ void harvest_timing(saras_mg *h) {
         h->ev_marks.clear();
         h->ev_used = 0;
     }
+    cudaGetLastError();  // a failed elapsed-time query must not surface as a solve error
 }
 
 static void ghost_axis_launch(saras_mg *h, cudaStream_t s, double *u, const Lay &L, int axis, bool wall_pass,
@@ -903,6 +909,18 @@ saras_status solve_common(saras_mg *h, double *lhs, const double *rhs, const int
 }
 
 }  // namespace
+
+namespace saras {
+
+// mgSolve on the finest-level arrays as they stand: the caller has written
+// the RHS core into lv[0].rhs and keeps the initial guess in lv[0].lhs.
+// Used by the RK3 integrator, whose pressure correction lives there.
+saras_status mg_solve_resident(saras_mg *h, int32_t *n_cycles) {
+    h->last_launches = 0;
+    return solve_loop(h, nullptr, 0, n_cycles);
+}
+
+}  // namespace saras
 
 // ------------------------------------------------------- C entry points ----
 

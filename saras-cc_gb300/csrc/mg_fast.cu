@@ -16,6 +16,8 @@
 #include <cmath>
 #include <vector>
 
+#include <math_constants.h>
+
 #include "mg_fast.cuh"
 
 using namespace saras;
@@ -220,6 +222,7 @@ __global__ void k_resid_norm64(const double *__restrict__ u, const double *__res
             const double ar = fabs(r), af = fabs(fv);
             if (ar > v[0]) v[0] = ar;
             if (af > v[1]) v[1] = af;
+            if (!isfinite(r)) v[0] = CUDART_INF;  // reported as SARAS_NAN by the host
         } else if (rtype == 1) {
             v[2] += fabs(r);
             v[3] += fabs(fv);

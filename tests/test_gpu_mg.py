@@ -105,12 +105,17 @@ def test_fp64_matches_oracle(name, gk, mk):
     np.testing.assert_allclose(gpu, orc, rtol=0, atol=1e-11 * scale)
 
 
+# Configurations on which the reference V-cycle reaches 1e-10 within the
+# cycle cap: point RBGS contracts slowly on strongly stretched cells, so the
+# stretched cases use 4/4 smoothing or mild stretching.
 MIXED_CASES = [
-    ("3d_uud_nnn", dict(n=(32, 32, 64), mesh="UUD", beta=(1, 1, 1.3), domain="NNN"), {}),
-    ("3d_ddd_ppn_dirichlet", dict(n=(32, 32, 32), mesh="DDD", beta=(1.2, 1.2, 1.2), domain="PPN"),
-     dict(bc_kind=[0, 0, 0, 0, 1, 1])),
+    ("3d_uuu_nnn", dict(n=(32, 32, 64), mesh="UUU", domain="NNN"), {}),
+    ("3d_uud_nnn_4x4", dict(n=(32, 32, 64), mesh="UUD", beta=(1, 1, 1.3), domain="NNN"),
+     dict(pre_smooth=4, post_smooth=4)),
+    ("3d_ddd_ppn_dirichlet", dict(n=(32, 32, 32), mesh="DDD", beta=(1.05, 1.05, 1.05), domain="PPN"),
+     dict(bc_kind=[0, 0, 0, 0, 1, 1], pre_smooth=4, post_smooth=4)),
     ("2d_nn", dict(n=(128, 1, 128), domain="NNN", dims=2), {}),
-    ("3d_odd_coarse", dict(n=(24, 24, 48), mesh="UUD", beta=(1, 1, 1.5), domain="NNN"), {}),
+    ("3d_odd_coarse", dict(n=(24, 24, 48), mesh="UUD", beta=(1, 1, 1.05), domain="NNN"), {}),
 ]
 
 
@@ -119,7 +124,7 @@ def test_mixed_converges_to_oracle(name, gk, mk):
     g = S.grid_desc(**gk)
     singular = all(k == 0 for k in mk.get("bc_kind", [0] * 6))
     rhs = random_rhs(g, 3, compatible=singular)
-    base = dict(vc_count=80, pre_smooth=2, post_smooth=2, mg_tolerance=1e-12)
+    base = dict(vc_count=120, pre_smooth=2, post_smooth=2, mg_tolerance=1e-12)
     base.update(mk)
     mix = S.padded_field(g)
     mg = S.Multigrid(g, S.mg_params(precision=S.PREC_MIXED, vc_tolerance=1e-10, **base))
@@ -135,8 +140,23 @@ def test_mixed_converges_to_oracle(name, gk, mk):
     assert err < 1e-9, err
 
 
-def test_mixed_two_solves_same_handle():
+def test_mixed_tracks_fp64_cycle_by_cycle():
+    """One MIXED outer iteration is the FP64 V-cycle applied to the error
+    equation: the residual histories agree until FP32 rounding shows."""
     g = S.grid_desc(n=(32, 32, 32), mesh="UUD", beta=(1, 1, 1.3), domain="NNN")
+    rhs = random_rhs(g, 6)
+    kw = dict(vc_count=8, vc_tolerance=1e-30, pre_smooth=2, post_smooth=2, mg_tolerance=1e-12)
+    h = []
+    for prec in (S.PREC_FP64, S.PREC_MIXED):
+        mg = S.Multigrid(g, S.mg_params(precision=prec, **kw))
+        lhs = S.padded_field(g)
+        mg.mg_solve(lhs, rhs)
+        h.append(mg.history.copy())
+    np.testing.assert_allclose(h[1], h[0], rtol=1e-4)
+
+
+def test_mixed_two_solves_same_handle():
+    g = S.grid_desc(n=(32, 32, 32), mesh="UUU", domain="NNN")
     rhs = random_rhs(g, 5)
     mg = S.Multigrid(g, S.mg_params(precision=S.PREC_MIXED, vc_count=60, vc_tolerance=1e-10, pre_smooth=2,
                                     post_smooth=2, mg_tolerance=1e-12))
