@@ -316,14 +316,43 @@ def run_gb300(args):
     print(json.dumps(out), flush=True)
 
 
+def run_profile(args):
+    """Short fixed-cycle solves of the same workload for profiler captures
+    (no timing, no CPU baseline): --profile N runs N V-cycles per form."""
+    import torch
+    import saras_gb300 as S
+    g, rhs = workload(S)
+    stream = torch.cuda.current_stream()
+    rhs_d = torch.from_numpy(rhs).cuda()
+    lhs_d = torch.zeros_like(rhs_d)
+    st = [s // 8 for s in rhs.strides]
+    off = st[0] + st[1] + st[2]
+    forms = {"mixed": S.PREC_MIXED, "fp64": S.PREC_FP64, "exact": S.PREC_FP64_EXACT}
+    for name in args.forms.split(","):
+        kw = dict(mg_kw(S, forms[name], args.profile), vc_tolerance=1e-30)
+        mg = S.Multigrid(g, S.mg_params(**kw), stream=stream.cuda_stream)
+        for _ in range(max(1, args.warmup)):
+            lhs_d.zero_()
+            mg.mg_solve_dev(lhs_d.data_ptr() + 8 * off, rhs_d.data_ptr() + 8 * off, st)
+        torch.cuda.synchronize()
+        print(json.dumps({"form": name, "cycles": mg.cycles, "levels": mg.levels,
+                          "last": float(mg.history[-1]), "launches": mg.last_launches()}), flush=True)
+        mg.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--profile", type=int, default=0,
+                    help="profiler mode: run this many fixed V-cycles per form and exit")
+    ap.add_argument("--forms", default="mixed,fp64")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile:
+        run_profile(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gb300(args)

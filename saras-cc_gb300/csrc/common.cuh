@@ -64,4 +64,19 @@ __device__ __forceinline__ double rdiv(double a, double b) { return __ddiv_rn(a,
 
 inline unsigned cdiv(int64_t a, int64_t b) { return (unsigned)((a + b - 1) / b); }
 
+// Visits the core cells of a level for grid-wide reductions: each warp takes
+// whole k-rows (32-bit index arithmetic only) and its lanes stride along k,
+// so loads stay coalesced.
+template <class Fn>
+__device__ __forceinline__ void for_core_rows(const Lay &L, Fn &&fn) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+    const int rows = L.n0 * L.n1;
+    for (int r = warp; r < rows; r += nwarps) {
+        const int i = r / L.n1, j = r - i * L.n1;
+        for (int k = lane; k < L.n2; k += 32) fn(i, j, k);
+    }
+}
+
 }  // namespace saras

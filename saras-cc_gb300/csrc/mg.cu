@@ -131,14 +131,8 @@ __device__ __forceinline__ double warp_sum(double v) {
 template <bool D3>
 __global__ void k_norm_exact(const double *__restrict__ u, const double *__restrict__ f, Lay L, Coef C,
                              int rtype, double *__restrict__ part) {
-    const int64_t total = (int64_t)L.n0 * L.n1 * L.n2;
     double mr = 0.0, mf = 0.0, sr = 0.0, sf = 0.0;
-    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total;
-         q += (int64_t)gridDim.x * blockDim.x) {
-        const int k = (int)(q % L.n2);
-        const int64_t rest = q / L.n2;
-        const int j = (int)(rest % L.n1);
-        const int i = (int)(rest / L.n1);
+    for_core_rows(L, [&](int i, int j, int k) {
         const double r = resid_exact<D3>(u, f, L, C, i, j, k);
         const double fv = f[L.at(i, j, k)];
         if (rtype == 0) {
@@ -153,7 +147,7 @@ __global__ void k_norm_exact(const double *__restrict__ u, const double *__restr
             sr = radd(sr, rmul(r, r));
             sf = radd(sf, rmul(fv, fv));
         }
-    }
+    });
     __shared__ double sh[4][32];
     mr = warp_max(mr);
     mf = warp_max(mf);
@@ -257,10 +251,26 @@ __device__ void block_colour(double *u, const double *f, const Lay &L, const Coe
     __syncthreads();
 }
 
-template <bool D3>
-__global__ void k_coarsest_exact(double *u, const double *__restrict__ f, Lay L, Coef C, Ghost G, double w,
+// The whole coarsest level fits in shared memory when it is small (the
+// usual 4^3 .. 12x12x6 grids): lhs and rhs are staged there, the iterations
+// run out of shared memory, and blocks of one warp keep the barriers cheap.
+template <bool D3, bool SMEM>
+__global__ void k_coarsest_exact(double *ug, const double *__restrict__ fg, Lay L, Coef C, Ghost G, double w,
                                  double omc, double tol, int max_count, int *sweeps_out) {
     __shared__ double sh[32];
+    extern __shared__ double stage[];
+    double *u = ug;
+    const double *f = fg;
+    if (SMEM) {
+        double *us = stage, *fs = stage + L.size;
+        for (int64_t q = threadIdx.x; q < L.size; q += blockDim.x) {
+            us[q] = ug[q];
+            fs[q] = fg[q];
+        }
+        __syncthreads();
+        u = us;
+        f = fs;
+    }
     int iter = 0, sweeps = 0;
     for (;;) {
         block_ghost_pass(u, L, G, D3, false);
@@ -296,8 +306,12 @@ __global__ void k_coarsest_exact(double *u, const double *__restrict__ f, Lay L,
     }
     block_ghost_pass(u, L, G, D3, false);
     block_ghost_pass(u, L, G, D3, true);
+    if (SMEM)
+        for (int64_t q = threadIdx.x; q < L.size; q += blockDim.x) ug[q] = u[q];
     if (threadIdx.x == 0) *sweeps_out += sweeps;
 }
+
+constexpr int64_t COARSE_SMEM_LIMIT = 96 * 1024;  // bytes of lhs + rhs staged in shared memory
 
 // ---- caller arrays ----
 
@@ -444,10 +458,39 @@ static void norm_exact(saras_mg *h, cudaStream_t s) {
     k_norm_final<<<1, 32, 0, s>>>(h->norm_part, h->norm_blocks, h->prm.res_type, pc, h->norm_out);
 }
 
+static void launch_coarsest(saras_mg *h, cudaStream_t s, Level &c) {
+    const Lay &C = c.lay;
+    const double w = h->prm.sor_param, omc = 1.0 - h->prm.sor_param;
+    const int64_t cells = (int64_t)C.n0 * C.n1 * C.n2;
+    const int threads = cells <= 1024 ? 32 : 256;
+    const size_t smem = (size_t)(2 * C.size) * sizeof(double);
+    const bool use_smem = (int64_t)smem <= COARSE_SMEM_LIMIT;
+    kbegin(h, s, KC_COARSE);
+    if (use_smem) {
+        if (h->d3)
+            k_coarsest_exact<true, true><<<1, threads, smem, s>>>(c.lhs, c.rhs, C, c.coef, h->ghost, w, omc,
+                                                                  h->prm.mg_tolerance, h->maxCount(),
+                                                                  h->coarse_sweeps);
+        else
+            k_coarsest_exact<false, true><<<1, threads, smem, s>>>(c.lhs, c.rhs, C, c.coef, h->ghost, w, omc,
+                                                                   h->prm.mg_tolerance, h->maxCount(),
+                                                                   h->coarse_sweeps);
+    } else {
+        if (h->d3)
+            k_coarsest_exact<true, false><<<1, threads, 0, s>>>(c.lhs, c.rhs, C, c.coef, h->ghost, w, omc,
+                                                                h->prm.mg_tolerance, h->maxCount(),
+                                                                h->coarse_sweeps);
+        else
+            k_coarsest_exact<false, false><<<1, threads, 0, s>>>(c.lhs, c.rhs, C, c.coef, h->ghost, w, omc,
+                                                                 h->prm.mg_tolerance, h->maxCount(),
+                                                                 h->coarse_sweeps);
+    }
+    kend(h, s, KC_COARSE);
+}
+
 // poisson::vCycle in the FP64_EXACT form.
 static void vcycle_exact(saras_mg *h, cudaStream_t s) {
     const int top = h->nl - 1;
-    const double w = h->prm.sor_param, omc = 1.0 - h->prm.sor_param;
     smooth_exact(h, s, 0, h->prm.pre_smooth, false);
     for (int l = 0; l < top; l++) {
         Level &f = h->lv[(size_t)l];
@@ -470,14 +513,7 @@ static void vcycle_exact(saras_mg *h, cudaStream_t s) {
             k_restrict_exact<false><<<cell_grid(C, false, C.n2, cbx), cbx, 0, s>>>(f.tmp, c.rhs, L, C, c.rt);
         cudaMemsetAsync(c.lhs, 0, (size_t)C.size * sizeof(double), s);
         if (l + 1 == top && h->prm.solve_flag) {
-            kbegin(h, s, KC_COARSE);
-            if (h->d3)
-                k_coarsest_exact<true><<<1, 256, 0, s>>>(c.lhs, c.rhs, C, c.coef, h->ghost, w, omc,
-                                                          h->prm.mg_tolerance, h->maxCount(), h->coarse_sweeps);
-            else
-                k_coarsest_exact<false><<<1, 256, 0, s>>>(c.lhs, c.rhs, C, c.coef, h->ghost, w, omc,
-                                                           h->prm.mg_tolerance, h->maxCount(), h->coarse_sweeps);
-            kend(h, s, KC_COARSE);
+            launch_coarsest(h, s, c);
         } else {
             smooth_exact(h, s, l + 1, h->prm.pre_smooth, true);
         }
@@ -501,15 +537,7 @@ void coarsest_level(saras_mg *h, cudaStream_t s) {
     const int top = h->nl - 1;
     Level &c = h->lv[(size_t)top];
     if (h->prm.solve_flag) {
-        const double w = h->prm.sor_param, omc = 1.0 - h->prm.sor_param;
-        kbegin(h, s, KC_COARSE);
-        if (h->d3)
-            k_coarsest_exact<true><<<1, 256, 0, s>>>(c.lhs, c.rhs, c.lay, c.coef, h->ghost, w, omc,
-                                                      h->prm.mg_tolerance, h->maxCount(), h->coarse_sweeps);
-        else
-            k_coarsest_exact<false><<<1, 256, 0, s>>>(c.lhs, c.rhs, c.lay, c.coef, h->ghost, w, omc,
-                                                       h->prm.mg_tolerance, h->maxCount(), h->coarse_sweeps);
-        kend(h, s, KC_COARSE);
+        launch_coarsest(h, s, c);
     } else {
         smooth_exact(h, s, top, h->prm.pre_smooth, true);
     }
@@ -784,6 +812,10 @@ saras_status create(const saras_grid_desc *gd, const saras_mg_params *prm, void 
     SARAS_TRY(dalloc(h, &h->stage_lhs, h->stage_elems));
     SARAS_TRY(dalloc(h, &h->stage_rhs, h->stage_elems));
     SARAS_CUDA(cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking));
+    SARAS_CUDA(cudaFuncSetAttribute(k_coarsest_exact<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)COARSE_SMEM_LIMIT));
+    SARAS_CUDA(cudaFuncSetAttribute(k_coarsest_exact<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)COARSE_SMEM_LIMIT));
     if (fast || mixed) SARAS_TRY(fast_setup(h));
     SARAS_CUDA(cudaDeviceSynchronize());
     return SARAS_OK;

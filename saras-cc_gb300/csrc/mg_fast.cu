@@ -207,14 +207,8 @@ __device__ __forceinline__ void block_store(double (&v)[NV], const bool (&is_max
 template <bool D3, bool MIX>
 __global__ void k_resid_norm64(const double *__restrict__ u, const double *__restrict__ f, Lay L, Tab3<double> t,
                                Bnd b, int rtype, double *__restrict__ part, float *__restrict__ r32) {
-    const int64_t total = (int64_t)L.n0 * L.n1 * L.n2;
     double v[4] = {0.0, 0.0, 0.0, 0.0};
-    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total;
-         q += (int64_t)gridDim.x * blockDim.x) {
-        const int k = (int)(q % L.n2);
-        const int64_t rest = q / L.n2;
-        const int j = (int)(rest % L.n1);
-        const int i = (int)(rest / L.n1);
+    for_core_rows(L, [&](int i, int j, int k) {
         const double r = resid<double, D3>(u, f, L, t, b, i, j, k);
         const double fv = f[L.at(i, j, k)];
         if (MIX) r32[L.at(i, j, k)] = (float)r;
@@ -230,7 +224,7 @@ __global__ void k_resid_norm64(const double *__restrict__ u, const double *__res
             v[2] = fmat(r, r, v[2]);
             v[3] = fmat(fv, fv, v[3]);
         }
-    }
+    });
     const bool mx[4] = {true, true, false, false};
     block_store<4>(v, mx, part);
 }
@@ -252,19 +246,13 @@ __device__ __forceinline__ void two_sum(double a, double b, double &s, double &c
 
 // Compensated (Neumaier) sum of the core of u: per-block (sum, error) pairs.
 __global__ void k_csum(const double *__restrict__ u, Lay L, double *__restrict__ part) {
-    const int64_t total = (int64_t)L.n0 * L.n1 * L.n2;
     double s = 0.0, c = 0.0;
-    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total;
-         q += (int64_t)gridDim.x * blockDim.x) {
-        const int k = (int)(q % L.n2);
-        const int64_t rest = q / L.n2;
-        const int j = (int)(rest % L.n1);
-        const int i = (int)(rest / L.n1);
+    for_core_rows(L, [&](int i, int j, int k) {
         double t, e;
         two_sum(s, u[L.at(i, j, k)], t, e);
         s = t;
         c += e;
-    }
+    });
     for (int o = 16; o > 0; o >>= 1) {
         const double s2 = __shfl_xor_sync(0xffffffffu, s, o), c2 = __shfl_xor_sync(0xffffffffu, c, o);
         double t, e;

@@ -178,14 +178,8 @@ __device__ __forceinline__ double warp_max(double v) {
 template <bool D3>
 __global__ void k_cn_resid(const double *__restrict__ F, const double *__restrict__ R, Lay L, RkTab T, RkScal S,
                            double bdc, double *__restrict__ part) {
-    const int64_t total = (int64_t)L.n0 * L.n1 * L.n2;
     double m = 0.0;
-    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total;
-         q += (int64_t)gridDim.x * blockDim.x) {
-        const int k = (int)(q % L.n2);
-        const int64_t rest = q / L.n2;
-        const int j = (int)(rest % L.n1);
-        const int i = (int)(rest / L.n1);
+    for_core_rows(L, [&](int i, int j, int k) {
         const int64_t c = L.at(i, j, k);
         const double u = F[c], u2 = rmul(2.0, u);
         const double xp = F[c + L.s0], xm = F[c - L.s0], zp = F[c + 1], zm = F[c - 1];
@@ -202,7 +196,7 @@ __global__ void k_cn_resid(const double *__restrict__ F, const double *__restric
         const double t = fabs(rsub(v, R[c]));
         if (t > m) m = t;
         if (!isfinite(t)) m = CUDART_INF;
-    }
+    });
     __shared__ double sh[32];
     m = warp_max(m);
     if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
