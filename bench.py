@@ -10,7 +10,8 @@ mesh "UUD" with z tanh-stretched (beta 1.3), Neumann walls ("NNN"), RHS
 i.i.d. uniform[-1,1] from seed 1 made compatible with the all-Neumann
 operator (its component along the discrete left null vector removed; plain
 mean subtraction on uniform axes), 2 pre / 2 post red-black Gauss-Seidel
-sweeps, coarsest level solved to 1e-12, V-cycle depth from setVCDepth.
+sweeps, coarsest level solved to 1e-6 (the Multigrid "Solve Tolerance" of the
+reference's own tests/mgTest input), V-cycle depth from setVCDepth.
 Synthetic data; every 256^3 FP64 array is 134 MB, above the 129 MB L2, so no
 flush is needed between steps.
 
@@ -59,14 +60,14 @@ def workload(S):
 
 
 def mg_kw(S, precision, cycles=2000):
-    return dict(vc_count=cycles, vc_tolerance=TOL, solve_flag=1, mg_tolerance=1e-12, sor_param=1.0,
+    return dict(vc_count=cycles, vc_tolerance=TOL, solve_flag=1, mg_tolerance=1e-6, sor_param=1.0,
                 pre_smooth=2, post_smooth=2, res_type=0, precision=precision)
 
 
 def config(levels):
     return {"workload": f"Poisson {N}^3, mesh UUD (z tanh beta 1.3), Neumann NNN, RHS U[-1,1] seed 1 "
                         f"projected compatible, 2/2 RBGS, {levels} levels, to rel-res 1e-10 (Linf)",
-            "n": N, "levels": levels, "pre_post_smooth": [2, 2], "tolerance": TOL,
+            "n": N, "levels": levels, "pre_post_smooth": [2, 2], "tolerance": TOL, "coarsest_tolerance": 1e-6,
             "l2": "inputs larger than L2 (each FP64 field 134 MB > 129 MB L2); no flush"}
 
 

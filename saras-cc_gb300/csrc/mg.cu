@@ -181,7 +181,7 @@ __global__ void k_norm_exact(const double *__restrict__ u, const double *__restr
 
 // Combines the partials in a fixed order and forms residualVal.
 __global__ void k_norm_final(const double *__restrict__ part, int nb, int rtype, double point_count,
-                             double *__restrict__ out) {
+                             double *__restrict__ out, const double *__restrict__ den_pre) {
     double mr = 0.0, mf = 0.0, sr = 0.0, sf = 0.0;
     for (int b = threadIdx.x; b < nb; b += 32) {
         const double a = part[4 * b], c = part[4 * b + 1];
@@ -196,6 +196,10 @@ __global__ void k_norm_final(const double *__restrict__ part, int nb, int rtype,
     sf = warp_sum(sf);
     if (threadIdx.x == 0) {
         double num, den, res;
+        if (den_pre) {  // the RHS norm of the solve, taken once
+            mf = den_pre[0];
+            sf = den_pre[0];
+        }
         if (rtype == 0) {
             num = mr;
             den = mf;
@@ -455,7 +459,7 @@ static void norm_exact(saras_mg *h, cudaStream_t s) {
                                                             h->norm_part);
     kend(h, s, KC_NORM);
     kbegin(h, s, -1);
-    k_norm_final<<<1, 32, 0, s>>>(h->norm_part, h->norm_blocks, h->prm.res_type, pc, h->norm_out);
+    k_norm_final<<<1, 32, 0, s>>>(h->norm_part, h->norm_blocks, h->prm.res_type, pc, h->norm_out, nullptr);
 }
 
 static void launch_coarsest(saras_mg *h, cudaStream_t s, Level &c) {
@@ -537,7 +541,7 @@ void coarsest_level(saras_mg *h, cudaStream_t s) {
     const int top = h->nl - 1;
     Level &c = h->lv[(size_t)top];
     if (h->prm.solve_flag) {
-        launch_coarsest(h, s, c);
+        coarsest_fast(h, s, c);
     } else {
         smooth_exact(h, s, top, h->prm.pre_smooth, true);
     }
@@ -547,7 +551,8 @@ void norm_final(saras_mg *h, cudaStream_t s) {
     const double pc = h->d3 ? (double)h->grid.N[0] * h->grid.N[1] * h->grid.N[2]
                             : (double)h->grid.N[0] * h->grid.N[2];
     kbegin(h, s, -1);
-    k_norm_final<<<1, 32, 0, s>>>(h->norm_part, h->norm_blocks, h->prm.res_type, pc, h->norm_out);
+    k_norm_final<<<1, 32, 0, s>>>(h->norm_part, h->norm_blocks, h->prm.res_type, pc, h->norm_out,
+                                  h->norm_out + 4);
 }
 
 void ghost_all_level(saras_mg *h, cudaStream_t s, int l, bool zeroBC) { ghost_all(h, s, l, zeroBC); }
@@ -726,6 +731,9 @@ void free_all(saras_mg *h) {
         cudaFree(v.tab32);
         cudaFree(v.inv_diag);
         cudaFree(v.inv_diag32);
+        cudaFree(v.dd);
+        cudaFree(v.lhs_alt);
+        cudaFree(v.e32_alt);
     }
     cudaFree(h->walls);
     cudaFree(h->norm_part);
@@ -788,8 +796,20 @@ saras_status create(const saras_grid_desc *gd, const saras_mg_params *prm, void 
         if (mixed && coarsest) {
             SARAS_TRY(dalloc(h, &v.tmp, sz));  // FP64 coarse residual scratch
         }
-        if (fast) SARAS_TRY(dalloc(h, &v.inv_diag, sz));
-        if (mixed && !coarsest) SARAS_TRY(dalloc(h, &v.inv_diag32, sz));
+        if (fast || (mixed && coarsest)) SARAS_TRY(dalloc(h, &v.inv_diag, sz));
+        if (fast || (mixed && (l == 0 || coarsest))) SARAS_TRY(dalloc(h, &v.dd, sz));
+        // fused red-black iterations on the larger levels whose periodic
+        // extents are even (so the wrap keeps the colouring)
+        bool even = true;
+        const int nn[3] = {v.lay.n0, v.lay.n1, v.lay.n2};
+        for (int d = 0; d < 3; d++)
+            if (h->grid.active(d) && h->grid.per[d] && (nn[d] & 1)) even = false;
+        const int64_t cells = (int64_t)nn[0] * nn[1] * nn[2];
+        v.fused = (fast || mixed) && !coarsest && even && cells >= 4096 && nn[0] >= 4;
+        if (v.fused && fast) SARAS_TRY(dalloc(h, &v.lhs_alt, sz));
+        if (v.fused && mixed) SARAS_TRY(dalloc(h, &v.e32_alt, sz));
+        v.cur64 = v.lhs;
+        v.cur32 = v.e32;
     }
     SARAS_TRY(build_tables(h));
     SARAS_TRY(build_walls(h));
@@ -882,6 +902,7 @@ saras_status solve_loop(saras_mg *h, double *res_hist, int32_t hist_cap, int32_t
     int cyc = 0;
     double r = 0.0;
     for (int c = 0; c < h->prm.vc_count; c++) {
+        if (h->prm.precision != SARAS_PREC_FP64_EXACT && c == 0) rhs_norm(h, s);
         if (h->prm.precision == SARAS_PREC_MIXED && c == 0) {
             // the defect-correction loop starts from the residual of the guess
             mixed_prepare(h, s);

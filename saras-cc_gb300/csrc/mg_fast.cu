@@ -87,14 +87,16 @@ __device__ __forceinline__ T diag(const Tab3<T> &t, int i, int j, int k) {
     return d + d;
 }
 
-// f - A u
+// f - A u; with `dd` the diagonal is read per cell instead of rebuilt (it
+// saves three FP64 additions per cell, the scarce resource on GB300).
 template <class T, bool D3>
 __device__ __forceinline__ T resid(const T *u, const T *f, const Lay &L, const Tab3<T> &t, const Bnd &b, int i,
-                                   int j, int k) {
+                                   int j, int k, const T *dd = nullptr) {
     const int64_t c = L.at(i, j, k);
     const T uc = u[c];
     const T s = offdiag<T, D3>(u, L, t, b, i, j, k, c, uc);
-    return f[c] - fmat(-diag<T, D3>(t, i, j, k), uc, s);
+    const T d = dd ? dd[c] : diag<T, D3>(t, i, j, k);
+    return f[c] - fmat(-d, uc, s);
 }
 
 // ------------------------------------------------------------ kernels ----
@@ -129,12 +131,108 @@ __global__ void k_rbgs32(float *e, const float *__restrict__ r, Lay L, Tab3<floa
     e[c] = fmat(omc, uc, __fdiv_rn(w * s, diag<float, D3>(t, i, j, k)));
 }
 
+// One full SOR red-black iteration (red then black) in a single pass.  The
+// previous iterate is read from `uo` and the new one written to `un`, so no
+// cell is read after another block has overwritten it.  A block owns a
+// (j,k) tile of TJ x TK cells and marches along i through a chunk of planes;
+// the new red values that black cells need (planes i-1, i, i+1 and a
+// one-cell halo in j,k) are computed once per plane into a shared ring.
+// Cells map to the red/black colours by their (i+j+k) parity, which the
+// periodic wrap preserves on even extents (the only ones this kernel runs).
+constexpr int FTJ = 8, FTK = 64, FTHREADS = 256;  // fused-iteration tile (j x k) and block size
+
+template <class T>
+__device__ __forceinline__ bool wrap_index(int &g, int n, int per) {
+    if (g >= 0 && g < n) return true;
+    if (!per) return false;
+    g = g < 0 ? g + n : g - n;
+    return true;
+}
+
+template <class T, bool D3, bool WD>
+__global__ void __launch_bounds__(FTHREADS) k_rbgs_fused(const T *__restrict__ uo, T *__restrict__ un,
+                                                         const T *__restrict__ f, const T *__restrict__ wd, Lay L,
+                                                         Tab3<T> t, Bnd b, T w, T omc, int chunk) {
+    __shared__ T ring[3][FTJ + 2][FTK + 2];
+    const int k0 = blockIdx.x * FTK;
+    const int j0 = D3 ? (int)blockIdx.y * FTJ : 0;
+    const int a = (int)blockIdx.z * chunk;
+    const int e = min(a + chunk, L.n0);
+    const int tj_n = D3 ? FTJ + 2 : 1;  // planar: a single row of the ring
+    const int ring_n = tj_n * (FTK + 2);
+    for (int p = a - 1; p <= e; p++) {
+        // red values of plane p over the tile and its halo
+        int gi = p;
+        const bool plane_ok = wrap_index<T>(gi, L.n0, b.per[0]);
+        const int slot = (p + 3) % 3;
+        if (plane_ok) {
+            for (int q = threadIdx.x; q < ring_n; q += FTHREADS) {
+                const int jj = D3 ? q / (FTK + 2) - 1 : 0;
+                const int kk = q % (FTK + 2) - 1;
+                int gj = j0 + jj, gk = k0 + kk;
+                if (D3 && !wrap_index<T>(gj, L.n1, b.per[1])) continue;
+                if (!wrap_index<T>(gk, L.n2, b.per[2])) continue;
+                if ((gi + gj + gk) & 1) continue;
+                const int64_t c = L.at(gi, gj, gk);
+                const T uc = uo[c];
+                const T s = offdiag<T, D3>(uo, L, t, b, gi, gj, gk, c, uc) - f[c];
+                T v;
+                if (WD)
+                    v = fmat(s, wd[c], omc * uc);
+                else
+                    v = fmat(omc, uc, w * s / diag<T, D3>(t, gi, gj, gk));
+                ring[slot][D3 ? jj + 1 : 0][kk + 1] = v;
+            }
+        }
+        __syncthreads();
+        // black values of plane p-1 over the tile; both colours written
+        const int pb = p - 1;
+        if (pb >= a && pb < e) {
+            const int sm = (pb - 1 + 3) % 3, s0 = (pb + 3) % 3, sp = (pb + 1 + 3) % 3;
+            const int tile_n = (D3 ? FTJ : 1) * FTK;
+            for (int q = threadIdx.x; q < tile_n; q += FTHREADS) {
+                const int jj = D3 ? q / FTK : 0;
+                const int kk = q % FTK;
+                const int gj = j0 + jj, gk = k0 + kk;
+                if (gj >= L.n1 || gk >= L.n2) continue;
+                const int rj = D3 ? jj + 1 : 0, rk = kk + 1;
+                const int64_t c = L.at(pb, gj, gk);
+                if (((pb + gj + gk) & 1) == 0) {
+                    un[c] = ring[s0][rj][rk];
+                    continue;
+                }
+                const T uc = uo[c];
+                const T xm = (pb > 0 || b.per[0]) ? ring[sm][rj][rk] : (b.sg_lo[0] > 0 ? uc : -uc);
+                const T xp = (pb < L.n0 - 1 || b.per[0]) ? ring[sp][rj][rk] : (b.sg_hi[0] > 0 ? uc : -uc);
+                const T zm = (gk > 0 || b.per[2]) ? ring[s0][rj][rk - 1] : (b.sg_lo[2] > 0 ? uc : -uc);
+                const T zp = (gk < L.n2 - 1 || b.per[2]) ? ring[s0][rj][rk + 1] : (b.sg_hi[2] > 0 ? uc : -uc);
+                T sum = t.cm[0][pb] * xm;
+                sum = fmat(t.cp[0][pb], xp, sum);
+                if (D3) {
+                    const T ym = (gj > 0 || b.per[1]) ? ring[s0][rj - 1][rk] : (b.sg_lo[1] > 0 ? uc : -uc);
+                    const T yp = (gj < L.n1 - 1 || b.per[1]) ? ring[s0][rj + 1][rk] : (b.sg_hi[1] > 0 ? uc : -uc);
+                    sum = fmat(t.cm[1][gj], ym, sum);
+                    sum = fmat(t.cp[1][gj], yp, sum);
+                }
+                sum = fmat(t.cm[2][gk], zm, sum);
+                sum = fmat(t.cp[2][gk], zp, sum);
+                const T sv = sum - f[c];
+                if (WD)
+                    un[c] = fmat(sv, wd[c], omc * uc);
+                else
+                    un[c] = fmat(omc, uc, w * sv / diag<T, D3>(t, pb, gj, gk));
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // Fused residual and restriction: one thread per coarse cell forms the
 // residuals of its 2x2x2 children and their weighted sum (the coarsen
 // weights v_abc / vTot of poisson_d3.cc:494-508, factorised per axis).
 template <class T, class TO, bool D3>
 __global__ void k_resid_restrict(const T *__restrict__ u, const T *__restrict__ f, Lay Lf, Tab3<T> t, Bnd b,
-                                 WTab<T> w, TO *__restrict__ rc, Lay Lc) {
+                                 WTab<T> w, TO *__restrict__ rc, Lay Lc, const T *__restrict__ dd) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = D3 ? (int)blockIdx.y : 0;
     const int i = blockIdx.z;
@@ -146,18 +244,18 @@ __global__ void k_resid_restrict(const T *__restrict__ u, const T *__restrict__ 
         for (int a = 0; a < 2; a++) {
             T sz[2];
             for (int bb = 0; bb < 2; bb++) {
-                const T r0 = resid<T, true>(u, f, Lf, t, b, i2 + a, j2 + bb, k2);
-                const T r1 = resid<T, true>(u, f, Lf, t, b, i2 + a, j2 + bb, k2 + 1);
+                const T r0 = resid<T, true>(u, f, Lf, t, b, i2 + a, j2 + bb, k2, dd);
+                const T r1 = resid<T, true>(u, f, Lf, t, b, i2 + a, j2 + bb, k2 + 1, dd);
                 sz[bb] = fmat(w.w1[2][k], r1, w.w0[2][k] * r0);
             }
             sy[a] = fmat(w.w1[1][j], sz[1], w.w0[1][j] * sz[0]);
         }
         out = fmat(w.w1[0][i], sy[1], w.w0[0][i] * sy[0]);
     } else {
-        const T r00 = resid<T, false>(u, f, Lf, t, b, i2, 0, k2);
-        const T r01 = resid<T, false>(u, f, Lf, t, b, i2, 0, k2 + 1);
-        const T r10 = resid<T, false>(u, f, Lf, t, b, i2 + 1, 0, k2);
-        const T r11 = resid<T, false>(u, f, Lf, t, b, i2 + 1, 0, k2 + 1);
+        const T r00 = resid<T, false>(u, f, Lf, t, b, i2, 0, k2, dd);
+        const T r01 = resid<T, false>(u, f, Lf, t, b, i2, 0, k2 + 1, dd);
+        const T r10 = resid<T, false>(u, f, Lf, t, b, i2 + 1, 0, k2, dd);
+        const T r11 = resid<T, false>(u, f, Lf, t, b, i2 + 1, 0, k2 + 1, dd);
         out = ((r00 + r01) + (r10 + r11)) * T(0.25);
     }
     rc[Lc.at(i, j, k)] = (TO)out;
@@ -204,29 +302,139 @@ __device__ __forceinline__ void block_store(double (&v)[NV], const bool (&is_max
 
 // FP64 residual of the finest level with norm partials; optionally writes
 // the residual in FP32 (MIXED form) and first applies u += e.
+// For the L-infinity norm |r| and the running maximum use integer
+// operations on the bit pattern (non-negative doubles order like their
+// bits; a NaN sorts above infinity and reaches the host as non-finite), so
+// the FP64 pipe only computes the stencil.  The RHS norm is taken once per
+// solve (k_rhs_norm).
 template <bool D3, bool MIX>
-__global__ void k_resid_norm64(const double *__restrict__ u, const double *__restrict__ f, Lay L, Tab3<double> t,
-                               Bnd b, int rtype, double *__restrict__ part, float *__restrict__ r32) {
+__global__ void k_resid_norm64(const double *__restrict__ u, const double *__restrict__ f,
+                               const double *__restrict__ dd, Lay L, Tab3<double> t, Bnd b, int rtype,
+                               double *__restrict__ part, float *__restrict__ r32) {
+    unsigned long long mbits = 0ull;
     double v[4] = {0.0, 0.0, 0.0, 0.0};
     for_core_rows(L, [&](int i, int j, int k) {
-        const double r = resid<double, D3>(u, f, L, t, b, i, j, k);
-        const double fv = f[L.at(i, j, k)];
+        const double r = resid<double, D3>(u, f, L, t, b, i, j, k, dd);
         if (MIX) r32[L.at(i, j, k)] = (float)r;
         if (rtype == 0) {
-            const double ar = fabs(r), af = fabs(fv);
-            if (ar > v[0]) v[0] = ar;
-            if (af > v[1]) v[1] = af;
-            if (!isfinite(r)) v[0] = CUDART_INF;  // reported as SARAS_NAN by the host
+            const unsigned long long bits = (unsigned long long)__double_as_longlong(r) & 0x7fffffffffffffffull;
+            mbits = bits > mbits ? bits : mbits;
         } else if (rtype == 1) {
             v[2] += fabs(r);
-            v[3] += fabs(fv);
         } else {
             v[2] = fmat(r, r, v[2]);
+        }
+    });
+    if (rtype == 0) {
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long w = __shfl_xor_sync(0xffffffffu, mbits, o);
+            mbits = w > mbits ? w : mbits;
+        }
+        __shared__ unsigned long long shm[32];
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        if (lane == 0) shm[wid] = mbits;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long m = 0ull;
+            for (int q = 0; q < nw; q++) m = shm[q] > m ? shm[q] : m;
+            part[4 * blockIdx.x] = __longlong_as_double((long long)m);
+            part[4 * blockIdx.x + 1] = 0.0;
+            part[4 * blockIdx.x + 2] = 0.0;
+            part[4 * blockIdx.x + 3] = 0.0;
+        }
+        return;
+    }
+    const bool mx[4] = {true, true, false, false};
+    block_store<4>(v, mx, part);
+}
+
+// RHS norm of the solve: max|f| (L-inf), sum|f| (L1) or sum f^2 (L2).
+__global__ void k_rhs_norm(const double *__restrict__ f, Lay L, int rtype, double *__restrict__ part) {
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    for_core_rows(L, [&](int i, int j, int k) {
+        const double fv = f[L.at(i, j, k)];
+        if (rtype == 0) {
+            const double af = fabs(fv);
+            if (af > v[1]) v[1] = af;
+        } else if (rtype == 1) {
+            v[3] += fabs(fv);
+        } else {
             v[3] = fmat(fv, fv, v[3]);
         }
     });
     const bool mx[4] = {true, true, false, false};
     block_store<4>(v, mx, part);
+}
+
+__global__ void k_rhs_norm_final(const double *__restrict__ part, int nb, int rtype, double *__restrict__ out) {
+    if (threadIdx.x != 0) return;
+    double m = 0.0, sm = 0.0;
+    for (int q = 0; q < nb; q++) {
+        const double a = part[4 * q + 1];
+        if (a > m) m = a;
+        sm += part[4 * q + 3];
+    }
+    out[0] = rtype == 0 ? m : sm;
+}
+
+// Coarsest level of the FP64 and MIXED forms: SOR red-black sweeps with
+// omega/D stored per cell and the boundary folded into the stencil, run to
+// the absolute tolerance or the iteration cap of poisson_d3.cc:249-432, by
+// one block in shared memory.
+template <bool D3>
+__global__ void k_coarsest_fast(double *ug, const double *__restrict__ fg, const double *__restrict__ wdg,
+                                const double *__restrict__ ddg, Lay L, Tab3<double> t, Bnd b, double omc, double tol,
+                                int max_count, int *sweeps_out) {
+    extern __shared__ double stage[];
+    __shared__ unsigned long long shm[32];
+    double *u = stage, *f = stage + L.size, *wd = stage + 2 * L.size, *dd = stage + 3 * L.size;
+    for (int64_t q = threadIdx.x; q < L.size; q += blockDim.x) {
+        u[q] = ug[q];
+        f[q] = fg[q];
+        wd[q] = wdg[q];
+        dd[q] = ddg[q];
+    }
+    __syncthreads();
+    const int half = (L.n2 + 1) / 2;
+    const int ncol = L.n0 * L.n1 * half;
+    const int ncell = L.n0 * L.n1 * L.n2;
+    int iter = 0, sweeps = 0;
+    for (;;) {
+        for (int colour = 0; colour < 2; colour++) {
+            for (int q = threadIdx.x; q < ncol; q += blockDim.x) {
+                const int kk = q % half, rest = q / half, j = rest % L.n1, i = rest / L.n1;
+                const int k = 2 * kk + ((i + j + colour) & 1);
+                if (k >= L.n2) continue;
+                const int64_t c = L.at(i, j, k);
+                const double uc = u[c];
+                const double sv = offdiag<double, D3>(u, L, t, b, i, j, k, c, uc) - f[c];
+                u[c] = fmat(sv, wd[c], omc * uc);
+            }
+            __syncthreads();
+        }
+        unsigned long long m = 0ull;
+        for (int q = threadIdx.x; q < ncell; q += blockDim.x) {
+            const int k = q % L.n2, rest = q / L.n2, j = rest % L.n1, i = rest / L.n1;
+            const double r = resid<double, D3>(u, f, L, t, b, i, j, k, dd);
+            const unsigned long long bits = (unsigned long long)__double_as_longlong(r) & 0x7fffffffffffffffull;
+            m = bits > m ? bits : m;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long w = __shfl_xor_sync(0xffffffffu, m, o);
+            m = w > m ? w : m;
+        }
+        if ((threadIdx.x & 31) == 0) shm[threadIdx.x >> 5] = m;
+        __syncthreads();
+        unsigned long long mm = 0ull;
+        for (int q = 0; q < (int)(blockDim.x >> 5); q++) mm = shm[q] > mm ? shm[q] : mm;
+        __syncthreads();
+        sweeps++;
+        if (__longlong_as_double((long long)mm) < tol) break;
+        iter++;
+        if (iter > max_count) break;
+    }
+    for (int64_t q = threadIdx.x; q < L.size; q += blockDim.x) ug[q] = u[q];
+    if (threadIdx.x == 0) *sweeps_out += sweeps;
 }
 
 // u += e over the core (MIXED form update, FP64 accumulate).
@@ -302,14 +510,16 @@ __global__ void k_shift(double *__restrict__ u, Lay L, const double *__restrict_
     u[q] = u[q] - (m[0] - m[1]);
 }
 
-// omega / D per cell for the FP64 form.
+// omega / D and D per cell for the FP64 kernels (either may be absent).
 template <bool D3>
-__global__ void k_inv_diag(double *__restrict__ wd, Lay L, Tab3<double> t, double w) {
+__global__ void k_inv_diag(double *__restrict__ wd, double *__restrict__ dd, Lay L, Tab3<double> t, double w) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = D3 ? (int)blockIdx.y : 0;
     const int i = blockIdx.z;
     if (k >= L.n2) return;
-    wd[L.at(i, j, k)] = w / diag<double, D3>(t, i, j, k);
+    const double d = diag<double, D3>(t, i, j, k);
+    if (wd) wd[L.at(i, j, k)] = w / d;
+    if (dd) dd[L.at(i, j, k)] = d;
 }
 
 // ------------------------------------------------------- host side ----
@@ -352,18 +562,18 @@ void colour64(saras_mg *h, cudaStream_t s, int l, int colour) {
     kbegin(h, s, l == 0 ? KC_SMOOTH0 : -1);
     if (h->d3) {
         if (w1)
-            k_rbgs64<true, true><<<cgrid(L, true, half, bx), bx, 0, s>>>(v.lhs, v.rhs, v.inv_diag, L, tab64(v), b,
-                                                                         colour, omc);
+            k_rbgs64<true, true><<<cgrid(L, true, half, bx), bx, 0, s>>>(v.cur64, v.rhs, v.inv_diag, L, tab64(v),
+                                                                         b, colour, omc);
         else
-            k_rbgs64<true, false><<<cgrid(L, true, half, bx), bx, 0, s>>>(v.lhs, v.rhs, v.inv_diag, L, tab64(v), b,
-                                                                          colour, omc);
+            k_rbgs64<true, false><<<cgrid(L, true, half, bx), bx, 0, s>>>(v.cur64, v.rhs, v.inv_diag, L, tab64(v),
+                                                                          b, colour, omc);
     } else {
         if (w1)
-            k_rbgs64<false, true><<<cgrid(L, false, half, bx), bx, 0, s>>>(v.lhs, v.rhs, v.inv_diag, L, tab64(v),
-                                                                           b, colour, omc);
+            k_rbgs64<false, true><<<cgrid(L, false, half, bx), bx, 0, s>>>(v.cur64, v.rhs, v.inv_diag, L,
+                                                                           tab64(v), b, colour, omc);
         else
-            k_rbgs64<false, false><<<cgrid(L, false, half, bx), bx, 0, s>>>(v.lhs, v.rhs, v.inv_diag, L, tab64(v),
-                                                                            b, colour, omc);
+            k_rbgs64<false, false><<<cgrid(L, false, half, bx), bx, 0, s>>>(v.cur64, v.rhs, v.inv_diag, L,
+                                                                            tab64(v), b, colour, omc);
     }
     kend(h, s, l == 0 ? KC_SMOOTH0 : -1);
 }
@@ -376,9 +586,9 @@ void colour32(saras_mg *h, cudaStream_t s, int l, int colour) {
     const Bnd b = bnd(h);
     kbegin(h, s, l == 0 ? KC_SMOOTH0 : -1);
     if (h->d3)
-        k_rbgs32<true><<<cgrid(L, true, half, bx), bx, 0, s>>>(v.e32, v.r32, L, tab32(v), b, colour, w, omc);
+        k_rbgs32<true><<<cgrid(L, true, half, bx), bx, 0, s>>>(v.cur32, v.r32, L, tab32(v), b, colour, w, omc);
     else
-        k_rbgs32<false><<<cgrid(L, false, half, bx), bx, 0, s>>>(v.e32, v.r32, L, tab32(v), b, colour, w, omc);
+        k_rbgs32<false><<<cgrid(L, false, half, bx), bx, 0, s>>>(v.cur32, v.r32, L, tab32(v), b, colour, w, omc);
     kend(h, s, l == 0 ? KC_SMOOTH0 : -1);
 }
 
@@ -405,24 +615,24 @@ void residual_restrict(saras_mg *h, cudaStream_t s, int l, bool mixed) {
     if (!mixed) {
         if (h->d3)
             k_resid_restrict<double, double, true><<<cgrid(Lc, true, Lc.n2, bx), bx, 0, s>>>(
-                f.lhs, f.rhs, f.lay, tab64(f), b, wt64(c), c.rhs, Lc);
+                f.cur64, f.rhs, f.lay, tab64(f), b, wt64(c), c.rhs, Lc, f.dd);
         else
             k_resid_restrict<double, double, false><<<cgrid(Lc, false, Lc.n2, bx), bx, 0, s>>>(
-                f.lhs, f.rhs, f.lay, tab64(f), b, wt64(c), c.rhs, Lc);
+                f.cur64, f.rhs, f.lay, tab64(f), b, wt64(c), c.rhs, Lc, f.dd);
     } else if (to64) {
         if (h->d3)
             k_resid_restrict<float, double, true><<<cgrid(Lc, true, Lc.n2, bx), bx, 0, s>>>(
-                f.e32, f.r32, f.lay, tab32(f), b, wt32(c), c.rhs, Lc);
+                f.cur32, f.r32, f.lay, tab32(f), b, wt32(c), c.rhs, Lc, nullptr);
         else
             k_resid_restrict<float, double, false><<<cgrid(Lc, false, Lc.n2, bx), bx, 0, s>>>(
-                f.e32, f.r32, f.lay, tab32(f), b, wt32(c), c.rhs, Lc);
+                f.cur32, f.r32, f.lay, tab32(f), b, wt32(c), c.rhs, Lc, nullptr);
     } else {
         if (h->d3)
             k_resid_restrict<float, float, true><<<cgrid(Lc, true, Lc.n2, bx), bx, 0, s>>>(
-                f.e32, f.r32, f.lay, tab32(f), b, wt32(c), c.r32, Lc);
+                f.cur32, f.r32, f.lay, tab32(f), b, wt32(c), c.r32, Lc, nullptr);
         else
             k_resid_restrict<float, float, false><<<cgrid(Lc, false, Lc.n2, bx), bx, 0, s>>>(
-                f.e32, f.r32, f.lay, tab32(f), b, wt32(c), c.r32, Lc);
+                f.cur32, f.r32, f.lay, tab32(f), b, wt32(c), c.r32, Lc, nullptr);
     }
     kend(h, s, l == 0 ? KC_RESTRICT : -1);
 }
@@ -435,17 +645,55 @@ void prolong_add(saras_mg *h, cudaStream_t s, int l, bool mixed) {
     const dim3 g(cdiv(L.n2, bx), (unsigned)L.n1, (unsigned)L.n0);
     kbegin(h, s, l == 1 ? KC_PROLONG : -1);
     if (!mixed)
-        k_prolong_add<double, double><<<g, bx, 0, s>>>(f.lhs, c.lhs, L, c.lay, h->d3 ? 1 : 0);
+        k_prolong_add<double, double><<<g, bx, 0, s>>>(f.cur64, c.cur64, L, c.lay, h->d3 ? 1 : 0);
     else if (l == h->nl - 1)
-        k_prolong_add<float, double><<<g, bx, 0, s>>>(f.e32, c.lhs, L, c.lay, h->d3 ? 1 : 0);
+        k_prolong_add<float, double><<<g, bx, 0, s>>>(f.cur32, c.lhs, L, c.lay, h->d3 ? 1 : 0);
     else
-        k_prolong_add<float, float><<<g, bx, 0, s>>>(f.e32, c.e32, L, c.lay, h->d3 ? 1 : 0);
+        k_prolong_add<float, float><<<g, bx, 0, s>>>(f.cur32, c.cur32, L, c.lay, h->d3 ? 1 : 0);
     kend(h, s, l == 1 ? KC_PROLONG : -1);
 }
 
+// One fused iteration: current buffer -> partner, then they swap roles.
+void fused_iteration(saras_mg *h, cudaStream_t s, int l, bool mixed) {
+    Level &v = h->lv[(size_t)l];
+    const Lay &L = v.lay;
+    const Bnd b = bnd(h);
+    const unsigned tk = cdiv(L.n2, FTK), tj = h->d3 ? cdiv(L.n1, FTJ) : 1u;
+    const int tiles = (int)(tk * tj);
+    const int nchunk = std::max(1, std::min(L.n0 / 4, (1216 + tiles - 1) / tiles));
+    const int chunk = (L.n0 + nchunk - 1) / nchunk;
+    const dim3 g(tk, tj, cdiv(L.n0, chunk));
+    kbegin(h, s, l == 0 ? KC_SMOOTH0 : -1);
+    if (mixed) {
+        float *dst = v.cur32 == v.e32 ? v.e32_alt : v.e32;
+        const float w = (float)h->prm.sor_param, omc = (float)(1.0 - h->prm.sor_param);
+        if (h->d3)
+            k_rbgs_fused<float, true, false><<<g, FTHREADS, 0, s>>>(v.cur32, dst, v.r32, nullptr, L, tab32(v), b, w,
+                                                                    omc, chunk);
+        else
+            k_rbgs_fused<float, false, false><<<g, FTHREADS, 0, s>>>(v.cur32, dst, v.r32, nullptr, L, tab32(v), b,
+                                                                     w, omc, chunk);
+        v.cur32 = dst;
+    } else {
+        double *dst = v.cur64 == v.lhs ? v.lhs_alt : v.lhs;
+        const double omc = 1.0 - h->prm.sor_param;
+        if (h->d3)
+            k_rbgs_fused<double, true, true><<<g, FTHREADS, 0, s>>>(v.cur64, dst, v.rhs, v.inv_diag, L, tab64(v),
+                                                                    b, 0.0, omc, chunk);
+        else
+            k_rbgs_fused<double, false, true><<<g, FTHREADS, 0, s>>>(v.cur64, dst, v.rhs, v.inv_diag, L, tab64(v),
+                                                                     b, 0.0, omc, chunk);
+        v.cur64 = dst;
+    }
+    kend(h, s, l == 0 ? KC_SMOOTH0 : -1);
+}
+
 void smooth(saras_mg *h, cudaStream_t s, int l, int count, bool mixed) {
+    Level &v = h->lv[(size_t)l];
     for (int n = 0; n < count; n++) {
-        if (mixed) {
+        if (v.fused) {
+            fused_iteration(h, s, l, mixed);
+        } else if (mixed) {
             colour32(h, s, l, 0);
             colour32(h, s, l, 1);
         } else {
@@ -461,17 +709,17 @@ void resid_norm(saras_mg *h, cudaStream_t s, bool mixed) {
     kbegin(h, s, KC_NORM);
     if (h->d3) {
         if (mixed)
-            k_resid_norm64<true, true><<<h->norm_blocks, 256, 0, s>>>(v.lhs, v.rhs, v.lay, tab64(v), b,
+            k_resid_norm64<true, true><<<h->norm_blocks, 256, 0, s>>>(v.lhs, v.rhs, v.dd, v.lay, tab64(v), b,
                                                                       h->prm.res_type, h->norm_part, v.r32);
         else
-            k_resid_norm64<true, false><<<h->norm_blocks, 256, 0, s>>>(v.lhs, v.rhs, v.lay, tab64(v), b,
+            k_resid_norm64<true, false><<<h->norm_blocks, 256, 0, s>>>(v.lhs, v.rhs, v.dd, v.lay, tab64(v), b,
                                                                        h->prm.res_type, h->norm_part, nullptr);
     } else {
         if (mixed)
-            k_resid_norm64<false, true><<<h->norm_blocks, 256, 0, s>>>(v.lhs, v.rhs, v.lay, tab64(v), b,
+            k_resid_norm64<false, true><<<h->norm_blocks, 256, 0, s>>>(v.lhs, v.rhs, v.dd, v.lay, tab64(v), b,
                                                                        h->prm.res_type, h->norm_part, v.r32);
         else
-            k_resid_norm64<false, false><<<h->norm_blocks, 256, 0, s>>>(v.lhs, v.rhs, v.lay, tab64(v), b,
+            k_resid_norm64<false, false><<<h->norm_blocks, 256, 0, s>>>(v.lhs, v.rhs, v.dd, v.lay, tab64(v), b,
                                                                         h->prm.res_type, h->norm_part, nullptr);
     }
     kend(h, s, KC_NORM);
@@ -505,17 +753,20 @@ saras_status fast_setup(saras_mg *h) {
             set_error("the TEST_POISSON wall kind is available in the FP64_EXACT form only");
             return SARAS_BAD_ARG;
         }
-    if (h->prm.precision == SARAS_PREC_FP64) {
-        for (int l = 0; l < h->nl; l++) {
-            Level &v = h->lv[(size_t)l];
-            const Lay &L = v.lay;
-            const int bx = bxfor(L.n2);
-            if (h->d3)
-                k_inv_diag<true><<<cgrid(L, true, L.n2, bx), bx>>>(v.inv_diag, L, tab64(v), h->prm.sor_param);
-            else
-                k_inv_diag<false><<<cgrid(L, false, L.n2, bx), bx>>>(v.inv_diag, L, tab64(v), h->prm.sor_param);
-        }
+    for (int l = 0; l < h->nl; l++) {
+        Level &v = h->lv[(size_t)l];
+        if (!v.inv_diag && !v.dd) continue;
+        const Lay &L = v.lay;
+        const int bx = bxfor(L.n2);
+        if (h->d3)
+            k_inv_diag<true><<<cgrid(L, true, L.n2, bx), bx>>>(v.inv_diag, v.dd, L, tab64(v), h->prm.sor_param);
+        else
+            k_inv_diag<false><<<cgrid(L, false, L.n2, bx), bx>>>(v.inv_diag, v.dd, L, tab64(v), h->prm.sor_param);
     }
+    SARAS_CUDA(cudaFuncSetAttribute(k_coarsest_fast<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    200 * 1024));
+    SARAS_CUDA(cudaFuncSetAttribute(k_coarsest_fast<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    200 * 1024));
     SARAS_CUDA(cudaGetLastError());
     return SARAS_OK;
 }
@@ -524,6 +775,10 @@ saras_status fast_setup(saras_mg *h) {
 void fast_cycle(saras_mg *h, cudaStream_t s) {
     const bool mixed = h->prm.precision == SARAS_PREC_MIXED;
     const int top = h->nl - 1;
+    for (Level &v : h->lv) {
+        v.cur64 = v.lhs;
+        v.cur32 = v.e32;
+    }
     if (mixed) {
         // error equation at the finest level starts from zero
         Level &v0 = h->lv[0];
@@ -557,7 +812,14 @@ void fast_cycle(saras_mg *h, cudaStream_t s) {
         const Lay &L = v0.lay;
         const int bx = bxfor(L.n2);
         kbegin(h, s, -1);
-        k_update64<<<dim3(cdiv(L.n2, bx), (unsigned)L.n1, (unsigned)L.n0), bx, 0, s>>>(v0.lhs, v0.e32, L);
+        k_update64<<<dim3(cdiv(L.n2, bx), (unsigned)L.n1, (unsigned)L.n0), bx, 0, s>>>(v0.lhs, v0.cur32, L);
+    } else {
+        Level &v0 = h->lv[0];
+        if (v0.cur64 != v0.lhs) {  // odd number of fused iterations: the solution returns to its own array
+            kbegin(h, s, -1);
+            cudaMemcpyAsync(v0.lhs, v0.cur64, (size_t)v0.lay.size * sizeof(double), cudaMemcpyDeviceToDevice, s);
+            v0.cur64 = v0.lhs;
+        }
     }
     resid_norm(h, s, mixed);
 }
@@ -570,6 +832,36 @@ void mixed_prepare(saras_mg *h, cudaStream_t s) {
 }
 
 void final_ghosts(saras_mg *h, cudaStream_t s) { ghost_all_level(h, s, 0, false); }
+
+void rhs_norm(saras_mg *h, cudaStream_t s) {
+    Level &v = h->lv[0];
+    kbegin(h, s, -1);
+    k_rhs_norm<<<h->norm_blocks, 256, 0, s>>>(v.rhs, v.lay, h->prm.res_type, h->norm_part);
+    kbegin(h, s, -1);
+    k_rhs_norm_final<<<1, 32, 0, s>>>(h->norm_part, h->norm_blocks, h->prm.res_type, h->norm_out + 4);
+}
+
+void coarsest_fast(saras_mg *h, cudaStream_t s, Level &c) {
+    const Lay &C = c.lay;
+    const size_t smem = (size_t)(4 * C.size) * sizeof(double);
+    if (smem > 200 * 1024) {  // coarsest grid too large for one block's shared memory
+        smooth(h, s, h->nl - 1, std::max(1, h->prm.pre_smooth), false);
+        return;
+    }
+    const int64_t cells = (int64_t)C.n0 * C.n1 * C.n2;
+    const int threads = cells <= 512 ? 32 : (cells <= 4096 ? 128 : 256);
+    const Bnd b = bnd(h);
+    kbegin(h, s, KC_COARSE);
+    if (h->d3)
+        k_coarsest_fast<true><<<1, threads, smem, s>>>(c.lhs, c.rhs, c.inv_diag, c.dd, C, tab64(c), b,
+                                                       1.0 - h->prm.sor_param, h->prm.mg_tolerance, h->maxCount(),
+                                                       h->coarse_sweeps);
+    else
+        k_coarsest_fast<false><<<1, threads, smem, s>>>(c.lhs, c.rhs, c.inv_diag, c.dd, C, tab64(c), b,
+                                                        1.0 - h->prm.sor_param, h->prm.mg_tolerance, h->maxCount(),
+                                                        h->coarse_sweeps);
+    kend(h, s, KC_COARSE);
+}
 
 void mixed_finish(saras_mg *h, cudaStream_t s) {
     if (singular(h)) {

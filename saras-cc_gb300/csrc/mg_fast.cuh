@@ -18,5 +18,7 @@ void mixed_prepare(saras_mg *h, cudaStream_t s);
 void mixed_finish(saras_mg *h, cudaStream_t s);
 void final_ghosts(saras_mg *h, cudaStream_t s);
 double kernel_bytes(const saras_mg *h, int kclass);
+void rhs_norm(saras_mg *h, cudaStream_t s);       // max|f| (or sums) of the solve, once
+void coarsest_fast(saras_mg *h, cudaStream_t s, Level &c);
 
 }  // namespace saras
