@@ -116,7 +116,7 @@ __global__ void k_ghost(double *u, Lay L, Ghost G, int axis, int wall_pass, int 
 __device__ __forceinline__ double warp_max(double v) {
     for (int o = 16; o > 0; o >>= 1) {
         const double w = __shfl_xor_sync(0xffffffffu, v, o);
-        v = w > v ? w : v;
+        v = (w > v || w != w) ? w : v;
     }
     return v;
 }
@@ -185,7 +185,7 @@ __global__ void k_norm_final(const double *__restrict__ part, int nb, int rtype,
     double mr = 0.0, mf = 0.0, sr = 0.0, sf = 0.0;
     for (int b = threadIdx.x; b < nb; b += 32) {
         const double a = part[4 * b], c = part[4 * b + 1];
-        if (a > mr) mr = a;
+        if (a > mr || a != a) mr = a;  // a NaN partial stays NaN (reported as SARAS_NAN)
         if (c > mf) mf = c;
         sr = radd(sr, part[4 * b + 2]);
         sf = radd(sf, part[4 * b + 3]);
@@ -732,8 +732,6 @@ void free_all(saras_mg *h) {
         cudaFree(v.inv_diag);
         cudaFree(v.inv_diag32);
         cudaFree(v.dd);
-        cudaFree(v.lhs_alt);
-        cudaFree(v.e32_alt);
     }
     cudaFree(h->walls);
     cudaFree(h->norm_part);
@@ -798,18 +796,6 @@ saras_status create(const saras_grid_desc *gd, const saras_mg_params *prm, void 
         }
         if (fast || (mixed && coarsest)) SARAS_TRY(dalloc(h, &v.inv_diag, sz));
         if (fast || (mixed && (l == 0 || coarsest))) SARAS_TRY(dalloc(h, &v.dd, sz));
-        // fused red-black iterations on the larger levels whose periodic
-        // extents are even (so the wrap keeps the colouring)
-        bool even = true;
-        const int nn[3] = {v.lay.n0, v.lay.n1, v.lay.n2};
-        for (int d = 0; d < 3; d++)
-            if (h->grid.active(d) && h->grid.per[d] && (nn[d] & 1)) even = false;
-        const int64_t cells = (int64_t)nn[0] * nn[1] * nn[2];
-        v.fused = (fast || mixed) && !coarsest && even && cells >= 4096 && nn[0] >= 4;
-        if (v.fused && fast) SARAS_TRY(dalloc(h, &v.lhs_alt, sz));
-        if (v.fused && mixed) SARAS_TRY(dalloc(h, &v.e32_alt, sz));
-        v.cur64 = v.lhs;
-        v.cur32 = v.e32;
     }
     SARAS_TRY(build_tables(h));
     SARAS_TRY(build_walls(h));

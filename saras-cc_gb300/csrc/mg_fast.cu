@@ -131,100 +131,127 @@ __global__ void k_rbgs32(float *e, const float *__restrict__ r, Lay L, Tab3<floa
     e[c] = fmat(omc, uc, __fdiv_rn(w * s, diag<float, D3>(t, i, j, k)));
 }
 
-// One full SOR red-black iteration (red then black) in a single pass.  The
-// previous iterate is read from `uo` and the new one written to `un`, so no
-// cell is read after another block has overwritten it.  A block owns a
-// (j,k) tile of TJ x TK cells and marches along i through a chunk of planes;
-// the new red values that black cells need (planes i-1, i, i+1 and a
-// one-cell halo in j,k) are computed once per plane into a shared ring.
-// Cells map to the red/black colours by their (i+j+k) parity, which the
-// periodic wrap preserves on even extents (the only ones this kernel runs).
-constexpr int FTJ = 8, FTK = 64, FTHREADS = 256;  // fused-iteration tile (j x k) and block size
+// Colour sweep with eight consecutive cells per thread along k: the rows a
+// strip needs (own, j+-1, i+-1, f and omega/D) are loaded as aligned 16-byte
+// vectors, so many loads are in flight per thread, and only the four cells of
+// the sweep's colour are stored.  Used when n_z is a multiple of 8; the core
+// of every row starts on a 32-byte boundary (Lay).
+template <class T>
+__device__ __forceinline__ void ld8(const T *__restrict__ p, T (&o)[8]);
+template <>
+__device__ __forceinline__ void ld8<float>(const float *__restrict__ p, float (&o)[8]) {
+    const float4 a = __ldg(reinterpret_cast<const float4 *>(p));
+    const float4 b = __ldg(reinterpret_cast<const float4 *>(p + 4));
+    o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+    o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w;
+}
+template <>
+__device__ __forceinline__ void ld8<double>(const double *__restrict__ p, double (&o)[8]) {
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const double2 a = __ldg(reinterpret_cast<const double2 *>(p + 2 * q));
+        o[2 * q] = a.x;
+        o[2 * q + 1] = a.y;
+    }
+}
+// plain (coherent) vector load for the array being updated in place
+template <class T>
+__device__ __forceinline__ void ld8u(const T *p, T (&o)[8]);
+template <>
+__device__ __forceinline__ void ld8u<float>(const float *p, float (&o)[8]) {
+    const float4 a = *reinterpret_cast<const float4 *>(p);
+    const float4 b = *reinterpret_cast<const float4 *>(p + 4);
+    o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+    o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w;
+}
+template <>
+__device__ __forceinline__ void ld8u<double>(const double *p, double (&o)[8]) {
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const double2 a = *reinterpret_cast<const double2 *>(p + 2 * q);
+        o[2 * q] = a.x;
+        o[2 * q + 1] = a.y;
+    }
+}
 
 template <class T>
-__device__ __forceinline__ bool wrap_index(int &g, int n, int per) {
-    if (g >= 0 && g < n) return true;
-    if (!per) return false;
-    g = g < 0 ? g + n : g - n;
-    return true;
+__device__ __forceinline__ void mirror8(const T (&cur)[8], int sg, T (&o)[8]) {
+#pragma unroll
+    for (int q = 0; q < 8; q++) o[q] = sg > 0 ? cur[q] : -cur[q];
+}
+
+template <class T, bool D3, bool WD, int T0>
+__device__ __forceinline__ void strip_update(T *u, const T (&cur)[8], const T (&xm)[8], const T (&xp)[8],
+                                             const T (&ym)[8], const T (&yp)[8], const T (&fr)[8], const T (&wv)[8],
+                                             T left, T right, const Tab3<T> &t, int i, int j, int k0, int64_t c0, T w,
+                                             T omc) {
+    const T cmx = t.cm[0][i], cpx = t.cp[0][i], dx = t.dg[0][i];
+    T cmy = T(0), cpy = T(0), dy = T(0);
+    if (D3) {
+        cmy = t.cm[1][j];
+        cpy = t.cp[1][j];
+        dy = t.dg[1][j];
+    }
+#pragma unroll
+    for (int q = T0; q < 8; q += 2) {
+        const int k = k0 + q;
+        const T zm = q > 0 ? cur[q - 1] : left;
+        const T zp = q < 7 ? cur[q + 1] : right;
+        T sm = cmx * xm[q];
+        sm = fmat(cpx, xp[q], sm);
+        if (D3) {
+            sm = fmat(cmy, ym[q], sm);
+            sm = fmat(cpy, yp[q], sm);
+        }
+        sm = fmat(t.cm[2][k], zm, sm);
+        sm = fmat(t.cp[2][k], zp, sm);
+        sm = sm - fr[q];
+        T v;
+        if (WD) {
+            v = fmat(sm, wv[q], omc * cur[q]);
+        } else {
+            T d = dx + t.dg[2][k];
+            if (D3) d += dy;
+            v = fmat(omc, cur[q], w * sm / (d + d));
+        }
+        u[c0 + q] = v;
+    }
 }
 
 template <class T, bool D3, bool WD>
-__global__ void __launch_bounds__(FTHREADS) k_rbgs_fused(const T *__restrict__ uo, T *__restrict__ un,
-                                                         const T *__restrict__ f, const T *__restrict__ wd, Lay L,
-                                                         Tab3<T> t, Bnd b, T w, T omc, int chunk) {
-    __shared__ T ring[3][FTJ + 2][FTK + 2];
-    const int k0 = blockIdx.x * FTK;
-    const int j0 = D3 ? (int)blockIdx.y * FTJ : 0;
-    const int a = (int)blockIdx.z * chunk;
-    const int e = min(a + chunk, L.n0);
-    const int tj_n = D3 ? FTJ + 2 : 1;  // planar: a single row of the ring
-    const int ring_n = tj_n * (FTK + 2);
-    for (int p = a - 1; p <= e; p++) {
-        // red values of plane p over the tile and its halo
-        int gi = p;
-        const bool plane_ok = wrap_index<T>(gi, L.n0, b.per[0]);
-        const int slot = (p + 3) % 3;
-        if (plane_ok) {
-            for (int q = threadIdx.x; q < ring_n; q += FTHREADS) {
-                const int jj = D3 ? q / (FTK + 2) - 1 : 0;
-                const int kk = q % (FTK + 2) - 1;
-                int gj = j0 + jj, gk = k0 + kk;
-                if (D3 && !wrap_index<T>(gj, L.n1, b.per[1])) continue;
-                if (!wrap_index<T>(gk, L.n2, b.per[2])) continue;
-                if ((gi + gj + gk) & 1) continue;
-                const int64_t c = L.at(gi, gj, gk);
-                const T uc = uo[c];
-                const T s = offdiag<T, D3>(uo, L, t, b, gi, gj, gk, c, uc) - f[c];
-                T v;
-                if (WD)
-                    v = fmat(s, wd[c], omc * uc);
-                else
-                    v = fmat(omc, uc, w * s / diag<T, D3>(t, gi, gj, gk));
-                ring[slot][D3 ? jj + 1 : 0][kk + 1] = v;
-            }
-        }
-        __syncthreads();
-        // black values of plane p-1 over the tile; both colours written
-        const int pb = p - 1;
-        if (pb >= a && pb < e) {
-            const int sm = (pb - 1 + 3) % 3, s0 = (pb + 3) % 3, sp = (pb + 1 + 3) % 3;
-            const int tile_n = (D3 ? FTJ : 1) * FTK;
-            for (int q = threadIdx.x; q < tile_n; q += FTHREADS) {
-                const int jj = D3 ? q / FTK : 0;
-                const int kk = q % FTK;
-                const int gj = j0 + jj, gk = k0 + kk;
-                if (gj >= L.n1 || gk >= L.n2) continue;
-                const int rj = D3 ? jj + 1 : 0, rk = kk + 1;
-                const int64_t c = L.at(pb, gj, gk);
-                if (((pb + gj + gk) & 1) == 0) {
-                    un[c] = ring[s0][rj][rk];
-                    continue;
-                }
-                const T uc = uo[c];
-                const T xm = (pb > 0 || b.per[0]) ? ring[sm][rj][rk] : (b.sg_lo[0] > 0 ? uc : -uc);
-                const T xp = (pb < L.n0 - 1 || b.per[0]) ? ring[sp][rj][rk] : (b.sg_hi[0] > 0 ? uc : -uc);
-                const T zm = (gk > 0 || b.per[2]) ? ring[s0][rj][rk - 1] : (b.sg_lo[2] > 0 ? uc : -uc);
-                const T zp = (gk < L.n2 - 1 || b.per[2]) ? ring[s0][rj][rk + 1] : (b.sg_hi[2] > 0 ? uc : -uc);
-                T sum = t.cm[0][pb] * xm;
-                sum = fmat(t.cp[0][pb], xp, sum);
-                if (D3) {
-                    const T ym = (gj > 0 || b.per[1]) ? ring[s0][rj - 1][rk] : (b.sg_lo[1] > 0 ? uc : -uc);
-                    const T yp = (gj < L.n1 - 1 || b.per[1]) ? ring[s0][rj + 1][rk] : (b.sg_hi[1] > 0 ? uc : -uc);
-                    sum = fmat(t.cm[1][gj], ym, sum);
-                    sum = fmat(t.cp[1][gj], yp, sum);
-                }
-                sum = fmat(t.cm[2][gk], zm, sum);
-                sum = fmat(t.cp[2][gk], zp, sum);
-                const T sv = sum - f[c];
-                if (WD)
-                    un[c] = fmat(sv, wd[c], omc * uc);
-                else
-                    un[c] = fmat(omc, uc, w * sv / diag<T, D3>(t, pb, gj, gk));
-            }
-        }
-        __syncthreads();
+__global__ void k_rbgs_v8(T *u, const T *__restrict__ f, const T *__restrict__ wd, Lay L, Tab3<T> t, Bnd b,
+                          int colour, T w, T omc) {
+    const int k0 = 8 * (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = D3 ? (int)(blockIdx.y * blockDim.y + threadIdx.y) : 0;
+    const int i = blockIdx.z;
+    if (k0 >= L.n2 || j >= L.n1) return;
+    const int64_t c0 = L.at(i, j, k0);
+    T cur[8], xm[8], xp[8], ym[8], yp[8], fr[8], wv[8];
+    ld8u(u + c0, cur);
+    if (i > 0) ld8u(u + c0 - L.s0, xm);
+    else if (b.per[0]) ld8u(u + c0 + (int64_t)(L.n0 - 1) * L.s0, xm);
+    else mirror8(cur, b.sg_lo[0], xm);
+    if (i < L.n0 - 1) ld8u(u + c0 + L.s0, xp);
+    else if (b.per[0]) ld8u(u + c0 - (int64_t)(L.n0 - 1) * L.s0, xp);
+    else mirror8(cur, b.sg_hi[0], xp);
+    if (D3) {
+        if (j > 0) ld8u(u + c0 - L.s1, ym);
+        else if (b.per[1]) ld8u(u + c0 + (int64_t)(L.n1 - 1) * L.s1, ym);
+        else mirror8(cur, b.sg_lo[1], ym);
+        if (j < L.n1 - 1) ld8u(u + c0 + L.s1, yp);
+        else if (b.per[1]) ld8u(u + c0 - (int64_t)(L.n1 - 1) * L.s1, yp);
+        else mirror8(cur, b.sg_hi[1], yp);
     }
+    ld8(f + c0, fr);
+    if (WD) ld8(wd + c0, wv);
+    const T left = k0 > 0 ? u[c0 - 1]
+                          : (b.per[2] ? u[c0 + L.n2 - 1] : (b.sg_lo[2] > 0 ? cur[0] : -cur[0]));
+    const T right = k0 + 8 < L.n2 ? u[c0 + 8]
+                                  : (b.per[2] ? u[c0 + 8 - L.n2] : (b.sg_hi[2] > 0 ? cur[7] : -cur[7]));
+    if (((colour + i + j + k0) & 1) == 0)
+        strip_update<T, D3, WD, 0>(u, cur, xm, xp, ym, yp, fr, wv, left, right, t, i, j, k0, c0, w, omc);
+    else
+        strip_update<T, D3, WD, 1>(u, cur, xm, xp, ym, yp, fr, wv, left, right, t, i, j, k0, c0, w, omc);
 }
 
 // Fused residual and restriction: one thread per coarse cell forms the
@@ -552,9 +579,34 @@ inline dim3 cgrid(const Lay &L, bool d3, int kcount, int bx) {
 }
 inline int bxfor(int n) { return std::min(BX, (n + 31) / 32 * 32); }
 
+// The eight-cells-per-thread sweep needs rows of whole strips.
+inline bool v8_ok(const Lay &L) { return L.n2 % 8 == 0 && L.n2 >= 16; }
+
+template <class T, bool WD>
+void colour_v8(saras_mg *h, cudaStream_t s, Level &v, T *u, const T *f, const T *wd, const Tab3<T> &tb, int colour,
+               T w, T omc) {
+    const Lay &L = v.lay;
+    const int strips = L.n2 / 8;
+    const int bx = std::min(strips, 32);
+    const int by = h->d3 ? std::max(1, 128 / bx) : 1;
+    const dim3 blk(bx, by);
+    const dim3 g(cdiv(strips, bx), h->d3 ? cdiv(L.n1, by) : 1u, (unsigned)L.n0);
+    const Bnd b = bnd(h);
+    if (h->d3)
+        k_rbgs_v8<T, true, WD><<<g, blk, 0, s>>>(u, f, wd, L, tb, b, colour, w, omc);
+    else
+        k_rbgs_v8<T, false, WD><<<g, blk, 0, s>>>(u, f, wd, L, tb, b, colour, w, omc);
+}
+
 void colour64(saras_mg *h, cudaStream_t s, int l, int colour) {
     Level &v = h->lv[(size_t)l];
     const Lay &L = v.lay;
+    if (v8_ok(L)) {
+        kbegin(h, s, l == 0 ? KC_SMOOTH0 : -1);
+        colour_v8<double, true>(h, s, v, v.lhs, v.rhs, v.inv_diag, tab64(v), colour, 0.0, 1.0 - h->prm.sor_param);
+        kend(h, s, l == 0 ? KC_SMOOTH0 : -1);
+        return;
+    }
     const int half = (L.n2 + 1) / 2, bx = bxfor(half);
     const double omc = 1.0 - h->prm.sor_param;
     const bool w1 = h->prm.sor_param == 1.0;
@@ -562,17 +614,17 @@ void colour64(saras_mg *h, cudaStream_t s, int l, int colour) {
     kbegin(h, s, l == 0 ? KC_SMOOTH0 : -1);
     if (h->d3) {
         if (w1)
-            k_rbgs64<true, true><<<cgrid(L, true, half, bx), bx, 0, s>>>(v.cur64, v.rhs, v.inv_diag, L, tab64(v),
+            k_rbgs64<true, true><<<cgrid(L, true, half, bx), bx, 0, s>>>(v.lhs, v.rhs, v.inv_diag, L, tab64(v),
                                                                          b, colour, omc);
         else
-            k_rbgs64<true, false><<<cgrid(L, true, half, bx), bx, 0, s>>>(v.cur64, v.rhs, v.inv_diag, L, tab64(v),
+            k_rbgs64<true, false><<<cgrid(L, true, half, bx), bx, 0, s>>>(v.lhs, v.rhs, v.inv_diag, L, tab64(v),
                                                                           b, colour, omc);
     } else {
         if (w1)
-            k_rbgs64<false, true><<<cgrid(L, false, half, bx), bx, 0, s>>>(v.cur64, v.rhs, v.inv_diag, L,
+            k_rbgs64<false, true><<<cgrid(L, false, half, bx), bx, 0, s>>>(v.lhs, v.rhs, v.inv_diag, L,
                                                                            tab64(v), b, colour, omc);
         else
-            k_rbgs64<false, false><<<cgrid(L, false, half, bx), bx, 0, s>>>(v.cur64, v.rhs, v.inv_diag, L,
+            k_rbgs64<false, false><<<cgrid(L, false, half, bx), bx, 0, s>>>(v.lhs, v.rhs, v.inv_diag, L,
                                                                             tab64(v), b, colour, omc);
     }
     kend(h, s, l == 0 ? KC_SMOOTH0 : -1);
@@ -581,14 +633,21 @@ void colour64(saras_mg *h, cudaStream_t s, int l, int colour) {
 void colour32(saras_mg *h, cudaStream_t s, int l, int colour) {
     Level &v = h->lv[(size_t)l];
     const Lay &L = v.lay;
+    if (v8_ok(L)) {
+        kbegin(h, s, l == 0 ? KC_SMOOTH0 : -1);
+        colour_v8<float, false>(h, s, v, v.e32, v.r32, (const float *)nullptr, tab32(v), colour,
+                                (float)h->prm.sor_param, (float)(1.0 - h->prm.sor_param));
+        kend(h, s, l == 0 ? KC_SMOOTH0 : -1);
+        return;
+    }
     const int half = (L.n2 + 1) / 2, bx = bxfor(half);
     const float w = (float)h->prm.sor_param, omc = (float)(1.0 - h->prm.sor_param);
     const Bnd b = bnd(h);
     kbegin(h, s, l == 0 ? KC_SMOOTH0 : -1);
     if (h->d3)
-        k_rbgs32<true><<<cgrid(L, true, half, bx), bx, 0, s>>>(v.cur32, v.r32, L, tab32(v), b, colour, w, omc);
+        k_rbgs32<true><<<cgrid(L, true, half, bx), bx, 0, s>>>(v.e32, v.r32, L, tab32(v), b, colour, w, omc);
     else
-        k_rbgs32<false><<<cgrid(L, false, half, bx), bx, 0, s>>>(v.cur32, v.r32, L, tab32(v), b, colour, w, omc);
+        k_rbgs32<false><<<cgrid(L, false, half, bx), bx, 0, s>>>(v.e32, v.r32, L, tab32(v), b, colour, w, omc);
     kend(h, s, l == 0 ? KC_SMOOTH0 : -1);
 }
 
@@ -615,24 +674,24 @@ void residual_restrict(saras_mg *h, cudaStream_t s, int l, bool mixed) {
     if (!mixed) {
         if (h->d3)
             k_resid_restrict<double, double, true><<<cgrid(Lc, true, Lc.n2, bx), bx, 0, s>>>(
-                f.cur64, f.rhs, f.lay, tab64(f), b, wt64(c), c.rhs, Lc, f.dd);
+                f.lhs, f.rhs, f.lay, tab64(f), b, wt64(c), c.rhs, Lc, f.dd);
         else
             k_resid_restrict<double, double, false><<<cgrid(Lc, false, Lc.n2, bx), bx, 0, s>>>(
-                f.cur64, f.rhs, f.lay, tab64(f), b, wt64(c), c.rhs, Lc, f.dd);
+                f.lhs, f.rhs, f.lay, tab64(f), b, wt64(c), c.rhs, Lc, f.dd);
     } else if (to64) {
         if (h->d3)
             k_resid_restrict<float, double, true><<<cgrid(Lc, true, Lc.n2, bx), bx, 0, s>>>(
-                f.cur32, f.r32, f.lay, tab32(f), b, wt32(c), c.rhs, Lc, nullptr);
+                f.e32, f.r32, f.lay, tab32(f), b, wt32(c), c.rhs, Lc, nullptr);
         else
             k_resid_restrict<float, double, false><<<cgrid(Lc, false, Lc.n2, bx), bx, 0, s>>>(
-                f.cur32, f.r32, f.lay, tab32(f), b, wt32(c), c.rhs, Lc, nullptr);
+                f.e32, f.r32, f.lay, tab32(f), b, wt32(c), c.rhs, Lc, nullptr);
     } else {
         if (h->d3)
             k_resid_restrict<float, float, true><<<cgrid(Lc, true, Lc.n2, bx), bx, 0, s>>>(
-                f.cur32, f.r32, f.lay, tab32(f), b, wt32(c), c.r32, Lc, nullptr);
+                f.e32, f.r32, f.lay, tab32(f), b, wt32(c), c.r32, Lc, nullptr);
         else
             k_resid_restrict<float, float, false><<<cgrid(Lc, false, Lc.n2, bx), bx, 0, s>>>(
-                f.cur32, f.r32, f.lay, tab32(f), b, wt32(c), c.r32, Lc, nullptr);
+                f.e32, f.r32, f.lay, tab32(f), b, wt32(c), c.r32, Lc, nullptr);
     }
     kend(h, s, l == 0 ? KC_RESTRICT : -1);
 }
@@ -645,55 +704,17 @@ void prolong_add(saras_mg *h, cudaStream_t s, int l, bool mixed) {
     const dim3 g(cdiv(L.n2, bx), (unsigned)L.n1, (unsigned)L.n0);
     kbegin(h, s, l == 1 ? KC_PROLONG : -1);
     if (!mixed)
-        k_prolong_add<double, double><<<g, bx, 0, s>>>(f.cur64, c.cur64, L, c.lay, h->d3 ? 1 : 0);
+        k_prolong_add<double, double><<<g, bx, 0, s>>>(f.lhs, c.lhs, L, c.lay, h->d3 ? 1 : 0);
     else if (l == h->nl - 1)
-        k_prolong_add<float, double><<<g, bx, 0, s>>>(f.cur32, c.lhs, L, c.lay, h->d3 ? 1 : 0);
+        k_prolong_add<float, double><<<g, bx, 0, s>>>(f.e32, c.lhs, L, c.lay, h->d3 ? 1 : 0);
     else
-        k_prolong_add<float, float><<<g, bx, 0, s>>>(f.cur32, c.cur32, L, c.lay, h->d3 ? 1 : 0);
+        k_prolong_add<float, float><<<g, bx, 0, s>>>(f.e32, c.e32, L, c.lay, h->d3 ? 1 : 0);
     kend(h, s, l == 1 ? KC_PROLONG : -1);
 }
 
-// One fused iteration: current buffer -> partner, then they swap roles.
-void fused_iteration(saras_mg *h, cudaStream_t s, int l, bool mixed) {
-    Level &v = h->lv[(size_t)l];
-    const Lay &L = v.lay;
-    const Bnd b = bnd(h);
-    const unsigned tk = cdiv(L.n2, FTK), tj = h->d3 ? cdiv(L.n1, FTJ) : 1u;
-    const int tiles = (int)(tk * tj);
-    const int nchunk = std::max(1, std::min(L.n0 / 4, (1216 + tiles - 1) / tiles));
-    const int chunk = (L.n0 + nchunk - 1) / nchunk;
-    const dim3 g(tk, tj, cdiv(L.n0, chunk));
-    kbegin(h, s, l == 0 ? KC_SMOOTH0 : -1);
-    if (mixed) {
-        float *dst = v.cur32 == v.e32 ? v.e32_alt : v.e32;
-        const float w = (float)h->prm.sor_param, omc = (float)(1.0 - h->prm.sor_param);
-        if (h->d3)
-            k_rbgs_fused<float, true, false><<<g, FTHREADS, 0, s>>>(v.cur32, dst, v.r32, nullptr, L, tab32(v), b, w,
-                                                                    omc, chunk);
-        else
-            k_rbgs_fused<float, false, false><<<g, FTHREADS, 0, s>>>(v.cur32, dst, v.r32, nullptr, L, tab32(v), b,
-                                                                     w, omc, chunk);
-        v.cur32 = dst;
-    } else {
-        double *dst = v.cur64 == v.lhs ? v.lhs_alt : v.lhs;
-        const double omc = 1.0 - h->prm.sor_param;
-        if (h->d3)
-            k_rbgs_fused<double, true, true><<<g, FTHREADS, 0, s>>>(v.cur64, dst, v.rhs, v.inv_diag, L, tab64(v),
-                                                                    b, 0.0, omc, chunk);
-        else
-            k_rbgs_fused<double, false, true><<<g, FTHREADS, 0, s>>>(v.cur64, dst, v.rhs, v.inv_diag, L, tab64(v),
-                                                                     b, 0.0, omc, chunk);
-        v.cur64 = dst;
-    }
-    kend(h, s, l == 0 ? KC_SMOOTH0 : -1);
-}
-
 void smooth(saras_mg *h, cudaStream_t s, int l, int count, bool mixed) {
-    Level &v = h->lv[(size_t)l];
     for (int n = 0; n < count; n++) {
-        if (v.fused) {
-            fused_iteration(h, s, l, mixed);
-        } else if (mixed) {
+        if (mixed) {
             colour32(h, s, l, 0);
             colour32(h, s, l, 1);
         } else {
@@ -775,10 +796,6 @@ saras_status fast_setup(saras_mg *h) {
 void fast_cycle(saras_mg *h, cudaStream_t s) {
     const bool mixed = h->prm.precision == SARAS_PREC_MIXED;
     const int top = h->nl - 1;
-    for (Level &v : h->lv) {
-        v.cur64 = v.lhs;
-        v.cur32 = v.e32;
-    }
     if (mixed) {
         // error equation at the finest level starts from zero
         Level &v0 = h->lv[0];
@@ -812,14 +829,7 @@ void fast_cycle(saras_mg *h, cudaStream_t s) {
         const Lay &L = v0.lay;
         const int bx = bxfor(L.n2);
         kbegin(h, s, -1);
-        k_update64<<<dim3(cdiv(L.n2, bx), (unsigned)L.n1, (unsigned)L.n0), bx, 0, s>>>(v0.lhs, v0.cur32, L);
-    } else {
-        Level &v0 = h->lv[0];
-        if (v0.cur64 != v0.lhs) {  // odd number of fused iterations: the solution returns to its own array
-            kbegin(h, s, -1);
-            cudaMemcpyAsync(v0.lhs, v0.cur64, (size_t)v0.lay.size * sizeof(double), cudaMemcpyDeviceToDevice, s);
-            v0.cur64 = v0.lhs;
-        }
+        k_update64<<<dim3(cdiv(L.n2, bx), (unsigned)L.n1, (unsigned)L.n0), bx, 0, s>>>(v0.lhs, v0.e32, L);
     }
     resid_norm(h, s, mixed);
 }

@@ -34,14 +34,6 @@ struct Level {
     double *inv_diag = nullptr;  // FP64 form: omega / D per cell
     double *dd = nullptr;        // FP64 forms: the diagonal D = 2 sum(xix2*ihx2) per cell
     float *inv_diag32 = nullptr; // MIXED form: omega / D per cell
-    // ping-pong partners of lhs / e32 for the fused red-black iteration, and
-    // the buffer that holds the level's current iterate while a cycle is
-    // being issued (the order of buffers is the same in every cycle)
-    double *lhs_alt = nullptr;
-    float *e32_alt = nullptr;
-    double *cur64 = nullptr;
-    float *cur32 = nullptr;
-    bool fused = false;
 };
 
 enum KClass { KC_SMOOTH0 = 0, KC_RESTRICT = 1, KC_PROLONG = 2, KC_NORM = 3, KC_COARSE = 4, KC_COUNT = 5 };

@@ -96,13 +96,19 @@ FAST_CASES = [c for c in EXACT_CASES if "bc_kind" not in c[2] or 2 not in c[2]["
 
 @pytest.mark.parametrize("name,gk,mk", FAST_CASES, ids=[c[0] for c in FAST_CASES])
 def test_fp64_matches_oracle(name, gk, mk):
+    """Reassociated FP64 (FMA, folded coefficients) against the reference
+    order after six unconverged cycles: rounding differences stay within
+    1e-10 of the solution's scale (constant null-space mode removed on
+    all-Neumann problems)."""
     g, gpu, hist, orc, r = _run_both(gk, mk, S.PREC_FP64, cycles=6)
     a, b = core(gpu, g), core(orc, g)
+    if all(k == 0 for k in mk.get("bc_kind", [0] * 6)):
+        a, b = demean(a), demean(b)
     scale = np.abs(b).max()
-    assert np.abs(a - b).max() <= 1e-11 * scale
+    assert np.abs(a - b).max() <= 1e-10 * scale
     np.testing.assert_allclose(hist[:3], r.history[:3], rtol=1e-8)
     # ghost layer follows the same boundary rules
-    np.testing.assert_allclose(gpu, orc, rtol=0, atol=1e-11 * scale)
+    np.testing.assert_allclose(gpu, orc, rtol=0, atol=1e-9 * np.abs(orc).max())
 
 
 # Configurations on which the reference V-cycle reaches 1e-10 within the
