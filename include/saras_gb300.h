@@ -195,6 +195,68 @@ saras_status saras_rk3_step(saras_rk3 *h, int32_t nsteps, int32_t *mg_cycles, in
 saras_status saras_rk3_destroy(saras_rk3 *h);
 int64_t saras_rk3_last_launches(const saras_rk3 *h);
 
+/* ------------------------------------------------------------ serving ---- */
+/*
+ * Continuous batching of independent Poisson requests (no counterpart in the
+ * reference, which solves one problem per MPI job): every admitted request
+ * keeps its MIXED-form hierarchy resident in HBM, and one graph launch runs
+ * one outer iteration (FP32 V-cycle + FP64 residual) of ALL admitted
+ * requests.  Requests are admitted while case slots and the HBM budget allow
+ * and retire when their relative residual (max|r| / max|f|) falls below
+ * `tolerance`.  Each request's arithmetic is independent of the others and
+ * of the schedule, so its result is the same alone and in any mix, and the
+ * same as saras_mg_solve in the MIXED form with the engine's parameters.
+ * Walls are Neumann on every non-periodic face.
+ */
+typedef struct saras_serve_params {
+    int64_t hbm_budget_bytes; /* resident hierarchies (pooled ones included) */
+    int32_t max_cases;        /* requests admitted at once (1..4096) */
+    int32_t max_cycles;       /* outer iterations before NOT_CONVERGED */
+    double tolerance;         /* relative residual that retires a request */
+    double mg_tolerance;      /* coarsest-level absolute tolerance */
+    double sor_param;
+    int32_t pre_smooth, post_smooth;
+    /* schedule (0 = default): cells per work item, threads per block,
+     * blocks per SM of the batched kernels; saras_serve_autotune sets them */
+    int32_t cells_per_item, threads, blocks_per_sm;
+    int32_t pad_;
+} saras_serve_params;
+
+typedef struct saras_serve_stats {
+    int64_t bytes_allocated; /* device bytes of resident + pooled hierarchies */
+    int64_t batched_cycles;  /* graph launches (outer iterations of the batch) */
+    int64_t launches;        /* kernels launched by those graphs */
+    int64_t admitted, retired;
+    int32_t active, pending, pooled, max_active;
+} saras_serve_stats;
+
+typedef struct saras_serve saras_serve;
+
+void saras_serve_default_params(saras_serve_params *p);
+saras_status saras_serve_create(const saras_serve_params *prm, saras_serve **out);
+/* Queues a request.  rhs and lhs are dense padded host boxes of the grid
+ * (pad from the descriptor, k fastest) that must stay valid until the
+ * request is returned by saras_serve_poll; lhs receives the solution core and
+ * its ghost layer. */
+saras_status saras_serve_submit(saras_serve *h, int64_t id, const saras_grid_desc *grid,
+                                const double *rhs, double *lhs);
+/* Admits what fits, runs one batched outer iteration, retires finished
+ * requests.  *active / *pending (may be NULL) receive the counts after it. */
+saras_status saras_serve_step(saras_serve *h, int32_t *active, int32_t *pending);
+/* Up to cap finished requests, oldest first: id, final relative residual,
+ * outer iterations, status (OK, NOT_CONVERGED, NAN, ...) and seconds from
+ * submit to retirement.  Any output pointer may be NULL. */
+saras_status saras_serve_poll(saras_serve *h, int64_t *ids, double *residuals, int32_t *cycles,
+                              int32_t *status, double *latency_s, int32_t cap, int32_t *n);
+/* Times `cycles` batched iterations of synthetic requests of the given
+ * shapes under each candidate schedule, keeps the fastest (written to
+ * *chosen when not NULL) and leaves the hierarchies pooled.  The engine
+ * must be idle (nothing active or pending). */
+saras_status saras_serve_autotune(saras_serve *h, const saras_grid_desc *grids, int32_t n,
+                                  int32_t cycles, saras_serve_params *chosen);
+saras_status saras_serve_get_stats(const saras_serve *h, saras_serve_stats *out);
+saras_status saras_serve_destroy(saras_serve *h);
+
 /* ------------------------------------------------------------- common ---- */
 
 const char *saras_status_string(saras_status s);

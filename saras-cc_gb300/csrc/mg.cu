@@ -583,7 +583,10 @@ saras_status dalloc(saras_mg *h, T **p, int64_t count) {
     return SARAS_OK;
 }
 
-saras_status build_tables(saras_mg *h) {
+// Builds the per-level 1-D tables.  On a retarget (new stretching, same
+// extents) the device tables are reused and refilled asynchronously on the
+// handle's stream from its pinned staging buffer.
+saras_status build_tables(saras_mg *h, bool async = false) {
     const HostGrid &g = h->grid;
     for (int l = 0; l < h->nl; l++) {
         Level &v = h->lv[(size_t)l];
@@ -594,9 +597,9 @@ saras_status build_tables(saras_mg *h) {
         int64_t total = 0;
         for (int d = 0; d < 3; d++) total += (int64_t)per_axis * n[d];
         std::vector<double> host((size_t)total, 0.0);
-        SARAS_TRY(dalloc(h, &v.tab, total));
+        if (!v.tab) SARAS_TRY(dalloc(h, &v.tab, total));
         std::vector<float> host32((size_t)total, 0.f);
-        SARAS_TRY(dalloc(h, &v.tab32, total));
+        if (!v.tab32) SARAS_TRY(dalloc(h, &v.tab32, total));
         int64_t off = 0;
         const double *dp[3][per_axis];
         const float *fp[3][per_axis];
@@ -635,8 +638,22 @@ saras_status build_tables(saras_mg *h) {
             }
             off += (int64_t)per_axis * n[d];
         }
-        SARAS_CUDA(cudaMemcpy(v.tab, host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice));
-        SARAS_CUDA(cudaMemcpy(v.tab32, host32.data(), host32.size() * sizeof(float), cudaMemcpyHostToDevice));
+        if (async) {
+            const size_t b64 = host.size() * sizeof(double), b32 = host32.size() * sizeof(float);
+            if (!h->tab_stage || h->tab_stage_bytes < h->tab_stage_used + b64 + b32) {
+                set_error("table staging buffer too small");
+                return SARAS_BAD_ARG;
+            }
+            char *st64 = h->tab_stage + h->tab_stage_used;
+            std::memcpy(st64, host.data(), b64);
+            std::memcpy(st64 + b64, host32.data(), b32);
+            h->tab_stage_used += (b64 + b32 + 255) / 256 * 256;
+            SARAS_CUDA(cudaMemcpyAsync(v.tab, st64, b64, cudaMemcpyHostToDevice, h->stream));
+            SARAS_CUDA(cudaMemcpyAsync(v.tab32, st64 + b64, b32, cudaMemcpyHostToDevice, h->stream));
+        } else {
+            SARAS_CUDA(cudaMemcpy(v.tab, host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice));
+            SARAS_CUDA(cudaMemcpy(v.tab32, host32.data(), host32.size() * sizeof(float), cudaMemcpyHostToDevice));
+        }
         v.coef = Coef{dp[0][0], dp[0][1], dp[1][0], dp[1][1], dp[2][0], dp[2][1]};
         v.rt = RTab{dp[0][5], dp[0][6], dp[0][7], dp[1][5], dp[1][6], dp[1][7], dp[2][5], dp[2][6], dp[2][7]};
         for (int d = 0; d < 3; d++) {
@@ -725,8 +742,6 @@ void free_all(saras_mg *h) {
         cudaFree(v.smd);
         cudaFree(v.e32);
         cudaFree(v.r32);
-        cudaFree(v.t32);
-        cudaFree(v.s32);
         cudaFree(v.tab);
         cudaFree(v.tab32);
         cudaFree(v.inv_diag);
@@ -741,9 +756,30 @@ void free_all(saras_mg *h) {
     cudaFree(h->stage_rhs);
     cudaFree(h->mix_scalar);
     if (h->norm_host) cudaFreeHost(h->norm_host);
+    if (h->tab_stage) cudaFreeHost(h->tab_stage);
     if (h->graph) cudaGraphExecDestroy(h->graph);
     for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
     if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
+}
+
+// Per-level device arrays of each form: FP64 u and f (every level in the
+// FP64 forms; the finest and the coarsest in MIXED), FP64 scratch for the
+// exact form's separate residual and smoothed copy, the FP32 error and
+// residual of MIXED's inner levels, and the stored omega/D and D.
+struct LevelArrays {
+    bool u_f, scratch, e_r32, inv_diag, dd;
+};
+
+LevelArrays level_arrays(int precision, int l, int nl) {
+    const bool mixed = precision == SARAS_PREC_MIXED, fast = precision == SARAS_PREC_FP64;
+    const bool coarsest = l == nl - 1;
+    LevelArrays a;
+    a.u_f = !mixed || l == 0 || coarsest;
+    a.scratch = precision == SARAS_PREC_FP64_EXACT;
+    a.e_r32 = mixed && !coarsest;
+    a.inv_diag = fast || (mixed && coarsest);
+    a.dd = fast || (mixed && (l == 0 || coarsest));
+    return a;
 }
 
 saras_status create(const saras_grid_desc *gd, const saras_mg_params *prm, void *stream, saras_mg *h) {
@@ -762,40 +798,34 @@ saras_status create(const saras_grid_desc *gd, const saras_mg_params *prm, void 
     for (int d = 0; d < 3; d++) h->ghost.per[d] = h->grid.per[d] ? 1 : 0;
     for (int f = 0; f < 6; f++) h->ghost.kind[f] = prm->bc_kind[f];
     h->lv.resize((size_t)h->nl);
-    const bool mixed = prm->precision == SARAS_PREC_MIXED;
-    if (mixed && h->nl < 2) {
+    if (prm->precision == SARAS_PREC_MIXED && h->nl < 2) {
         set_error("the MIXED form needs at least two levels");
         return SARAS_BAD_ARG;
     }
-    const bool fast = prm->precision == SARAS_PREC_FP64;
     for (int l = 0; l < h->nl; l++) {
         Level &v = h->lv[(size_t)l];
         const AxisLevel *a = h->grid.lv[(size_t)l].data();
         v.lay = make_lay(a[0].n, h->d3 ? a[1].n : 1, a[2].n);
         const int64_t sz = v.lay.size;
-        const bool coarsest = l == h->nl - 1;
-        if (!mixed || l == 0 || coarsest) {
+        const LevelArrays use = level_arrays(prm->precision, l, h->nl);
+        if (use.u_f) {
             SARAS_TRY(dalloc(h, &v.lhs, sz));
             SARAS_TRY(dalloc(h, &v.rhs, sz));
             SARAS_CUDA(cudaMemset(v.lhs, 0, (size_t)sz * sizeof(double)));
             SARAS_CUDA(cudaMemset(v.rhs, 0, (size_t)sz * sizeof(double)));
         }
-        if (!mixed) {
+        if (use.scratch) {
             SARAS_TRY(dalloc(h, &v.tmp, sz));
             SARAS_TRY(dalloc(h, &v.smd, sz));
         }
-        if (mixed && !coarsest) {
+        if (use.e_r32) {
             SARAS_TRY(dalloc(h, &v.e32, sz));
             SARAS_TRY(dalloc(h, &v.r32, sz));
-            SARAS_TRY(dalloc(h, &v.s32, sz));
             SARAS_CUDA(cudaMemset(v.e32, 0, (size_t)sz * sizeof(float)));
             SARAS_CUDA(cudaMemset(v.r32, 0, (size_t)sz * sizeof(float)));
         }
-        if (mixed && coarsest) {
-            SARAS_TRY(dalloc(h, &v.tmp, sz));  // FP64 coarse residual scratch
-        }
-        if (fast || (mixed && coarsest)) SARAS_TRY(dalloc(h, &v.inv_diag, sz));
-        if (fast || (mixed && (l == 0 || coarsest))) SARAS_TRY(dalloc(h, &v.dd, sz));
+        if (use.inv_diag) SARAS_TRY(dalloc(h, &v.inv_diag, sz));
+        if (use.dd) SARAS_TRY(dalloc(h, &v.dd, sz));
     }
     SARAS_TRY(build_tables(h));
     SARAS_TRY(build_walls(h));
@@ -815,14 +845,12 @@ saras_status create(const saras_grid_desc *gd, const saras_mg_params *prm, void 
     h->stage_st[1] = L0.n2 + 2 * p;
     h->stage_st[0] = h->stage_st[1] * (L0.n1 + 2 * py);
     h->stage_elems = h->stage_st[0] * (L0.n0 + 2 * p);
-    SARAS_TRY(dalloc(h, &h->stage_lhs, h->stage_elems));
-    SARAS_TRY(dalloc(h, &h->stage_rhs, h->stage_elems));
     SARAS_CUDA(cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking));
     SARAS_CUDA(cudaFuncSetAttribute(k_coarsest_exact<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)COARSE_SMEM_LIMIT));
     SARAS_CUDA(cudaFuncSetAttribute(k_coarsest_exact<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)COARSE_SMEM_LIMIT));
-    if (fast || mixed) SARAS_TRY(fast_setup(h));
+    if (prm->precision != SARAS_PREC_FP64_EXACT) SARAS_TRY(fast_setup(h));
     SARAS_CUDA(cudaDeviceSynchronize());
     return SARAS_OK;
 }
@@ -951,6 +979,81 @@ saras_status solve_common(saras_mg *h, double *lhs, const double *rhs, const int
 
 namespace saras {
 
+// Device bytes saras_mg_create allocates for a grid and form (the host
+// solve's staging boxes, made on first use, excluded), from the same
+// per-level rule; the serving engine admits against it.
+int64_t mg_estimate_bytes(const saras_grid_desc *gd, const saras_mg_params *prm) {
+    HostGrid g;
+    if (g.build(*gd, prm->levels) != SARAS_OK) return -1;
+    const bool d3 = g.dims == 3;
+    int64_t bytes = 0;
+    int64_t cells0 = 0;
+    for (int l = 0; l < g.levels; l++) {
+        const AxisLevel *a = g.lv[(size_t)l].data();
+        const Lay L = make_lay(a[0].n, d3 ? a[1].n : 1, a[2].n);
+        if (l == 0) cells0 = (int64_t)L.n0 * L.n1 * L.n2;
+        const LevelArrays u = level_arrays(prm->precision, l, g.levels);
+        bytes += L.size * (16 * u.u_f + 16 * u.scratch + 8 * u.e_r32 + 8 * u.inv_diag + 8 * u.dd);
+        bytes += (int64_t)10 * (L.n0 + L.n1 + L.n2) * 12;  // 1-D tables, FP64 and FP32
+        if (l == 0) {
+            bool walls = false;
+            for (int f = 0; f < 6; f++) walls = walls || prm->bc_kind[f] == SARAS_BC_DIRICHLET_TEST;
+            if (walls)
+                bytes += 8 * ((int64_t)(L.n1 + 2) * (L.n2 + 2) + (int64_t)(L.n0 + 2) * (L.n2 + 2) +
+                              (int64_t)(L.n0 + 2) * (L.n1 + 2));
+        }
+    }
+    const int64_t nb = std::max<int64_t>(1, std::min<int64_t>(1216, (cells0 + 255) / 256));
+    bytes += 32 * nb + 8 * 8 + 4 * 4 + 16 * 8;
+    return bytes;
+}
+
+// Re-points a handle at a grid with the same extents, periodicity and depth
+// but other stretching (serving engine: hierarchies are reused across
+// requests of one shape).  Tables and per-cell diagonals are refilled on the
+// handle's stream; no allocation.
+saras_status mg_retarget(saras_mg *h, const saras_grid_desc *gd) {
+    HostGrid g;
+    SARAS_TRY(g.build(*gd, h->prm.levels));
+    if (g.levels != h->nl || g.dims != h->grid.dims || g.pad != h->grid.pad) return SARAS_BAD_ARG;
+    for (int d = 0; d < 3; d++)
+        if (g.N[d] != h->grid.N[d] || g.per[d] != h->grid.per[d]) return SARAS_BAD_ARG;
+    if (!h->tab_stage) {
+        size_t bytes = 0;
+        for (const Level &v : h->lv) bytes += (size_t)10 * (v.lay.n0 + v.lay.n1 + v.lay.n2) * 12 + 512;
+        SARAS_CUDA(cudaMallocHost((void **)&h->tab_stage, bytes));
+        h->tab_stage_bytes = bytes;
+    }
+    h->tab_stage_used = 0;
+    h->grid = g;
+    SARAS_TRY(build_tables(h, true));
+    return fast_setup(h);
+}
+
+// Finest-level fields of a resident handle: zero initial guess and the RHS
+// core from a dense padded device box (serving admissions).
+saras_status mg_load_rhs(saras_mg *h, const double *rhs_box_origin, const int64_t st[3]) {
+    cudaStream_t s = h->stream;
+    Level &v0 = h->lv[0];
+    const Lay &L = v0.lay;
+    SARAS_CUDA(cudaMemsetAsync(v0.lhs, 0, (size_t)L.size * sizeof(double), s));
+    SARAS_CUDA(cudaMemsetAsync(v0.rhs, 0, (size_t)L.size * sizeof(double), s));
+    const int bx = std::min(BX, (L.n2 + 31) / 32 * 32);
+    k_scatter<<<dim3(cdiv(L.n2, bx), (unsigned)L.n1, (unsigned)L.n0), bx, 0, s>>>(
+        rhs_box_origin, rhs_box_origin, st[0], st[1], st[2], v0.lhs, v0.rhs, L);
+    SARAS_CUDA(cudaMemsetAsync(v0.lhs, 0, (size_t)L.size * sizeof(double), s));
+    return SARAS_OK;
+}
+
+// Core plus one ghost layer of the finest lhs into a dense padded device box.
+void mg_store_lhs(saras_mg *h, double *box_origin, const int64_t st[3]) {
+    Level &v0 = h->lv[0];
+    const Lay &L = v0.lay;
+    const int gbx = std::min(BX, (L.n2 + 2 + 31) / 32 * 32);
+    k_gather<<<dim3(cdiv(L.n2 + 2, gbx), (unsigned)L.n1 + 2, (unsigned)L.n0 + 2), gbx, 0, h->stream>>>(
+        v0.lhs, L, box_origin, st[0], st[1], st[2]);
+}
+
 // mgSolve on the finest-level arrays as they stand: the caller has written
 // the RHS core into lv[0].rhs and keeps the initial guess in lv[0].lhs.
 // Used by the RK3 integrator, whose pressure correction lives there.
@@ -1028,6 +1131,10 @@ saras_status saras_mg_solve(saras_mg *h, double *lhs, const double *rhs, const i
     const int64_t origin = p * h->stage_st[0] + py * h->stage_st[1] + p;
     const size_t bytes = (size_t)h->stage_elems * sizeof(double);
     cudaStream_t s = h->stream;
+    if (!h->stage_lhs) {  // device copies of the caller's boxes, made on first use
+        SARAS_TRY(dalloc(h, &h->stage_lhs, h->stage_elems));
+        SARAS_TRY(dalloc(h, &h->stage_rhs, h->stage_elems));
+    }
     SARAS_CUDA(cudaMemcpyAsync(h->stage_lhs, lhs - origin, bytes, cudaMemcpyHostToDevice, s));
     SARAS_CUDA(cudaMemcpyAsync(h->stage_rhs, rhs - origin, bytes, cudaMemcpyHostToDevice, s));
     saras_status st = solve_common(h, h->stage_lhs + origin, h->stage_rhs + origin, h->stage_st, res_hist,

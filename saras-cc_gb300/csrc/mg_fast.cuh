@@ -21,4 +21,10 @@ double kernel_bytes(const saras_mg *h, int kclass);
 void rhs_norm(saras_mg *h, cudaStream_t s);       // max|f| (or sums) of the solve, once
 void coarsest_fast(saras_mg *h, cudaStream_t s, Level &c);
 
+// mg.cu: handle reuse by the serving engine
+saras_status mg_retarget(saras_mg *h, const saras_grid_desc *gd);
+saras_status mg_load_rhs(saras_mg *h, const double *rhs_box_origin, const int64_t st[3]);
+void mg_store_lhs(saras_mg *h, double *box_origin, const int64_t st[3]);
+int64_t mg_estimate_bytes(const saras_grid_desc *gd, const saras_mg_params *prm);
+
 }  // namespace saras

@@ -15,7 +15,7 @@ namespace saras {
 struct Level {
     Lay lay;
     double *lhs = nullptr, *rhs = nullptr, *tmp = nullptr, *smd = nullptr;
-    float *e32 = nullptr, *r32 = nullptr, *t32 = nullptr, *s32 = nullptr;
+    float *e32 = nullptr, *r32 = nullptr;
     double *tab = nullptr;  // all 1-D tables of the level in one allocation
     Coef coef{};
     RTab rt{};
@@ -82,4 +82,7 @@ struct saras_mg {
     double kc_bytes[saras::KC_COUNT] = {0, 0, 0, 0, 0};
     int64_t issued = 0;  // launches issued while recording the current sequence
     int maxCount() const;  // coarsest-level iteration limit (poisson.cc:430-436)
+    // pinned staging of table refills (serving retargets)
+    char *tab_stage = nullptr;
+    size_t tab_stage_bytes = 0, tab_stage_used = 0;
 };

@@ -384,6 +384,139 @@ class RK3:
             pass
 
 
+class ServeParams(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_int64), ("max_cases", C.c_int32), ("max_cycles", C.c_int32),
+                ("tolerance", C.c_double), ("mg_tolerance", C.c_double), ("sor_param", C.c_double),
+                ("pre_smooth", C.c_int32), ("post_smooth", C.c_int32),
+                ("cells_per_item", C.c_int32), ("threads", C.c_int32), ("blocks_per_sm", C.c_int32),
+                ("pad_", C.c_int32)]
+
+
+class ServeStats(C.Structure):
+    _fields_ = [("bytes_allocated", C.c_int64), ("batched_cycles", C.c_int64), ("launches", C.c_int64),
+                ("admitted", C.c_int64), ("retired", C.c_int64), ("active", C.c_int32),
+                ("pending", C.c_int32), ("pooled", C.c_int32), ("max_active", C.c_int32)]
+
+
+_serve_bound = False
+
+
+def _bind_serve(lib):
+    global _serve_bound
+    if _serve_bound:
+        return lib
+    vp, i32, i64, dp = C.c_void_p, C.c_int32, C.c_int64, C.POINTER(C.c_double)
+    lib.saras_serve_default_params.argtypes = [C.POINTER(ServeParams)]
+    lib.saras_serve_default_params.restype = None
+    lib.saras_serve_create.argtypes = [C.POINTER(ServeParams), C.POINTER(vp)]
+    lib.saras_serve_create.restype = C.c_int
+    lib.saras_serve_submit.argtypes = [vp, i64, C.POINTER(GridDesc), vp, vp]
+    lib.saras_serve_submit.restype = C.c_int
+    lib.saras_serve_step.argtypes = [vp, C.POINTER(i32), C.POINTER(i32)]
+    lib.saras_serve_step.restype = C.c_int
+    lib.saras_serve_poll.argtypes = [vp, C.POINTER(i64), dp, C.POINTER(i32), C.POINTER(i32), dp, i32,
+                                     C.POINTER(i32)]
+    lib.saras_serve_poll.restype = C.c_int
+    lib.saras_serve_autotune.argtypes = [vp, C.POINTER(GridDesc), i32, i32, C.POINTER(ServeParams)]
+    lib.saras_serve_autotune.restype = C.c_int
+    lib.saras_serve_get_stats.argtypes = [vp, C.POINTER(ServeStats)]
+    lib.saras_serve_get_stats.restype = C.c_int
+    lib.saras_serve_destroy.argtypes = [vp]
+    lib.saras_serve_destroy.restype = C.c_int
+    _serve_bound = True
+    return lib
+
+
+def serve_params(**kw) -> ServeParams:
+    lib = _bind_serve(load())
+    p = ServeParams()
+    lib.saras_serve_default_params(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+class Serve:
+    """Continuous-batching engine of independent Poisson requests (MIXED
+    form, all admitted requests advanced by one graph launch per step).
+    Request buffers are padded host fields (``padded_field(grid)``) that
+    must stay alive until the request is returned by ``poll``."""
+
+    def __init__(self, params: ServeParams | None = None):
+        self.lib = _bind_serve(load())
+        self.params = params or serve_params()
+        h = C.c_void_p()
+        check(self.lib.saras_serve_create(C.byref(self.params), C.byref(h)), "saras_serve_create")
+        self.h = h
+        self._keep = {}
+
+    def submit(self, rid: int, grid: GridDesc, rhs: np.ndarray, lhs: np.ndarray):
+        for a in (rhs, lhs):
+            if a.dtype != np.float64 or not a.flags.c_contiguous or a.shape != padded_field(grid).shape:
+                raise ValueError("request fields must be C-contiguous float64 padded boxes of the grid")
+        check(self.lib.saras_serve_submit(self.h, rid, C.byref(grid), C.c_void_p(rhs.ctypes.data),
+                                          C.c_void_p(lhs.ctypes.data)), "saras_serve_submit")
+        self._keep[rid] = (grid, rhs, lhs)
+
+    def step(self):
+        a, p = C.c_int32(), C.c_int32()
+        check(self.lib.saras_serve_step(self.h, C.byref(a), C.byref(p)), "saras_serve_step")
+        return a.value, p.value
+
+    def poll(self, cap: int = 4096):
+        ids = np.zeros(cap, np.int64)
+        res = np.zeros(cap)
+        cyc = np.zeros(cap, np.int32)
+        st = np.zeros(cap, np.int32)
+        lat = np.zeros(cap)
+        n = C.c_int32()
+        i32p = C.POINTER(C.c_int32)
+        dp = C.POINTER(C.c_double)
+        check(self.lib.saras_serve_poll(self.h, ids.ctypes.data_as(C.POINTER(C.c_int64)), res.ctypes.data_as(dp),
+                                        cyc.ctypes.data_as(i32p), st.ctypes.data_as(i32p),
+                                        lat.ctypes.data_as(dp), cap, C.byref(n)), "saras_serve_poll")
+        out = []
+        for q in range(n.value):
+            rid = int(ids[q])
+            self._keep.pop(rid, None)
+            out.append(dict(id=rid, residual=float(res[q]), cycles=int(cyc[q]), status=int(st[q]),
+                            latency_s=float(lat[q])))
+        return out
+
+    def run(self, max_steps: int = 1_000_000):
+        """Steps until nothing is active or pending; returns every finished request."""
+        done = []
+        for _ in range(max_steps):
+            a, p = self.step()
+            done += self.poll()
+            if a == 0 and p == 0:
+                break
+        return done
+
+    def autotune(self, grids, cycles: int = 3) -> ServeParams:
+        arr = (GridDesc * len(grids))(*grids)
+        chosen = ServeParams()
+        check(self.lib.saras_serve_autotune(self.h, arr, len(grids), cycles, C.byref(chosen)),
+              "saras_serve_autotune")
+        return chosen
+
+    def stats(self) -> dict:
+        s = ServeStats()
+        check(self.lib.saras_serve_get_stats(self.h, C.byref(s)), "saras_serve_get_stats")
+        return {k: getattr(s, k) for k, _ in ServeStats._fields_}
+
+    def close(self):
+        if self.h:
+            self.lib.saras_serve_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def exported_symbols():
     """Names declared by include/saras_gb300.h (checked by the tests)."""
     import re

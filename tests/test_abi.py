@@ -44,3 +44,33 @@ def test_struct_layout():
     # sizes the C compiler gives the header structs on LP64 targets
     assert C.sizeof(S.GridDesc) == 96
     assert C.sizeof(S.FieldBC) == 24 + 48
+
+
+def test_struct_layout_matches_c_compiler(tmp_path):
+    """Every header struct has the size and field offsets the C compiler
+    gives it (the ctypes mirrors are what the Python side passes)."""
+    import shutil
+    import subprocess
+    if not shutil.which("gcc"):
+        import pytest
+        pytest.skip("no C compiler")
+    structs = {"saras_grid_desc": S.GridDesc, "saras_mg_params": S.MgParams, "saras_field_bc": S.FieldBC,
+               "saras_rk3_params": S.Rk3Params, "saras_serve_params": S.ServeParams,
+               "saras_serve_stats": S.ServeStats}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "saras_gb300.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    inc = S.HERE.parent / "include"
+    subprocess.run(["gcc", "-I", str(inc), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {(a, b): int(c) for a, b, c in (l.split() for l in out if l)}
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == C.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
