@@ -59,9 +59,13 @@ def workload(S):
     return g, rhs
 
 
+INNER = int(os.environ.get("SARAS_BENCH_INNER", "16"))
+
+
 def mg_kw(S, precision, cycles=2000):
     return dict(vc_count=cycles, vc_tolerance=TOL, solve_flag=1, mg_tolerance=1e-6, sor_param=1.0,
-                pre_smooth=2, post_smooth=2, res_type=0, precision=precision)
+                pre_smooth=2, post_smooth=2, res_type=0, precision=precision,
+                inner_cycles=INNER if precision == S.PREC_MIXED else 1)
 
 
 def config(levels):
@@ -291,6 +295,12 @@ def run_gb300(args):
     tf = ROOT / "profiles" / "traffic.json"
     if tf.exists():
         traffic = json.loads(tf.read_text()).get(names[dom])
+    serving = None
+    if not args.no_serve:
+        del rhs_d, lhs_d, h_rhs, h_lhs
+        mix.close()
+        f64.close()
+        serving = run_serving(S, args)
     cpu_pc, cpu_hist, nt = cpu_sample(S, g, rhs)
     cpu_ms = cpu_pc * np.median(cyc_f64) * 1e3
     clocks = clk.summary()
@@ -298,7 +308,9 @@ def run_gb300(args):
         "metric": METRIC, "value": ms_mix, "unit": "ms", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_mix, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64", "data": "synthetic", "config": config(levels),
-        "mixed_cycles": int(np.median(cyc_mix)), "fp64_ms": ms_f64, "fp64_cycles": int(np.median(cyc_f64)),
+        "mixed_outer_iterations": int(np.median(cyc_mix)), "mixed_inner_vcycles": INNER,
+        "mixed_vcycles": int(np.median(cyc_mix)) * INNER,
+        "fp64_ms": ms_f64, "fp64_cycles": int(np.median(cyc_f64)),
         "speedup_mixed_vs_fp64": ms_f64 / ms_mix, "mixed_vs_fp64_rel_err": err,
         "wall_ms_per_step": wall_mix,
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": 2 * field_bytes,
@@ -313,8 +325,140 @@ def run_gb300(args):
                          "sample": f"{CPU_SAMPLE_CYCLES} V-cycles of the {N}^3 FP64 mgSolve (oracle, OpenMP {nt} "
                                    f"threads) x {int(np.median(cyc_f64))} cycles of the FP64 solve"},
         "clocks": clocks,
+        "serving": serving,
     }
     print(json.dumps(out), flush=True)
+
+
+SERVE_SIZES = [("2D 512^2", (512, 1, 512), 2), ("64^3", (64, 64, 64), 3), ("96x96x48", (96, 96, 48), 3),
+               ("128^3", (128, 128, 128), 3), ("192x192x96", (192, 192, 96), 3)]
+SERVE_TOL = 1e-8
+# algorithmic bytes per finest cell per outer iteration of the MIXED form
+# with 3/6 smoothing: finest level zero e (4), 6 colour sweeps down and 12
+# up (6 each), fused residual+restriction (8.5), prolongation (8.5), FP64
+# update (20) and residual with its FP32 copy (28); coarser levels add 1/7
+# in 3-D (1/3 in 2-D).
+_FINE = 4 + 18 * 6 + 8.5 + 8.5 + 20 + 28
+SERVE_BYTES_PER_CELL = {3: _FINE * 8 / 7, 2: _FINE * 4 / 3}
+
+
+SERVE_MG = dict(mg_tolerance=1e-9, pre_smooth=3, post_smooth=6)
+
+
+def serve_grid(S, size, dims, beta):
+    top = max(size)
+    length = tuple(x / top for x in size) if dims == 3 else (1.0, 1.0, 1.0)
+    return S.grid_desc(n=size, length=length, mesh="UUD", beta=(1.0, 1.0, beta), domain="NNN", dims=dims)
+
+
+def serve_stream(S, n, rate, seed=7):
+    """Seeded request stream: Poisson arrivals, sizes drawn uniformly from
+    SERVE_SIZES, z tanh-stretched with beta ~ U[1, 1.5], Neumann walls, RHS
+    i.i.d. U[-1,1] made compatible with the all-Neumann operator.  Domain
+    lengths follow the cell counts (cells of equal extent before
+    stretching): the reference V-cycle diverges on strongly anisotropic
+    cells."""
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
+    kinds = rng.integers(0, len(SERVE_SIZES), n)
+    betas = rng.uniform(1.0, 1.5, n)
+    reqs = []
+    for q in range(n):
+        _, size, dims = SERVE_SIZES[kinds[q]]
+        g = serve_grid(S, size, dims, float(betas[q]))
+        ny = 1 if dims == 2 else size[1]
+        f = np.random.default_rng([seed, q]).uniform(-1.0, 1.0, (size[0], ny, size[2]))
+        rhs = S.padded_field(g)
+        rhs[1:1 + size[0], 1:1 + ny, 1:1 + size[2]] = S.project_compatible(g, f)
+        reqs.append((g, rhs))
+    return arrivals, kinds, reqs
+
+
+def run_serving(S, args):
+    """Continuous-batching stream through the serving engine (host API,
+    host buffers): latency = completion seen by the host minus the request's
+    scheduled arrival."""
+    n, rate = args.serve_requests, args.serve_rate
+    arrivals, kinds, reqs = serve_stream(S, n, rate)
+    eng = S.Serve(S.serve_params(hbm_budget_bytes=40 << 30, max_cases=256, tolerance=SERVE_TOL, max_cycles=400,
+                                 **SERVE_MG))
+    tune = [serve_grid(S, size, dims, 1.25) for _, size, dims in SERVE_SIZES]
+    chosen = eng.autotune(tune, cycles=2)
+    done, outs = {}, {}
+    nxt = 0
+    t0 = time.perf_counter()
+    deadline = args.serve_timeout
+    while len(done) < n:
+        now = time.perf_counter() - t0
+        if now > deadline:
+            break
+        while nxt < n and arrivals[nxt] <= now:
+            g, rhs = reqs[nxt]
+            outs[nxt] = S.padded_field(g)
+            eng.submit(nxt, g, rhs, outs[nxt])
+            nxt += 1
+        a, p = eng.step()
+        t = time.perf_counter() - t0
+        for d in eng.poll():
+            q = d["id"]
+            d["latency_s"] = t - arrivals[q]
+            d["finish_s"] = t
+            done[q] = d
+            outs.pop(q, None)
+            reqs[q] = None
+        if a == 0 and p == 0 and nxt < n and len(done) == nxt:
+            time.sleep(max(0.0, arrivals[nxt] - (time.perf_counter() - t0)))
+    st = eng.stats()
+    eng.close()
+    lat = np.array([d["latency_s"] for d in done.values()]) * 1e3
+    cyc = np.array([d["cycles"] for d in done.values()])
+    cells = {q: SERVE_SIZES[kinds[q]][1][0] * SERVE_SIZES[kinds[q]][1][1] * SERVE_SIZES[kinds[q]][1][2]
+             for q in done}
+    cell_cycles = float(sum(cells[q] * done[q]["cycles"] for q in done))
+    model_bytes = float(sum(cells[q] * done[q]["cycles"] * SERVE_BYTES_PER_CELL[SERVE_SIZES[kinds[q]][2]]
+                            for q in done))
+    makespan = max(d["finish_s"] for d in done.values()) if done else float("nan")
+    hbm, src = peaks()
+    statuses = {}
+    for d in done.values():
+        nm = S.STATUS_NAMES[d["status"]]
+        statuses[nm] = statuses.get(nm, 0) + 1
+    by_size = {}
+    for k, (name, _, _) in enumerate(SERVE_SIZES):
+        ls = [done[q]["latency_s"] * 1e3 for q in done if kinds[q] == k]
+        cs = [done[q]["cycles"] for q in done if kinds[q] == k]
+        if ls:
+            by_size[name] = {"count": len(ls), "p50_ms": float(np.percentile(ls, 50)),
+                             "p99_ms": float(np.percentile(ls, 99)), "cycles_median": float(np.median(cs))}
+    return {
+        "workload": f"{n} Poisson requests, Poisson arrivals {rate}/s (seed 7), sizes uniform over "
+                    + ", ".join(x[0] for x in SERVE_SIZES) + ", cubic cells before z tanh stretching with beta "
+                    "U[1,1.5], Neumann walls, RHS U[-1,1] projected compatible, MIXED form to rel-res 1e-8 (Linf), "
+                    "3/6 RBGS (reference defaults), coarsest tolerance 1e-9, 40 GB HBM budget, 256 case slots",
+        "requests": n, "completed": len(done), "statuses": statuses,
+        "p50_ms": float(np.percentile(lat, 50)) if len(lat) else None,
+        "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,
+        "mean_ms": float(lat.mean()) if len(lat) else None,
+        "makespan_s": makespan, "throughput_req_per_s": len(done) / makespan if done else None,
+        "cycles_median": float(np.median(cyc)) if len(cyc) else None,
+        "cell_cycles_per_s": cell_cycles / makespan if done else None,
+        "model_hbm_GBps": model_bytes / makespan / 1e9 if done else None,
+        "model_hbm_frac": model_bytes / makespan / 1e9 / hbm if done else None,
+        "model_bytes_per_cell_cycle": SERVE_BYTES_PER_CELL,
+        "max_active": st["max_active"], "batched_cycles": st["batched_cycles"], "gpu_launches": st["launches"],
+        "device_bytes_resident_peak": st["bytes_allocated"],
+        "schedule": {"cells_per_item": chosen.cells_per_item, "threads": chosen.threads,
+                     "blocks_per_sm": chosen.blocks_per_sm},
+        "by_size": by_size,
+    }
+
+
+def run_serve_only(args):
+    import torch
+    torch.cuda.set_device(0)
+    import saras_gb300 as S
+    out = run_serving(S, args)
+    print(json.dumps({"serving": out}), flush=True)
 
 
 def run_profile(args):
@@ -350,9 +494,18 @@ def main():
     ap.add_argument("--profile", type=int, default=0,
                     help="profiler mode: run this many fixed V-cycles per form and exit")
     ap.add_argument("--forms", default="mixed,fp64")
+    ap.add_argument("--serve-requests", type=int, default=300,
+                    help="requests of the serving stream (the full stream is 2000)")
+    ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-timeout", type=float, default=240.0,
+                    help="seconds after which the serving stream stops waiting for requests")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-only", action="store_true")
     args = ap.parse_args()
     if args.profile:
         run_profile(args)
+    elif args.serve_only:
+        run_serve_only(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -95,6 +95,8 @@ typedef struct saras_mg_params {
     int32_t test_poisson;  /* TEST_POISSON build semantics: no early exit */
     int32_t precision;     /* SARAS_PREC_* */
     int32_t levels;        /* 0: reference depth from setVCDepth; >0: that many levels */
+    int32_t inner_cycles;  /* MIXED form: FP32 V-cycles per FP64 defect correction (>= 1;
+                              1 repeats the FP64 form cycle by cycle); ignored by the others */
 } saras_mg_params;
 
 typedef struct saras_mg saras_mg;

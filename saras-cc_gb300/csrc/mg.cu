@@ -722,7 +722,8 @@ saras_status build_walls(saras_mg *h) {
 
 saras_status check_params(const saras_mg_params &p) {
     if (p.vc_count < 1 || p.pre_smooth < 0 || p.post_smooth < 0 || p.res_type < 0 || p.res_type > 2 ||
-        p.precision < 0 || p.precision > 2 || p.levels < 0 || !(p.sor_param > 0.0 && p.sor_param < 2.0)) {
+        p.precision < 0 || p.precision > 2 || p.levels < 0 || p.inner_cycles < 0 ||
+        !(p.sor_param > 0.0 && p.sor_param < 2.0)) {
         set_error("invalid multigrid parameters");
         return SARAS_BAD_ARG;
     }
@@ -1085,6 +1086,7 @@ void saras_mg_default_params(saras_mg_params *p) {
     p->test_poisson = 0;
     p->precision = SARAS_PREC_FP64_EXACT;
     p->levels = 0;
+    p->inner_cycles = 1;
 }
 
 saras_status saras_mg_create(const saras_grid_desc *grid, const saras_mg_params *prm, void *stream,

@@ -722,38 +722,43 @@ saras_status fast_setup(saras_mg *h) {
     return SARAS_OK;
 }
 
-// One V-cycle of the FP64 form, or one outer iteration of the MIXED form.
+// One V-cycle over the whole hierarchy: u (FP64 form) or e (MIXED form) at
+// the finest level is smoothed from its current value.
+void vcycle_fast(saras_mg *h, cudaStream_t s, bool mixed) {
+    const int top = h->nl - 1;
+    smooth(h, s, 0, h->prm.pre_smooth, mixed);
+    for (int l = 0; l < top; l++) {
+        residual_restrict(h, s, l, mixed);
+        Level &c = h->lv[(size_t)l + 1];
+        if (l + 1 == top) {
+            cudaMemsetAsync(c.lhs, 0, (size_t)c.lay.size * sizeof(double), s);
+            coarsest_level(h, s);
+        } else {
+            if (mixed)
+                cudaMemsetAsync(c.e32, 0, (size_t)c.lay.size * sizeof(float), s);
+            else
+                cudaMemsetAsync(c.lhs, 0, (size_t)c.lay.size * sizeof(double), s);
+            smooth(h, s, l + 1, h->prm.pre_smooth, mixed);
+        }
+    }
+    for (int l = top; l > 0; l--) {
+        prolong_add(h, s, l, mixed);
+        smooth(h, s, l - 1, h->prm.post_smooth, mixed);
+    }
+}
+
+// One V-cycle of the FP64 form, or one outer iteration of the MIXED form:
+// `inner_cycles` FP32 V-cycles on the error equation A e = r (the first from
+// e = 0, the others from the current e), then the FP64 update and residual.
 void fast_cycle(saras_mg *h, cudaStream_t s) {
     const bool mixed = h->prm.precision == SARAS_PREC_MIXED;
-    const int top = h->nl - 1;
     if (mixed) {
         // error equation at the finest level starts from zero
         Level &v0 = h->lv[0];
         cudaMemsetAsync(v0.e32, 0, (size_t)v0.lay.size * sizeof(float), s);
     }
-    if (top == 0) {
-        smooth(h, s, 0, h->prm.pre_smooth, mixed);
-    } else {
-        smooth(h, s, 0, h->prm.pre_smooth, mixed);
-        for (int l = 0; l < top; l++) {
-            residual_restrict(h, s, l, mixed);
-            Level &c = h->lv[(size_t)l + 1];
-            if (l + 1 == top) {
-                cudaMemsetAsync(c.lhs, 0, (size_t)c.lay.size * sizeof(double), s);
-                coarsest_level(h, s);
-            } else {
-                if (mixed)
-                    cudaMemsetAsync(c.e32, 0, (size_t)c.lay.size * sizeof(float), s);
-                else
-                    cudaMemsetAsync(c.lhs, 0, (size_t)c.lay.size * sizeof(double), s);
-                smooth(h, s, l + 1, h->prm.pre_smooth, mixed);
-            }
-        }
-        for (int l = top; l > 0; l--) {
-            prolong_add(h, s, l, mixed);
-            smooth(h, s, l - 1, h->prm.post_smooth, mixed);
-        }
-    }
+    const int inner = mixed ? std::max(1, h->prm.inner_cycles) : 1;
+    for (int q = 0; q < inner; q++) vcycle_fast(h, s, mixed);
     if (mixed) {
         Level &v0 = h->lv[0];
         const Lay &L = v0.lay;

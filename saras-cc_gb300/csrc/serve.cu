@@ -89,7 +89,7 @@ __device__ __forceinline__ unsigned long long block_max_bits(unsigned long long 
 
 // ---- batched stage kernels (grid-stride over items) ----
 
-__global__ void kb_zero(const BItem *__restrict__ items, const int *__restrict__ count,
+__global__ void __launch_bounds__(512) kb_zero(const BItem *__restrict__ items, const int *__restrict__ count,
                         const BLev *__restrict__ lv) {
     const int n = *count;
     for (int it = blockIdx.x; it < n; it += gridDim.x) {
@@ -105,7 +105,7 @@ __global__ void kb_zero(const BItem *__restrict__ items, const int *__restrict__
 }
 
 // FP32 colour sweep of the error equation (k_rbgs32 / k_rbgs_v8 arithmetic).
-__global__ void kb_rbgs(const BItem *__restrict__ items, const int *__restrict__ count,
+__global__ void __launch_bounds__(512) kb_rbgs(const BItem *__restrict__ items, const int *__restrict__ count,
                         const BLev *__restrict__ lv, int colour) {
     const int n = *count;
     for (int it = blockIdx.x; it < n; it += gridDim.x) {
@@ -135,7 +135,7 @@ __global__ void kb_rbgs(const BItem *__restrict__ items, const int *__restrict__
 // Residual of the fine level restricted into the coarse one (items are rows
 // of the coarse level; k_resid_restrict arithmetic).  The coarse target is
 // FP64 when it is the case's coarsest level.
-__global__ void kb_restrict(const BItem *__restrict__ items, const int *__restrict__ count,
+__global__ void __launch_bounds__(512) kb_restrict(const BItem *__restrict__ items, const int *__restrict__ count,
                             const BLev *__restrict__ lv) {
     const int n = *count;
     for (int it = blockIdx.x; it < n; it += gridDim.x) {
@@ -233,7 +233,7 @@ __global__ void kb_coarsest(const BItem *__restrict__ items, const int *__restri
 }
 
 // e_fine += e_coarse (injection); the coarse source is FP64 at the coarsest.
-__global__ void kb_prolong(const BItem *__restrict__ items, const int *__restrict__ count,
+__global__ void __launch_bounds__(512) kb_prolong(const BItem *__restrict__ items, const int *__restrict__ count,
                            const BLev *__restrict__ lv) {
     const int n = *count;
     for (int it = blockIdx.x; it < n; it += gridDim.x) {
@@ -253,7 +253,7 @@ __global__ void kb_prolong(const BItem *__restrict__ items, const int *__restric
 }
 
 // u += e over the finest level (FP64 accumulate).
-__global__ void kb_update(const BItem *__restrict__ items, const int *__restrict__ count,
+__global__ void __launch_bounds__(512) kb_update(const BItem *__restrict__ items, const int *__restrict__ count,
                           const BLev *__restrict__ lv) {
     const int n = *count;
     for (int it = blockIdx.x; it < n; it += gridDim.x) {
@@ -271,7 +271,7 @@ __global__ void kb_update(const BItem *__restrict__ items, const int *__restrict
 
 // FP64 residual of the finest level, its FP32 copy for the next outer
 // iteration and one L-infinity partial per item.
-__global__ void kb_resid(const BItem *__restrict__ items, const int *__restrict__ count,
+__global__ void __launch_bounds__(512) kb_resid(const BItem *__restrict__ items, const int *__restrict__ count,
                          const BLev *__restrict__ lv, double *__restrict__ part) {
     __shared__ unsigned long long shm[32];
     const int n = *count;
@@ -359,7 +359,9 @@ struct saras_serve {
     BItem *d_items = nullptr, *h_items = nullptr;
     int *d_counts = nullptr, *h_counts = nullptr;
     double *d_part = nullptr, *d_fden = nullptr, *d_res = nullptr, *h_res = nullptr;
-    int lev_cap = 0, cap_table = 0;
+    int lev_cap = 0;
+    int reg_off[NREG] = {}, reg_cap[NREG] = {};  // fixed item regions (baked into the graphs)
+    int64_t items_total = 0;
     double *d_box = nullptr;  // staging of one request's padded box
     int64_t box_cap = 0;
     cudaGraphExec_t graphs[DMAX + 1] = {};
@@ -426,8 +428,29 @@ std::array<int, NREG> case_items(const saras_serve *h, const saras_mg *m) {
 
 bool fits(const saras_serve *h, const std::array<int, NREG> &c) {
     for (int r = 0; r < NREG; r++)
-        if (h->used[r] + c[r] > h->cap_table) return false;
+        if (h->used[r] + c[r] > h->reg_cap[r]) return false;
     return true;
+}
+
+// Region capacities: the finest level's items shrink about fourfold per
+// coarser level (2-D) or eightfold (3-D); every case has one item per level
+// at least, and one coarsest and one norm item.
+void plan_regions(saras_serve *h) {
+    const int per_case = 4 * h->prm.max_cases + 1024;
+    int64_t off = 0;
+    for (int r = 0; r < NREG; r++) {
+        int cap;
+        if (r >= REG_TOP)
+            cap = h->prm.max_cases;
+        else {
+            const int l = r % DMAX;
+            cap = std::max((1 << 18) >> (2 * l), per_case);
+        }
+        h->reg_off[r] = (int)off;
+        h->reg_cap[r] = cap;
+        off += cap;
+    }
+    h->items_total = off;
 }
 
 void recount(saras_serve *h) {
@@ -481,7 +504,7 @@ saras_status upload_tables(saras_serve *h) {
         saras_mg *m = c.mg;
         const int base = nlev;
         for (int l = 0; l < m->nl; l++) h->h_lev[nlev++] = level_desc(m, l);
-        auto push = [&](int reg, BItem it) { h->h_items[(size_t)reg * h->cap_table + fill[reg]++] = it; };
+        auto push = [&](int reg, BItem it) { h->h_items[(size_t)h->reg_off[reg] + fill[reg]++] = it; };
         const int first0 = fill[REG_SMOOTH];
         for (int l = 0; l + 1 < m->nl; l++) {
             const Lay &L = m->lv[(size_t)l].lay;
@@ -502,7 +525,7 @@ saras_status upload_tables(saras_serve *h) {
                                    h->stream));
     for (int r = 0; r < NREG; r++)
         if (fill[r] > 0)
-            SARAS_CUDA(cudaMemcpyAsync(h->d_items + (size_t)r * h->cap_table, h->h_items + (size_t)r * h->cap_table,
+            SARAS_CUDA(cudaMemcpyAsync(h->d_items + h->reg_off[r], h->h_items + h->reg_off[r],
                                        (size_t)fill[r] * sizeof(BItem), cudaMemcpyHostToDevice, h->stream));
     SARAS_CUDA(cudaMemcpyAsync(h->d_counts, h->h_counts, NREG * sizeof(int), cudaMemcpyHostToDevice, h->stream));
     h->dirty = false;
@@ -516,7 +539,7 @@ int64_t issue_batched(saras_serve *h, cudaStream_t s, int depth) {
     const int B = h->bps * h->sms, T = h->threads;
     const int pre = h->prm.pre_smooth, post = h->prm.post_smooth;
     int64_t n = 0;
-    auto items = [&](int reg) { return h->d_items + (size_t)reg * h->cap_table; };
+    auto items = [&](int reg) { return h->d_items + h->reg_off[reg]; };
     auto cnt = [&](int reg) { return h->d_counts + reg; };
     auto sweeps = [&](int l, int count) {
         for (int q = 0; q < count; q++) {
@@ -805,17 +828,17 @@ saras_status saras_serve_create(const saras_serve_params *prm, saras_serve **out
     if (prm->blocks_per_sm) h->bps = prm->blocks_per_sm;
     cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, dev);
     h->lev_cap = prm->max_cases * DMAX;
-    h->cap_table = 1 << 15;
+    plan_regions(h);
     bool ok = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) == cudaSuccess;
     ok = ok && cudaMalloc((void **)&h->d_lev, (size_t)h->lev_cap * sizeof(BLev)) == cudaSuccess;
-    ok = ok && cudaMalloc((void **)&h->d_items, (size_t)NREG * h->cap_table * sizeof(BItem)) == cudaSuccess;
+    ok = ok && cudaMalloc((void **)&h->d_items, (size_t)h->items_total * sizeof(BItem)) == cudaSuccess;
     ok = ok && cudaMalloc((void **)&h->d_counts, NREG * sizeof(int)) == cudaSuccess;
-    ok = ok && cudaMalloc((void **)&h->d_part, (size_t)h->cap_table * sizeof(double)) == cudaSuccess;
+    ok = ok && cudaMalloc((void **)&h->d_part, (size_t)h->reg_cap[REG_SMOOTH] * sizeof(double)) == cudaSuccess;
     ok = ok && cudaMalloc((void **)&h->d_fden, (size_t)prm->max_cases * sizeof(double)) == cudaSuccess;
     ok = ok && cudaMalloc((void **)&h->d_res, (size_t)prm->max_cases * sizeof(double)) == cudaSuccess;
     ok = ok && cudaMallocHost((void **)&h->h_res, (size_t)prm->max_cases * sizeof(double)) == cudaSuccess;
     ok = ok && cudaMallocHost((void **)&h->h_lev, (size_t)h->lev_cap * sizeof(BLev)) == cudaSuccess;
-    ok = ok && cudaMallocHost((void **)&h->h_items, (size_t)NREG * h->cap_table * sizeof(BItem)) == cudaSuccess;
+    ok = ok && cudaMallocHost((void **)&h->h_items, (size_t)h->items_total * sizeof(BItem)) == cudaSuccess;
     ok = ok && cudaMallocHost((void **)&h->h_counts, NREG * sizeof(int)) == cudaSuccess;
     ok = ok && cudaMemsetAsync(h->d_counts, 0, NREG * sizeof(int), h->stream) == cudaSuccess;
     ok = ok && cudaMemsetAsync(h->d_res, 0, (size_t)prm->max_cases * sizeof(double), h->stream) == cudaSuccess;
@@ -925,7 +948,7 @@ saras_status saras_serve_autotune(saras_serve *h, const saras_grid_desc *grids, 
                 if (st != SARAS_OK) break;
                 apply_schedule(h, ci, ti, bi);
                 bool ok = true;
-                for (int r = 0; r < NREG; r++) ok = ok && h->used[r] <= h->cap_table;
+                for (int r = 0; r < NREG; r++) ok = ok && h->used[r] <= h->reg_cap[r];
                 if (!ok) continue;
                 st = run_batched(h);  // warm-up (and graph capture)
                 if (st != SARAS_OK) break;

@@ -47,7 +47,8 @@ class MgParams(C.Structure):
                 ("mg_tolerance", C.c_double), ("sor_param", C.c_double),
                 ("pre_smooth", C.c_int32), ("post_smooth", C.c_int32), ("res_type", C.c_int32),
                 ("print_residual", C.c_int32), ("bc_kind", C.c_int32 * 6),
-                ("test_poisson", C.c_int32), ("precision", C.c_int32), ("levels", C.c_int32)]
+                ("test_poisson", C.c_int32), ("precision", C.c_int32), ("levels", C.c_int32),
+                ("inner_cycles", C.c_int32)]
 
 
 class FieldBC(C.Structure):
@@ -85,7 +86,7 @@ def grid_desc(n=(16, 16, 16), length=(1.0, 1.0, 1.0), mesh="UUU", beta=(1.0, 1.0
 # Multigrid section of the reference's input/parameters.yaml
 DEFAULT_MG = dict(vc_count=20, vc_tolerance=1.0e-6, solve_flag=1, mg_tolerance=1.0e-2, sor_param=1.0,
                   pre_smooth=3, post_smooth=6, res_type=0, print_residual=0, test_poisson=0,
-                  precision=PREC_FP64_EXACT, levels=0)
+                  precision=PREC_FP64_EXACT, levels=0, inner_cycles=1)
 
 
 def mg_params(**kw) -> MgParams:

@@ -161,6 +161,29 @@ def test_mixed_tracks_fp64_cycle_by_cycle():
     np.testing.assert_allclose(h[1], h[0], rtol=1e-4)
 
 
+@pytest.mark.parametrize("inner", [4, 16])
+def test_mixed_inner_cycles_converge_to_oracle(inner):
+    """Several FP32 V-cycles per FP64 defect correction: the same converged
+    solution (1e-9 relative, null-space component removed) in about 1/inner
+    of the outer iterations."""
+    g = S.grid_desc(n=(32, 32, 64), length=(0.5, 0.5, 1.0), mesh="UUD", beta=(1, 1, 1.3), domain="NNN")
+    rhs = random_rhs(g, 8)
+    base = dict(pre_smooth=2, post_smooth=2, mg_tolerance=1e-9)
+    one = S.Multigrid(g, S.mg_params(precision=S.PREC_MIXED, vc_count=400, vc_tolerance=1e-10, **base))
+    a1 = S.padded_field(g)
+    assert one.mg_solve(a1, rhs) == S.OK
+    mg = S.Multigrid(g, S.mg_params(precision=S.PREC_MIXED, vc_count=400, vc_tolerance=1e-11,
+                                    inner_cycles=inner, **base))
+    mix = S.padded_field(g)
+    assert mg.mg_solve(mix, rhs) == S.OK and mg.history[-1] < 1e-11
+    assert mg.cycles < one.cycles
+    orc = S.padded_field(g)
+    r = O.mg_solve(g, S.mg_params(vc_count=400, vc_tolerance=1e-12, **base), orc, rhs)
+    assert r.status == 0
+    a, b = demean(core(mix, g)), demean(core(orc, g))
+    assert np.abs(a - b).max() / np.abs(b).max() < 1e-9
+
+
 def test_mixed_two_solves_same_handle():
     g = S.grid_desc(n=(32, 32, 32), mesh="UUU", domain="NNN")
     rhs = random_rhs(g, 5)
