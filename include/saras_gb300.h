@@ -259,6 +259,30 @@ saras_status saras_serve_autotune(saras_serve *h, const saras_grid_desc *grids, 
 saras_status saras_serve_get_stats(const saras_serve *h, saras_serve_stats *out);
 saras_status saras_serve_destroy(saras_serve *h);
 
+/* ----------------------------------------------------- static scratch ---- */
+/*
+ * No counterpart in the reference.  saras_mg_solve_static runs one mgSolve
+ * (FP64 or MIXED form) on device fields without allocating device memory:
+ * its working memory is one file-scope __device__ array of
+ * SARAS_STATIC_SCRATCH_BYTES (32 MiB) per device, which holds the hierarchy
+ * of a 3-D grid up to about 80^3 (a 2-D grid up to about 512^2); a grid that
+ * does not fit returns SARAS_BUDGET, naming the bytes it needs, before any
+ * device work.  It is for callers that cannot allocate at solve time:
+ * cudaMalloc/cudaFree synchronise the whole device, a caching allocator may
+ * already hold the free HBM, and a time step must not fail half-way for want
+ * of memory.  The first call on a device does the set-up (it looks up the
+ * scratch's address with that device current); make that first call before
+ * any stream capture.  Nothing in the scratch has to start at zero.  Every
+ * call on a device uses the same scratch, so calls that overlap in time (on
+ * different streams or host threads) race; the caller serialises them.
+ * Arguments as saras_mg_create (grid, params, stream) plus
+ * saras_mg_solve_dev (device fields, strides, residual history).
+ */
+#define SARAS_STATIC_SCRATCH_BYTES (32u << 20)
+saras_status saras_mg_solve_static(const saras_grid_desc *grid, const saras_mg_params *prm, void *stream,
+                                   double *lhs, const double *rhs, const int64_t strides[3],
+                                   double *res_hist, int32_t hist_cap, int32_t *n_cycles);
+
 /* ------------------------------------------------------------- common ---- */
 
 const char *saras_status_string(saras_status s);

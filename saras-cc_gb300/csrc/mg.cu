@@ -1181,3 +1181,103 @@ saras_status saras_mg_kernel_stats(saras_mg *h, int32_t kclass, int64_t *launche
 int64_t saras_mg_last_launches(const saras_mg *h) { return h ? h->last_launches : -1; }
 
 }  // extern "C"
+
+// ------------------------------------------- solve in caller scratch ----
+
+namespace saras {
+
+// One mgSolve (FP64 or MIXED form) whose device working memory is carved
+// out of `scratch` (scratch_bytes long, 256-byte aligned) instead of being
+// allocated: the hierarchy, its 1-D tables and the residual-norm scratch.
+// The call allocates no device or pinned memory; its host-side grid tables
+// and the staging of their upload are ordinary host memory.  Nothing in the
+// scratch needs to start at zero: the finest arrays are cleared by the solve
+// itself, every coarse array is written before it is read, and the norm
+// outputs and coarse-sweep counter are cleared here.  The work is ordered on
+// `stream`; the scratch is reused by the next call, so calls that overlap in
+// time (other streams, other host threads) race on it.
+saras_status mg_solve_in_scratch(const saras_grid_desc *gd, const saras_mg_params *prm, cudaStream_t stream,
+                                 char *scratch, size_t scratch_bytes, double *lhs, const double *rhs,
+                                 const int64_t st[3], double *res_hist, int32_t hist_cap, int32_t *n_cycles) {
+    SARAS_TRY(check_params(*prm));
+    if (prm->precision != SARAS_PREC_FP64 && prm->precision != SARAS_PREC_MIXED) {
+        set_error("the static-scratch solve runs the FP64 and MIXED forms only");
+        return SARAS_BAD_ARG;
+    }
+    saras_mg h;
+    h.prm = *prm;
+    SARAS_TRY(h.grid.build(*gd, prm->levels));
+    h.d3 = h.grid.dims == 3;
+    h.nl = h.grid.levels;
+    h.stream = stream;
+    h.use_graph = false;
+    if (prm->precision == SARAS_PREC_MIXED && h.nl < 2) {
+        set_error("the MIXED form needs at least two levels");
+        return SARAS_BAD_ARG;
+    }
+    for (int d = 0; d < 3; d++) h.ghost.per[d] = h.grid.per[d] ? 1 : 0;
+    for (int f = 0; f < 6; f++) h.ghost.kind[f] = prm->bc_kind[f];
+    h.lv.resize((size_t)h.nl);
+    // carve the scratch: every array starts on a 256-byte boundary
+    size_t off = 0;
+    auto take = [&](auto **p, int64_t count) {
+        using T = std::remove_reference_t<decltype(**p)>;
+        off = (off + 255) / 256 * 256;
+        const size_t bytes = (size_t)std::max<int64_t>(count, 1) * sizeof(T);
+        *p = off + bytes <= scratch_bytes ? reinterpret_cast<T *>(scratch + off) : nullptr;
+        off += bytes;
+    };
+    size_t stage_bytes = 0;
+    for (int l = 0; l < h.nl; l++) {
+        Level &v = h.lv[(size_t)l];
+        const AxisLevel *a = h.grid.lv[(size_t)l].data();
+        v.lay = make_lay(a[0].n, h.d3 ? a[1].n : 1, a[2].n);
+        const int64_t sz = v.lay.size;
+        const LevelArrays use = level_arrays(prm->precision, l, h.nl);
+        if (use.u_f) {
+            take(&v.lhs, sz);
+            take(&v.rhs, sz);
+        }
+        if (use.e_r32) {
+            take(&v.e32, sz);
+            take(&v.r32, sz);
+        }
+        if (use.inv_diag) take(&v.inv_diag, sz);
+        if (use.dd) take(&v.dd, sz);
+        const int64_t total = (int64_t)10 * (v.lay.n0 + v.lay.n1 + v.lay.n2);
+        take(&v.tab, total);
+        take(&v.tab32, total);
+        stage_bytes += (size_t)total * 12 + 256;
+    }
+    const Lay &L0 = h.lv[0].lay;
+    const int64_t cells = (int64_t)L0.n0 * L0.n1 * L0.n2;
+    h.norm_blocks = (int)std::max<int64_t>(1, std::min<int64_t>(1216, (cells + 255) / 256));
+    take(&h.norm_part, 4 * (int64_t)h.norm_blocks);
+    take(&h.norm_out, 8);
+    take(&h.coarse_sweeps, 4);
+    take(&h.mix_scalar, 16);
+    if (off > scratch_bytes) {
+        set_error("grid needs %zu bytes of solver scratch; the static scratch holds %zu bytes", off, scratch_bytes);
+        return SARAS_BUDGET;
+    }
+    h.dev_bytes = 0;
+    double norm_host[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    h.norm_host = norm_host;
+    std::vector<char> stage(stage_bytes);
+    h.tab_stage = stage.data();
+    h.tab_stage_bytes = stage.size();
+    h.tab_stage_used = 0;
+    SARAS_CUDA(cudaMemsetAsync(h.norm_out, 0, 8 * sizeof(double), stream));
+    SARAS_CUDA(cudaMemsetAsync(h.coarse_sweeps, 0, 4 * sizeof(int), stream));
+    saras_status s = build_tables(&h, true);  // pageable sources: staged at the call, ordered on the stream
+    h.tab_stage = nullptr;
+    h.norm_host = nullptr;
+    SARAS_TRY(s);
+    h.norm_host = norm_host;
+    s = fast_setup(&h);
+    if (s == SARAS_OK) s = solve_common(&h, lhs, rhs, st, res_hist, hist_cap, n_cycles);
+    h.norm_host = nullptr;
+    return s;
+}
+
+}  // namespace saras
