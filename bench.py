@@ -237,8 +237,7 @@ def run_gb300(args):
         f64.mg_solve_dev(lhs_d.data_ptr() + 8 * off, rhs_d.data_ptr() + 8 * off, st)
     torch.cuda.synchronize()
 
-    # ---- timed region: MIXED form (headline) with per-kernel events ----
-    mix.set_kernel_timing(True)
+    # ---- timed region: MIXED form (headline) ----
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -250,6 +249,10 @@ def run_gb300(args):
         dist.barrier()
     sol_mix = lhs_d[1:-1, 1:-1, 1:-1].double().cpu().numpy()
     launches = mix.last_launches()
+    # ---- the same solves again with every finest-level launch bracketed by
+    # CUDA events on the solve stream (kernel durations for the roofline) ----
+    mix.set_kernel_timing(True)
+    ms_mix_events, _ = time_solves(mix, lhs_d, rhs_d, st, off, args.steps, torch, stream)
     kstats = {k: mix.kernel_stats(k) for k in range(5)}
     mix.set_kernel_timing(False)
 
@@ -312,7 +315,7 @@ def run_gb300(args):
         "mixed_vcycles": int(np.median(cyc_mix)) * INNER,
         "fp64_ms": ms_f64, "fp64_cycles": int(np.median(cyc_f64)),
         "speedup_mixed_vs_fp64": ms_f64 / ms_mix, "mixed_vs_fp64_rel_err": err,
-        "wall_ms_per_step": wall_mix,
+        "wall_ms_per_step": wall_mix, "ms_per_step_with_kernel_events": ms_mix_events,
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": 2 * field_bytes,
                 "d2h_bytes_per_step": field_bytes},
         "gpu_launches": int(launches) * args.steps,
@@ -383,7 +386,10 @@ def run_serving(S, args):
     eng = S.Serve(S.serve_params(hbm_budget_bytes=40 << 30, max_cases=256, tolerance=SERVE_TOL, max_cycles=400,
                                  **SERVE_MG))
     tune = [serve_grid(S, size, dims, 1.25) for _, size, dims in SERVE_SIZES]
-    chosen = eng.autotune(tune, cycles=2)
+    if args.serve_no_tune:
+        chosen = eng.params
+    else:
+        chosen = eng.autotune(tune, cycles=2)
     done, outs = {}, {}
     nxt = 0
     t0 = time.perf_counter()
@@ -500,6 +506,7 @@ def main():
     ap.add_argument("--serve-timeout", type=float, default=240.0,
                     help="seconds after which the serving stream stops waiting for requests")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-no-tune", action="store_true", help="keep the default schedule (no autotune)")
     ap.add_argument("--serve-only", action="store_true")
     args = ap.parse_args()
     if args.profile:

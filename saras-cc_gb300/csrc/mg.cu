@@ -933,6 +933,13 @@ saras_status solve_loop(saras_mg *h, double *res_hist, int32_t hist_cap, int32_t
         harvest_timing(h);
         r = h->norm_host[0];
         cyc++;
+        int tma_err = 0;
+        std::memcpy(&tma_err, h->norm_host + 7, sizeof(int));
+        if (tma_err) {
+            if (n_cycles) *n_cycles = cyc;
+            set_error("a bounded wait of the TMA sweep ran out in V-cycle %d", c);
+            return SARAS_TIMEOUT;
+        }
         if (res_hist && c < hist_cap) res_hist[c] = r;
         if (h->prm.print_residual) std::printf("\nResidual after V Cycle %d is %.3e\n", c, r);
         if (!std::isfinite(r)) {

@@ -56,7 +56,7 @@ __global__ void k_rbgs32(float *e, const float *__restrict__ r, Lay L, Tab3<floa
     const int64_t c = L.at(i, j, k);
     const float uc = e[c];
     const float s = offdiag<float, D3>(e, L, t, b, i, j, k, c, uc) - r[c];
-    e[c] = fmat(omc, uc, __fdiv_rn(w * s, diag<float, D3>(t, i, j, k)));
+    e[c] = fmat(omc, uc, sweep_div(w * s, diag<float, D3>(t, i, j, k)));
 }
 
 // Colour sweep with eight consecutive cells per thread along k: the rows a
@@ -140,7 +140,7 @@ __device__ __forceinline__ void strip_update(T *u, const T (&cur)[8], const T (&
         } else {
             T d = dx + t.dg[2][k];
             if (D3) d += dy;
-            v = fmat(omc, cur[q], w * sm / (d + d));
+            v = fmat(omc, cur[q], sweep_div(w * sm, d + d));
         }
         u[c0 + q] = v;
     }
@@ -216,6 +216,102 @@ __global__ void k_resid_restrict(const T *__restrict__ u, const T *__restrict__ 
     rc[Lc.at(i, j, k)] = (TO)out;
 }
 
+// Residuals of eight consecutive fine cells of one row (k_resid_restrict's
+// resid() arithmetic, cell by cell) from vector loads of the row, its x and y
+// neighbour rows, f and the stored diagonal.
+template <class T, bool D3>
+__device__ __forceinline__ void resid_row8(const T *__restrict__ u, const T *__restrict__ f, const Lay &L,
+                                           const Tab3<T> &t, const Bnd &b, int i, int j, int k0,
+                                           const T *__restrict__ dd, T (&r)[8]) {
+    const int64_t c0 = L.at(i, j, k0);
+    T cur[8], xm[8], xp[8], ym[8], yp[8], fr[8];
+    ld8(u + c0, cur);
+    if (i > 0) ld8(u + c0 - L.s0, xm);
+    else if (b.per[0]) ld8(u + c0 + (int64_t)(L.n0 - 1) * L.s0, xm);
+    else mirror8(cur, b.sg_lo[0], xm);
+    if (i < L.n0 - 1) ld8(u + c0 + L.s0, xp);
+    else if (b.per[0]) ld8(u + c0 - (int64_t)(L.n0 - 1) * L.s0, xp);
+    else mirror8(cur, b.sg_hi[0], xp);
+    if (D3) {
+        if (j > 0) ld8(u + c0 - L.s1, ym);
+        else if (b.per[1]) ld8(u + c0 + (int64_t)(L.n1 - 1) * L.s1, ym);
+        else mirror8(cur, b.sg_lo[1], ym);
+        if (j < L.n1 - 1) ld8(u + c0 + L.s1, yp);
+        else if (b.per[1]) ld8(u + c0 - (int64_t)(L.n1 - 1) * L.s1, yp);
+        else mirror8(cur, b.sg_hi[1], yp);
+    }
+    ld8(f + c0, fr);
+    const T left = k0 > 0 ? __ldg(u + c0 - 1) : (b.per[2] ? __ldg(u + c0 + L.n2 - 1) : (b.sg_lo[2] > 0 ? cur[0] : -cur[0]));
+    const T right = k0 + 8 < L.n2 ? __ldg(u + c0 + 8)
+                                  : (b.per[2] ? __ldg(u + c0 + 8 - L.n2) : (b.sg_hi[2] > 0 ? cur[7] : -cur[7]));
+    T dv[8];
+    if (dd) ld8(dd + c0, dv);
+    const T cmx = t.cm[0][i], cpx = t.cp[0][i];
+    T cmy = T(0), cpy = T(0);
+    if (D3) {
+        cmy = t.cm[1][j];
+        cpy = t.cp[1][j];
+    }
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        const int k = k0 + q;
+        const T zm = q > 0 ? cur[q - 1] : left;
+        const T zp = q < 7 ? cur[q + 1] : right;
+        T sm = cmx * xm[q];
+        sm = fmat(cpx, xp[q], sm);
+        if (D3) {
+            sm = fmat(cmy, ym[q], sm);
+            sm = fmat(cpy, yp[q], sm);
+        }
+        sm = fmat(t.cm[2][k], zm, sm);
+        sm = fmat(t.cp[2][k], zp, sm);
+        const T d = dd ? dv[q] : diag<T, D3>(t, i, j, k);
+        r[q] = fr[q] - fmat(-d, cur[q], sm);
+    }
+}
+
+// Fused residual and restriction, four coarse cells along k per thread (fine
+// n_z a multiple of 8), the same arithmetic as k_resid_restrict.
+template <class T, bool D3>
+__global__ void __launch_bounds__(128, 4) k_resid_restrict8(const T *__restrict__ u, const T *__restrict__ f, Lay Lf, Tab3<T> t, Bnd b,
+                                  WTab<T> w, T *__restrict__ rc, Lay Lc, const T *__restrict__ dd) {
+    const int kc0 = 4 * (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = D3 ? (int)(blockIdx.y * blockDim.y + threadIdx.y) : 0;
+    const int i = blockIdx.z;
+    if (kc0 >= Lc.n2 || j >= Lc.n1) return;
+    T out[4];
+    if (D3) {
+        T sy[2][4];
+        for (int a = 0; a < 2; a++) {
+            T sz[2][4];
+            for (int bb = 0; bb < 2; bb++) {
+                T r[8];
+                resid_row8<T, true>(u, f, Lf, t, b, 2 * i + a, 2 * j + bb, 2 * kc0, dd, r);
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    sz[bb][q] = fmat(w.w1[2][kc0 + q], r[2 * q + 1], w.w0[2][kc0 + q] * r[2 * q]);
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) sy[a][q] = fmat(w.w1[1][j], sz[1][q], w.w0[1][j] * sz[0][q]);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) out[q] = fmat(w.w1[0][i], sy[1][q], w.w0[0][i] * sy[0][q]);
+    } else {
+        T r0[8], r1[8];
+        resid_row8<T, false>(u, f, Lf, t, b, 2 * i, 0, 2 * kc0, dd, r0);
+        resid_row8<T, false>(u, f, Lf, t, b, 2 * i + 1, 0, 2 * kc0, dd, r1);
+#pragma unroll
+        for (int q = 0; q < 4; q++) out[q] = ((r0[2 * q] + r0[2 * q + 1]) + (r1[2 * q] + r1[2 * q + 1])) * T(0.25);
+    }
+    T *dst = rc + Lc.at(i, j, kc0);
+    if (sizeof(T) == 4) {
+        reinterpret_cast<float4 *>(dst)[0] = make_float4((float)out[0], (float)out[1], (float)out[2], (float)out[3]);
+    } else {
+        reinterpret_cast<double2 *>(dst)[0] = make_double2((double)out[0], (double)out[1]);
+        reinterpret_cast<double2 *>(dst)[1] = make_double2((double)out[2], (double)out[3]);
+    }
+}
+
 // Injection prolongation and correction in place: fine += coarse(i/2,..).
 template <class TF, class TC>
 __global__ void k_prolong_add(TF *__restrict__ f, const TC *__restrict__ c, Lay Lf, Lay Lc, int d3) {
@@ -224,6 +320,49 @@ __global__ void k_prolong_add(TF *__restrict__ f, const TC *__restrict__ c, Lay 
     if (k >= Lf.n2) return;
     const int64_t q = Lf.at(i, j, k);
     f[q] = f[q] + (TF)c[Lc.at(i >> 1, d3 ? (j >> 1) : 0, k >> 1)];
+}
+
+// Injection prolongation and correction, eight fine cells along k per
+// thread (n_z a multiple of 8): two aligned vector loads and stores of the
+// fine row, one of the four coarse cells.
+template <class T>
+__device__ __forceinline__ void st8(T *p, const T (&v)[8]);
+template <>
+__device__ __forceinline__ void st8<float>(float *p, const float (&v)[8]) {
+    reinterpret_cast<float4 *>(p)[0] = make_float4(v[0], v[1], v[2], v[3]);
+    reinterpret_cast<float4 *>(p)[1] = make_float4(v[4], v[5], v[6], v[7]);
+}
+template <>
+__device__ __forceinline__ void st8<double>(double *p, const double (&v)[8]) {
+#pragma unroll
+    for (int q = 0; q < 4; q++) reinterpret_cast<double2 *>(p)[q] = make_double2(v[2 * q], v[2 * q + 1]);
+}
+template <class T>
+__device__ __forceinline__ void ld4(const T *__restrict__ p, T (&o)[4]);
+template <>
+__device__ __forceinline__ void ld4<float>(const float *__restrict__ p, float (&o)[4]) {
+    const float4 a = __ldg(reinterpret_cast<const float4 *>(p));
+    o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+}
+template <>
+__device__ __forceinline__ void ld4<double>(const double *__restrict__ p, double (&o)[4]) {
+    const double2 a = __ldg(reinterpret_cast<const double2 *>(p));
+    const double2 b = __ldg(reinterpret_cast<const double2 *>(p + 2));
+    o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
+}
+
+template <class T>
+__global__ void k_prolong_add8(T *__restrict__ f, const T *__restrict__ c, Lay Lf, Lay Lc, int d3) {
+    const int k0 = 8 * (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = (int)(blockIdx.y * blockDim.y + threadIdx.y), i = blockIdx.z;
+    if (k0 >= Lf.n2 || j >= Lf.n1) return;
+    const int64_t q = Lf.at(i, j, k0);
+    T v[8], w[4];
+    ld8u(f + q, v);
+    ld4(c + Lc.at(i >> 1, d3 ? (j >> 1) : 0, k0 >> 1), w);
+#pragma unroll
+    for (int t = 0; t < 8; t++) v[t] = v[t] + w[t >> 1];
+    st8(f + q, v);
 }
 
 __device__ __forceinline__ double warp_max(double v) {
@@ -321,15 +460,18 @@ __global__ void k_rhs_norm(const double *__restrict__ f, Lay L, int rtype, doubl
     block_store<4>(v, mx, part);
 }
 
+// One warp: lane t reduces partials t, t+32, ... in order, then a fixed
+// shuffle tree combines the lanes (the same order on every run).
 __global__ void k_rhs_norm_final(const double *__restrict__ part, int nb, int rtype, double *__restrict__ out) {
-    if (threadIdx.x != 0) return;
     double m = 0.0, sm = 0.0;
-    for (int q = 0; q < nb; q++) {
+    for (int q = threadIdx.x; q < nb; q += 32) {
         const double a = part[4 * q + 1];
         if (a > m) m = a;
         sm += part[4 * q + 3];
     }
-    out[0] = rtype == 0 ? m : sm;
+    m = warp_max(m);
+    sm = warp_sum(sm);
+    if (threadIdx.x == 0) out[0] = rtype == 0 ? m : sm;
 }
 
 // Coarsest level of the FP64 and MIXED forms: SOR red-black sweeps with
@@ -445,16 +587,24 @@ __global__ void k_csum(const double *__restrict__ u, Lay L, double *__restrict__
 
 // Mean of u from the (sum, error) partials, in a fixed order; slot 0 of
 // `out` receives the mean; with `sub` set, out[0] becomes mean - out[1].
+// One warp, lanes over strided partials in order, then a fixed shuffle tree
+// of compensated additions.
 __global__ void k_csum_final(const double *__restrict__ part, int nb, double count, double *out, int slot) {
-    if (threadIdx.x != 0) return;
     double S = 0.0, Cc = 0.0;
-    for (int q = 0; q < nb; q++) {
+    for (int q = threadIdx.x; q < nb; q += 32) {
         double t, e;
         two_sum(S, part[2 * q], t, e);
         S = t;
         Cc += part[2 * q + 1] + e;
     }
-    out[slot] = (S + Cc) / count;
+    for (int o = 16; o > 0; o >>= 1) {
+        const double s2 = __shfl_xor_sync(0xffffffffu, S, o), c2 = __shfl_xor_sync(0xffffffffu, Cc, o);
+        double t, e;
+        two_sum(S, s2, t, e);
+        S = t;
+        Cc += c2 + e;
+    }
+    if (threadIdx.x == 0) out[slot] = (S + Cc) / count;
 }
 
 __global__ void k_shift(double *__restrict__ u, Lay L, const double *__restrict__ m) {
@@ -561,6 +711,12 @@ void colour64(saras_mg *h, cudaStream_t s, int l, int colour) {
 void colour32(saras_mg *h, cudaStream_t s, int l, int colour) {
     Level &v = h->lv[(size_t)l];
     const Lay &L = v.lay;
+    if (v.tma.ok) {
+        kbegin(h, s, l == 0 ? KC_SMOOTH0 : -1);
+        tma_colour(h, s, v, colour);
+        kend(h, s, l == 0 ? KC_SMOOTH0 : -1);
+        return;
+    }
     if (v8_ok(L)) {
         kbegin(h, s, l == 0 ? KC_SMOOTH0 : -1);
         colour_v8<float, false>(h, s, v, v.e32, v.r32, (const float *)nullptr, tab32(v), colour,
@@ -599,7 +755,26 @@ void residual_restrict(saras_mg *h, cudaStream_t s, int l, bool mixed) {
     const Bnd b = bnd(h);
     const bool to64 = l + 1 == h->nl - 1;  // the coarsest level is FP64 in every form
     kbegin(h, s, l == 0 ? KC_RESTRICT : -1);
-    if (!mixed) {
+    if (v8_ok(f.lay) && (!mixed || !to64)) {
+        const int strips = Lc.n2 / 4, bx4 = std::min(strips, 32), by = h->d3 ? std::max(1, 128 / bx4) : 1;
+        const dim3 g4(cdiv(strips, bx4), h->d3 ? cdiv(Lc.n1, by) : 1u, (unsigned)Lc.n0);
+        const dim3 blk(bx4, by);
+        if (!mixed) {
+            if (h->d3)
+                k_resid_restrict8<double, true><<<g4, blk, 0, s>>>(f.lhs, f.rhs, f.lay, tab64(f), b, wt64(c), c.rhs,
+                                                                   Lc, f.dd);
+            else
+                k_resid_restrict8<double, false><<<g4, blk, 0, s>>>(f.lhs, f.rhs, f.lay, tab64(f), b, wt64(c),
+                                                                    c.rhs, Lc, f.dd);
+        } else {
+            if (h->d3)
+                k_resid_restrict8<float, true><<<g4, blk, 0, s>>>(f.e32, f.r32, f.lay, tab32(f), b, wt32(c), c.r32,
+                                                                  Lc, nullptr);
+            else
+                k_resid_restrict8<float, false><<<g4, blk, 0, s>>>(f.e32, f.r32, f.lay, tab32(f), b, wt32(c),
+                                                                   c.r32, Lc, nullptr);
+        }
+    } else if (!mixed) {
         if (h->d3)
             k_resid_restrict<double, double, true><<<cgrid(Lc, true, Lc.n2, bx), bx, 0, s>>>(
                 f.lhs, f.rhs, f.lay, tab64(f), b, wt64(c), c.rhs, Lc, f.dd);
@@ -631,7 +806,15 @@ void prolong_add(saras_mg *h, cudaStream_t s, int l, bool mixed) {
     const int bx = bxfor(L.n2);
     const dim3 g(cdiv(L.n2, bx), (unsigned)L.n1, (unsigned)L.n0);
     kbegin(h, s, l == 1 ? KC_PROLONG : -1);
-    if (!mixed)
+    const bool to_top = l == h->nl - 1;
+    if (v8_ok(L) && (!mixed || !to_top)) {
+        const int strips = L.n2 / 8, bx8 = std::min(strips, 32), by = h->d3 ? std::max(1, 128 / bx8) : 1;
+        const dim3 g8(cdiv(strips, bx8), cdiv(L.n1, by), (unsigned)L.n0);
+        if (!mixed)
+            k_prolong_add8<double><<<g8, dim3(bx8, by), 0, s>>>(f.lhs, c.lhs, L, c.lay, h->d3 ? 1 : 0);
+        else
+            k_prolong_add8<float><<<g8, dim3(bx8, by), 0, s>>>(f.e32, c.e32, L, c.lay, h->d3 ? 1 : 0);
+    } else if (!mixed)
         k_prolong_add<double, double><<<g, bx, 0, s>>>(f.lhs, c.lhs, L, c.lay, h->d3 ? 1 : 0);
     else if (l == h->nl - 1)
         k_prolong_add<float, double><<<g, bx, 0, s>>>(f.e32, c.lhs, L, c.lay, h->d3 ? 1 : 0);
@@ -714,6 +897,8 @@ saras_status fast_setup(saras_mg *h) {
             k_inv_diag<false><<<cgrid(L, false, L.n2, bx), bx, 0, h->stream>>>(v.inv_diag, v.dd, L, tab64(v),
                                                                             h->prm.sor_param);
     }
+    if (h->prm.precision == SARAS_PREC_MIXED)
+        for (int l = 0; l < h->nl; l++) tma_plan(h, h->lv[(size_t)l]);
     SARAS_CUDA(cudaFuncSetAttribute(k_coarsest_fast<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     200 * 1024));
     SARAS_CUDA(cudaFuncSetAttribute(k_coarsest_fast<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,

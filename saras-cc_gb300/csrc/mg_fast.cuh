@@ -21,6 +21,10 @@ double kernel_bytes(const saras_mg *h, int kclass);
 void rhs_norm(saras_mg *h, cudaStream_t s);       // max|f| (or sums) of the solve, once
 void coarsest_fast(saras_mg *h, cudaStream_t s, Level &c);
 
+// mg_tma.cu: TMA-staged FP32 colour sweep of the large 3-D levels
+void tma_plan(saras_mg *h, Level &v);
+bool tma_colour(saras_mg *h, cudaStream_t s, Level &v, int colour);
+
 // mg.cu: handle reuse by the serving engine
 saras_status mg_retarget(saras_mg *h, const saras_grid_desc *gd);
 saras_status mg_load_rhs(saras_mg *h, const double *rhs_box_origin, const int64_t st[3]);

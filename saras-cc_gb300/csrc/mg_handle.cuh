@@ -1,6 +1,8 @@
 // Device-resident multigrid hierarchy behind the saras_mg_* entry points.
 #pragma once
 
+#include <cuda.h>
+
 #include <vector>
 
 #include "common.cuh"
@@ -8,6 +10,14 @@
 #include "mg_exact.cuh"
 
 namespace saras {
+
+// TMA plan of a level's FP32 colour sweep (mg_tma.cu): tensor maps of e
+// (tile with one halo row each side, tile alone) and r, tile rows and planes
+// per block.
+struct TmaPlan {
+    CUtensorMap eld, est, rld;
+    int tj = 0, chunk = 0, ok = 0;
+};
 
 // Per-level device state.  FP64 arrays serve the FP64_EXACT and FP64 forms
 // and the finest level of the MIXED form; FP32 arrays hold the MIXED form's
@@ -34,6 +44,7 @@ struct Level {
     double *inv_diag = nullptr;  // FP64 form: omega / D per cell
     double *dd = nullptr;        // FP64 forms: the diagonal D = 2 sum(xix2*ihx2) per cell
     float *inv_diag32 = nullptr; // MIXED form: omega / D per cell
+    TmaPlan tma{};
 };
 
 enum KClass { KC_SMOOTH0 = 0, KC_RESTRICT = 1, KC_PROLONG = 2, KC_NORM = 3, KC_COARSE = 4, KC_COUNT = 5 };

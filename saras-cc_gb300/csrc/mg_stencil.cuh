@@ -27,6 +27,12 @@ struct WTab {
 __device__ __forceinline__ float fmat(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 __device__ __forceinline__ double fmat(double a, double b, double c) { return __fma_rn(a, b, c); }
 
+// Quotient of the FP32 colour sweeps: the hardware reciprocal path of
+// __fdividef (about two ulp).  Every FP32 sweep kernel uses it, so the
+// single-problem, TMA and batched sweeps produce identical bits.
+__device__ __forceinline__ float sweep_div(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double sweep_div(double a, double b) { return a / b; }
+
 template <class T>
 __device__ __forceinline__ T nb_lo(const T *u, int64_t c, int i, int n, int64_t s, int per, int sg, T uc) {
     if (i > 0) return u[c - s];

@@ -127,7 +127,7 @@ __global__ void __launch_bounds__(512) kb_rbgs(const BItem *__restrict__ items, 
                 s = offdiag<float, false>(L.e, L.lay, L.t32, L.b, i, j, k, c, uc) - L.r[c];
                 d = diag<float, false>(L.t32, i, j, k);
             }
-            L.e[c] = fmat(L.omc, uc, __fdiv_rn(L.w * s, d));
+            L.e[c] = fmat(L.omc, uc, sweep_div(L.w * s, d));
         }
     }
 }
