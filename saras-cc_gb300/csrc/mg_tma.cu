@@ -2,16 +2,16 @@
 // large 3-D levels.
 //
 // A block owns a tile of `tj` rows (j) by the whole row (k) and marches
-// through a chunk of planes (i).  Planes stream through a four-slot ring in
-// shared memory: the tensor-memory accelerator (cp.async.bulk.tensor) loads
-// the e tile with one halo row on each side and the r tile three planes
-// ahead of the plane being updated, an mbarrier per slot signals arrival, the
-// threads update the sweep's colour in place in shared memory, and a TMA
-// store writes the tile's rows back whole.  Cells of the other colour are
-// only read, so the in-place update needs no copy: every value a cell of the
-// sweep's colour reads (its six neighbours) is of the other colour, within
-// the block and across blocks.  The arithmetic per cell is that of
-// k_rbgs_v8 (mg_fast.cu), so results are bit-identical.
+// through a chunk of planes (i).  Planes stream through a ring of slots in
+// shared memory: a producer lane loads the e tile (with one halo row on each
+// side) and the r tile with cp.async.bulk.tensor as soon as a slot is free,
+// and eight consumer warps, each owning tj/8 rows, update the sweep's colour
+// in place in shared memory and write their rows back whole with their own
+// TMA stores.  Cells of the other colour are only read, so the in-place
+// update needs no copy and the warps never wait for one another: every
+// value a cell of the sweep's colour reads (its six neighbours) is of the
+// other colour, within the block and across blocks.  The arithmetic per cell
+// is that of k_rbgs_v8 (mg_fast.cu), so results are bit-identical.
 //
 // Every wait on an mbarrier is bounded; a wait that runs out sets an error
 // word the host reads with the residual (norm_out[7]), waits (bounded) for
@@ -27,8 +27,7 @@
 namespace saras {
 namespace {
 
-constexpr int TMA_THREADS = 256;
-constexpr int TMA_SLOTS = 4;
+constexpr int TMA_SLOTS = 5;
 constexpr unsigned TMA_WAIT_LIMIT = 1u << 24;
 
 __device__ __forceinline__ uint32_t sa(const void *p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
@@ -113,146 +112,165 @@ __device__ __forceinline__ float4 mirror4(float4 c, int sg) {
 }
 __device__ __forceinline__ float4 lds4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
 
-__global__ void __launch_bounds__(TMA_THREADS) k_rbgs_tma(const __grid_constant__ CUtensorMap eld,
-                                                          const __grid_constant__ CUtensorMap est,
-                                                          const __grid_constant__ CUtensorMap rld,
-                                                          const float *__restrict__ eg, Lay L, Tab3<float> t, Bnd b,
-                                                          int colour, float w, float omc, int tj, int chunk,
-                                                          int *err) {
+// Warp-specialised pipeline: warp 0 (one lane) loads planes into a ring of
+// TMA_SLOTS slots, each with a "full" mbarrier (completed by the TMA
+// transaction count) and an "empty" mbarrier (one arrival per consumer warp).
+// Each of the TMA_CONSUMERS consumer warps owns tj / TMA_CONSUMERS rows of
+// the tile: for plane i it waits for plane i+1 to land, updates the sweep's
+// colour in its rows in place, stores its rows with its own TMA store, and
+// releases plane i-1.  Warps never wait for one another: a warp reads other
+// warps' rows only at cells of the other colour, which nobody writes in this
+// sweep.
+constexpr int TMA_CONSUMERS = 8;
+constexpr int TMA_WS_THREADS = 32 * (TMA_CONSUMERS + 1);
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(sa(bar)) : "memory");
+}
+
+__global__ void __launch_bounds__(TMA_WS_THREADS) k_rbgs_tma(const __grid_constant__ CUtensorMap eld,
+                                                             const __grid_constant__ CUtensorMap est,
+                                                             const __grid_constant__ CUtensorMap rld,
+                                                             const float *__restrict__ eg, Lay L, Tab3<float> t,
+                                                             Bnd b, int colour, float w, float omc, int tj,
+                                                             int chunk, int *err) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ int s_fail;
     const int n2 = L.n2;
     const int e_slot = (tj + 2) * n2, r_slot = tj * n2;
     float *es = reinterpret_cast<float *>(smem);
     float *rs = es + TMA_SLOTS * e_slot;
-    uint64_t *bar = reinterpret_cast<uint64_t *>(rs + TMA_SLOTS * r_slot);
-    float *zt = reinterpret_cast<float *>(bar + TMA_SLOTS);  // c-, c+, d of the z axis
-    for (int k = threadIdx.x; k < n2; k += blockDim.x) {
-        zt[k] = t.cm[2][k];
-        zt[n2 + k] = t.cp[2][k];
-        zt[2 * n2 + k] = t.dg[2][k];
-    }
+    uint64_t *full = reinterpret_cast<uint64_t *>(rs + TMA_SLOTS * r_slot);
+    uint64_t *empty = full + TMA_SLOTS;
     const int j0 = (int)blockIdx.x * tj;
     const int i0 = (int)blockIdx.y * chunk;
     const int i1 = min(L.n0, i0 + chunk);
     if (i0 >= i1) return;
-    const uint32_t bytes = (uint32_t)((e_slot + r_slot) * sizeof(float));
-    auto slot = [](int p) { return (p + 1) & (TMA_SLOTS - 1); };
     if (threadIdx.x == 0) {
-        for (int s = 0; s < TMA_SLOTS; s++) mbar_init(&bar[s], 1);
+        for (int q = 0; q < TMA_SLOTS; q++) {
+            mbar_init(&full[q], 1);
+            mbar_init(&empty[q], TMA_CONSUMERS);
+        }
         mbar_init_fence();
         s_fail = 0;
     }
     __syncthreads();
-    // plane p: e rows j0-1 .. j0+tj (memory rows j0 .. j0+tj+1) and r rows j0 .. j0+tj-1
-    auto issue = [&](int p) {
-        const int s = slot(p);
-        mbar_expect_tx(&bar[s], bytes);
-        tma_load3(es + s * e_slot, &eld, &bar[s], KOFF, j0, p + 1);
-        tma_load3(rs + s * r_slot, &rld, &bar[s], KOFF, j0 + 1, p + 1);
-    };
-    const int last = i1;  // planes i0-1 .. i1 are read
-    int issued = i0 - 2;  // last plane issued
-    if (threadIdx.x == 0)
-        for (int p = i0 - 1; p <= min(i0 + 2, last); p++) issue(p);
-    issued = min(i0 + 2, last);
-    uint32_t phase = 0;
-    int waited = i0 - 2;  // last plane waited for
-    // one thread waits on the slot's mbarrier; the block barrier that follows
-    // every wait releases the others (and orders the landed tile before
-    // their reads)
-    auto wait_plane = [&](int p) {
-        const int s = slot(p);
-        if (threadIdx.x == 0 && !mbar_wait(&bar[s], (phase >> s) & 1u)) s_fail = 1;
-        phase ^= 1u << s;
-        waited = p;
-    };
-    wait_plane(i0 - 1);
-    wait_plane(i0);
-    __syncthreads();
-    // thread -> (row, 4-cell strip): rows jj = sj, sj + rstep, ...; the
-    // z-axis coefficients of the thread's four cells stay in registers
-    const int s4 = n2 >> 2;
-    const int rstep = blockDim.x / s4;
-    const int sj = threadIdx.x / s4;
-    const int k0 = (threadIdx.x - sj * s4) * 4;
-    float zc[3][4];
+    // plane p (i0-1 .. i1) uses slot u % TMA_SLOTS for u = p - (i0-1); its
+    // full phase is (u / TMA_SLOTS) & 1, and it may be loaded once the
+    // previous occupant (u - TMA_SLOTS) has been released
+    const int first = i0 - 1;
+    auto slot_of = [&](int p) { return (p - first) % TMA_SLOTS; };
+    auto par_of = [&](int p) { return (uint32_t)(((p - first) / TMA_SLOTS) & 1); };
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp == 0) {
+        // ---- producer ----
+        if (lane == 0) {
+            const uint32_t bytes = (uint32_t)((e_slot + r_slot) * sizeof(float));
+            int p = first;
+            for (; p <= i1; p++) {
+                const int q = slot_of(p);
+                if (p - first >= TMA_SLOTS && !s_fail) {
+                    if (!mbar_wait(&empty[q], (uint32_t)(((p - first) / TMA_SLOTS - 1) & 1))) {
+                        s_fail = 1;
+                        atomicExch(err, 1);
+                    }
+                }
+                if (s_fail) break;
+                mbar_expect_tx(&full[q], bytes);
+                tma_load3(es + q * e_slot, &eld, &full[q], KOFF, j0, p + 1);
+                tma_load3(rs + q * r_slot, &rld, &full[q], KOFF, j0 + 1, p + 1);
+            }
+            // nothing may be in flight when the block exits: wait (bounded)
+            // for the last planes issued to land
+            for (int x = max(first, p - TMA_SLOTS); x < p; x++) mbar_wait(&full[slot_of(x)], par_of(x));
+        }
+        return;
+    }
+    // ---- consumers ----
+    // A tile holds 2048 cells (tj * n2), so each lane owns exactly two
+    // 4-cell strips per plane, at fixed (row, k) positions: their z and y
+    // coefficients and boundary flags stay in registers for the whole chunk.
+    const int cw = warp - 1;
+    const int rows = tj / TMA_CONSUMERS;  // rows of this warp
+    const int r0 = cw * rows;             // first tile row of this warp
+    const int s4 = n2 >> 2;               // 4-cell strips per row
+    int jj[2], k0[2];
+    float zc[2][3][4], cmy[2], cpy[2], dy[2];
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
-        zc[0][q] = zt[k0 + q];
-        zc[1][q] = zt[n2 + k0 + q];
-        zc[2][q] = zt[2 * n2 + k0 + q];
+    for (int m = 0; m < 2; m++) {
+        const int q = lane + 32 * m;
+        jj[m] = r0 + q / s4;
+        k0[m] = (q % s4) * 4;
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            zc[m][0][c] = t.cm[2][k0[m] + c];
+            zc[m][1][c] = t.cp[2][k0[m] + c];
+            zc[m][2][c] = t.dg[2][k0[m] + c];
+        }
+        const int j = j0 + jj[m];
+        cmy[m] = t.cm[1][j];
+        cpy[m] = t.cp[1][j];
+        dy[m] = t.dg[1][j];
     }
-    const bool kfirst = k0 == 0, klast = k0 + 4 >= n2;
-    // y-axis coefficients of the thread's rows (at most two with 256 threads)
-    float ycm[2] = {0.f, 0.f}, ycp[2] = {0.f, 0.f}, ydg[2] = {0.f, 0.f};
-    for (int m = 0, jj = sj; m < 2 && jj < tj; m++, jj += rstep) {
-        ycm[m] = t.cm[1][j0 + jj];
-        ycp[m] = t.cp[1][j0 + jj];
-        ydg[m] = t.dg[1][j0 + jj];
-    }
-    for (int i = i0; i < i1 && !s_fail; i++) {
-        wait_plane(i + 1);
-        __syncthreads();
-        if (s_fail) break;
-        float *pc = es + slot(i) * e_slot;
-        const float *pm = es + slot(i - 1) * e_slot;
-        const float *pp = es + slot(i + 1) * e_slot;
-        const float *rr = rs + slot(i) * r_slot;
+    auto wait_full = [&](int p) {
+        if (s_fail) return false;
+        if (!mbar_wait(&full[slot_of(p)], par_of(p))) {
+            s_fail = 1;
+            atomicExch(err, 1);
+            return false;
+        }
+        return true;
+    };
+    bool ok = wait_full(first) && wait_full(i0);
+    for (int i = i0; i < i1 && ok; i++) {
+        ok = wait_full(i + 1);
+        if (!ok) break;
+        float *pc = es + slot_of(i) * e_slot;
+        const float *pm = es + slot_of(i - 1) * e_slot;
+        const float *pp = es + slot_of(i + 1) * e_slot;
+        const float *rr = rs + slot_of(i) * r_slot;
         const float cmx = t.cm[0][i], cpx = t.cp[0][i], dx = t.dg[0][i];
 #pragma unroll
         for (int m = 0; m < 2; m++) {
-            const int jj = sj + m * rstep;
-            if (jj >= tj) break;
-            const int j = j0 + jj;
-            float *row = pc + (jj + 1) * n2;
-            const float4 cur = lds4(row + k0);
+            const int j = j0 + jj[m], kk = k0[m];
+            float *row = pc + (jj[m] + 1) * n2;
+            const float4 cur = lds4(row + kk);
             float4 xm, xp, ym, yp;
-            if (i > 0) xm = lds4(pm + (jj + 1) * n2 + k0);
-            else if (b.per[0]) xm = *reinterpret_cast<const float4 *>(eg + L.at(L.n0 - 1, j, k0));
+            if (i > 0) xm = lds4(pm + (jj[m] + 1) * n2 + kk);
+            else if (b.per[0]) xm = *reinterpret_cast<const float4 *>(eg + L.at(L.n0 - 1, j, kk));
             else xm = mirror4(cur, b.sg_lo[0]);
-            if (i < L.n0 - 1) xp = lds4(pp + (jj + 1) * n2 + k0);
-            else if (b.per[0]) xp = *reinterpret_cast<const float4 *>(eg + L.at(0, j, k0));
+            if (i < L.n0 - 1) xp = lds4(pp + (jj[m] + 1) * n2 + kk);
+            else if (b.per[0]) xp = *reinterpret_cast<const float4 *>(eg + L.at(0, j, kk));
             else xp = mirror4(cur, b.sg_hi[0]);
-            if (j > 0) ym = lds4(row - n2 + k0);
-            else if (b.per[1]) ym = *reinterpret_cast<const float4 *>(eg + L.at(i, L.n1 - 1, k0));
+            if (j > 0) ym = lds4(row - n2 + kk);
+            else if (b.per[1]) ym = *reinterpret_cast<const float4 *>(eg + L.at(i, L.n1 - 1, kk));
             else ym = mirror4(cur, b.sg_lo[1]);
-            if (j < L.n1 - 1) yp = lds4(row + n2 + k0);
-            else if (b.per[1]) yp = *reinterpret_cast<const float4 *>(eg + L.at(i, 0, k0));
+            if (j < L.n1 - 1) yp = lds4(row + n2 + kk);
+            else if (b.per[1]) yp = *reinterpret_cast<const float4 *>(eg + L.at(i, 0, kk));
             else yp = mirror4(cur, b.sg_hi[1]);
-            const float4 fr = lds4(rr + jj * n2 + k0);
-            const float left = !kfirst ? row[k0 - 1] : (b.per[2] ? row[n2 - 1] : (b.sg_lo[2] > 0 ? cur.x : -cur.x));
-            const float right = !klast ? row[k0 + 4] : (b.per[2] ? row[0] : (b.sg_hi[2] > 0 ? cur.w : -cur.w));
-            const float cmy = ycm[m], cpy = ycp[m], dy = ydg[m];
+            const float4 fr = lds4(rr + jj[m] * n2 + kk);
+            const float left = kk > 0 ? row[kk - 1] : (b.per[2] ? row[n2 - 1] : (b.sg_lo[2] > 0 ? cur.x : -cur.x));
+            const float right = kk + 4 < n2 ? row[kk + 4] : (b.per[2] ? row[0] : (b.sg_hi[2] > 0 ? cur.w : -cur.w));
             if (((colour + i + j) & 1) == 0)
-                strip4<0>(row + k0, cur, xm, xp, ym, yp, fr, left, right, cmx, cpx, dx, cmy, cpy, dy, zc, w, omc);
+                strip4<0>(row + kk, cur, xm, xp, ym, yp, fr, left, right, cmx, cpx, dx, cmy[m], cpy[m], dy[m], zc[m],
+                          w, omc);
             else
-                strip4<1>(row + k0, cur, xm, xp, ym, yp, fr, left, right, cmx, cpx, dx, cmy, cpy, dy, zc, w, omc);
+                strip4<1>(row + kk, cur, xm, xp, ym, yp, fr, left, right, cmx, cpx, dx, cmy[m], cpy[m], dy[m], zc[m],
+                          w, omc);
         }
         fence_async_smem();
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            tma_store3(&est, pc + n2, KOFF, j0 + 1, i + 1);
+        __syncwarp();
+        if (lane == 0) {
+            tma_store3(&est, pc + (r0 + 1) * n2, KOFF, j0 + r0 + 1, i + 1);
             bulk_commit();
-            if (i + 3 <= last) {
-                bulk_wait_read1();  // the store of plane i-1 has read the slot plane i+3 reuses
-                issue(i + 3);
+            if (i > i0 - 1) {
+                bulk_wait_read1();  // this warp's store of plane i-1 has read the slot
+                mbar_arrive(&empty[slot_of(i - 1)]);
             }
         }
-        if (i + 3 <= last) issued = i + 3;
+        __syncwarp();
     }
-    if (threadIdx.x == 0) {
-        if (s_fail) {
-            atomicExch(err, 1);
-            // let every load still in flight land before the block's shared memory goes away
-            for (int p = waited + 1; p <= issued; p++) {
-                const int s = slot(p);
-                mbar_wait(&bar[s], (phase >> s) & 1u);
-                phase ^= 1u << s;
-            }
-        }
-        bulk_wait_all();
-    }
+    if (lane == 0) bulk_wait_all();
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -285,8 +303,7 @@ bool encode3(CUtensorMap *m, const float *base, const Lay &L, int rows) {
 }
 
 size_t tma_smem(int tj, int n2) {
-    return (size_t)TMA_SLOTS * ((size_t)(tj + 2) * n2 + (size_t)tj * n2) * sizeof(float) + TMA_SLOTS * 8 +
-           (size_t)3 * n2 * sizeof(float);
+    return (size_t)TMA_SLOTS * ((size_t)(tj + 2) * n2 + (size_t)tj * n2) * sizeof(float) + 2 * TMA_SLOTS * 8;
 }
 
 }  // namespace
@@ -298,21 +315,22 @@ void tma_plan(saras_mg *h, Level &v) {
     v.tma.ok = 0;
     const Lay &L = v.lay;
     if (!h->d3 || !v.e32 || !v.r32) return;
-    // rows of 32..256 cells, a power of two: 256 threads cover a tile as
-    // (row, 4-cell strip) pairs, two rows each
+    // rows of 32..256 cells (a power of two); tiles of 2048 cells shared by
+    // the consumer warps row-wise
     if (L.n2 < 32 || L.n2 > 256 || 1024 % L.n2 != 0 || (int64_t)L.n0 * L.n1 * L.n2 < (1 << 20)) return;
-    int tj = std::max(2, 2048 / L.n2);
-    while (tj >= 2 && (L.n1 % tj != 0 || tj + 2 > 256)) tj /= 2;
-    if (tj < 2) return;
-    if (tma_smem(tj, L.n2) > 200 * 1024) return;
+    // tiles of exactly 2048 cells: two 4-cell strips per consumer lane
+    const int tj = 2048 / L.n2;
+    if (L.n1 % tj != 0 || tj % TMA_CONSUMERS != 0 || tj + 2 > 256) return;
+    const size_t smem = tma_smem(tj, L.n2);
+    if (smem > 200 * 1024) return;
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int per_sm = std::max(1, (int)((227 * 1024) / smem));
     const int jt = L.n1 / tj;
-    const int want = 3 * sms;
-    const int nchunks = std::max(1, want / jt);  // one wave: at most three blocks per SM
+    const int nchunks = std::max(1, per_sm * sms / jt);  // one wave
     const int chunk = std::max(4, (L.n0 + nchunks - 1) / nchunks);
-    if (!encode3(&v.tma.eld, v.e32, L, tj + 2) || !encode3(&v.tma.est, v.e32, L, tj) ||
+    if (!encode3(&v.tma.eld, v.e32, L, tj + 2) || !encode3(&v.tma.est, v.e32, L, tj / TMA_CONSUMERS) ||
         !encode3(&v.tma.rld, v.r32, L, tj))
         return;
     // one attribute for every level and handle: the largest ring any plan may use
@@ -339,7 +357,7 @@ bool tma_colour(saras_mg *h, cudaStream_t s, Level &v, int colour) {
         b.sg_hi[d] = h->ghost.kind[2 * d + 1] == SARAS_BC_NEUMANN ? 1 : -1;
     }
     int *err = reinterpret_cast<int *>(h->norm_out + 7);
-    k_rbgs_tma<<<grid, TMA_THREADS, tma_smem(v.tma.tj, L.n2), s>>>(
+    k_rbgs_tma<<<grid, TMA_WS_THREADS, tma_smem(v.tma.tj, L.n2), s>>>(
         v.tma.eld, v.tma.est, v.tma.rld, v.e32, L, t, b, colour, (float)h->prm.sor_param,
         (float)(1.0 - h->prm.sor_param), v.tma.tj, v.tma.chunk, err);
     return true;
