@@ -459,6 +459,113 @@ def run_serving(S, args):
     }
 
 
+def blob_rhs(S, g, count=16, sigma=0.05, seed=3):
+    """Sum of `count` seeded Gaussian blobs (centres uniform in the domain,
+    amplitudes N(0,1)), evaluated separably at the cell centres."""
+    rng = np.random.default_rng(seed)
+    cen = rng.uniform(0.0, 1.0, (count, 3)) * np.array(list(g.len))
+    amp = rng.normal(0.0, 1.0, count)
+    xs = [S.grid_metrics(g, 0, d)[0][1:-1] for d in range(3)]
+    f = np.zeros((g.n[0], g.n[1], g.n[2]))
+    for c, a in zip(cen, amp):
+        gx, gy, gz = (np.exp(-((xs[d] - c[d]) ** 2) / (2 * sigma * sigma)) for d in range(3))
+        f += a * gx[:, None, None] * gy[None, :, None] * gz[None, None, :]
+    rhs = S.padded_field(g)
+    rhs[1:-1, 1:-1, 1:-1] = f
+    return rhs
+
+
+def run_c3(args):
+    """512^3 MIXED against FP64: mesh DDD (tanh beta 1.2 on every axis),
+    periodic x and y, Dirichlet walls in z, RHS of 16 Gaussian blobs
+    (sigma 0.05), to rel-res 1e-10.  3/6 smoothing (the reference defaults):
+    the 2/2 V-cycle diverges on this stretching."""
+    import torch
+    import saras_gb300 as S
+    n = args.c3_n
+    g = S.grid_desc(n=(n, n, n), mesh="DDD", beta=(1.2, 1.2, 1.2), domain="PPN")
+    rhs = blob_rhs(S, g)
+    stream = torch.cuda.current_stream()
+    rhs_d = torch.from_numpy(rhs).cuda()
+    lhs_d = torch.zeros_like(rhs_d)
+    st = [x // 8 for x in rhs.strides]
+    off = st[0] + st[1] + st[2]
+    kw = dict(vc_count=2000, vc_tolerance=TOL, mg_tolerance=1e-9, pre_smooth=3, post_smooth=6,
+              bc_kind=[0, 0, 0, 0, 1, 1])
+    out = {"config": "c3", "workload": f"Poisson {n}^3, mesh DDD beta 1.2, periodic x/y, Dirichlet z, 16 Gaussian "
+                                       "blobs sigma 0.05 (seed 3), 3/6 RBGS, coarsest tol 1e-9, to rel-res 1e-10"}
+    sols = {}
+    for name, prec, inner in (("mixed", S.PREC_MIXED, 8), ("fp64", S.PREC_FP64, 1)):
+        mg = S.Multigrid(g, S.mg_params(precision=prec, inner_cycles=inner, **kw), stream=stream.cuda_stream)
+        lhs_d.zero_()
+        mg.mg_solve_dev(lhs_d.data_ptr() + 8 * off, rhs_d.data_ptr() + 8 * off, st)  # warm-up
+        ms, cyc = time_solves(mg, lhs_d, rhs_d, st, off, args.steps, torch, stream)
+        out[f"{name}_ms"] = ms
+        out[f"{name}_cycles"] = int(np.median(cyc))
+        out[f"{name}_final_residual"] = float(mg.history[-1])
+        sols[name] = lhs_d[1:-1, 1:-1, 1:-1].cpu().numpy()
+        mg.close()
+    out["mixed_vcycles"] = out["mixed_cycles"] * 8
+    out["speedup_mixed_vs_fp64"] = out["fp64_ms"] / out["mixed_ms"]
+    out["mixed_vs_fp64_rel_err"] = float(np.abs(sols["mixed"] - sols["fp64"]).max() / np.abs(sols["fp64"]).max())
+    print(json.dumps(out), flush=True)
+
+
+def run_rk3(args):
+    """Time steps of 3-D Rayleigh-Benard convection: 256^3, Ra 1e7, Pr 1,
+    z tanh-stretched, no-slip isothermal plates, periodic sides, u = 0 and
+    T = conductive profile + seeded noise 1e-3; CN Jacobi to 1e-6 and the
+    reference's Multigrid defaults (3/6, coarsest tol 1e-2, 20 cycles,
+    1e-6); dt 1e-4 (the reference default time step).  FP64 and MIXED
+    pressure solves.  The stretching defaults to beta 1.3: at 1.5 the
+    reference pressure V-cycle diverges in the first sub-step on this machine
+    (the CPU restatement does the same)."""
+    import saras_gb300 as S
+    n = args.rk3_n
+    beta = args.rk3_beta
+    g = S.grid_desc(n=(n, n, n), mesh="UUD", beta=(1.0, 1.0, beta), domain="PPN")
+    nu, ka, fb = S.rbc_coefficients(2, 1e7, 1.0)
+    out = {"config": "rk3", "workload": f"RK3 Rayleigh-Benard {n}^3, Ra 1e7, Pr 1, z tanh beta {beta}, PPN, "
+                                        f"dt 1e-4, CN tol 1e-6, MG 3/6 tol 1e-6 coarsest 1e-2, {args.rk3_steps} steps"}
+    for name, prec in (("fp64", S.PREC_FP64), ("mixed", S.PREC_MIXED)):
+        p = S.Rk3Params()
+        p.nu, p.kappa, p.dt = nu, ka, 1e-4
+        p.cn_tolerance = 1e-6
+        p.max_iterations = 0
+        p.g_terms[0], p.g_terms[1], p.g_terms[2] = 0.0, 0.0, -fb
+        p.with_scalar = 1
+        p.nl_scheme = 1
+        zero = S.field_bc([S.FBC_DIRICHLET] * 6, [0.0] * 6)
+        p.bc_vx, p.bc_vy, p.bc_vz = zero, zero, zero
+        p.bc_t = S.field_bc([S.FBC_NEUMANN] * 4 + [S.FBC_DIRICHLET] * 2, [0, 0, 0, 0, 1.0, 0.0])
+        p.bc_p = S.field_bc([S.FBC_NEUMANN] * 6, [0.0] * 6)
+        p.mg = S.mg_params(vc_count=20, vc_tolerance=1e-6, pre_smooth=3, post_smooth=6, mg_tolerance=1e-2,
+                           precision=prec)
+        rng = np.random.default_rng(4)
+        f = {k: S.padded_field(g) for k in ("vx", "vy", "vz", "p", "t", "pp")}
+        zc = S.grid_metrics(g, 0, 2)[0]
+        f["t"][...] = (1.0 - zc)[None, None, :] + rng.uniform(-5e-4, 5e-4, f["t"].shape)
+        f["p"][...] = 1.0
+        rk = S.RK3(g, p)
+        rk.upload(f["vx"], f["vy"], f["vz"], f["p"], f["t"], f["pp"])
+        rk.step(1)  # warm-up
+        import torch
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        mgc, cni = rk.step(args.rk3_steps)
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) * 1e3 / args.rk3_steps
+        rk.download(f["vx"], f["vy"], f["vz"], f["p"], f["t"], f["pp"])
+        rk.close()
+        out[f"{name}_ms_per_step"] = dt
+        out[f"{name}_mg_cycles_per_step"] = mgc / args.rk3_steps
+        out[f"{name}_cn_iters_per_step"] = cni / args.rk3_steps
+        out[f"{name}_max_w"] = float(np.abs(f["vz"][1:-1, 1:-1, 1:-1]).max())
+        out[f"{name}_t_mean"] = float(f["t"][1:-1, 1:-1, 1:-1].mean())
+    out["speedup_mixed_vs_fp64"] = out["fp64_ms_per_step"] / out["mixed_ms_per_step"]
+    print(json.dumps(out), flush=True)
+
+
 def run_serve_only(args):
     import torch
     torch.cuda.set_device(0)
@@ -508,8 +615,18 @@ def main():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-no-tune", action="store_true", help="keep the default schedule (no autotune)")
     ap.add_argument("--serve-only", action="store_true")
+    ap.add_argument("--config", choices=["mg256", "c3", "rk3"], default="mg256",
+                    help="mg256: the headline line; c3: 512^3 MIXED vs FP64; rk3: RK3 Rayleigh-Benard steps")
+    ap.add_argument("--c3-n", type=int, default=512)
+    ap.add_argument("--rk3-n", type=int, default=256)
+    ap.add_argument("--rk3-steps", type=int, default=5)
+    ap.add_argument("--rk3-beta", type=float, default=1.3)
     args = ap.parse_args()
-    if args.profile:
+    if args.config == "c3":
+        run_c3(args)
+    elif args.config == "rk3":
+        run_rk3(args)
+    elif args.profile:
         run_profile(args)
     elif args.serve_only:
         run_serve_only(args)
