@@ -6,6 +6,7 @@
 
 #include <cstdint>
 #include <cstdio>
+#include <utility>
 
 #include "../../include/saras_gb300.h"
 
@@ -63,6 +64,32 @@ __device__ __forceinline__ double rmul(double a, double b) { return __dmul_rn(a,
 __device__ __forceinline__ double rdiv(double a, double b) { return __ddiv_rn(a, b); }
 
 inline unsigned cdiv(int64_t a, int64_t b) { return (unsigned)((a + b - 1) / b); }
+
+// Programmatic dependent launch: the V-cycle kernels are launched with
+// programmatic stream serialisation, so the next kernel's blocks are
+// scheduled while this one drains.  Every such kernel first lets its
+// dependants launch and then waits until the kernel before it has finished
+// and its writes are visible; launched without the attribute both are no-ops.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
+template <typename... KArgs, typename... Args>
+inline void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                       Args &&...args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 // Visits the core cells of a level for grid-wide reductions: each warp takes
 // whole k-rows (32-bit index arithmetic only) and its lanes stride along k,

@@ -541,8 +541,9 @@ void coarsest_level(saras_mg *h, cudaStream_t s) {
     const int top = h->nl - 1;
     Level &c = h->lv[(size_t)top];
     if (h->prm.solve_flag) {
-        coarsest_fast(h, s, c);
+        coarsest_fast(h, s, c);  // starts from zero itself
     } else {
+        cudaMemsetAsync(c.lhs, 0, (size_t)c.lay.size * sizeof(double), s);
         smooth_exact(h, s, top, h->prm.pre_smooth, true);
     }
 }

@@ -33,6 +33,7 @@ constexpr int BX = 128;
 template <bool D3, bool W1>
 __global__ void k_rbgs64(double *u, const double *__restrict__ f, const double *__restrict__ wd, Lay L,
                          Tab3<double> t, Bnd b, int colour, double omc) {
+    pdl_enter();
     const int kk = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = D3 ? (int)blockIdx.y : 0;
     const int i = blockIdx.z;
@@ -48,6 +49,7 @@ __global__ void k_rbgs64(double *u, const double *__restrict__ f, const double *
 template <bool D3>
 __global__ void k_rbgs32(float *e, const float *__restrict__ r, Lay L, Tab3<float> t, Bnd b, int colour, float w,
                          float omc) {
+    pdl_enter();
     const int kk = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = D3 ? (int)blockIdx.y : 0;
     const int i = blockIdx.z;
@@ -149,6 +151,7 @@ __device__ __forceinline__ void strip_update(T *u, const T (&cur)[8], const T (&
 template <class T, bool D3, bool WD>
 __global__ void k_rbgs_v8(T *u, const T *__restrict__ f, const T *__restrict__ wd, Lay L, Tab3<T> t, Bnd b,
                           int colour, T w, T omc) {
+    pdl_enter();
     const int k0 = 8 * (int)(blockIdx.x * blockDim.x + threadIdx.x);
     const int j = D3 ? (int)(blockIdx.y * blockDim.y + threadIdx.y) : 0;
     const int i = blockIdx.z;
@@ -187,7 +190,9 @@ __global__ void k_rbgs_v8(T *u, const T *__restrict__ f, const T *__restrict__ w
 // weights v_abc / vTot of poisson_d3.cc:494-508, factorised per axis).
 template <class T, class TO, bool D3>
 __global__ void k_resid_restrict(const T *__restrict__ u, const T *__restrict__ f, Lay Lf, Tab3<T> t, Bnd b,
-                                 WTab<T> w, TO *__restrict__ rc, Lay Lc, const T *__restrict__ dd) {
+                                 WTab<T> w, TO *__restrict__ rc, Lay Lc, const T *__restrict__ dd,
+                                 TO *__restrict__ ezero) {
+    pdl_enter();
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = D3 ? (int)blockIdx.y : 0;
     const int i = blockIdx.z;
@@ -214,6 +219,7 @@ __global__ void k_resid_restrict(const T *__restrict__ u, const T *__restrict__ 
         out = ((r00 + r01) + (r10 + r11)) * T(0.25);
     }
     rc[Lc.at(i, j, k)] = (TO)out;
+    if (ezero) ezero[Lc.at(i, j, k)] = TO(0);  // the coarse level's error starts from zero
 }
 
 // Residuals of eight consecutive fine cells of one row (k_resid_restrict's
@@ -274,7 +280,9 @@ __device__ __forceinline__ void resid_row8(const T *__restrict__ u, const T *__r
 // n_z a multiple of 8), the same arithmetic as k_resid_restrict.
 template <class T, bool D3>
 __global__ void __launch_bounds__(128, 4) k_resid_restrict8(const T *__restrict__ u, const T *__restrict__ f, Lay Lf, Tab3<T> t, Bnd b,
-                                  WTab<T> w, T *__restrict__ rc, Lay Lc, const T *__restrict__ dd) {
+                                  WTab<T> w, T *__restrict__ rc, Lay Lc, const T *__restrict__ dd,
+                                  T *__restrict__ ezero) {
+    pdl_enter();
     const int kc0 = 4 * (int)(blockIdx.x * blockDim.x + threadIdx.x);
     const int j = D3 ? (int)(blockIdx.y * blockDim.y + threadIdx.y) : 0;
     const int i = blockIdx.z;
@@ -304,17 +312,24 @@ __global__ void __launch_bounds__(128, 4) k_resid_restrict8(const T *__restrict_
         for (int q = 0; q < 4; q++) out[q] = ((r0[2 * q] + r0[2 * q + 1]) + (r1[2 * q] + r1[2 * q + 1])) * T(0.25);
     }
     T *dst = rc + Lc.at(i, j, kc0);
+    T *ez = ezero ? ezero + Lc.at(i, j, kc0) : nullptr;  // the coarse level's error starts from zero
     if (sizeof(T) == 4) {
         reinterpret_cast<float4 *>(dst)[0] = make_float4((float)out[0], (float)out[1], (float)out[2], (float)out[3]);
+        if (ez) reinterpret_cast<float4 *>(ez)[0] = make_float4(0.f, 0.f, 0.f, 0.f);
     } else {
         reinterpret_cast<double2 *>(dst)[0] = make_double2((double)out[0], (double)out[1]);
         reinterpret_cast<double2 *>(dst)[1] = make_double2((double)out[2], (double)out[3]);
+        if (ez) {
+            reinterpret_cast<double2 *>(ez)[0] = make_double2(0.0, 0.0);
+            reinterpret_cast<double2 *>(ez)[1] = make_double2(0.0, 0.0);
+        }
     }
 }
 
 // Injection prolongation and correction in place: fine += coarse(i/2,..).
 template <class TF, class TC>
 __global__ void k_prolong_add(TF *__restrict__ f, const TC *__restrict__ c, Lay Lf, Lay Lc, int d3) {
+    pdl_enter();
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y, i = blockIdx.z;
     if (k >= Lf.n2) return;
@@ -353,6 +368,7 @@ __device__ __forceinline__ void ld4<double>(const double *__restrict__ p, double
 
 template <class T>
 __global__ void k_prolong_add8(T *__restrict__ f, const T *__restrict__ c, Lay Lf, Lay Lc, int d3) {
+    pdl_enter();
     const int k0 = 8 * (int)(blockIdx.x * blockDim.x + threadIdx.x);
     const int j = (int)(blockIdx.y * blockDim.y + threadIdx.y), i = blockIdx.z;
     if (k0 >= Lf.n2 || j >= Lf.n1) return;
@@ -482,11 +498,12 @@ template <bool D3>
 __global__ void k_coarsest_fast(double *ug, const double *__restrict__ fg, const double *__restrict__ wdg,
                                 const double *__restrict__ ddg, Lay L, Tab3<double> t, Bnd b, double omc, double tol,
                                 int max_count, int *sweeps_out) {
+    pdl_enter();
     extern __shared__ double stage[];
     __shared__ unsigned long long shm[32];
     double *u = stage, *f = stage + L.size, *wd = stage + 2 * L.size, *dd = stage + 3 * L.size;
     for (int64_t q = threadIdx.x; q < L.size; q += blockDim.x) {
-        u[q] = ug[q];
+        u[q] = 0.0;  // the coarsest solve starts from zero
         f[q] = fg[q];
         wd[q] = wdg[q];
         dd[q] = ddg[q];
@@ -536,6 +553,7 @@ __global__ void k_coarsest_fast(double *ug, const double *__restrict__ fg, const
 
 // u += e over the core (MIXED form update, FP64 accumulate).
 __global__ void k_update64(double *__restrict__ u, const float *__restrict__ e, Lay L) {
+    pdl_enter();
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y, i = blockIdx.z;
     if (k >= L.n2) return;
@@ -671,9 +689,9 @@ void colour_v8(saras_mg *h, cudaStream_t s, Level &v, T *u, const T *f, const T 
     const dim3 g(cdiv(strips, bx), h->d3 ? cdiv(L.n1, by) : 1u, (unsigned)L.n0);
     const Bnd b = bnd(h);
     if (h->d3)
-        k_rbgs_v8<T, true, WD><<<g, blk, 0, s>>>(u, f, wd, L, tb, b, colour, w, omc);
+        launch_pdl(k_rbgs_v8<T, true, WD>, g, blk, 0, s, u, f, wd, L, tb, b, colour, w, omc);
     else
-        k_rbgs_v8<T, false, WD><<<g, blk, 0, s>>>(u, f, wd, L, tb, b, colour, w, omc);
+        launch_pdl(k_rbgs_v8<T, false, WD>, g, blk, 0, s, u, f, wd, L, tb, b, colour, w, omc);
 }
 
 void colour64(saras_mg *h, cudaStream_t s, int l, int colour) {
@@ -692,17 +710,17 @@ void colour64(saras_mg *h, cudaStream_t s, int l, int colour) {
     kbegin(h, s, l == 0 ? KC_SMOOTH0 : -1);
     if (h->d3) {
         if (w1)
-            k_rbgs64<true, true><<<cgrid(L, true, half, bx), bx, 0, s>>>(v.lhs, v.rhs, v.inv_diag, L, tab64(v),
+            launch_pdl(k_rbgs64<true, true>, cgrid(L, true, half, bx), bx, 0, s, v.lhs, v.rhs, v.inv_diag, L, tab64(v),
                                                                          b, colour, omc);
         else
-            k_rbgs64<true, false><<<cgrid(L, true, half, bx), bx, 0, s>>>(v.lhs, v.rhs, v.inv_diag, L, tab64(v),
+            launch_pdl(k_rbgs64<true, false>, cgrid(L, true, half, bx), bx, 0, s, v.lhs, v.rhs, v.inv_diag, L, tab64(v),
                                                                           b, colour, omc);
     } else {
         if (w1)
-            k_rbgs64<false, true><<<cgrid(L, false, half, bx), bx, 0, s>>>(v.lhs, v.rhs, v.inv_diag, L,
+            launch_pdl(k_rbgs64<false, true>, cgrid(L, false, half, bx), bx, 0, s, v.lhs, v.rhs, v.inv_diag, L,
                                                                            tab64(v), b, colour, omc);
         else
-            k_rbgs64<false, false><<<cgrid(L, false, half, bx), bx, 0, s>>>(v.lhs, v.rhs, v.inv_diag, L,
+            launch_pdl(k_rbgs64<false, false>, cgrid(L, false, half, bx), bx, 0, s, v.lhs, v.rhs, v.inv_diag, L,
                                                                             tab64(v), b, colour, omc);
     }
     kend(h, s, l == 0 ? KC_SMOOTH0 : -1);
@@ -729,9 +747,9 @@ void colour32(saras_mg *h, cudaStream_t s, int l, int colour) {
     const Bnd b = bnd(h);
     kbegin(h, s, l == 0 ? KC_SMOOTH0 : -1);
     if (h->d3)
-        k_rbgs32<true><<<cgrid(L, true, half, bx), bx, 0, s>>>(v.e32, v.r32, L, tab32(v), b, colour, w, omc);
+        launch_pdl(k_rbgs32<true>, cgrid(L, true, half, bx), bx, 0, s, v.e32, v.r32, L, tab32(v), b, colour, w, omc);
     else
-        k_rbgs32<false><<<cgrid(L, false, half, bx), bx, 0, s>>>(v.e32, v.r32, L, tab32(v), b, colour, w, omc);
+        launch_pdl(k_rbgs32<false>, cgrid(L, false, half, bx), bx, 0, s, v.e32, v.r32, L, tab32(v), b, colour, w, omc);
     kend(h, s, l == 0 ? KC_SMOOTH0 : -1);
 }
 
@@ -754,6 +772,11 @@ void residual_restrict(saras_mg *h, cudaStream_t s, int l, bool mixed) {
     const int bx = bxfor(Lc.n2);
     const Bnd b = bnd(h);
     const bool to64 = l + 1 == h->nl - 1;  // the coarsest level is FP64 in every form
+    // the coarse level's iterate starts from zero; the restriction clears it
+    // (the coarsest solve clears its own)
+    double *z64 = to64 ? nullptr : c.lhs;
+    float *z32 = to64 ? nullptr : c.e32;
+    const dim3 gs = cgrid(Lc, h->d3, Lc.n2, bx);
     kbegin(h, s, l == 0 ? KC_RESTRICT : -1);
     if (v8_ok(f.lay) && (!mixed || !to64)) {
         const int strips = Lc.n2 / 4, bx4 = std::min(strips, 32), by = h->d3 ? std::max(1, 128 / bx4) : 1;
@@ -761,40 +784,40 @@ void residual_restrict(saras_mg *h, cudaStream_t s, int l, bool mixed) {
         const dim3 blk(bx4, by);
         if (!mixed) {
             if (h->d3)
-                k_resid_restrict8<double, true><<<g4, blk, 0, s>>>(f.lhs, f.rhs, f.lay, tab64(f), b, wt64(c), c.rhs,
-                                                                   Lc, f.dd);
+                launch_pdl(k_resid_restrict8<double, true>, g4, blk, 0, s, f.lhs, f.rhs, f.lay, tab64(f), b, wt64(c),
+                           c.rhs, Lc, f.dd, z64);
             else
-                k_resid_restrict8<double, false><<<g4, blk, 0, s>>>(f.lhs, f.rhs, f.lay, tab64(f), b, wt64(c),
-                                                                    c.rhs, Lc, f.dd);
+                launch_pdl(k_resid_restrict8<double, false>, g4, blk, 0, s, f.lhs, f.rhs, f.lay, tab64(f), b,
+                           wt64(c), c.rhs, Lc, f.dd, z64);
         } else {
             if (h->d3)
-                k_resid_restrict8<float, true><<<g4, blk, 0, s>>>(f.e32, f.r32, f.lay, tab32(f), b, wt32(c), c.r32,
-                                                                  Lc, nullptr);
+                launch_pdl(k_resid_restrict8<float, true>, g4, blk, 0, s, f.e32, f.r32, f.lay, tab32(f), b, wt32(c),
+                           c.r32, Lc, (const float *)nullptr, z32);
             else
-                k_resid_restrict8<float, false><<<g4, blk, 0, s>>>(f.e32, f.r32, f.lay, tab32(f), b, wt32(c),
-                                                                   c.r32, Lc, nullptr);
+                launch_pdl(k_resid_restrict8<float, false>, g4, blk, 0, s, f.e32, f.r32, f.lay, tab32(f), b,
+                           wt32(c), c.r32, Lc, (const float *)nullptr, z32);
         }
     } else if (!mixed) {
         if (h->d3)
-            k_resid_restrict<double, double, true><<<cgrid(Lc, true, Lc.n2, bx), bx, 0, s>>>(
-                f.lhs, f.rhs, f.lay, tab64(f), b, wt64(c), c.rhs, Lc, f.dd);
+            launch_pdl(k_resid_restrict<double, double, true>, gs, bx, 0, s, f.lhs, f.rhs, f.lay, tab64(f), b,
+                       wt64(c), c.rhs, Lc, f.dd, z64);
         else
-            k_resid_restrict<double, double, false><<<cgrid(Lc, false, Lc.n2, bx), bx, 0, s>>>(
-                f.lhs, f.rhs, f.lay, tab64(f), b, wt64(c), c.rhs, Lc, f.dd);
+            launch_pdl(k_resid_restrict<double, double, false>, gs, bx, 0, s, f.lhs, f.rhs, f.lay, tab64(f), b,
+                       wt64(c), c.rhs, Lc, f.dd, z64);
     } else if (to64) {
         if (h->d3)
-            k_resid_restrict<float, double, true><<<cgrid(Lc, true, Lc.n2, bx), bx, 0, s>>>(
-                f.e32, f.r32, f.lay, tab32(f), b, wt32(c), c.rhs, Lc, nullptr);
+            launch_pdl(k_resid_restrict<float, double, true>, gs, bx, 0, s, f.e32, f.r32, f.lay, tab32(f), b,
+                       wt32(c), c.rhs, Lc, (const float *)nullptr, (double *)nullptr);
         else
-            k_resid_restrict<float, double, false><<<cgrid(Lc, false, Lc.n2, bx), bx, 0, s>>>(
-                f.e32, f.r32, f.lay, tab32(f), b, wt32(c), c.rhs, Lc, nullptr);
+            launch_pdl(k_resid_restrict<float, double, false>, gs, bx, 0, s, f.e32, f.r32, f.lay, tab32(f), b,
+                       wt32(c), c.rhs, Lc, (const float *)nullptr, (double *)nullptr);
     } else {
         if (h->d3)
-            k_resid_restrict<float, float, true><<<cgrid(Lc, true, Lc.n2, bx), bx, 0, s>>>(
-                f.e32, f.r32, f.lay, tab32(f), b, wt32(c), c.r32, Lc, nullptr);
+            launch_pdl(k_resid_restrict<float, float, true>, gs, bx, 0, s, f.e32, f.r32, f.lay, tab32(f), b,
+                       wt32(c), c.r32, Lc, (const float *)nullptr, z32);
         else
-            k_resid_restrict<float, float, false><<<cgrid(Lc, false, Lc.n2, bx), bx, 0, s>>>(
-                f.e32, f.r32, f.lay, tab32(f), b, wt32(c), c.r32, Lc, nullptr);
+            launch_pdl(k_resid_restrict<float, float, false>, gs, bx, 0, s, f.e32, f.r32, f.lay, tab32(f), b,
+                       wt32(c), c.r32, Lc, (const float *)nullptr, z32);
     }
     kend(h, s, l == 0 ? KC_RESTRICT : -1);
 }
@@ -811,15 +834,15 @@ void prolong_add(saras_mg *h, cudaStream_t s, int l, bool mixed) {
         const int strips = L.n2 / 8, bx8 = std::min(strips, 32), by = h->d3 ? std::max(1, 128 / bx8) : 1;
         const dim3 g8(cdiv(strips, bx8), cdiv(L.n1, by), (unsigned)L.n0);
         if (!mixed)
-            k_prolong_add8<double><<<g8, dim3(bx8, by), 0, s>>>(f.lhs, c.lhs, L, c.lay, h->d3 ? 1 : 0);
+            launch_pdl(k_prolong_add8<double>, g8, dim3(bx8, by), 0, s, f.lhs, c.lhs, L, c.lay, h->d3 ? 1 : 0);
         else
-            k_prolong_add8<float><<<g8, dim3(bx8, by), 0, s>>>(f.e32, c.e32, L, c.lay, h->d3 ? 1 : 0);
+            launch_pdl(k_prolong_add8<float>, g8, dim3(bx8, by), 0, s, f.e32, c.e32, L, c.lay, h->d3 ? 1 : 0);
     } else if (!mixed)
-        k_prolong_add<double, double><<<g, bx, 0, s>>>(f.lhs, c.lhs, L, c.lay, h->d3 ? 1 : 0);
+        launch_pdl(k_prolong_add<double, double>, g, bx, 0, s, f.lhs, c.lhs, L, c.lay, h->d3 ? 1 : 0);
     else if (l == h->nl - 1)
-        k_prolong_add<float, double><<<g, bx, 0, s>>>(f.e32, c.lhs, L, c.lay, h->d3 ? 1 : 0);
+        launch_pdl(k_prolong_add<float, double>, g, bx, 0, s, f.e32, c.lhs, L, c.lay, h->d3 ? 1 : 0);
     else
-        k_prolong_add<float, float><<<g, bx, 0, s>>>(f.e32, c.e32, L, c.lay, h->d3 ? 1 : 0);
+        launch_pdl(k_prolong_add<float, float>, g, bx, 0, s, f.e32, c.e32, L, c.lay, h->d3 ? 1 : 0);
     kend(h, s, l == 1 ? KC_PROLONG : -1);
 }
 
@@ -914,17 +937,10 @@ void vcycle_fast(saras_mg *h, cudaStream_t s, bool mixed) {
     smooth(h, s, 0, h->prm.pre_smooth, mixed);
     for (int l = 0; l < top; l++) {
         residual_restrict(h, s, l, mixed);
-        Level &c = h->lv[(size_t)l + 1];
-        if (l + 1 == top) {
-            cudaMemsetAsync(c.lhs, 0, (size_t)c.lay.size * sizeof(double), s);
+        if (l + 1 == top)
             coarsest_level(h, s);
-        } else {
-            if (mixed)
-                cudaMemsetAsync(c.e32, 0, (size_t)c.lay.size * sizeof(float), s);
-            else
-                cudaMemsetAsync(c.lhs, 0, (size_t)c.lay.size * sizeof(double), s);
+        else
             smooth(h, s, l + 1, h->prm.pre_smooth, mixed);
-        }
     }
     for (int l = top; l > 0; l--) {
         prolong_add(h, s, l, mixed);
@@ -949,7 +965,7 @@ void fast_cycle(saras_mg *h, cudaStream_t s) {
         const Lay &L = v0.lay;
         const int bx = bxfor(L.n2);
         kbegin(h, s, -1);
-        k_update64<<<dim3(cdiv(L.n2, bx), (unsigned)L.n1, (unsigned)L.n0), bx, 0, s>>>(v0.lhs, v0.e32, L);
+        launch_pdl(k_update64, dim3(cdiv(L.n2, bx), (unsigned)L.n1, (unsigned)L.n0), bx, 0, s, v0.lhs, v0.e32, L);
     }
     resid_norm(h, s, mixed);
 }
@@ -975,6 +991,7 @@ void coarsest_fast(saras_mg *h, cudaStream_t s, Level &c) {
     const Lay &C = c.lay;
     const size_t smem = (size_t)(4 * C.size) * sizeof(double);
     if (smem > 200 * 1024) {  // coarsest grid too large for one block's shared memory
+        cudaMemsetAsync(c.lhs, 0, (size_t)C.size * sizeof(double), s);
         smooth(h, s, h->nl - 1, std::max(1, h->prm.pre_smooth), false);
         return;
     }
@@ -983,11 +1000,11 @@ void coarsest_fast(saras_mg *h, cudaStream_t s, Level &c) {
     const Bnd b = bnd(h);
     kbegin(h, s, KC_COARSE);
     if (h->d3)
-        k_coarsest_fast<true><<<1, threads, smem, s>>>(c.lhs, c.rhs, c.inv_diag, c.dd, C, tab64(c), b,
+        launch_pdl(k_coarsest_fast<true>, 1, threads, smem, s, c.lhs, c.rhs, c.inv_diag, c.dd, C, tab64(c), b,
                                                        1.0 - h->prm.sor_param, h->prm.mg_tolerance, h->maxCount(),
                                                        h->coarse_sweeps);
     else
-        k_coarsest_fast<false><<<1, threads, smem, s>>>(c.lhs, c.rhs, c.inv_diag, c.dd, C, tab64(c), b,
+        launch_pdl(k_coarsest_fast<false>, 1, threads, smem, s, c.lhs, c.rhs, c.inv_diag, c.dd, C, tab64(c), b,
                                                         1.0 - h->prm.sor_param, h->prm.mg_tolerance, h->maxCount(),
                                                         h->coarse_sweeps);
     kend(h, s, KC_COARSE);

@@ -134,6 +134,7 @@ __global__ void __launch_bounds__(TMA_WS_THREADS) k_rbgs_tma(const __grid_consta
                                                              const float *__restrict__ eg, Lay L, Tab3<float> t,
                                                              Bnd b, int colour, float w, float omc, int tj,
                                                              int chunk, int *err) {
+    pdl_enter();
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ int s_fail;
     const int n2 = L.n2;
@@ -357,9 +358,9 @@ bool tma_colour(saras_mg *h, cudaStream_t s, Level &v, int colour) {
         b.sg_hi[d] = h->ghost.kind[2 * d + 1] == SARAS_BC_NEUMANN ? 1 : -1;
     }
     int *err = reinterpret_cast<int *>(h->norm_out + 7);
-    k_rbgs_tma<<<grid, TMA_WS_THREADS, tma_smem(v.tma.tj, L.n2), s>>>(
-        v.tma.eld, v.tma.est, v.tma.rld, v.e32, L, t, b, colour, (float)h->prm.sor_param,
-        (float)(1.0 - h->prm.sor_param), v.tma.tj, v.tma.chunk, err);
+    launch_pdl(k_rbgs_tma, grid, dim3(TMA_WS_THREADS), tma_smem(v.tma.tj, L.n2), s, v.tma.eld, v.tma.est, v.tma.rld,
+               (const float *)v.e32, L, t, b, colour, (float)h->prm.sor_param, (float)(1.0 - h->prm.sor_param),
+               v.tma.tj, v.tma.chunk, err);
     return true;
 }
 
