@@ -66,88 +66,6 @@ __global__ void k_rbgs32(float *e, const float *__restrict__ r, Lay L, Tab3<floa
 // vectors, so many loads are in flight per thread, and only the four cells of
 // the sweep's colour are stored.  Used when n_z is a multiple of 8; the core
 // of every row starts on a 32-byte boundary (Lay).
-template <class T>
-__device__ __forceinline__ void ld8(const T *__restrict__ p, T (&o)[8]);
-template <>
-__device__ __forceinline__ void ld8<float>(const float *__restrict__ p, float (&o)[8]) {
-    const float4 a = __ldg(reinterpret_cast<const float4 *>(p));
-    const float4 b = __ldg(reinterpret_cast<const float4 *>(p + 4));
-    o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
-    o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w;
-}
-template <>
-__device__ __forceinline__ void ld8<double>(const double *__restrict__ p, double (&o)[8]) {
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-        const double2 a = __ldg(reinterpret_cast<const double2 *>(p + 2 * q));
-        o[2 * q] = a.x;
-        o[2 * q + 1] = a.y;
-    }
-}
-// plain (coherent) vector load for the array being updated in place
-template <class T>
-__device__ __forceinline__ void ld8u(const T *p, T (&o)[8]);
-template <>
-__device__ __forceinline__ void ld8u<float>(const float *p, float (&o)[8]) {
-    const float4 a = *reinterpret_cast<const float4 *>(p);
-    const float4 b = *reinterpret_cast<const float4 *>(p + 4);
-    o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
-    o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w;
-}
-template <>
-__device__ __forceinline__ void ld8u<double>(const double *p, double (&o)[8]) {
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-        const double2 a = *reinterpret_cast<const double2 *>(p + 2 * q);
-        o[2 * q] = a.x;
-        o[2 * q + 1] = a.y;
-    }
-}
-
-template <class T>
-__device__ __forceinline__ void mirror8(const T (&cur)[8], int sg, T (&o)[8]) {
-#pragma unroll
-    for (int q = 0; q < 8; q++) o[q] = sg > 0 ? cur[q] : -cur[q];
-}
-
-template <class T, bool D3, bool WD, int T0>
-__device__ __forceinline__ void strip_update(T *u, const T (&cur)[8], const T (&xm)[8], const T (&xp)[8],
-                                             const T (&ym)[8], const T (&yp)[8], const T (&fr)[8], const T (&wv)[8],
-                                             T left, T right, const Tab3<T> &t, int i, int j, int k0, int64_t c0, T w,
-                                             T omc) {
-    const T cmx = t.cm[0][i], cpx = t.cp[0][i], dx = t.dg[0][i];
-    T cmy = T(0), cpy = T(0), dy = T(0);
-    if (D3) {
-        cmy = t.cm[1][j];
-        cpy = t.cp[1][j];
-        dy = t.dg[1][j];
-    }
-#pragma unroll
-    for (int q = T0; q < 8; q += 2) {
-        const int k = k0 + q;
-        const T zm = q > 0 ? cur[q - 1] : left;
-        const T zp = q < 7 ? cur[q + 1] : right;
-        T sm = cmx * xm[q];
-        sm = fmat(cpx, xp[q], sm);
-        if (D3) {
-            sm = fmat(cmy, ym[q], sm);
-            sm = fmat(cpy, yp[q], sm);
-        }
-        sm = fmat(t.cm[2][k], zm, sm);
-        sm = fmat(t.cp[2][k], zp, sm);
-        sm = sm - fr[q];
-        T v;
-        if (WD) {
-            v = fmat(sm, wv[q], omc * cur[q]);
-        } else {
-            T d = dx + t.dg[2][k];
-            if (D3) d += dy;
-            v = fmat(omc, cur[q], sweep_div(w * sm, d + d));
-        }
-        u[c0 + q] = v;
-    }
-}
-
 template <class T, bool D3, bool WD>
 __global__ void k_rbgs_v8(T *u, const T *__restrict__ f, const T *__restrict__ wd, Lay L, Tab3<T> t, Bnd b,
                           int colour, T w, T omc) {
@@ -156,33 +74,7 @@ __global__ void k_rbgs_v8(T *u, const T *__restrict__ f, const T *__restrict__ w
     const int j = D3 ? (int)(blockIdx.y * blockDim.y + threadIdx.y) : 0;
     const int i = blockIdx.z;
     if (k0 >= L.n2 || j >= L.n1) return;
-    const int64_t c0 = L.at(i, j, k0);
-    T cur[8], xm[8], xp[8], ym[8], yp[8], fr[8], wv[8];
-    ld8u(u + c0, cur);
-    if (i > 0) ld8u(u + c0 - L.s0, xm);
-    else if (b.per[0]) ld8u(u + c0 + (int64_t)(L.n0 - 1) * L.s0, xm);
-    else mirror8(cur, b.sg_lo[0], xm);
-    if (i < L.n0 - 1) ld8u(u + c0 + L.s0, xp);
-    else if (b.per[0]) ld8u(u + c0 - (int64_t)(L.n0 - 1) * L.s0, xp);
-    else mirror8(cur, b.sg_hi[0], xp);
-    if (D3) {
-        if (j > 0) ld8u(u + c0 - L.s1, ym);
-        else if (b.per[1]) ld8u(u + c0 + (int64_t)(L.n1 - 1) * L.s1, ym);
-        else mirror8(cur, b.sg_lo[1], ym);
-        if (j < L.n1 - 1) ld8u(u + c0 + L.s1, yp);
-        else if (b.per[1]) ld8u(u + c0 - (int64_t)(L.n1 - 1) * L.s1, yp);
-        else mirror8(cur, b.sg_hi[1], yp);
-    }
-    ld8(f + c0, fr);
-    if (WD) ld8(wd + c0, wv);
-    const T left = k0 > 0 ? u[c0 - 1]
-                          : (b.per[2] ? u[c0 + L.n2 - 1] : (b.sg_lo[2] > 0 ? cur[0] : -cur[0]));
-    const T right = k0 + 8 < L.n2 ? u[c0 + 8]
-                                  : (b.per[2] ? u[c0 + 8 - L.n2] : (b.sg_hi[2] > 0 ? cur[7] : -cur[7]));
-    if (((colour + i + j + k0) & 1) == 0)
-        strip_update<T, D3, WD, 0>(u, cur, xm, xp, ym, yp, fr, wv, left, right, t, i, j, k0, c0, w, omc);
-    else
-        strip_update<T, D3, WD, 1>(u, cur, xm, xp, ym, yp, fr, wv, left, right, t, i, j, k0, c0, w, omc);
+    rbgs_strip8<T, D3, WD>(u, f, wd, L, t, b, colour, w, omc, i, j, k0);
 }
 
 // Fused residual and restriction: one thread per coarse cell forms the
@@ -222,60 +114,6 @@ __global__ void k_resid_restrict(const T *__restrict__ u, const T *__restrict__ 
     if (ezero) ezero[Lc.at(i, j, k)] = TO(0);  // the coarse level's error starts from zero
 }
 
-// Residuals of eight consecutive fine cells of one row (k_resid_restrict's
-// resid() arithmetic, cell by cell) from vector loads of the row, its x and y
-// neighbour rows, f and the stored diagonal.
-template <class T, bool D3>
-__device__ __forceinline__ void resid_row8(const T *__restrict__ u, const T *__restrict__ f, const Lay &L,
-                                           const Tab3<T> &t, const Bnd &b, int i, int j, int k0,
-                                           const T *__restrict__ dd, T (&r)[8]) {
-    const int64_t c0 = L.at(i, j, k0);
-    T cur[8], xm[8], xp[8], ym[8], yp[8], fr[8];
-    ld8(u + c0, cur);
-    if (i > 0) ld8(u + c0 - L.s0, xm);
-    else if (b.per[0]) ld8(u + c0 + (int64_t)(L.n0 - 1) * L.s0, xm);
-    else mirror8(cur, b.sg_lo[0], xm);
-    if (i < L.n0 - 1) ld8(u + c0 + L.s0, xp);
-    else if (b.per[0]) ld8(u + c0 - (int64_t)(L.n0 - 1) * L.s0, xp);
-    else mirror8(cur, b.sg_hi[0], xp);
-    if (D3) {
-        if (j > 0) ld8(u + c0 - L.s1, ym);
-        else if (b.per[1]) ld8(u + c0 + (int64_t)(L.n1 - 1) * L.s1, ym);
-        else mirror8(cur, b.sg_lo[1], ym);
-        if (j < L.n1 - 1) ld8(u + c0 + L.s1, yp);
-        else if (b.per[1]) ld8(u + c0 - (int64_t)(L.n1 - 1) * L.s1, yp);
-        else mirror8(cur, b.sg_hi[1], yp);
-    }
-    ld8(f + c0, fr);
-    const T left = k0 > 0 ? __ldg(u + c0 - 1) : (b.per[2] ? __ldg(u + c0 + L.n2 - 1) : (b.sg_lo[2] > 0 ? cur[0] : -cur[0]));
-    const T right = k0 + 8 < L.n2 ? __ldg(u + c0 + 8)
-                                  : (b.per[2] ? __ldg(u + c0 + 8 - L.n2) : (b.sg_hi[2] > 0 ? cur[7] : -cur[7]));
-    T dv[8];
-    if (dd) ld8(dd + c0, dv);
-    const T cmx = t.cm[0][i], cpx = t.cp[0][i];
-    T cmy = T(0), cpy = T(0);
-    if (D3) {
-        cmy = t.cm[1][j];
-        cpy = t.cp[1][j];
-    }
-#pragma unroll
-    for (int q = 0; q < 8; q++) {
-        const int k = k0 + q;
-        const T zm = q > 0 ? cur[q - 1] : left;
-        const T zp = q < 7 ? cur[q + 1] : right;
-        T sm = cmx * xm[q];
-        sm = fmat(cpx, xp[q], sm);
-        if (D3) {
-            sm = fmat(cmy, ym[q], sm);
-            sm = fmat(cpy, yp[q], sm);
-        }
-        sm = fmat(t.cm[2][k], zm, sm);
-        sm = fmat(t.cp[2][k], zp, sm);
-        const T d = dd ? dv[q] : diag<T, D3>(t, i, j, k);
-        r[q] = fr[q] - fmat(-d, cur[q], sm);
-    }
-}
-
 // Fused residual and restriction, four coarse cells along k per thread (fine
 // n_z a multiple of 8), the same arithmetic as k_resid_restrict.
 template <class T, bool D3>
@@ -288,29 +126,7 @@ __global__ void __launch_bounds__(128, 4) k_resid_restrict8(const T *__restrict_
     const int i = blockIdx.z;
     if (kc0 >= Lc.n2 || j >= Lc.n1) return;
     T out[4];
-    if (D3) {
-        T sy[2][4];
-        for (int a = 0; a < 2; a++) {
-            T sz[2][4];
-            for (int bb = 0; bb < 2; bb++) {
-                T r[8];
-                resid_row8<T, true>(u, f, Lf, t, b, 2 * i + a, 2 * j + bb, 2 * kc0, dd, r);
-#pragma unroll
-                for (int q = 0; q < 4; q++)
-                    sz[bb][q] = fmat(w.w1[2][kc0 + q], r[2 * q + 1], w.w0[2][kc0 + q] * r[2 * q]);
-            }
-#pragma unroll
-            for (int q = 0; q < 4; q++) sy[a][q] = fmat(w.w1[1][j], sz[1][q], w.w0[1][j] * sz[0][q]);
-        }
-#pragma unroll
-        for (int q = 0; q < 4; q++) out[q] = fmat(w.w1[0][i], sy[1][q], w.w0[0][i] * sy[0][q]);
-    } else {
-        T r0[8], r1[8];
-        resid_row8<T, false>(u, f, Lf, t, b, 2 * i, 0, 2 * kc0, dd, r0);
-        resid_row8<T, false>(u, f, Lf, t, b, 2 * i + 1, 0, 2 * kc0, dd, r1);
-#pragma unroll
-        for (int q = 0; q < 4; q++) out[q] = ((r0[2 * q] + r0[2 * q + 1]) + (r1[2 * q] + r1[2 * q + 1])) * T(0.25);
-    }
+    restrict4<T, D3>(u, f, Lf, t, b, w, dd, i, j, kc0, out);
     T *dst = rc + Lc.at(i, j, kc0);
     T *ez = ezero ? ezero + Lc.at(i, j, kc0) : nullptr;  // the coarse level's error starts from zero
     if (sizeof(T) == 4) {
@@ -341,44 +157,12 @@ __global__ void k_prolong_add(TF *__restrict__ f, const TC *__restrict__ c, Lay 
 // thread (n_z a multiple of 8): two aligned vector loads and stores of the
 // fine row, one of the four coarse cells.
 template <class T>
-__device__ __forceinline__ void st8(T *p, const T (&v)[8]);
-template <>
-__device__ __forceinline__ void st8<float>(float *p, const float (&v)[8]) {
-    reinterpret_cast<float4 *>(p)[0] = make_float4(v[0], v[1], v[2], v[3]);
-    reinterpret_cast<float4 *>(p)[1] = make_float4(v[4], v[5], v[6], v[7]);
-}
-template <>
-__device__ __forceinline__ void st8<double>(double *p, const double (&v)[8]) {
-#pragma unroll
-    for (int q = 0; q < 4; q++) reinterpret_cast<double2 *>(p)[q] = make_double2(v[2 * q], v[2 * q + 1]);
-}
-template <class T>
-__device__ __forceinline__ void ld4(const T *__restrict__ p, T (&o)[4]);
-template <>
-__device__ __forceinline__ void ld4<float>(const float *__restrict__ p, float (&o)[4]) {
-    const float4 a = __ldg(reinterpret_cast<const float4 *>(p));
-    o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
-}
-template <>
-__device__ __forceinline__ void ld4<double>(const double *__restrict__ p, double (&o)[4]) {
-    const double2 a = __ldg(reinterpret_cast<const double2 *>(p));
-    const double2 b = __ldg(reinterpret_cast<const double2 *>(p + 2));
-    o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
-}
-
-template <class T>
 __global__ void k_prolong_add8(T *__restrict__ f, const T *__restrict__ c, Lay Lf, Lay Lc, int d3) {
     pdl_enter();
     const int k0 = 8 * (int)(blockIdx.x * blockDim.x + threadIdx.x);
     const int j = (int)(blockIdx.y * blockDim.y + threadIdx.y), i = blockIdx.z;
     if (k0 >= Lf.n2 || j >= Lf.n1) return;
-    const int64_t q = Lf.at(i, j, k0);
-    T v[8], w[4];
-    ld8u(f + q, v);
-    ld4(c + Lc.at(i >> 1, d3 ? (j >> 1) : 0, k0 >> 1), w);
-#pragma unroll
-    for (int t = 0; t < 8; t++) v[t] = v[t] + w[t >> 1];
-    st8(f + q, v);
+    prolong8(f, c, Lf, Lc, d3, i, j, k0);
 }
 
 __device__ __forceinline__ double warp_max(double v) {
@@ -497,7 +281,7 @@ __global__ void k_rhs_norm_final(const double *__restrict__ part, int nb, int rt
 template <bool D3>
 __global__ void k_coarsest_fast(double *ug, const double *__restrict__ fg, const double *__restrict__ wdg,
                                 const double *__restrict__ ddg, Lay L, Tab3<double> t, Bnd b, double omc, double tol,
-                                int max_count, int *sweeps_out) {
+                                int max_count, int stall_check, int *sweeps_out) {
     pdl_enter();
     extern __shared__ double stage[];
     __shared__ unsigned long long shm[32];
@@ -513,6 +297,7 @@ __global__ void k_coarsest_fast(double *ug, const double *__restrict__ fg, const
     const int ncol = L.n0 * L.n1 * half;
     const int ncell = L.n0 * L.n1 * L.n2;
     int iter = 0, sweeps = 0;
+    double stall_ref = __longlong_as_double(0x7ff0000000000000ll);  // +infinity
     for (;;) {
         for (int colour = 0; colour < 2; colour++) {
             for (int q = threadIdx.x; q < ncol; q += blockDim.x) {
@@ -543,7 +328,15 @@ __global__ void k_coarsest_fast(double *ug, const double *__restrict__ fg, const
         for (int q = 0; q < (int)(blockDim.x >> 5); q++) mm = shm[q] > mm ? shm[q] : mm;
         __syncthreads();
         sweeps++;
-        if (__longlong_as_double((long long)mm) < tol) break;
+        const double rn = __longlong_as_double((long long)mm);
+        if (rn < tol) break;
+        if (stall_check > 0 && iter % stall_check == 0) {
+            // a singular coarsest problem whose restricted RHS is slightly
+            // incompatible stops improving at the incompatible part: stop
+            // once `stall_check` sweeps gain less than 0.1%
+            if (rn > 0.999 * stall_ref) break;
+            stall_ref = rn;
+        }
         iter++;
         if (iter > max_count) break;
     }
@@ -998,15 +791,16 @@ void coarsest_fast(saras_mg *h, cudaStream_t s, Level &c) {
     const int64_t cells = (int64_t)C.n0 * C.n1 * C.n2;
     const int threads = cells <= 512 ? 32 : (cells <= 4096 ? 128 : 256);
     const Bnd b = bnd(h);
+    // the MIXED form also stops a stagnating coarsest solve; the FP64 form
+    // keeps mgSolve's tolerance-or-cap rule
+    const int stall = h->prm.precision == SARAS_PREC_MIXED ? COARSE_STALL_CHECK : 0;
     kbegin(h, s, KC_COARSE);
     if (h->d3)
         launch_pdl(k_coarsest_fast<true>, 1, threads, smem, s, c.lhs, c.rhs, c.inv_diag, c.dd, C, tab64(c), b,
-                                                       1.0 - h->prm.sor_param, h->prm.mg_tolerance, h->maxCount(),
-                                                       h->coarse_sweeps);
+                   1.0 - h->prm.sor_param, h->prm.mg_tolerance, h->maxCount(), stall, h->coarse_sweeps);
     else
         launch_pdl(k_coarsest_fast<false>, 1, threads, smem, s, c.lhs, c.rhs, c.inv_diag, c.dd, C, tab64(c), b,
-                                                        1.0 - h->prm.sor_param, h->prm.mg_tolerance, h->maxCount(),
-                                                        h->coarse_sweeps);
+                   1.0 - h->prm.sor_param, h->prm.mg_tolerance, h->maxCount(), stall, h->coarse_sweeps);
     kend(h, s, KC_COARSE);
 }
 

@@ -27,6 +27,9 @@ struct WTab {
 __device__ __forceinline__ float fmat(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 __device__ __forceinline__ double fmat(double a, double b, double c) { return __fma_rn(a, b, c); }
 
+// Sweeps between the stagnation checks of the MIXED form's coarsest solve.
+constexpr int COARSE_STALL_CHECK = 8;
+
 // Quotient of the FP32 colour sweeps: the hardware reciprocal path of
 // __fdividef (about two ulp).  Every FP32 sweep kernel uses it, so the
 // single-problem, TMA and batched sweeps produce identical bits.
@@ -84,6 +87,257 @@ __device__ __forceinline__ T resid(const T *u, const T *f, const Lay &L, const T
     const T s = offdiag<T, D3>(u, L, t, b, i, j, k, c, uc);
     const T d = dd ? dd[c] : diag<T, D3>(t, i, j, k);
     return f[c] - fmat(-d, uc, s);
+}
+
+// ---- 8-cell strips along k (rows start on 32-byte boundaries, Lay) ----
+// Shared by the single-problem kernels (mg_fast.cu) and the batched serving
+// kernels (serve.cu), so both sweep with the same arithmetic.
+
+template <class T>
+__device__ __forceinline__ void ld8(const T *__restrict__ p, T (&o)[8]);
+template <>
+__device__ __forceinline__ void ld8<float>(const float *__restrict__ p, float (&o)[8]) {
+    const float4 a = __ldg(reinterpret_cast<const float4 *>(p));
+    const float4 b = __ldg(reinterpret_cast<const float4 *>(p + 4));
+    o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+    o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w;
+}
+template <>
+__device__ __forceinline__ void ld8<double>(const double *__restrict__ p, double (&o)[8]) {
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const double2 a = __ldg(reinterpret_cast<const double2 *>(p + 2 * q));
+        o[2 * q] = a.x;
+        o[2 * q + 1] = a.y;
+    }
+}
+// plain (coherent) vector load for the array being updated in place
+template <class T>
+__device__ __forceinline__ void ld8u(const T *p, T (&o)[8]);
+template <>
+__device__ __forceinline__ void ld8u<float>(const float *p, float (&o)[8]) {
+    const float4 a = *reinterpret_cast<const float4 *>(p);
+    const float4 b = *reinterpret_cast<const float4 *>(p + 4);
+    o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+    o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w;
+}
+template <>
+__device__ __forceinline__ void ld8u<double>(const double *p, double (&o)[8]) {
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const double2 a = *reinterpret_cast<const double2 *>(p + 2 * q);
+        o[2 * q] = a.x;
+        o[2 * q + 1] = a.y;
+    }
+}
+
+template <class T>
+__device__ __forceinline__ void mirror8(const T (&cur)[8], int sg, T (&o)[8]) {
+#pragma unroll
+    for (int q = 0; q < 8; q++) o[q] = sg > 0 ? cur[q] : -cur[q];
+}
+
+template <class T, bool D3, bool WD, int T0>
+__device__ __forceinline__ void strip_update(T *u, const T (&cur)[8], const T (&xm)[8], const T (&xp)[8],
+                                             const T (&ym)[8], const T (&yp)[8], const T (&fr)[8], const T (&wv)[8],
+                                             T left, T right, const Tab3<T> &t, int i, int j, int k0, int64_t c0, T w,
+                                             T omc) {
+    const T cmx = t.cm[0][i], cpx = t.cp[0][i], dx = t.dg[0][i];
+    T cmy = T(0), cpy = T(0), dy = T(0);
+    if (D3) {
+        cmy = t.cm[1][j];
+        cpy = t.cp[1][j];
+        dy = t.dg[1][j];
+    }
+#pragma unroll
+    for (int q = T0; q < 8; q += 2) {
+        const int k = k0 + q;
+        const T zm = q > 0 ? cur[q - 1] : left;
+        const T zp = q < 7 ? cur[q + 1] : right;
+        T sm = cmx * xm[q];
+        sm = fmat(cpx, xp[q], sm);
+        if (D3) {
+            sm = fmat(cmy, ym[q], sm);
+            sm = fmat(cpy, yp[q], sm);
+        }
+        sm = fmat(t.cm[2][k], zm, sm);
+        sm = fmat(t.cp[2][k], zp, sm);
+        sm = sm - fr[q];
+        T v;
+        if (WD) {
+            v = fmat(sm, wv[q], omc * cur[q]);
+        } else {
+            T d = dx + t.dg[2][k];
+            if (D3) d += dy;
+            v = fmat(omc, cur[q], sweep_div(w * sm, d + d));
+        }
+        u[c0 + q] = v;
+    }
+}
+
+
+template <class T>
+__device__ __forceinline__ void st8(T *p, const T (&v)[8]);
+template <>
+__device__ __forceinline__ void st8<float>(float *p, const float (&v)[8]) {
+    reinterpret_cast<float4 *>(p)[0] = make_float4(v[0], v[1], v[2], v[3]);
+    reinterpret_cast<float4 *>(p)[1] = make_float4(v[4], v[5], v[6], v[7]);
+}
+template <>
+__device__ __forceinline__ void st8<double>(double *p, const double (&v)[8]) {
+#pragma unroll
+    for (int q = 0; q < 4; q++) reinterpret_cast<double2 *>(p)[q] = make_double2(v[2 * q], v[2 * q + 1]);
+}
+template <class T>
+__device__ __forceinline__ void ld4(const T *__restrict__ p, T (&o)[4]);
+template <>
+__device__ __forceinline__ void ld4<float>(const float *__restrict__ p, float (&o)[4]) {
+    const float4 a = __ldg(reinterpret_cast<const float4 *>(p));
+    o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+}
+template <>
+__device__ __forceinline__ void ld4<double>(const double *__restrict__ p, double (&o)[4]) {
+    const double2 a = __ldg(reinterpret_cast<const double2 *>(p));
+    const double2 b = __ldg(reinterpret_cast<const double2 *>(p + 2));
+    o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
+}
+
+
+// One colour of the RBGS sweep on the 8-cell strip (i, j, k0 .. k0+7): the
+// strip and its neighbour rows as vectors, boundary ghosts folded in, only
+// the sweep's colour cells stored.
+template <class T, bool D3, bool WD>
+__device__ __forceinline__ void rbgs_strip8(T *u, const T *__restrict__ f, const T *__restrict__ wd, const Lay &L,
+                                            const Tab3<T> &t, const Bnd &b, int colour, T w, T omc, int i, int j,
+                                            int k0) {
+    const int64_t c0 = L.at(i, j, k0);
+    T cur[8], xm[8], xp[8], ym[8], yp[8], fr[8], wv[8];
+    ld8u(u + c0, cur);
+    if (i > 0) ld8u(u + c0 - L.s0, xm);
+    else if (b.per[0]) ld8u(u + c0 + (int64_t)(L.n0 - 1) * L.s0, xm);
+    else mirror8(cur, b.sg_lo[0], xm);
+    if (i < L.n0 - 1) ld8u(u + c0 + L.s0, xp);
+    else if (b.per[0]) ld8u(u + c0 - (int64_t)(L.n0 - 1) * L.s0, xp);
+    else mirror8(cur, b.sg_hi[0], xp);
+    if (D3) {
+        if (j > 0) ld8u(u + c0 - L.s1, ym);
+        else if (b.per[1]) ld8u(u + c0 + (int64_t)(L.n1 - 1) * L.s1, ym);
+        else mirror8(cur, b.sg_lo[1], ym);
+        if (j < L.n1 - 1) ld8u(u + c0 + L.s1, yp);
+        else if (b.per[1]) ld8u(u + c0 - (int64_t)(L.n1 - 1) * L.s1, yp);
+        else mirror8(cur, b.sg_hi[1], yp);
+    }
+    ld8(f + c0, fr);
+    if (WD) ld8(wd + c0, wv);
+    const T left = k0 > 0 ? u[c0 - 1]
+                          : (b.per[2] ? u[c0 + L.n2 - 1] : (b.sg_lo[2] > 0 ? cur[0] : -cur[0]));
+    const T right = k0 + 8 < L.n2 ? u[c0 + 8]
+                                  : (b.per[2] ? u[c0 + 8 - L.n2] : (b.sg_hi[2] > 0 ? cur[7] : -cur[7]));
+    if (((colour + i + j + k0) & 1) == 0)
+        strip_update<T, D3, WD, 0>(u, cur, xm, xp, ym, yp, fr, wv, left, right, t, i, j, k0, c0, w, omc);
+    else
+        strip_update<T, D3, WD, 1>(u, cur, xm, xp, ym, yp, fr, wv, left, right, t, i, j, k0, c0, w, omc);
+}
+
+// Residuals of eight consecutive fine cells of one row (k_resid_restrict's
+// resid() arithmetic, cell by cell) from vector loads of the row, its x and y
+// neighbour rows, f and the stored diagonal.
+template <class T, bool D3>
+__device__ __forceinline__ void resid_row8(const T *__restrict__ u, const T *__restrict__ f, const Lay &L,
+                                           const Tab3<T> &t, const Bnd &b, int i, int j, int k0,
+                                           const T *__restrict__ dd, T (&r)[8]) {
+    const int64_t c0 = L.at(i, j, k0);
+    T cur[8], xm[8], xp[8], ym[8], yp[8], fr[8];
+    ld8(u + c0, cur);
+    if (i > 0) ld8(u + c0 - L.s0, xm);
+    else if (b.per[0]) ld8(u + c0 + (int64_t)(L.n0 - 1) * L.s0, xm);
+    else mirror8(cur, b.sg_lo[0], xm);
+    if (i < L.n0 - 1) ld8(u + c0 + L.s0, xp);
+    else if (b.per[0]) ld8(u + c0 - (int64_t)(L.n0 - 1) * L.s0, xp);
+    else mirror8(cur, b.sg_hi[0], xp);
+    if (D3) {
+        if (j > 0) ld8(u + c0 - L.s1, ym);
+        else if (b.per[1]) ld8(u + c0 + (int64_t)(L.n1 - 1) * L.s1, ym);
+        else mirror8(cur, b.sg_lo[1], ym);
+        if (j < L.n1 - 1) ld8(u + c0 + L.s1, yp);
+        else if (b.per[1]) ld8(u + c0 - (int64_t)(L.n1 - 1) * L.s1, yp);
+        else mirror8(cur, b.sg_hi[1], yp);
+    }
+    ld8(f + c0, fr);
+    const T left = k0 > 0 ? __ldg(u + c0 - 1) : (b.per[2] ? __ldg(u + c0 + L.n2 - 1) : (b.sg_lo[2] > 0 ? cur[0] : -cur[0]));
+    const T right = k0 + 8 < L.n2 ? __ldg(u + c0 + 8)
+                                  : (b.per[2] ? __ldg(u + c0 + 8 - L.n2) : (b.sg_hi[2] > 0 ? cur[7] : -cur[7]));
+    T dv[8];
+    if (dd) ld8(dd + c0, dv);
+    const T cmx = t.cm[0][i], cpx = t.cp[0][i];
+    T cmy = T(0), cpy = T(0);
+    if (D3) {
+        cmy = t.cm[1][j];
+        cpy = t.cp[1][j];
+    }
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        const int k = k0 + q;
+        const T zm = q > 0 ? cur[q - 1] : left;
+        const T zp = q < 7 ? cur[q + 1] : right;
+        T sm = cmx * xm[q];
+        sm = fmat(cpx, xp[q], sm);
+        if (D3) {
+            sm = fmat(cmy, ym[q], sm);
+            sm = fmat(cpy, yp[q], sm);
+        }
+        sm = fmat(t.cm[2][k], zm, sm);
+        sm = fmat(t.cp[2][k], zp, sm);
+        const T d = dd ? dv[q] : diag<T, D3>(t, i, j, k);
+        r[q] = fr[q] - fmat(-d, cur[q], sm);
+    }
+}
+
+// The four coarse cells (i, j, kc0 .. kc0+3) of the fused residual and
+// restriction: residuals of their 2x2x2 children from 8-cell fine rows,
+// weighted by the coarsen factors v_abc / vTot (poisson_d3.cc:494-508) per
+// axis, or the mean of four children in 2-D.
+template <class T, bool D3>
+__device__ __forceinline__ void restrict4(const T *__restrict__ u, const T *__restrict__ f, const Lay &Lf,
+                                          const Tab3<T> &t, const Bnd &b, const WTab<T> &w,
+                                          const T *__restrict__ dd, int i, int j, int kc0, T (&out)[4]) {
+    if (D3) {
+        T sy[2][4];
+        for (int a = 0; a < 2; a++) {
+            T sz[2][4];
+            for (int bb = 0; bb < 2; bb++) {
+                T r[8];
+                resid_row8<T, true>(u, f, Lf, t, b, 2 * i + a, 2 * j + bb, 2 * kc0, dd, r);
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    sz[bb][q] = fmat(w.w1[2][kc0 + q], r[2 * q + 1], w.w0[2][kc0 + q] * r[2 * q]);
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) sy[a][q] = fmat(w.w1[1][j], sz[1][q], w.w0[1][j] * sz[0][q]);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) out[q] = fmat(w.w1[0][i], sy[1][q], w.w0[0][i] * sy[0][q]);
+    } else {
+        T r0[8], r1[8];
+        resid_row8<T, false>(u, f, Lf, t, b, 2 * i, 0, 2 * kc0, dd, r0);
+        resid_row8<T, false>(u, f, Lf, t, b, 2 * i + 1, 0, 2 * kc0, dd, r1);
+#pragma unroll
+        for (int q = 0; q < 4; q++) out[q] = ((r0[2 * q] + r0[2 * q + 1]) + (r1[2 * q] + r1[2 * q + 1])) * T(0.25);
+    }
+}
+
+// fine (i, j, k0 .. k0+7) += coarse (i/2, j/2, k0/2 ..): injection
+// prolongation and correction with vector loads and stores.
+template <class T>
+__device__ __forceinline__ void prolong8(T *__restrict__ f, const T *__restrict__ c, const Lay &Lf, const Lay &Lc,
+                                         int d3, int i, int j, int k0) {
+    const int64_t q = Lf.at(i, j, k0);
+    T v[8], w[4];
+    ld8u(f + q, v);
+    ld4(c + Lc.at(i >> 1, d3 ? (j >> 1) : 0, k0 >> 1), w);
+#pragma unroll
+    for (int s = 0; s < 8; s++) v[s] = v[s] + w[s >> 1];
+    st8(f + q, v);
 }
 
 }  // namespace saras

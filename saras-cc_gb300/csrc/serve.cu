@@ -87,6 +87,10 @@ __device__ __forceinline__ unsigned long long block_max_bits(unsigned long long 
     return mm;
 }
 
+// Rows of 8-cell strips (n_z a multiple of 8, at least 16): the vector
+// paths of the single-problem kernels apply (same arithmetic).
+__device__ __forceinline__ bool v8_level(const Lay &L) { return (L.n2 & 7) == 0 && L.n2 >= 16; }
+
 // ---- batched stage kernels (grid-stride over items) ----
 
 __global__ void __launch_bounds__(512) kb_zero(const BItem *__restrict__ items, const int *__restrict__ count,
@@ -95,7 +99,19 @@ __global__ void __launch_bounds__(512) kb_zero(const BItem *__restrict__ items, 
     for (int it = blockIdx.x; it < n; it += gridDim.x) {
         const BItem m = items[it];
         const BLev &L = lv[m.lev];
-        const int n2 = L.lay.n2, cells = m.nrows * n2;
+        const int n2 = L.lay.n2;
+        if (v8_level(L.lay)) {
+            const int s8 = n2 >> 3, strips = m.nrows * s8;
+            for (int q = threadIdx.x; q < strips; q += blockDim.x) {
+                int i, j;
+                row_ij(L.lay, m.row0 + q / s8, i, j);
+                float4 *p = reinterpret_cast<float4 *>(L.e + L.lay.at(i, j, (q % s8) * 8));
+                p[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+                p[1] = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+            continue;
+        }
+        const int cells = m.nrows * n2;
         for (int q = threadIdx.x; q < cells; q += blockDim.x) {
             int i, j;
             row_ij(L.lay, m.row0 + q / n2, i, j);
@@ -111,6 +127,20 @@ __global__ void __launch_bounds__(512) kb_rbgs(const BItem *__restrict__ items, 
     for (int it = blockIdx.x; it < n; it += gridDim.x) {
         const BItem m = items[it];
         const BLev &L = lv[m.lev];
+        if (v8_level(L.lay)) {
+            const int s8 = L.lay.n2 >> 3, strips = m.nrows * s8;
+            for (int q = threadIdx.x; q < strips; q += blockDim.x) {
+                int i, j;
+                row_ij(L.lay, m.row0 + q / s8, i, j);
+                const int k0 = (q % s8) * 8;
+                if (L.d3)
+                    rbgs_strip8<float, true, false>(L.e, L.r, nullptr, L.lay, L.t32, L.b, colour, L.w, L.omc, i, j, k0);
+                else
+                    rbgs_strip8<float, false, false>(L.e, L.r, nullptr, L.lay, L.t32, L.b, colour, L.w, L.omc, i, j,
+                                                     k0);
+            }
+            continue;
+        }
         const int half = (L.lay.n2 + 1) / 2, cells = m.nrows * half;
         for (int q = threadIdx.x; q < cells; q += blockDim.x) {
             int i, j;
@@ -142,7 +172,23 @@ __global__ void __launch_bounds__(512) kb_restrict(const BItem *__restrict__ ite
         const BItem m = items[it];
         const BLev &F = lv[m.lev];
         const BLev &C = lv[m.clev];
-        const int n2 = C.lay.n2, cells = m.nrows * n2;
+        const int n2 = C.lay.n2;
+        if (v8_level(F.lay) && !C.top) {
+            const int s4 = n2 >> 2, strips = m.nrows * s4;
+            for (int q = threadIdx.x; q < strips; q += blockDim.x) {
+                int i, j;
+                row_ij(C.lay, m.row0 + q / s4, i, j);
+                const int kc0 = (q % s4) * 4;
+                float out[4];
+                if (F.d3)
+                    restrict4<float, true>(F.e, F.r, F.lay, F.t32, F.b, C.w32, nullptr, i, j, kc0, out);
+                else
+                    restrict4<float, false>(F.e, F.r, F.lay, F.t32, F.b, C.w32, nullptr, i, j, kc0, out);
+                *reinterpret_cast<float4 *>(C.r + C.lay.at(i, j, kc0)) = make_float4(out[0], out[1], out[2], out[3]);
+            }
+            continue;
+        }
+        const int cells = m.nrows * n2;
         for (int q = threadIdx.x; q < cells; q += blockDim.x) {
             int i, j;
             row_ij(C.lay, m.row0 + q / n2, i, j);
@@ -178,9 +224,10 @@ __global__ void __launch_bounds__(512) kb_restrict(const BItem *__restrict__ ite
 }
 
 // Coarsest level of each listed case, one block per case: FP64 red-black
-// sweeps from zero to the absolute tolerance or the iteration cap
-// (poisson_d3.cc:249-432, k_coarsest_fast arithmetic), or a fixed number of
-// sweeps when the level is too large for the single-problem block solve.
+// sweeps from zero to the absolute tolerance, the iteration cap
+// (poisson_d3.cc:249-432) or stagnation (k_coarsest_fast's MIXED-form
+// rule), or a fixed number of sweeps when the level is too large for the
+// single-problem block solve.
 __global__ void kb_coarsest(const BItem *__restrict__ items, const int *__restrict__ count,
                             const BLev *__restrict__ lv) {
     __shared__ unsigned long long shm[32];
@@ -196,6 +243,7 @@ __global__ void kb_coarsest(const BItem *__restrict__ items, const int *__restri
         __syncthreads();
         const int half = (Y.n2 + 1) / 2, ncol = Y.n0 * Y.n1 * half;
         int iter = 0;
+        double stall_ref = __longlong_as_double(0x7ff0000000000000ll);  // +infinity
         for (;;) {
             for (int colour = 0; colour < 2; colour++) {
                 for (int q = threadIdx.x; q < ncol; q += blockDim.x) {
@@ -224,7 +272,12 @@ __global__ void kb_coarsest(const BItem *__restrict__ items, const int *__restri
                 mx = bits > mx ? bits : mx;
             }
             const unsigned long long mm = block_max_bits(mx, shm);
-            if (__longlong_as_double((long long)mm) < L.tol) break;
+            const double rn = __longlong_as_double((long long)mm);
+            if (rn < L.tol) break;
+            if (iter % COARSE_STALL_CHECK == 0) {  // MIXED form: stop a stagnating solve
+                if (rn > 0.999 * stall_ref) break;
+                stall_ref = rn;
+            }
             iter++;
             if (iter > L.max_count) break;
         }
@@ -240,7 +293,17 @@ __global__ void __launch_bounds__(512) kb_prolong(const BItem *__restrict__ item
         const BItem m = items[it];
         const BLev &F = lv[m.lev];
         const BLev &C = lv[m.clev];
-        const int n2 = F.lay.n2, cells = m.nrows * n2;
+        const int n2 = F.lay.n2;
+        if (v8_level(F.lay) && !C.top) {
+            const int s8 = n2 >> 3, strips = m.nrows * s8;
+            for (int q = threadIdx.x; q < strips; q += blockDim.x) {
+                int i, j;
+                row_ij(F.lay, m.row0 + q / s8, i, j);
+                prolong8(F.e, C.e, F.lay, C.lay, F.d3, i, j, (q % s8) * 8);
+            }
+            continue;
+        }
+        const int cells = m.nrows * n2;
         for (int q = threadIdx.x; q < cells; q += blockDim.x) {
             int i, j;
             row_ij(F.lay, m.row0 + q / n2, i, j);
@@ -259,7 +322,24 @@ __global__ void __launch_bounds__(512) kb_update(const BItem *__restrict__ items
     for (int it = blockIdx.x; it < n; it += gridDim.x) {
         const BItem m = items[it];
         const BLev &L = lv[m.lev];
-        const int n2 = L.lay.n2, cells = m.nrows * n2;
+        const int n2 = L.lay.n2;
+        if (v8_level(L.lay)) {
+            const int s8 = n2 >> 3, strips = m.nrows * s8;
+            for (int q = threadIdx.x; q < strips; q += blockDim.x) {
+                int i, j;
+                row_ij(L.lay, m.row0 + q / s8, i, j);
+                const int64_t c = L.lay.at(i, j, (q % s8) * 8);
+                double u[8];
+                float e[8];
+                ld8u(L.u + c, u);
+                ld8(L.e + c, e);
+#pragma unroll
+                for (int t = 0; t < 8; t++) u[t] = u[t] + (double)e[t];
+                st8(L.u + c, u);
+            }
+            continue;
+        }
+        const int cells = m.nrows * n2;
         for (int q = threadIdx.x; q < cells; q += blockDim.x) {
             int i, j;
             row_ij(L.lay, m.row0 + q / n2, i, j);
@@ -280,6 +360,27 @@ __global__ void __launch_bounds__(512) kb_resid(const BItem *__restrict__ items,
         const BLev &L = lv[m.lev];
         const int n2 = L.lay.n2, cells = m.nrows * n2;
         unsigned long long mx = 0ull;
+        if (v8_level(L.lay)) {
+            const int s8 = n2 >> 3, strips = m.nrows * s8;
+            for (int q = threadIdx.x; q < strips; q += blockDim.x) {
+                int i, j;
+                row_ij(L.lay, m.row0 + q / s8, i, j);
+                const int k0 = (q % s8) * 8;
+                double r[8];
+                if (L.d3)
+                    resid_row8<double, true>(L.u, L.f, L.lay, L.t64, L.b, i, j, k0, L.dd, r);
+                else
+                    resid_row8<double, false>(L.u, L.f, L.lay, L.t64, L.b, i, j, k0, L.dd, r);
+                float4 *p = reinterpret_cast<float4 *>(L.r + L.lay.at(i, j, k0));
+                p[0] = make_float4((float)r[0], (float)r[1], (float)r[2], (float)r[3]);
+                p[1] = make_float4((float)r[4], (float)r[5], (float)r[6], (float)r[7]);
+#pragma unroll
+                for (int t = 0; t < 8; t++) {
+                    const unsigned long long bits = abs_bits(r[t]);
+                    mx = bits > mx ? bits : mx;
+                }
+            }
+        } else
         for (int q = threadIdx.x; q < cells; q += blockDim.x) {
             int i, j;
             row_ij(L.lay, m.row0 + q / n2, i, j);
