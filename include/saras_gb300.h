@@ -168,7 +168,7 @@ typedef struct saras_rk3_params {
     int32_t max_iterations; /* 0: int(pow(log(Nx*Ny*Nz), 3)) as timestep.cc:115 */
     double  g_terms[3];     /* buoyancy Fb*g/|g|; all zero for zeroForcing */
     int32_t with_scalar;    /* 1: timeAdvance(V,P,T); 0: timeAdvance(V,P) */
-    int32_t nl_scheme;      /* "Non-Linear Term": 1 (central) */
+    int32_t nl_scheme;      /* "Non-Linear Term": 1 (central) or 3 (Morinishi, second-order branch) */
     saras_field_bc bc_vx, bc_vy, bc_vz, bc_t;
     saras_field_bc bc_p;    /* pressure field walls */
     saras_mg_params mg;     /* pressure-correction solve */

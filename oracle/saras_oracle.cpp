@@ -807,6 +807,7 @@ struct Rk3 {
     Multigrid *mg = nullptr;
     double dih[3], dih2[3];  /* derivative: ihx = 1/dXi, ihx2 = pow(ihx, 2) */
     double tih2[3], ti2h[3]; /* timestep: ihx2 = 1/pow(dXi,2), i2hx = 0.5/dXi */
+    double mi2d[3];          /* vfield/sfield: i2dx = 1/(2 dXi) (vfield.cc:133-135) */
     double hwall[6];
     int maxIterations = 0;
 
@@ -831,6 +832,7 @@ struct Rk3 {
             double h2 = std::pow(g.dxi[d], 2.0);
             ti2h[d] = 0.5 / g.dxi[d];
             tih2[d] = 1.0 / h2;
+            mi2d[d] = 1.0 / (2.0 * g.dxi[d]);
         }
         /* neumann::neumann (lib/boundary/neumann.cc:50-66) */
         hwall[0] = 2 * g.xG[0][0];
@@ -852,6 +854,23 @@ struct Rk3 {
         int idx = d == 0 ? i : (d == 1 ? j : k);
         double c12 = (F(i + o[0], j + o[1], k + o[2]) - F(i - o[0], j - o[1], k - o[2])) * 0.5;
         return g.xi_x[d][idx] * (c12 * dih[d]);
+    }
+    /* One direction of Morinishi's skew-symmetric convection term,
+     * second-order branch (dScheme 1): vfield::morinishiNLin
+     * (vfield.cc:271-474) and sfield::morinishiNLin (sfield.cc:200-323).
+     * adv = Va * xi * (F+ - F-) * i2d, div = xi * (Va+ F+ - Va- F-) * i2d
+     * (the Blitz products tempXX = V.Vx*Vx etc. at the neighbours); the
+     * caller subtracts (adv + div)/2. */
+    inline double mterm(const Arr3 &F, const Arr3 &Va, int d, int i, int j, int k) const {
+        int o[3] = {0, 0, 0};
+        o[d] = 1;
+        int idx = d == 0 ? i : (d == 1 ? j : k);
+        const int ip = i + o[0], jp = j + o[1], kp = k + o[2];
+        const int im = i - o[0], jm = j - o[1], km = k - o[2];
+        const double x = g.xi_x[d][idx];
+        const double adv = Va(i, j, k) * x * (F(ip, jp, kp) - F(im, jm, km)) * mi2d[d];
+        const double div = x * (Va(ip, jp, kp) * F(ip, jp, kp) - Va(im, jm, km) * F(im, jm, km)) * mi2d[d];
+        return (adv + div) / 2;
     }
     /* calcDerivative2{xx,yy,zz} with dScheme 1 (derivative.cc:206-318). */
     inline double d2(const Arr3 &F, int d, int i, int j, int k) const {
@@ -1075,25 +1094,41 @@ struct Rk3 {
                     full_loop(*nse[c], [&](size_t q) { nse[c]->v[q] += ab * tv[c]->v[q]; });
                 if (sc) full_loop(tmpRHS, [&](size_t q) { tmpRHS.v[q] += ab * tSF.v[q]; });
             }
-            /* non-linear terms (nlScheme 1) */
+            /* non-linear terms: nlScheme 1 (vfield.cc:205-245, sfield.cc:160-
+             * 198) or 3, Morinishi (vfield.cc:271-474, sfield.cc:200-323) */
             for (int c = 0; c < 3; c++) tv[c]->fill(0.0);
             tSF.fill(0.0);
             for (int c = 0; c < 3; c++) {
                 if (!d3 && c == 1) continue;
                 Arr3 &F = *vel[c];
                 Arr3 &H = *tv[c];
-                core_loop([&](int i, int j, int k) {
-                    H(i, j, k) -= Vx(i, j, k) * d1(F, 0, i, j, k);
-                    if (d3) H(i, j, k) -= Vy(i, j, k) * d1(F, 1, i, j, k);
-                    H(i, j, k) -= Vz(i, j, k) * d1(F, 2, i, j, k);
-                });
+                if (prm.nl_scheme == 3)
+                    core_loop([&](int i, int j, int k) {
+                        H(i, j, k) -= mterm(F, Vx, 0, i, j, k);
+                        if (d3) H(i, j, k) -= mterm(F, Vy, 1, i, j, k);
+                        H(i, j, k) -= mterm(F, Vz, 2, i, j, k);
+                    });
+                else
+                    core_loop([&](int i, int j, int k) {
+                        H(i, j, k) -= Vx(i, j, k) * d1(F, 0, i, j, k);
+                        if (d3) H(i, j, k) -= Vy(i, j, k) * d1(F, 1, i, j, k);
+                        H(i, j, k) -= Vz(i, j, k) * d1(F, 2, i, j, k);
+                    });
             }
-            if (sc)
-                core_loop([&](int i, int j, int k) {
-                    tSF(i, j, k) -= Vx(i, j, k) * d1(T, 0, i, j, k);
-                    if (d3) tSF(i, j, k) -= Vy(i, j, k) * d1(T, 1, i, j, k);
-                    tSF(i, j, k) -= Vz(i, j, k) * d1(T, 2, i, j, k);
-                });
+            if (sc) {
+                if (prm.nl_scheme == 3)
+                    core_loop([&](int i, int j, int k) {
+                        tSF(i, j, k) -= mterm(T, Vx, 0, i, j, k);
+                        if (d3) tSF(i, j, k) -= mterm(T, Vy, 1, i, j, k);
+                        tSF(i, j, k) -= mterm(T, Vz, 2, i, j, k);
+                    });
+                else
+                    core_loop([&](int i, int j, int k) {
+                        tSF(i, j, k) -= Vx(i, j, k) * d1(T, 0, i, j, k);
+                        if (d3) tSF(i, j, k) -= Vy(i, j, k) * d1(T, 1, i, j, k);
+                        tSF(i, j, k) -= Vz(i, j, k) * d1(T, 2, i, j, k);
+                    });
+            }
             {
                 double gm = gam[rk];
                 for (int c = 0; c < 3; c++)

@@ -5,7 +5,8 @@
 // Reference: lsRK3_d3::timeAdvance(V,P,T) and (V,P) (lib/timestep/
 // lsRK3_d3.cc:94-177, 190-305; lsRK3_d2.cc), timestep::solveVx/Vy/Vz/T
 // (lib/timestep/predictors.cc:59-423), vfield/sfield::computeDiff,
-// computeNLin (nlScheme 1), divergence, gradient (lib/field/vfield.cc,
+// computeNLin (nlScheme 1 and 3, Morinishi's second-order branch),
+// divergence, gradient (lib/field/vfield.cc,
 // sfield.cc, plainsf.cc), derivative::calcDerivative1_* / 2** with
 // dScheme 1 (lib/field/derivative.cc:104-318), field BC writers
 // (lib/boundary/dirichlet.cc, neumann.cc) and buoyantForce::addForcing
@@ -43,6 +44,7 @@ struct RkTab {
 struct RkScal {
     double ih[3], ih2d[3];  // derivative: 1/dXi, pow(1/dXi, 2)
     double ih2t[3], i2ht[3]; // timestep: 1/pow(dXi,2), 0.5/dXi
+    double i2d[3];           // vfield/sfield: 1/(2 dXi) (vfield.cc:133-135)
 };
 
 // Field boundary rules: periodic flags, per face Dirichlet (2v) or Neumann
@@ -80,6 +82,19 @@ __device__ __forceinline__ double d2(const double *F, const Lay &L, const RkTab 
     return radd(rmul(T.xixx[a][idx], rmul(c12, S.ih[a])), rmul(T.xix2[a][idx], rmul(c22, S.ih2d[a])));
 }
 
+// One direction of Morinishi's skew-symmetric convection term, second-order
+// branch (dScheme 1; vfield.cc:271-474, sfield.cc:200-323):
+// (adv + div)/2 with adv = Va*xi*(F+ - F-)*i2d and div = xi*(Va+ F+ - Va- F-)*i2d,
+// the products standing for the Blitz temporaries tempXX = V.Vx*Vx etc.
+__device__ __forceinline__ double mterm(const double *F, const double *Va, const Lay &L, const RkTab &T,
+                                        const RkScal &S, int a, int idx, int64_t c) {
+    const int64_t st = axis_stride(L, a);
+    const double x = T.xi_x[a][idx];
+    const double adv = rmul(rmul(rmul(Va[c], x), rsub(F[c + st], F[c - st])), S.i2d[a]);
+    const double div = rmul(rmul(x, rsub(rmul(Va[c + st], F[c + st]), rmul(Va[c - st], F[c - st]))), S.i2d[a]);
+    return rdiv(radd(adv, div), 2.0);
+}
+
 struct Fields {
     const double *V[3];
     const double *P, *T;
@@ -90,7 +105,7 @@ struct Fields {
 // Right-hand sides of one RK3 sub-stage for every velocity component and T
 // (lsRK3_d3.cc:199-252): zeta*NL_prev + alpha*nu*Diff + (alpha+beta)*(F - grad P)
 // + gamma*NL, times dt, plus the field.  NL is kept for the next stage.
-template <bool D3, bool SC>
+template <bool D3, bool SC, int NLS>
 __global__ void k_rk3_rhs(Fields f, Lay L, RkTab T, RkScal S, Stage sg) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = D3 ? (int)blockIdx.y : 0;
@@ -111,9 +126,16 @@ __global__ void k_rk3_rhs(Fields f, Lay L, RkTab T, RkScal S, Stage sg) {
         if (SC) t = rsub(t, rmul(sg.g[comp], f.T[c]));
         t = rsub(t, d1(f.P, L, T, S, comp, id[comp], c));
         r = radd(r, rmul(sg.ab, t));
-        double n = rsub(0.0, rmul(f.V[0][c], d1(F, L, T, S, 0, i, c)));
-        if (D3) n = rsub(n, rmul(f.V[1][c], d1(F, L, T, S, 1, j, c)));
-        n = rsub(n, rmul(f.V[2][c], d1(F, L, T, S, 2, k, c)));
+        double n;
+        if (NLS == 3) {
+            n = rsub(0.0, mterm(F, f.V[0], L, T, S, 0, i, c));
+            if (D3) n = rsub(n, mterm(F, f.V[1], L, T, S, 1, j, c));
+            n = rsub(n, mterm(F, f.V[2], L, T, S, 2, k, c));
+        } else {
+            n = rsub(0.0, rmul(f.V[0][c], d1(F, L, T, S, 0, i, c)));
+            if (D3) n = rsub(n, rmul(f.V[1][c], d1(F, L, T, S, 1, j, c)));
+            n = rsub(n, rmul(f.V[2][c], d1(F, L, T, S, 2, k, c)));
+        }
         r = radd(r, rmul(sg.gam, n));
         r = rmul(r, sg.dt);
         r = radd(r, F[c]);
@@ -129,9 +151,16 @@ __global__ void k_rk3_rhs(Fields f, Lay L, RkTab T, RkScal S, Stage sg) {
         dif = radd(dif, d2(F, L, T, S, 2, k, c));
         r = radd(r, rmul(sg.akap, dif));
         r = radd(r, rmul(sg.ab, 0.0));  // zeroForcing adds nothing, multAdd still runs
-        double n = rsub(0.0, rmul(f.V[0][c], d1(F, L, T, S, 0, i, c)));
-        if (D3) n = rsub(n, rmul(f.V[1][c], d1(F, L, T, S, 1, j, c)));
-        n = rsub(n, rmul(f.V[2][c], d1(F, L, T, S, 2, k, c)));
+        double n;
+        if (NLS == 3) {
+            n = rsub(0.0, mterm(F, f.V[0], L, T, S, 0, i, c));
+            if (D3) n = rsub(n, mterm(F, f.V[1], L, T, S, 1, j, c));
+            n = rsub(n, mterm(F, f.V[2], L, T, S, 2, k, c));
+        } else {
+            n = rsub(0.0, rmul(f.V[0][c], d1(F, L, T, S, 0, i, c)));
+            if (D3) n = rsub(n, rmul(f.V[1][c], d1(F, L, T, S, 1, j, c)));
+            n = rsub(n, rmul(f.V[2][c], d1(F, L, T, S, 2, k, c)));
+        }
         r = radd(r, rmul(sg.gam, n));
         r = rmul(r, sg.dt);
         r = radd(r, F[c]);
@@ -450,16 +479,15 @@ saras_status time_advance(saras_rk3 *h, int *mgc, int *cni) {
         f.tmpR = h->tmpR;
         f.nlT = h->nlT;
         const dim3 g = cgrid(L, h->d3, bx);
-        if (h->d3) {
-            if (h->sc)
-                k_rk3_rhs<true, true><<<g, bx, 0, s>>>(f, L, h->tabs, h->scal, sg);
-            else
-                k_rk3_rhs<true, false><<<g, bx, 0, s>>>(f, L, h->tabs, h->scal, sg);
-        } else {
-            if (h->sc)
-                k_rk3_rhs<false, true><<<g, bx, 0, s>>>(f, L, h->tabs, h->scal, sg);
-            else
-                k_rk3_rhs<false, false><<<g, bx, 0, s>>>(f, L, h->tabs, h->scal, sg);
+        {
+            // (dimension, scalar, non-linear scheme) -> kernel
+            using K = void (*)(Fields, Lay, RkTab, RkScal, Stage);
+            const K ks[2][2][2] = {{{k_rk3_rhs<false, false, 1>, k_rk3_rhs<false, false, 3>},
+                                    {k_rk3_rhs<false, true, 1>, k_rk3_rhs<false, true, 3>}},
+                                   {{k_rk3_rhs<true, false, 1>, k_rk3_rhs<true, false, 3>},
+                                    {k_rk3_rhs<true, true, 1>, k_rk3_rhs<true, true, 3>}}};
+            ks[h->d3 ? 1 : 0][h->sc ? 1 : 0][h->prm.nl_scheme == 3 ? 1 : 0]<<<g, bx, 0, s>>>(f, L, h->tabs, h->scal,
+                                                                                          sg);
         }
         h->launches++;
         for (int comp = 0; comp < 3; comp++) {
@@ -500,7 +528,7 @@ saras_status rk3_create(const saras_grid_desc *gd, const saras_rk3_params *p, vo
         set_error("the RK3 stencils use Differentiation Scheme 1 (pad 1)");
         return SARAS_BAD_ARG;
     }
-    if (p->nl_scheme != 1 || !(p->dt > 0.0) || !(p->nu >= 0.0) || !(p->kappa >= 0.0) || p->max_iterations < 0) {
+    if ((p->nl_scheme != 1 && p->nl_scheme != 3) || !(p->dt > 0.0) || !(p->nu >= 0.0) || !(p->kappa >= 0.0) || p->max_iterations < 0) {
         set_error("invalid RK3 parameters");
         return SARAS_BAD_ARG;
     }
@@ -538,6 +566,7 @@ saras_status rk3_create(const saras_grid_desc *gd, const saras_rk3_params *p, vo
         h->scal.ih2d[d] = std::pow(ih, 2.0);
         const double hx2 = std::pow(g.dxi[d], 2.0);
         h->scal.i2ht[d] = 0.5 / g.dxi[d];
+        h->scal.i2d[d] = 1.0 / (2.0 * g.dxi[d]);
         h->scal.ih2t[d] = 1.0 / hx2;
         double *dst[5];
         for (int q = 0; q < 5; q++) dst[q] = h->tab + off + (int64_t)q * n[d];

@@ -15,7 +15,8 @@ import saras_gb300 as S
 pytestmark = pytest.mark.gpu
 
 
-def rbc_params(g, ra=1e5, pr=1.0, dt=2e-3, mg_precision=S.PREC_FP64_EXACT, with_scalar=1, vc_tol=1e-6):
+def rbc_params(g, ra=1e5, pr=1.0, dt=2e-3, mg_precision=S.PREC_FP64_EXACT, with_scalar=1, vc_tol=1e-6,
+               nl_scheme=1):
     nu, ka, fb = S.rbc_coefficients(2, ra, pr)
     p = S.Rk3Params()
     p.nu, p.kappa, p.dt = nu, ka, dt
@@ -24,7 +25,7 @@ def rbc_params(g, ra=1e5, pr=1.0, dt=2e-3, mg_precision=S.PREC_FP64_EXACT, with_
     for d, gv in enumerate((0.0, 0.0, -fb)):
         p.g_terms[d] = gv if with_scalar else 0.0
     p.with_scalar = with_scalar
-    p.nl_scheme = 1
+    p.nl_scheme = nl_scheme
     dirich0 = S.field_bc([S.FBC_DIRICHLET] * 6, [0.0] * 6)
     p.bc_vx = dirich0
     p.bc_vy = dirich0
@@ -114,3 +115,22 @@ def test_rk3_mixed_pressure_solve():
     for k in ("vx", "vy", "vz", "t"):
         a, b = gpu[k][1:-1, 1:-1, 1:-1], orc[k][1:-1, 1:-1, 1:-1]
         assert np.abs(a - b).max() <= 1e-5 * np.abs(b).max(), k
+
+
+@pytest.mark.parametrize("gk,amp", [
+    (dict(n=(16, 16, 32), mesh="UUD", beta=(1, 1, 1.5), domain="PPN"), 0.0),
+    (dict(n=(16, 16, 16), mesh="DDD", beta=(1.1, 1.2, 1.3), domain="NNN"), 0.05),
+    (dict(n=(32, 1, 32), mesh="UUD", beta=(1, 1, 1.3), domain="PNN", dims=2), 0.05),
+], ids=["rbc_ppn_uud", "box_nnn_ddd", "planar_pnn"])
+def test_rk3_morinishi_bitwise(gk, amp):
+    """Non-Linear Term 3 (Morinishi's skew-symmetric form, second-order
+    branch of vfield/sfield::morinishiNLin) against the oracle, bit for bit."""
+    g, gpu, orc, gc, oc = run_pair(gk, vel_amp=amp, nl_scheme=3)
+    assert gc == oc, (gc, oc)
+    planar = gk.get("dims") == 2
+    for k in (("vx", "vz", "p", "t", "pp") if planar else ("vx", "vy", "vz", "p", "t", "pp")):
+        a, b = (gpu[k][:, 1, :], orc[k][:, 1, :]) if planar else (gpu[k], orc[k])
+        assert np.array_equal(a, b), (k, np.abs(a - b).max())
+    # the scheme changes the step: the convection term differs from nlScheme 1
+    g1, gpu1, _, _, _ = run_pair(gk, vel_amp=amp, nl_scheme=1)
+    assert not np.array_equal(gpu1["vx"], gpu["vx"])
