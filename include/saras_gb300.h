@@ -17,7 +17,9 @@
  *   saras_rk3_create  <- lsRK3_d3::lsRK3_d3 / lsRK3_d2::lsRK3_d2
  *                        (lib/timestep/lsRK3_d3.cc:58-79; timestep.cc:58-121)
  *   saras_rk3_step    <- lsRK3_d3::timeAdvance(vfield&, sfield&, sfield&) and
- *                        timeAdvance(vfield&, sfield&) (lsRK3_d3.cc:94-177,190-305)
+ *                        timeAdvance(vfield&, sfield&) (lsRK3_d3.cc:94-177,190-305);
+ *                        with integration 1 eulerCN_d3::timeAdvance
+ *                        (eulerCN_d3.cc:88-176, 178-268)
  *   saras_grid_metrics<- grid::mgGridMetrics / createTanHypGrid / setVCDepth
  *                        (lib/grid/grid.cc:411-742), as copied by
  *                        poisson::copyDerivs (lib/poisson/poisson.cc:501-622)
@@ -168,11 +170,22 @@ typedef struct saras_rk3_params {
     int32_t max_iterations; /* 0: int(pow(log(Nx*Ny*Nz), 3)) as timestep.cc:115 */
     double  g_terms[3];     /* buoyancy Fb*g/|g|; all zero for zeroForcing */
     int32_t with_scalar;    /* 1: timeAdvance(V,P,T); 0: timeAdvance(V,P) */
-    int32_t nl_scheme;      /* "Non-Linear Term": 1 (central) or 3 (Morinishi, second-order branch) */
+    int32_t nl_scheme;      /* "Non-Linear Term": 1 central, 2 hybrid upwind, 3 Morinishi */
     saras_field_bc bc_vx, bc_vy, bc_vz, bc_t;
     saras_field_bc bc_p;    /* pressure field walls */
     saras_mg_params mg;     /* pressure-correction solve */
+    /* Solver "Peclet Limit" and "Central Bias" of the hybrid upwind term
+     * (nl_scheme 2; vfield.cc:114-130); the Peclet number uses nu for the
+     * velocity and kappa for the temperature (scalar_d3.cc:166-167) */
+    double  pe_limit, up_param;
+    /* "Integration Scheme": 2 (or 0) low-storage RK3, lsRK3_d3/_d2;
+     * 1 Euler/Crank-Nicolson, eulerCN_d3/_d2 (scalar_d3.cc:156-163) */
+    int32_t integration;
+    int32_t pad_;
 } saras_rk3_params;
+/* The Differentiation Scheme follows the grid descriptor's pad: pad 1 is
+ * dScheme 1 (second order), pad 2 is dScheme 2 (fourth order in the interior,
+ * second order on the first and last core cell of every axis). */
 
 typedef struct saras_rk3 saras_rk3;
 

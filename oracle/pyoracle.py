@@ -46,6 +46,8 @@ def load():
                                     C.POINTER(i64), dp, i32, C.POINTER(i32), C.POINTER(i32), dp]
     lib.oracle_rk3_run.argtypes = [C.POINTER(abi.GridDesc), C.POINTER(abi.Rk3Params), vp, vp, vp, vp,
                                    vp, vp, C.POINTER(i64), i32, C.POINTER(i32), C.POINTER(i32), dp]
+    lib.oracle_field_op.argtypes = [C.POINTER(abi.GridDesc), C.POINTER(abi.Rk3Params), i32, i32, C.c_double,
+                                    vp, vp, vp, vp, vp, C.POINTER(i64)]
     _lib = lib
     return lib
 
@@ -123,3 +125,18 @@ def rk3_run(grid, params, vx, vy, vz, p, t, pp, nsteps=1):
     r = Result()
     r.status, r.mg_cycles, r.cn_iters, r.seconds = s, mgc.value, cni.value, sec.value
     return r
+
+
+def field_op(grid, params, op, f, axis=0, v=(None, None, None), dcoef=1.0):
+    """Core of one stencil operator applied to padded field f: op 1 first
+    derivative, 2 second derivative along `axis`, 3 the convection term of
+    f by velocity v (computeNLin into a zero H)."""
+    lib = load()
+    out = np.zeros_like(f)
+    pf, st = abi.field_origin(f, grid)
+    po, _ = abi.field_origin(out, grid)
+    pv = [abi.field_origin(a, grid)[0] if a is not None else C.c_void_p(0) for a in v]
+    s = lib.oracle_field_op(C.byref(grid), C.byref(params), op, axis, dcoef, pf, *pv, po, st)
+    if s:
+        raise RuntimeError(f"oracle_field_op status {s}")
+    return out

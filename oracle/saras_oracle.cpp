@@ -808,6 +808,8 @@ struct Rk3 {
     double dih[3], dih2[3];  /* derivative: ihx = 1/dXi, ihx2 = pow(ihx, 2) */
     double tih2[3], ti2h[3]; /* timestep: ihx2 = 1/pow(dXi,2), i2hx = 0.5/dXi */
     double mi2d[3];          /* vfield/sfield: i2dx = 1/(2 dXi) (vfield.cc:133-135) */
+    int ds = 1;              /* Differentiation Scheme: 1 (pad 1) or 2 (pad 2) */
+    double ua = 0, ub = 0, uc = 0, ud = 0; /* upwind stencil weights (vfield.cc:114-130) */
     double hwall[6];
     int maxIterations = 0;
 
@@ -818,9 +820,26 @@ struct Rk3 {
     int setup(const saras_grid_desc &gd, const saras_rk3_params &p) {
         int s = g.build(gd, p.mg.levels);
         if (s) return s;
-        if (gd.pad != 1) return SARAS_BAD_ARG; /* dScheme 1 stencils */
+        if (gd.pad != 1 && gd.pad != 2) return SARAS_BAD_ARG;
+        if (p.nl_scheme < 1 || p.nl_scheme > 3) return SARAS_BAD_ARG;
+        if (p.integration < 0 || p.integration > 2) return SARAS_BAD_ARG;
         prm = p;
         d3 = g.dims == 3;
+        /* grid::grid (grid.cc:69-77): the pad width follows dScheme */
+        ds = gd.pad;
+        /* vfield::vfield / sfield::sfield (vfield.cc:107-130, sfield.cc:89-
+         * 111): firstOrder upwinding for dScheme 1, omega = "Central Bias" */
+        const double omega = p.up_param;
+        if (ds == 1) {
+            ua = 2.0 - omega;
+            ub = 2.0 * (1.0 - omega);
+            uc = -omega;
+        } else {
+            ua = 1.0 - omega;
+            ub = 4.0 - 3.0 * omega;
+            uc = 3.0 * (1.0 - omega);
+            ud = -omega;
+        }
         Arr3 *all[] = {&Vx, &Vy, &Vz, &P, &T, &Pp, &mgRHS, &nseX, &nseY, &nseZ, &tmpRHS,
                        &tvX, &tvY, &tvZ, &tSF, &pgX, &pgY, &pgZ, &iterTemp};
         for (Arr3 *a : all) alloc(*a);
@@ -847,13 +866,34 @@ struct Rk3 {
         return SARAS_OK;
     }
 
-    /* calcDerivative1_{x,y,z} with dScheme 1 (derivative.cc:104-204). */
+    /* True on the first and last core cell of axis d: every rank of a
+     * single-rank run is first and last on every axis (derivative.cc:80-
+     * 86), periodic or not, so the dScheme-2 boundary forms apply there. */
+    inline bool edge(int d, int idx) const { return idx == 0 || idx == g.N[d] - 1; }
+
+    /* calcDerivative1_{x,y,z} (derivative.cc:104-204).  dScheme 1:
+     * central12n = (F+ - F-) * 0.5.  dScheme 2: central14n in the interior
+     * and 0.5 * (F+ - F-) on the first and last core cell.  Blitz++ (not
+     * vendored) defines central14n; it is taken here as the unique 5-point
+     * fourth-order central first difference in index units,
+     * (8 (F+1 - F-1) - (F+2 - F-2)) / 12 -- the operation order is this
+     * build's, shared with the GPU. */
     inline double d1(const Arr3 &F, int d, int i, int j, int k) const {
         int o[3] = {0, 0, 0};
         o[d] = 1;
         int idx = d == 0 ? i : (d == 1 ? j : k);
-        double c12 = (F(i + o[0], j + o[1], k + o[2]) - F(i - o[0], j - o[1], k - o[2])) * 0.5;
-        return g.xi_x[d][idx] * (c12 * dih[d]);
+        const double fp = F(i + o[0], j + o[1], k + o[2]), fm = F(i - o[0], j - o[1], k - o[2]);
+        double c;
+        if (ds == 1) {
+            c = (fp - fm) * 0.5;
+        } else if (edge(d, idx)) {
+            c = 0.5 * (fp - fm);
+        } else {
+            const double fp2 = F(i + 2 * o[0], j + 2 * o[1], k + 2 * o[2]);
+            const double fm2 = F(i - 2 * o[0], j - 2 * o[1], k - 2 * o[2]);
+            c = (8.0 * (fp - fm) - (fp2 - fm2)) / 12.0;
+        }
+        return g.xi_x[d][idx] * (c * dih[d]);
     }
     /* One direction of Morinishi's skew-symmetric convection term,
      * second-order branch (dScheme 1): vfield::morinishiNLin
@@ -868,19 +908,88 @@ struct Rk3 {
         const int ip = i + o[0], jp = j + o[1], kp = k + o[2];
         const int im = i - o[0], jm = j - o[1], km = k - o[2];
         const double x = g.xi_x[d][idx];
+        /* fourth-order branch (dScheme 2) away from the first and last
+         * point.  The reference tests the last z point against the y extent
+         * (core.ubound(1), vfield.cc:337,427; sfield.cc:239,290), so along z
+         * the second-order form is taken at k == 0 and k == Ny - 1 (0 for a
+         * planar run) and k = Nz - 1 uses the fourth-order form, which reads
+         * the second ghost layer. */
+        const int last = (d == 2 ? g.N[1] : g.N[d]) - 1;
+        if (ds == 2 && idx != 0 && idx != last) {
+            const int ip2 = i + 2 * o[0], jp2 = j + 2 * o[1], kp2 = k + 2 * o[2];
+            const int im2 = i - 2 * o[0], jm2 = j - 2 * o[1], km2 = k - 2 * o[2];
+            const double adv = Va(i, j, k) * x *
+                               (-F(ip2, jp2, kp2) + 8.0 * F(ip, jp, kp) - 8.0 * F(im, jm, km) + F(im2, jm2, km2)) *
+                               mi2d[d] / 6.0;
+            const double div = x *
+                               (-(Va(ip2, jp2, kp2) * F(ip2, jp2, kp2)) + 8.0 * (Va(ip, jp, kp) * F(ip, jp, kp)) -
+                                8.0 * (Va(im, jm, km) * F(im, jm, km)) + Va(im2, jm2, km2) * F(im2, jm2, km2)) *
+                               mi2d[d] / 6.0;
+            return (adv + div) / 2;
+        }
         const double adv = Va(i, j, k) * x * (F(ip, jp, kp) - F(im, jm, km)) * mi2d[d];
         const double div = x * (Va(ip, jp, kp) * F(ip, jp, kp) - Va(im, jm, km) * F(im, jm, km)) * mi2d[d];
         return (adv + div) / 2;
     }
-    /* calcDerivative2{xx,yy,zz} with dScheme 1 (derivative.cc:206-318). */
+    /* One direction of the hybrid upwind convection term, vfield::upwindNLin
+     * (vfield.cc:475-690) and sfield::upwindNLin (sfield.cc:324-495): the
+     * cell Peclet number |u| dh / diffCoeff (dh = x(i+1) - x(i)) picks the
+     * central form below "Peclet Limit", else the stencil biased against
+     * the local velocity.  dScheme 1 takes first-order upwinding with
+     * second-order central differences; dScheme 2 second-order upwinding
+     * with fourth-order central differences, and second-order central
+     * differences on the first and last core cell.  The caller subtracts
+     * the returned value. */
+    inline double uterm(const Arr3 &F, const Arr3 &Va, double dcoef, int d, int i, int j, int k) const {
+        int o[3] = {0, 0, 0};
+        o[d] = 1;
+        int idx = d == 0 ? i : (d == 1 ? j : k);
+        const double u = Va(i, j, k);
+        const double x = g.xi_x[d][idx];
+        const double f0 = F(i, j, k);
+        const double fp = F(i + o[0], j + o[1], k + o[2]), fm = F(i - o[0], j - o[1], k - o[2]);
+        if (ds == 1) {
+            const double dh = g.xG[d][idx + 1] - g.xG[d][idx];
+            const double pe = std::fabs(u) * dh / dcoef;
+            if (pe < prm.pe_limit) return u * x * (fp - fm) * mi2d[d];
+            if (u > 0) return u * x * (-ua * fm + ub * f0 - uc * fp) * mi2d[d];
+            return u * x * (ua * fp - ub * f0 + uc * fm) * mi2d[d];
+        }
+        if (edge(d, idx)) return u * x * (fp - fm) * mi2d[d];
+        const double fp2 = F(i + 2 * o[0], j + 2 * o[1], k + 2 * o[2]);
+        const double fm2 = F(i - 2 * o[0], j - 2 * o[1], k - 2 * o[2]);
+        const double dh = g.xG[d][idx + 1] - g.xG[d][idx];
+        const double pe = std::fabs(u) * dh / dcoef;
+        if (pe < prm.pe_limit) return u * x * (-fp2 + 8.0 * fp - 8.0 * fm + fm2) * mi2d[d] / 6.0;
+        if (u > 0) return u * x * (ua * fm2 - ub * fm + uc * f0 - ud * fp) * mi2d[d];
+        return u * x * (-ua * fp2 + ub * fp - uc * f0 + ud * fm) * mi2d[d];
+    }
+    /* calcDerivative2{xx,yy,zz} (derivative.cc:206-318).  dScheme 1:
+     * central12n and central22n = (F- - 2F) + F+.  dScheme 2: central14n
+     * as in d1 and central24n taken as (16 (F+1 + F-1) - 30 F - (F+2 + F-2))
+     * / 12 in the interior; 0.5 (F+ - F-) and (F+ - 2F) + F- (the
+     * reference's own boundary forms, derivative.cc:214-223) on the first
+     * and last core cell. */
     inline double d2(const Arr3 &F, int d, int i, int j, int k) const {
         int o[3] = {0, 0, 0};
         o[d] = 1;
         int idx = d == 0 ? i : (d == 1 ? j : k);
+        const double f0 = F(i, j, k);
         double fp = F(i + o[0], j + o[1], k + o[2]), fm = F(i - o[0], j - o[1], k - o[2]);
-        double c12 = (fp - fm) * 0.5;
-        double c22 = fm - 2.0 * F(i, j, k) + fp;
-        return g.xixx[d][idx] * (c12 * dih[d]) + g.xix2[d][idx] * (c22 * dih2[d]);
+        double c1, c2;
+        if (ds == 1) {
+            c1 = (fp - fm) * 0.5;
+            c2 = fm - 2.0 * f0 + fp;
+        } else if (edge(d, idx)) {
+            c1 = 0.5 * (fp - fm);
+            c2 = fp - 2.0 * f0 + fm;
+        } else {
+            const double fp2 = F(i + 2 * o[0], j + 2 * o[1], k + 2 * o[2]);
+            const double fm2 = F(i - 2 * o[0], j - 2 * o[1], k - 2 * o[2]);
+            c1 = (8.0 * (fp - fm) - (fp2 - fm2)) / 12.0;
+            c2 = (16.0 * (fp + fm) - 30.0 * f0 - (fp2 + fm2)) / 12.0;
+        }
+        return g.xixx[d][idx] * (c1 * dih[d]) + g.xix2[d][idx] * (c2 * dih2[d]);
     }
 
     template <class Fn> void core_loop(Fn fn) {
@@ -983,9 +1092,12 @@ struct Rk3 {
                         (1.0 + 2.0 * dt * coef * beta * (hx2 * cx2 + hz2 * cz2));
                 }
             });
-            /* F = iterTemp copies the core; the pads it would copy are
-             * rewritten by the boundary conditions that follow. */
-            core_loop([&](int i, int j, int k) { F(i, j, k) = iterTemp(i, j, k); });
+            /* F = iterTemp copies the whole padded array; the sweep never
+             * writes iterTemp's pads (timestep.cc:117-118 allocates it
+             * without a fill), taken here as zero -- what a fresh
+             * allocation reads.  The boundary conditions then rewrite the
+             * first ghost layer; on wall axes the second stays zero. */
+            full_loop(F, [&](size_t q) { F.v[q] = iterTemp.v[q]; });
             impose_bcs(F, bc);
             double m = 0.0;
             const int n0 = g.N[0], n1 = g.N[1], n2 = g.N[2];
@@ -1022,6 +1134,154 @@ struct Rk3 {
         }
     }
 
+    /* H += the diffusion term of F over the core, x then y then z
+     * (vfield::computeDiff, vfield.cc:150-203; sfield::computeDiff,
+     * sfield.cc:133-158). */
+    void diff_into(const Arr3 &F, Arr3 &H) {
+        core_loop([&](int i, int j, int k) {
+            H(i, j, k) += d2(F, 0, i, j, k);
+            if (d3) H(i, j, k) += d2(F, 1, i, j, k);
+            H(i, j, k) += d2(F, 2, i, j, k);
+        });
+    }
+    /* H -= the convection of F by V over the core, direction by direction
+     * (computeNLin, vfield.cc:205-269, sfield.cc:160-198): nlScheme 1 the
+     * standard form u dF/dx, 2 hybrid upwinding with diffusion coefficient
+     * dcoef, 3 Morinishi.  A planar run has no y direction; the reference's
+     * upwind loops still visit it with Vy = 0, which subtracts a zero. */
+    void nlin_into(const Arr3 &F, Arr3 &H, double dcoef) {
+        const int nl = prm.nl_scheme;
+        core_loop([&](int i, int j, int k) {
+            for (int d = 0; d < 3; d++) {
+                if (!d3 && d == 1) continue;
+                const Arr3 &Va = d == 0 ? Vx : (d == 1 ? Vy : Vz);
+                double t;
+                if (nl == 3)
+                    t = mterm(F, Va, d, i, j, k);
+                else if (nl == 2)
+                    t = uterm(F, Va, dcoef, d, i, j, k);
+                else
+                    t = Va(i, j, k) * d1(F, d, i, j, k);
+                H(i, j, k) -= t;
+            }
+        });
+    }
+    /* mgRHS = div V * scale, mgSolve into Pp, Pp.syncFaces(), P += Pp,
+     * V -= fac * grad Pp, boundary conditions of V, P and T (lsRK3_d3.cc:
+     * 270-304, eulerCN_d3.cc:240-268). */
+    void project(double scale, double fac, int *mgc) {
+        Arr3 *vel[3] = {&Vx, &Vy, &Vz};
+        Arr3 *pg[3] = {&pgX, &pgY, &pgZ};
+        const saras_field_bc *vbc[3] = {&prm.bc_vx, &prm.bc_vy, &prm.bc_vz};
+        mgRHS.fill(0.0);
+        core_loop([&](int i, int j, int k) {
+            mgRHS(i, j, k) += d1(Vx, 0, i, j, k);
+            if (d3) mgRHS(i, j, k) += d1(Vy, 1, i, j, k);
+            mgRHS(i, j, k) += d1(Vz, 2, i, j, k);
+        });
+        full_loop(mgRHS, [&](size_t q) { mgRHS.v[q] *= scale; });
+        int64_t st[3] = {Pp.s0, Pp.s1, 1};
+        double *pp0 = &Pp(0, 0, 0);
+        const double *rh0 = &mgRHS(0, 0, 0);
+        int nc = 0;
+        int ms = mg->mg_solve(pp0, rh0, st, nullptr, 0, &nc, nullptr);
+        if (mgc) *mgc += nc;
+        (void)ms;
+        sync_faces(Pp);
+        full_loop(P, [&](size_t q) { P.v[q] += Pp.v[q]; });
+        core_loop([&](int i, int j, int k) {
+            pgX(i, j, k) = d1(Pp, 0, i, j, k);
+            if (d3) pgY(i, j, k) = d1(Pp, 1, i, j, k);
+            pgZ(i, j, k) = d1(Pp, 2, i, j, k);
+        });
+        for (int c = 0; c < 3; c++) {
+            Arr3 &F = *vel[c];
+            full_loop(*pg[c], [&](size_t q) {
+                pg[c]->v[q] *= fac;
+                F.v[q] -= pg[c]->v[q];
+            });
+        }
+        for (int c = 0; c < 3; c++) {
+            if (!d3 && c == 1) continue;
+            impose_bcs(*vel[c], *vbc[c]);
+        }
+        impose_bcs(P, prm.bc_p);
+        if (prm.with_scalar) impose_bcs(T, prm.bc_t);
+    }
+
+    /* eulerCN_d3::timeAdvance(V, P[, T]) (lib/timestep/eulerCN_d3.cc:
+     * 88-176, 178-268); eulerCN_d2 skips Vy.  Crank-Nicolson weights
+     * alpha = beta = 1/2 (eulerCN_d3.cc:62-63). */
+    int euler_advance(int *mgc, int *cni) {
+        const double alphCN2 = 1.0 / 2.0, betaCN2 = 1.0 / 2.0;
+        const bool sc = prm.with_scalar != 0;
+        const double nu = prm.nu, kappa = prm.kappa, dt = prm.dt;
+        Arr3 *vel[3] = {&Vx, &Vy, &Vz};
+        Arr3 *nse[3] = {&nseX, &nseY, &nseZ};
+        Arr3 *pg[3] = {&pgX, &pgY, &pgZ};
+        const saras_field_bc *vbc[3] = {&prm.bc_vx, &prm.bc_vy, &prm.bc_vz};
+        for (int c = 0; c < 3; c++) nse[c]->fill(0.0);
+        tmpRHS.fill(0.0);
+        for (int c = 0; c < 3; c++) {
+            if (!d3 && c == 1) continue;
+            diff_into(*vel[c], *nse[c]);
+        }
+        {
+            const double f = nu * alphCN2;
+            for (int c = 0; c < 3; c++) full_loop(*nse[c], [&](size_t q) { nse[c]->v[q] *= f; });
+        }
+        if (sc) {
+            diff_into(T, tmpRHS);
+            const double f = kappa * alphCN2;
+            full_loop(tmpRHS, [&](size_t q) { tmpRHS.v[q] *= f; });
+        }
+        for (int c = 0; c < 3; c++) {
+            if (!d3 && c == 1) continue;
+            nlin_into(*vel[c], *nse[c], nu);
+        }
+        if (sc) nlin_into(T, tmpRHS, kappa);
+        /* buoyantForce::addForcing (buoyantForce.cc:64-69); the zero forcing
+         * of a run without temperature adds nothing */
+        if (sc)
+            for (int c = 0; c < 3; c++) {
+                const double gt = prm.g_terms[c];
+                full_loop(*nse[c], [&](size_t q) { nse[c]->v[q] -= gt * T.v[q]; });
+            }
+        for (int c = 0; c < 3; c++) pg[c]->fill(0.0);
+        core_loop([&](int i, int j, int k) {
+            pgX(i, j, k) = d1(P, 0, i, j, k);
+            if (d3) pgY(i, j, k) = d1(P, 1, i, j, k);
+            pgZ(i, j, k) = d1(P, 2, i, j, k);
+        });
+        for (int c = 0; c < 3; c++) {
+            Arr3 &F = *vel[c];
+            full_loop(*nse[c], [&](size_t q) {
+                nse[c]->v[q] -= pg[c]->v[q];
+                nse[c]->v[q] *= dt;
+                nse[c]->v[q] += F.v[q];
+            });
+            sync_faces(*nse[c]);
+        }
+        if (sc) {
+            full_loop(tmpRHS, [&](size_t q) {
+                tmpRHS.v[q] *= dt;
+                tmpRHS.v[q] += T.v[q];
+            });
+            sync_faces(tmpRHS);
+        }
+        for (int c = 0; c < 3; c++) {
+            if (!d3 && c == 1) continue;
+            int s = cn_solve(*vel[c], *nse[c], nu, betaCN2, *vbc[c], cni);
+            if (s) return s;
+        }
+        if (sc) {
+            int s = cn_solve(T, tmpRHS, kappa, betaCN2, prm.bc_t, cni);
+            if (s) return s;
+        }
+        project(1.0 / dt, dt, mgc);
+        return SARAS_OK;
+    }
+
     /* lsRK3_d3::timeAdvance(V, P[, T]) (lib/timestep/lsRK3_d3.cc:94-177,
      * 190-305); lsRK3_d2 skips Vy. */
     int time_advance(int *mgc, int *cni) {
@@ -1051,20 +1311,9 @@ struct Rk3 {
             tSF.fill(0.0);
             for (int c = 0; c < 3; c++) {
                 if (!d3 && c == 1) continue;
-                Arr3 &F = *vel[c];
-                Arr3 &H = *tv[c];
-                core_loop([&](int i, int j, int k) {
-                    H(i, j, k) += d2(F, 0, i, j, k);
-                    if (d3) H(i, j, k) += d2(F, 1, i, j, k);
-                    H(i, j, k) += d2(F, 2, i, j, k);
-                });
+                diff_into(*vel[c], *tv[c]);
             }
-            if (sc)
-                core_loop([&](int i, int j, int k) {
-                    tSF(i, j, k) += d2(T, 0, i, j, k);
-                    if (d3) tSF(i, j, k) += d2(T, 1, i, j, k);
-                    tSF(i, j, k) += d2(T, 2, i, j, k);
-                });
+            if (sc) diff_into(T, tSF);
             {
                 double an = alph[rk] * nu, ak = alph[rk] * kappa;
                 for (int c = 0; c < 3; c++)
@@ -1094,41 +1343,14 @@ struct Rk3 {
                     full_loop(*nse[c], [&](size_t q) { nse[c]->v[q] += ab * tv[c]->v[q]; });
                 if (sc) full_loop(tmpRHS, [&](size_t q) { tmpRHS.v[q] += ab * tSF.v[q]; });
             }
-            /* non-linear terms: nlScheme 1 (vfield.cc:205-245, sfield.cc:160-
-             * 198) or 3, Morinishi (vfield.cc:271-474, sfield.cc:200-323) */
+            /* non-linear terms */
             for (int c = 0; c < 3; c++) tv[c]->fill(0.0);
             tSF.fill(0.0);
             for (int c = 0; c < 3; c++) {
                 if (!d3 && c == 1) continue;
-                Arr3 &F = *vel[c];
-                Arr3 &H = *tv[c];
-                if (prm.nl_scheme == 3)
-                    core_loop([&](int i, int j, int k) {
-                        H(i, j, k) -= mterm(F, Vx, 0, i, j, k);
-                        if (d3) H(i, j, k) -= mterm(F, Vy, 1, i, j, k);
-                        H(i, j, k) -= mterm(F, Vz, 2, i, j, k);
-                    });
-                else
-                    core_loop([&](int i, int j, int k) {
-                        H(i, j, k) -= Vx(i, j, k) * d1(F, 0, i, j, k);
-                        if (d3) H(i, j, k) -= Vy(i, j, k) * d1(F, 1, i, j, k);
-                        H(i, j, k) -= Vz(i, j, k) * d1(F, 2, i, j, k);
-                    });
+                nlin_into(*vel[c], *tv[c], nu);
             }
-            if (sc) {
-                if (prm.nl_scheme == 3)
-                    core_loop([&](int i, int j, int k) {
-                        tSF(i, j, k) -= mterm(T, Vx, 0, i, j, k);
-                        if (d3) tSF(i, j, k) -= mterm(T, Vy, 1, i, j, k);
-                        tSF(i, j, k) -= mterm(T, Vz, 2, i, j, k);
-                    });
-                else
-                    core_loop([&](int i, int j, int k) {
-                        tSF(i, j, k) -= Vx(i, j, k) * d1(T, 0, i, j, k);
-                        if (d3) tSF(i, j, k) -= Vy(i, j, k) * d1(T, 1, i, j, k);
-                        tSF(i, j, k) -= Vz(i, j, k) * d1(T, 2, i, j, k);
-                    });
-            }
+            if (sc) nlin_into(T, tSF, kappa);
             {
                 double gm = gam[rk];
                 for (int c = 0; c < 3; c++)
@@ -1161,46 +1383,7 @@ struct Rk3 {
                 if (s) return s;
             }
             /* pressure correction */
-            mgRHS.fill(0.0);
-            core_loop([&](int i, int j, int k) {
-                mgRHS(i, j, k) += d1(Vx, 0, i, j, k);
-                if (d3) mgRHS(i, j, k) += d1(Vy, 1, i, j, k);
-                mgRHS(i, j, k) += d1(Vz, 2, i, j, k);
-            });
-            {
-                double sc2 = 1.0 / ((alph[rk] + bet[rk]) * dt);
-                full_loop(mgRHS, [&](size_t q) { mgRHS.v[q] *= sc2; });
-            }
-            int64_t st[3] = {Pp.s0, Pp.s1, 1};
-            double *pp0 = &Pp(0, 0, 0);
-            const double *rh0 = &mgRHS(0, 0, 0);
-            int nc = 0;
-            int ms = mg->mg_solve(pp0, rh0, st, nullptr, 0, &nc, nullptr);
-            if (mgc) *mgc += nc;
-            (void)ms;
-            sync_faces(Pp);
-            full_loop(P, [&](size_t q) { P.v[q] += Pp.v[q]; });
-            core_loop([&](int i, int j, int k) {
-                pgX(i, j, k) = d1(Pp, 0, i, j, k);
-                if (d3) pgY(i, j, k) = d1(Pp, 1, i, j, k);
-                pgZ(i, j, k) = d1(Pp, 2, i, j, k);
-            });
-            {
-                double ab = (alph[rk] + bet[rk]) * dt;
-                for (int c = 0; c < 3; c++) {
-                    Arr3 &F = *vel[c];
-                    full_loop(*pg[c], [&](size_t q) {
-                        pg[c]->v[q] *= ab;
-                        F.v[q] -= pg[c]->v[q];
-                    });
-                }
-            }
-            for (int c = 0; c < 3; c++) {
-                if (!d3 && c == 1) continue;
-                impose_bcs(*vel[c], *vbc[c]);
-            }
-            impose_bcs(P, prm.bc_p);
-            if (sc) impose_bcs(T, prm.bc_t);
+            project(1.0 / ((alph[rk] + bet[rk]) * dt), (alph[rk] + bet[rk]) * dt, mgc);
         }
         return SARAS_OK;
     }
@@ -1297,7 +1480,38 @@ int oracle_mg_solve(const saras_grid_desc *gd, const saras_mg_params *prm, doubl
     return s;
 }
 
-/* `nsteps` calls of lsRK3 timeAdvance on full padded fields (pad 1). */
+/* One field operator of the time step on a padded field, over the core
+ * (test hook for the stencils): op 1 calcDerivative1 along `axis`, op 2
+ * calcDerivative2 along `axis`, op 3 the convection term of F by the
+ * velocity (vx, vy, vz) as computeNLin adds it to a zero H, with diffusion
+ * coefficient `dcoef` for the upwind Peclet number.  out receives the core
+ * (its pads are left alone). */
+int oracle_field_op(const saras_grid_desc *gd, const saras_rk3_params *prm, int op, int axis, double dcoef,
+                    const double *f, const double *vx, const double *vy, const double *vz, double *out,
+                    const int64_t *strides) {
+    Rk3 r;
+    int s = r.setup(*gd, *prm);
+    if (s) return s;
+    if (op < 1 || op > 3 || axis < 0 || axis > 2 || !r.g.active(axis)) return SARAS_BAD_ARG;
+    copy_in(r.T, f, strides);
+    copy_in(r.Vx, vx, strides);
+    if (gd->dims == 3) copy_in(r.Vy, vy, strides);
+    copy_in(r.Vz, vz, strides);
+    r.tSF.fill(0.0);
+    if (op == 3)
+        r.nlin_into(r.T, r.tSF, dcoef);
+    else
+        r.core_loop([&](int i, int j, int k) {
+            r.tSF(i, j, k) = op == 1 ? r.d1(r.T, axis, i, j, k) : r.d2(r.T, axis, i, j, k);
+        });
+    for (int i = 0; i < r.g.N[0]; i++)
+        for (int j = 0; j < r.g.N[1]; j++)
+            for (int k = 0; k < r.g.N[2]; k++) out[i * strides[0] + j * strides[1] + k * strides[2]] = r.tSF(i, j, k);
+    return SARAS_OK;
+}
+
+/* `nsteps` calls of lsRK3 (integration 0 or 2) or eulerCN (integration 1)
+ * timeAdvance on full padded fields (pad 1 or 2). */
 int oracle_rk3_run(const saras_grid_desc *gd, const saras_rk3_params *prm, double *vx, double *vy,
                    double *vz, double *p, double *t, double *pp, const int64_t *strides, int nsteps,
                    int *mg_cycles, int *cn_iters, double *seconds) {
@@ -1313,7 +1527,8 @@ int oracle_rk3_run(const saras_grid_desc *gd, const saras_rk3_params *prm, doubl
     if (mg_cycles) *mg_cycles = 0;
     if (cn_iters) *cn_iters = 0;
     double t0 = now_s();
-    for (int n = 0; n < nsteps && !s; n++) s = r.time_advance(mg_cycles, cn_iters);
+    for (int n = 0; n < nsteps && !s; n++)
+        s = prm->integration == 1 ? r.euler_advance(mg_cycles, cn_iters) : r.time_advance(mg_cycles, cn_iters);
     if (seconds) *seconds = now_s() - t0;
     copy_out(r.Vx, vx, strides);
     if (gd->dims == 3) copy_out(r.Vy, vy, strides);

@@ -94,8 +94,8 @@ inline void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t s
 // Visits the core cells of a level for grid-wide reductions: each warp takes
 // whole k-rows (32-bit index arithmetic only) and its lanes stride along k,
 // so loads stay coalesced.
-template <class Fn>
-__device__ __forceinline__ void for_core_rows(const Lay &L, Fn &&fn) {
+template <class LY, class Fn>
+__device__ __forceinline__ void for_core_rows(const LY &L, Fn &&fn) {
     const int lane = threadIdx.x & 31;
     const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);

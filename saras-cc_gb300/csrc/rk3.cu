@@ -1,22 +1,25 @@
-// Low-storage RK3 time step of SARAS on GB300: the sub-step stencils around
+// Time step of SARAS on GB300 -- the low-storage RK3 (lsRK3) and the
+// Euler/Crank-Nicolson (eulerCN) integrators: the sub-step stencils around
 // the pressure-Poisson solve, one fused kernel per stage of the reference's
 // sequence of full-array Blitz operations.
 //
 // Reference: lsRK3_d3::timeAdvance(V,P,T) and (V,P) (lib/timestep/
-// lsRK3_d3.cc:94-177, 190-305; lsRK3_d2.cc), timestep::solveVx/Vy/Vz/T
-// (lib/timestep/predictors.cc:59-423), vfield/sfield::computeDiff,
-// computeNLin (nlScheme 1 and 3, Morinishi's second-order branch),
-// divergence, gradient (lib/field/vfield.cc,
-// sfield.cc, plainsf.cc), derivative::calcDerivative1_* / 2** with
-// dScheme 1 (lib/field/derivative.cc:104-318), field BC writers
-// (lib/boundary/dirichlet.cc, neumann.cc) and buoyantForce::addForcing
+// lsRK3_d3.cc:94-177, 190-305; lsRK3_d2.cc), eulerCN_d3::timeAdvance
+// (lib/timestep/eulerCN_d3.cc:88-268; eulerCN_d2.cc), timestep::solveVx/Vy/
+// Vz/T (lib/timestep/predictors.cc:59-423), vfield/sfield::computeDiff,
+// computeNLin (nlScheme 1 standard, 2 hybrid upwind, 3 Morinishi),
+// divergence, gradient (lib/field/vfield.cc, sfield.cc, plainsf.cc),
+// derivative::calcDerivative1_* / 2** with dScheme 1 and 2
+// (lib/field/derivative.cc:104-318), field BC writers (lib/boundary/
+// dirichlet.cc, neumann.cc) and buoyantForce::addForcing
 // (lib/force/buoyantForce.cc:64-69).
 //
 // Every per-cell value is formed in the reference's operation order with
 // separately rounded FP64 operations, so one step is bit-identical to the
 // single-rank reference arithmetic (given the same multigrid form).  The
-// Blitz stencils are taken as central12n = (F[+1]-F[-1])*0.5 and
-// central22n = (F[-1]-2F)+F[+1].
+// Blitz stencils are taken as central12n = (F[+1]-F[-1])*0.5, central22n =
+// (F[-1]-2F)+F[+1], central14n = (8(F[+1]-F[-1]) - (F[+2]-F[-2]))/12 and
+// central24n = (16(F[+1]+F[-1]) - 30F - (F[+2]+F[-2]))/12.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -36,15 +39,50 @@ namespace {
 
 constexpr int BX = 128;
 
+// Field layout: core plus `p` ghost layers on x and z and `py` on y (1 for
+// the planar case, grid.cc:91-95).  Element (i,j,k) sits at (i+p)*s0 +
+// (j+py)*s1 + (k+KOFF): k-rows start their core on a 32-byte boundary and
+// the ghosts k = -p.. -1 sit just below.  With p = 1 this is the multigrid
+// level layout (Lay).
+struct FLay {
+    int n0, n1, n2;
+    int p, py;
+    int64_t s0, s1;
+    int64_t size;
+
+    __host__ __device__ __forceinline__ int64_t at(int i, int j, int k) const {
+        return (int64_t)(i + p) * s0 + (int64_t)(j + py) * s1 + (int64_t)(k + KOFF);
+    }
+    __host__ __device__ __forceinline__ int ext(int a) const { return a == 0 ? n0 : (a == 1 ? n1 : n2); }
+    __host__ __device__ __forceinline__ int pad(int a) const { return a == 1 ? py : p; }
+};
+
+FLay make_flay(int n0, int n1, int n2, int p, int py) {
+    FLay l;
+    l.n0 = n0;
+    l.n1 = n1;
+    l.n2 = n2;
+    l.p = p;
+    l.py = py;
+    l.s1 = ((int64_t)n2 + KOFF + p + 3) / 4 * 4;
+    l.s0 = l.s1 * (n1 + 2 * py);
+    l.size = l.s0 * (n0 + 2 * p);
+    return l;
+}
+
 // Per-axis finest-level metric tables over core indices and scalars.
 struct RkTab {
     const double *xi_x[3], *xixx[3], *xix2[3];
     const double *a2[3], *a1[3];  // ihx2*xix2, i2hx*xixx (timestep coefficients)
+    const double *dh[3];          // x(i+1) - x(i): the upwind Peclet length
 };
 struct RkScal {
     double ih[3], ih2d[3];  // derivative: 1/dXi, pow(1/dXi, 2)
     double ih2t[3], i2ht[3]; // timestep: 1/pow(dXi,2), 0.5/dXi
     double i2d[3];           // vfield/sfield: 1/(2 dXi) (vfield.cc:133-135)
+    double pe_limit;         // "Peclet Limit"
+    double ua, ub, uc, ud;   // upwind stencil weights (vfield.cc:114-130)
+    double dc_v, dc_t;       // diffusion coefficients of V and T (Peclet number)
 };
 
 // Field boundary rules: periodic flags, per face Dirichlet (2v) or Neumann
@@ -58,41 +96,130 @@ struct FBC {
 
 struct Stage {
     int rk;
+    int euler;  // eulerCN right-hand side instead of the RK3 sub-stage
+    int nls;    // non-linear scheme 1, 2 or 3
     double zeta, anu, akap, ab, gam, dt;
     double g[3];
 };
 
-__device__ __forceinline__ int64_t axis_stride(const Lay &L, int a) { return a == 0 ? L.s0 : (a == 1 ? L.s1 : 1); }
-
-// calcDerivative1 (derivative.cc:104-204): xi_x * ((F+ - F-) * 0.5 * ihx)
-__device__ __forceinline__ double d1(const double *F, const Lay &L, const RkTab &T, const RkScal &S, int a,
-                                     int idx, int64_t c) {
-    const int64_t st = axis_stride(L, a);
-    const double c12 = rmul(rsub(F[c + st], F[c - st]), 0.5);
-    return rmul(T.xi_x[a][idx], rmul(c12, S.ih[a]));
+template <class LY>
+__device__ __forceinline__ int64_t axis_stride(const LY &L, int a) {
+    return a == 0 ? L.s0 : (a == 1 ? L.s1 : 1);
+}
+template <class LY>
+__device__ __forceinline__ int axis_ext(const LY &L, int a) {
+    return a == 0 ? L.n0 : (a == 1 ? L.n1 : L.n2);
 }
 
-// calcDerivative2 (derivative.cc:206-318): xixx*(c12*ihx) + xix2*(c22*ihx2)
-__device__ __forceinline__ double d2(const double *F, const Lay &L, const RkTab &T, const RkScal &S, int a,
+// calcDerivative1 (derivative.cc:104-204): xi_x * (c * ihx), c = central12n
+// for dScheme 1; for dScheme 2 central14n, or 0.5*(F+ - F-) on the first and
+// last core cell of the axis (on one rank every axis has both).
+template <int DS, class LY>
+__device__ __forceinline__ double d1(const double *F, const LY &L, const RkTab &T, const RkScal &S, int a,
                                      int idx, int64_t c) {
     const int64_t st = axis_stride(L, a);
     const double fp = F[c + st], fm = F[c - st];
-    const double c12 = rmul(rsub(fp, fm), 0.5);
-    const double c22 = radd(rsub(fm, rmul(2.0, F[c])), fp);
-    return radd(rmul(T.xixx[a][idx], rmul(c12, S.ih[a])), rmul(T.xix2[a][idx], rmul(c22, S.ih2d[a])));
+    double cc;
+    if (DS == 1) {
+        cc = rmul(rsub(fp, fm), 0.5);
+    } else if (idx == 0 || idx == axis_ext(L, a) - 1) {
+        cc = rmul(0.5, rsub(fp, fm));
+    } else {
+        cc = rdiv(rsub(rmul(8.0, rsub(fp, fm)), rsub(F[c + 2 * st], F[c - 2 * st])), 12.0);
+    }
+    return rmul(T.xi_x[a][idx], rmul(cc, S.ih[a]));
 }
 
-// One direction of Morinishi's skew-symmetric convection term, second-order
-// branch (dScheme 1; vfield.cc:271-474, sfield.cc:200-323):
-// (adv + div)/2 with adv = Va*xi*(F+ - F-)*i2d and div = xi*(Va+ F+ - Va- F-)*i2d,
-// the products standing for the Blitz temporaries tempXX = V.Vx*Vx etc.
-__device__ __forceinline__ double mterm(const double *F, const double *Va, const Lay &L, const RkTab &T,
+// calcDerivative2 (derivative.cc:206-318): xixx*(c1*ihx) + xix2*(c2*ihx2);
+// dScheme 2 takes the reference's F+ - 2F + F- on the first and last cell.
+template <int DS>
+__device__ __forceinline__ double d2(const double *F, const FLay &L, const RkTab &T, const RkScal &S, int a,
+                                     int idx, int64_t c) {
+    const int64_t st = axis_stride(L, a);
+    const double fp = F[c + st], fm = F[c - st], f0 = F[c];
+    double c1, c2;
+    if (DS == 1) {
+        c1 = rmul(rsub(fp, fm), 0.5);
+        c2 = radd(rsub(fm, rmul(2.0, f0)), fp);
+    } else if (idx == 0 || idx == L.ext(a) - 1) {
+        c1 = rmul(0.5, rsub(fp, fm));
+        c2 = radd(rsub(fp, rmul(2.0, f0)), fm);
+    } else {
+        const double fp2 = F[c + 2 * st], fm2 = F[c - 2 * st];
+        c1 = rdiv(rsub(rmul(8.0, rsub(fp, fm)), rsub(fp2, fm2)), 12.0);
+        c2 = rdiv(rsub(rsub(rmul(16.0, radd(fp, fm)), rmul(30.0, f0)), radd(fp2, fm2)), 12.0);
+    }
+    return radd(rmul(T.xixx[a][idx], rmul(c1, S.ih[a])), rmul(T.xix2[a][idx], rmul(c2, S.ih2d[a])));
+}
+
+// One direction of Morinishi's skew-symmetric convection term
+// (vfield.cc:271-474, sfield.cc:200-323): (adv + div)/2 with
+// adv = Va*xi*dF*i2d and div = xi*d(Va F)*i2d, the products standing for the
+// Blitz temporaries tempXX = V.Vx*Vx etc.  dF is F+ - F- (dScheme 1, and
+// dScheme 2 at the first and last point) or (-F+2 + 8F+1 - 8F-1 + F-2)/6.
+// The reference tests the last z point against the y extent (core.ubound(1),
+// vfield.cc:337,427), which is kept: along z the second-order form is taken
+// at k = 0 and k = n1 - 1.
+template <int DS>
+__device__ __forceinline__ double mterm(const double *F, const double *Va, const FLay &L, const RkTab &T,
                                         const RkScal &S, int a, int idx, int64_t c) {
     const int64_t st = axis_stride(L, a);
     const double x = T.xi_x[a][idx];
+    const int last = (a == 2 ? L.n1 : L.ext(a)) - 1;
+    if (DS == 2 && idx != 0 && idx != last) {
+        const double f2 = F[c + 2 * st], f1 = F[c + st], g1 = F[c - st], g2 = F[c - 2 * st];
+        const double sf = radd(rsub(radd(-f2, rmul(8.0, f1)), rmul(8.0, g1)), g2);
+        const double sv = radd(rsub(radd(-rmul(Va[c + 2 * st], f2), rmul(8.0, rmul(Va[c + st], f1))),
+                                    rmul(8.0, rmul(Va[c - st], g1))),
+                               rmul(Va[c - 2 * st], g2));
+        const double adv = rdiv(rmul(rmul(rmul(Va[c], x), sf), S.i2d[a]), 6.0);
+        const double div = rdiv(rmul(rmul(x, sv), S.i2d[a]), 6.0);
+        return rdiv(radd(adv, div), 2.0);
+    }
     const double adv = rmul(rmul(rmul(Va[c], x), rsub(F[c + st], F[c - st])), S.i2d[a]);
     const double div = rmul(rmul(x, rsub(rmul(Va[c + st], F[c + st]), rmul(Va[c - st], F[c - st]))), S.i2d[a]);
     return rdiv(radd(adv, div), 2.0);
+}
+
+// One direction of the hybrid upwind convection term (vfield.cc:475-690,
+// sfield.cc:324-495): below the "Peclet Limit" (Pe = |u| dh / diffCoeff)
+// central differences, above it the stencil biased against the local
+// velocity; dScheme 1 first-order upwinding with second-order central
+// differences, dScheme 2 second-order upwinding with fourth-order central
+// differences and second-order central differences on the end cells.
+template <int DS>
+__device__ __forceinline__ double uterm(const double *F, const double *Va, const FLay &L, const RkTab &T,
+                                        const RkScal &S, double dcoef, int a, int idx, int64_t c) {
+    const int64_t st = axis_stride(L, a);
+    const double u = Va[c];
+    const double ux = rmul(u, T.xi_x[a][idx]);
+    const double f0 = F[c], fp = F[c + st], fm = F[c - st];
+    if (DS == 2 && (idx == 0 || idx == L.ext(a) - 1)) return rmul(rmul(ux, rsub(fp, fm)), S.i2d[a]);
+    const double pe = rdiv(rmul(fabs(u), T.dh[a][idx]), dcoef);
+    if (DS == 1) {
+        if (pe < S.pe_limit) return rmul(rmul(ux, rsub(fp, fm)), S.i2d[a]);
+        if (u > 0) return rmul(rmul(ux, rsub(radd(rmul(-S.ua, fm), rmul(S.ub, f0)), rmul(S.uc, fp))), S.i2d[a]);
+        return rmul(rmul(ux, radd(rsub(rmul(S.ua, fp), rmul(S.ub, f0)), rmul(S.uc, fm))), S.i2d[a]);
+    }
+    const double fp2 = F[c + 2 * st], fm2 = F[c - 2 * st];
+    if (pe < S.pe_limit)
+        return rdiv(rmul(rmul(ux, radd(rsub(radd(-fp2, rmul(8.0, fp)), rmul(8.0, fm)), fm2)), S.i2d[a]), 6.0);
+    if (u > 0)
+        return rmul(rmul(ux, rsub(radd(rsub(rmul(S.ua, fm2), rmul(S.ub, fm)), rmul(S.uc, f0)), rmul(S.ud, fp))),
+                    S.i2d[a]);
+    return rmul(rmul(ux, radd(rsub(radd(rmul(-S.ua, fp2), rmul(S.ub, fp)), rmul(S.uc, f0)), rmul(S.ud, fm))),
+                S.i2d[a]);
+}
+
+// The convection contribution of one direction for the selected scheme; the
+// caller subtracts it.  nlScheme 1 is u dF/dx (vfield.cc:205-245).
+template <int DS>
+__device__ __forceinline__ double nterm(int nls, const double *F, const double *Va, const FLay &L,
+                                        const RkTab &T, const RkScal &S, double dcoef, int a, int idx,
+                                        int64_t c) {
+    if (nls == 3) return mterm<DS>(F, Va, L, T, S, a, idx, c);
+    if (nls == 2) return uterm<DS>(F, Va, L, T, S, dcoef, a, idx, c);
+    return rmul(Va[c], d1<DS>(F, L, T, S, a, idx, c));
 }
 
 struct Fields {
@@ -102,77 +229,80 @@ struct Fields {
     double *tmpR, *nlT;
 };
 
-// Right-hand sides of one RK3 sub-stage for every velocity component and T
-// (lsRK3_d3.cc:199-252): zeta*NL_prev + alpha*nu*Diff + (alpha+beta)*(F - grad P)
-// + gamma*NL, times dt, plus the field.  NL is kept for the next stage.
-template <bool D3, bool SC, int NLS>
-__global__ void k_rk3_rhs(Fields f, Lay L, RkTab T, RkScal S, Stage sg) {
+// Right-hand side of one field at one cell.  RK3 sub-stage (lsRK3_d3.cc:
+// 199-268): zeta*NL_prev + alpha*nu*Diff + (alpha+beta)*(F - grad P) +
+// gamma*NL, times dt, plus the field; NL is kept for the next stage.
+// eulerCN (eulerCN_d3.cc:178-241): Diff*(nu/2) - NL - F - grad P, times dt,
+// plus the field.  comp 0..2 are the velocity components, 3 the scalar.
+template <bool D3, bool SC, int DS>
+__device__ __forceinline__ void rhs_cell(const Fields &f, const FLay &L, const RkTab &T, const RkScal &S,
+                                         const Stage &sg, int comp, int i, int j, int k, int64_t c,
+                                         double &rhs_out, double &nl_out) {
+    const int id[3] = {i, j, k};
+    const bool vel = comp < 3;
+    const double *F = vel ? f.V[comp] : f.T;
+    const double dcoef = vel ? S.dc_v : S.dc_t;
+    double dif = radd(0.0, d2<DS>(F, L, T, S, 0, i, c));
+    if (D3) dif = radd(dif, d2<DS>(F, L, T, S, 1, j, c));
+    dif = radd(dif, d2<DS>(F, L, T, S, 2, k, c));
+    if (sg.euler) {
+        double h = rmul(dif, vel ? sg.anu : sg.akap);
+        h = rsub(h, nterm<DS>(sg.nls, F, f.V[0], L, T, S, dcoef, 0, i, c));
+        if (D3) h = rsub(h, nterm<DS>(sg.nls, F, f.V[1], L, T, S, dcoef, 1, j, c));
+        h = rsub(h, nterm<DS>(sg.nls, F, f.V[2], L, T, S, dcoef, 2, k, c));
+        if (vel) {
+            if (SC) h = rsub(h, rmul(sg.g[comp], f.T[c]));
+            h = rsub(h, d1<DS>(f.P, L, T, S, comp, id[comp], c));
+        }
+        h = rmul(h, sg.dt);
+        rhs_out = radd(h, F[c]);
+        nl_out = 0.0;
+        return;
+    }
+    double r = 0.0;
+    if (sg.rk > 0) r = radd(r, rmul(sg.zeta, vel ? f.nl[comp][c] : f.nlT[c]));
+    r = radd(r, rmul(vel ? sg.anu : sg.akap, dif));
+    double t = 0.0;
+    if (vel) {
+        if (SC) t = rsub(t, rmul(sg.g[comp], f.T[c]));
+        t = rsub(t, d1<DS>(f.P, L, T, S, comp, id[comp], c));
+    }
+    r = radd(r, rmul(sg.ab, t));  // for T: the zero forcing, multAdd still runs
+    double n = rsub(0.0, nterm<DS>(sg.nls, F, f.V[0], L, T, S, dcoef, 0, i, c));
+    if (D3) n = rsub(n, nterm<DS>(sg.nls, F, f.V[1], L, T, S, dcoef, 1, j, c));
+    n = rsub(n, nterm<DS>(sg.nls, F, f.V[2], L, T, S, dcoef, 2, k, c));
+    r = radd(r, rmul(sg.gam, n));
+    r = rmul(r, sg.dt);
+    rhs_out = radd(r, F[c]);
+    nl_out = n;
+}
+
+template <bool D3, bool SC, int DS>
+__global__ void k_rhs(Fields f, FLay L, RkTab T, RkScal S, Stage sg) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = D3 ? (int)blockIdx.y : 0;
     const int i = blockIdx.z;
     if (k >= L.n2) return;
     const int64_t c = L.at(i, j, k);
-    const int id[3] = {i, j, k};
     for (int comp = 0; comp < 3; comp++) {
         if (!D3 && comp == 1) continue;
-        const double *F = f.V[comp];
-        double r = 0.0;
-        if (sg.rk > 0) r = radd(r, rmul(sg.zeta, f.nl[comp][c]));
-        double dif = radd(0.0, d2(F, L, T, S, 0, i, c));
-        if (D3) dif = radd(dif, d2(F, L, T, S, 1, j, c));
-        dif = radd(dif, d2(F, L, T, S, 2, k, c));
-        r = radd(r, rmul(sg.anu, dif));
-        double t = 0.0;
-        if (SC) t = rsub(t, rmul(sg.g[comp], f.T[c]));
-        t = rsub(t, d1(f.P, L, T, S, comp, id[comp], c));
-        r = radd(r, rmul(sg.ab, t));
-        double n;
-        if (NLS == 3) {
-            n = rsub(0.0, mterm(F, f.V[0], L, T, S, 0, i, c));
-            if (D3) n = rsub(n, mterm(F, f.V[1], L, T, S, 1, j, c));
-            n = rsub(n, mterm(F, f.V[2], L, T, S, 2, k, c));
-        } else {
-            n = rsub(0.0, rmul(f.V[0][c], d1(F, L, T, S, 0, i, c)));
-            if (D3) n = rsub(n, rmul(f.V[1][c], d1(F, L, T, S, 1, j, c)));
-            n = rsub(n, rmul(f.V[2][c], d1(F, L, T, S, 2, k, c)));
-        }
-        r = radd(r, rmul(sg.gam, n));
-        r = rmul(r, sg.dt);
-        r = radd(r, F[c]);
+        double r, n;
+        rhs_cell<D3, SC, DS>(f, L, T, S, sg, comp, i, j, k, c, r, n);
         f.nse[comp][c] = r;
-        f.nl[comp][c] = n;
+        if (!sg.euler) f.nl[comp][c] = n;
     }
     if (SC) {
-        const double *F = f.T;
-        double r = 0.0;
-        if (sg.rk > 0) r = radd(r, rmul(sg.zeta, f.nlT[c]));
-        double dif = radd(0.0, d2(F, L, T, S, 0, i, c));
-        if (D3) dif = radd(dif, d2(F, L, T, S, 1, j, c));
-        dif = radd(dif, d2(F, L, T, S, 2, k, c));
-        r = radd(r, rmul(sg.akap, dif));
-        r = radd(r, rmul(sg.ab, 0.0));  // zeroForcing adds nothing, multAdd still runs
-        double n;
-        if (NLS == 3) {
-            n = rsub(0.0, mterm(F, f.V[0], L, T, S, 0, i, c));
-            if (D3) n = rsub(n, mterm(F, f.V[1], L, T, S, 1, j, c));
-            n = rsub(n, mterm(F, f.V[2], L, T, S, 2, k, c));
-        } else {
-            n = rsub(0.0, rmul(f.V[0][c], d1(F, L, T, S, 0, i, c)));
-            if (D3) n = rsub(n, rmul(f.V[1][c], d1(F, L, T, S, 1, j, c)));
-            n = rsub(n, rmul(f.V[2][c], d1(F, L, T, S, 2, k, c)));
-        }
-        r = radd(r, rmul(sg.gam, n));
-        r = rmul(r, sg.dt);
-        r = radd(r, F[c]);
+        double r, n;
+        rhs_cell<D3, SC, DS>(f, L, T, S, sg, 3, i, j, k, c, r, n);
         f.tmpR[c] = r;
-        f.nlT[c] = n;
+        if (!sg.euler) f.nlT[c] = n;
     }
 }
 
 // One Jacobi sweep of (1 - beta*dt*coef*L) u = rhs (predictors.cc:65-91).
 template <bool D3>
 __global__ void k_cn_jacobi(const double *__restrict__ F, const double *__restrict__ R, double *__restrict__ out,
-                            Lay L, RkTab T, double dt, double coef, double beta, double den_fac) {
+                            FLay L, RkTab T, double dt, double coef, double beta, double den_fac) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = D3 ? (int)blockIdx.y : 0;
     const int i = blockIdx.z;
@@ -205,7 +335,7 @@ __device__ __forceinline__ double warp_max(double v) {
 // max |u - beta*dt*coef*L u - rhs| over the core (predictors.cc:96-131),
 // per-block partials.
 template <bool D3>
-__global__ void k_cn_resid(const double *__restrict__ F, const double *__restrict__ R, Lay L, RkTab T, RkScal S,
+__global__ void k_cn_resid(const double *__restrict__ F, const double *__restrict__ R, FLay L, RkTab T, RkScal S,
                            double bdc, double *__restrict__ part) {
     double m = 0.0;
     for_core_rows(L, [&](int i, int j, int k) {
@@ -247,77 +377,96 @@ __global__ void k_max_final(const double *__restrict__ part, int nb, double *__r
     if (threadIdx.x == 0) out[0] = m;
 }
 
-// Ghost planes of a field (field::syncFaces then the wall BC writers).
-__global__ void k_fbc(double *u, Lay L, FBC B, int axis, int wall_pass, int a_lo, int b_lo, int b_cnt) {
-    const int b = b_lo + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    const int a = a_lo + (int)blockIdx.y;
-    if (b >= b_lo + b_cnt) return;
-    const int n[3] = {L.n0, L.n1, L.n2};
-    int lo[3], hi[3], in0[3], in1[3];
+enum { FBC_PERIODIC = 0, FBC_WALL = 1, FBC_ZERO_OUTER = 2 };
+
+// Ghost planes of a field along `axis`, over the full padded extents of the
+// other two axes: the periodic copy of all ghost layers (field::syncFaces on
+// one rank, mpidata.cc:371-397), the wall writers of the first ghost layer
+// (dirichlet.cc:72-76, neumann.cc:87-93), or zeros in the second ghost layer
+// of a wall axis.
+__global__ void k_fbc(double *u, FLay L, FBC B, int axis, int mode) {
     const int o0 = axis == 0 ? 1 : 0, o1 = axis == 2 ? 1 : 2;
-    lo[axis] = -1;
-    hi[axis] = n[axis];
-    in0[axis] = 0;
-    in1[axis] = n[axis] - 1;
-    lo[o0] = hi[o0] = in0[o0] = in1[o0] = a;
-    lo[o1] = hi[o1] = in0[o1] = in1[o1] = b;
-    const int64_t glo = L.at(lo[0], lo[1], lo[2]), ghi = L.at(hi[0], hi[1], hi[2]);
-    const int64_t ilo = L.at(in0[0], in0[1], in0[2]), ihi = L.at(in1[0], in1[1], in1[2]);
-    if (!wall_pass) {
-        u[ghi] = u[ilo];
-        u[glo] = u[ihi];
+    const int b = (int)(blockIdx.x * blockDim.x + threadIdx.x) - L.pad(o1);
+    const int a = (int)blockIdx.y - L.pad(o0);
+    if (b >= L.ext(o1) + L.pad(o1)) return;
+    const int n = L.ext(axis);
+    int q[3];
+    q[o0] = a;
+    q[o1] = b;
+    auto at = [&](int x) {
+        q[axis] = x;
+        return L.at(q[0], q[1], q[2]);
+    };
+    if (mode == FBC_PERIODIC) {
+        const int p = L.pad(axis);
+        for (int m = 0; m < p; m++) {
+            u[at(n + m)] = u[at(m)];
+            u[at(-p + m)] = u[at(n - p + m)];
+        }
+        return;
+    }
+    if (mode == FBC_ZERO_OUTER) {
+        u[at(-2)] = 0.0;
+        u[at(n + 1)] = 0.0;
         return;
     }
     const int f0 = 2 * axis, f1 = 2 * axis + 1;
-    u[glo] = B.type[f0] == SARAS_FBC_DIRICHLET ? rsub(B.two_v[f0], u[ilo]) : rsub(u[ilo], B.kh[f0]);
-    u[ghi] = B.type[f1] == SARAS_FBC_DIRICHLET ? rsub(B.two_v[f1], u[ihi]) : rsub(u[ihi], B.kh[f1]);
+    const double lo = u[at(0)], hi = u[at(n - 1)];
+    u[at(-1)] = B.type[f0] == SARAS_FBC_DIRICHLET ? rsub(B.two_v[f0], lo) : rsub(lo, B.kh[f0]);
+    u[at(n)] = B.type[f1] == SARAS_FBC_DIRICHLET ? rsub(B.two_v[f1], hi) : rsub(hi, B.kh[f1]);
 }
 
-// divergence of V into the multigrid RHS, scaled (lsRK3_d3.cc:272-276).
-template <bool D3>
+// divergence of V into the multigrid RHS (level layout), scaled
+// (lsRK3_d3.cc:272-276, eulerCN_d3.cc:243-244).
+template <bool D3, int DS>
 __global__ void k_divergence(const double *__restrict__ vx, const double *__restrict__ vy,
-                             const double *__restrict__ vz, double *__restrict__ out, Lay L, RkTab T, RkScal S,
-                             double scale) {
+                             const double *__restrict__ vz, double *__restrict__ out, FLay L, Lay LM, RkTab T,
+                             RkScal S, double scale) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = D3 ? (int)blockIdx.y : 0;
     const int i = blockIdx.z;
     if (k >= L.n2) return;
     const int64_t c = L.at(i, j, k);
-    double d = radd(0.0, d1(vx, L, T, S, 0, i, c));
-    if (D3) d = radd(d, d1(vy, L, T, S, 1, j, c));
-    d = radd(d, d1(vz, L, T, S, 2, k, c));
-    out[c] = rmul(d, scale);
+    double d = radd(0.0, d1<DS>(vx, L, T, S, 0, i, c));
+    if (D3) d = radd(d, d1<DS>(vy, L, T, S, 1, j, c));
+    d = radd(d, d1<DS>(vz, L, T, S, 2, k, c));
+    out[LM.at(i, j, k)] = rmul(d, scale);
 }
 
-// P += Pp; V -= (alpha+beta) dt grad Pp (lsRK3_d3.cc:281-294).
-template <bool D3>
+// P += Pp; V -= fac * grad Pp (lsRK3_d3.cc:281-294, eulerCN_d3.cc:253-260).
+// Pp is the multigrid level-0 iterate (one ghost layer: the fourth-order
+// stencil reaches two cells only away from the end cells).
+template <bool D3, int DS>
 __global__ void k_correct(double *__restrict__ vx, double *__restrict__ vy, double *__restrict__ vz,
-                          double *__restrict__ p, const double *__restrict__ pp, Lay L, RkTab T, RkScal S,
-                          double fac) {
+                          double *__restrict__ p, const double *__restrict__ pp, FLay L, Lay LM, RkTab T,
+                          RkScal S, double fac) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = D3 ? (int)blockIdx.y : 0;
     const int i = blockIdx.z;
     if (k >= L.n2) return;
-    const int64_t c = L.at(i, j, k);
-    p[c] = radd(p[c], pp[c]);
-    vx[c] = rsub(vx[c], rmul(d1(pp, L, T, S, 0, i, c), fac));
-    if (D3) vy[c] = rsub(vy[c], rmul(d1(pp, L, T, S, 1, j, c), fac));
-    vz[c] = rsub(vz[c], rmul(d1(pp, L, T, S, 2, k, c), fac));
+    const int64_t c = L.at(i, j, k), cm = LM.at(i, j, k);
+    p[c] = radd(p[c], pp[cm]);
+    vx[c] = rsub(vx[c], rmul(d1<DS>(pp, LM, T, S, 0, i, cm), fac));
+    if (D3) vy[c] = rsub(vy[c], rmul(d1<DS>(pp, LM, T, S, 1, j, cm), fac));
+    vz[c] = rsub(vz[c], rmul(d1<DS>(pp, LM, T, S, 2, k, cm), fac));
 }
 
-// Dense padded box <-> level layout (full box including the ghost layer).
-__global__ void k_box_in(const double *__restrict__ src, int64_t s0, int64_t s1, double *__restrict__ dst, Lay L,
-                         int jlo, int jhi) {
-    const int k = (int)(blockIdx.x * blockDim.x + threadIdx.x) - 1;
-    const int j = jlo + (int)blockIdx.y, i = (int)blockIdx.z - 1;
-    if (k > L.n2 || j > jhi) return;
+// Dense padded host box <-> device layout over the box -q..n+q-1 per axis
+// (q = the box's ghost layers, at most the layout's).
+template <class LY>
+__global__ void k_box_in(const double *__restrict__ src, int64_t s0, int64_t s1, double *__restrict__ dst, LY L,
+                         int qx, int qy) {
+    const int k = (int)(blockIdx.x * blockDim.x + threadIdx.x) - qx;
+    const int j = (int)blockIdx.y - qy, i = (int)blockIdx.z - qx;
+    if (k >= L.n2 + qx) return;
     dst[L.at(i, j, k)] = src[(int64_t)i * s0 + (int64_t)j * s1 + k];
 }
-__global__ void k_box_out(const double *__restrict__ src, Lay L, double *__restrict__ dst, int64_t s0, int64_t s1,
-                          int jlo, int jhi) {
-    const int k = (int)(blockIdx.x * blockDim.x + threadIdx.x) - 1;
-    const int j = jlo + (int)blockIdx.y, i = (int)blockIdx.z - 1;
-    if (k > L.n2 || j > jhi) return;
+template <class LY>
+__global__ void k_box_out(const double *__restrict__ src, LY L, double *__restrict__ dst, int64_t s0, int64_t s1,
+                          int qx, int qy) {
+    const int k = (int)(blockIdx.x * blockDim.x + threadIdx.x) - qx;
+    const int j = (int)blockIdx.y - qy, i = (int)blockIdx.z - qx;
+    if (k >= L.n2 + qx) return;
     dst[(int64_t)i * s0 + (int64_t)j * s1 + k] = src[L.at(i, j, k)];
 }
 
@@ -328,9 +477,10 @@ struct saras_rk3 {
     saras_rk3_params prm{};
     bool d3 = true;
     bool sc = true;
+    int ds = 1;  // Differentiation Scheme (the grid's pad)
     cudaStream_t stream = nullptr;
     saras_mg *mg = nullptr;
-    Lay L{};
+    FLay L{};
     double *V[3] = {nullptr, nullptr, nullptr}, *Vb[3] = {nullptr, nullptr, nullptr};
     double *P = nullptr, *T = nullptr, *Tb = nullptr;
     double *nse[3] = {nullptr, nullptr, nullptr}, *nl[3] = {nullptr, nullptr, nullptr};
@@ -357,7 +507,7 @@ saras_status rk_alloc(saras_rk3 *h, double **p, int64_t n) {
     cudaError_t e = cudaMalloc((void **)p, (size_t)std::max<int64_t>(n, 1) * sizeof(double));
     if (e != cudaSuccess) {
         cudaGetLastError();
-        set_error("cudaMalloc failed in the RK3 integrator: %s", cudaGetErrorString(e));
+        set_error("cudaMalloc failed in the time integrator: %s", cudaGetErrorString(e));
         return e == cudaErrorMemoryAllocation ? SARAS_OOM : SARAS_CUDA_ERR;
     }
     h->allocs.push_back(*p);
@@ -385,28 +535,41 @@ FBC make_fbc(const saras_rk3 *h, const saras_field_bc &b) {
     return f;
 }
 
-// field::syncFaces then the wall writers, x, y, z (sfield.cc:520-547).
-void impose(saras_rk3 *h, cudaStream_t s, double *u, const FBC &B) {
-    const Lay &L = h->L;
+void fbc_pass(saras_rk3 *h, cudaStream_t s, double *u, const FBC &B, int axis, int mode) {
+    const FLay &L = h->L;
+    const int o0 = axis == 0 ? 1 : 0, o1 = axis == 2 ? 1 : 2;
+    const int acnt = L.ext(o0) + 2 * L.pad(o0), bcnt = L.ext(o1) + 2 * L.pad(o1);
+    const int bx = bxfor(bcnt);
+    k_fbc<<<dim3(cdiv(bcnt, bx), (unsigned)acnt), bx, 0, s>>>(u, L, B, axis, mode);
+    h->launches++;
+}
+
+// field::syncFaces then the wall writers, x, y, z (sfield.cc:520-547).  After
+// a Crank-Nicolson sweep (`after_sweep`) the field was assigned from the
+// sweep's iterTemp, whose pads the reference never writes (timestep.cc:
+// 117-118) and which read as zero; the first ghost layer and every periodic
+// ghost are rewritten below, so only the second ghost layer of the wall
+// axes keeps that zero.
+void impose(saras_rk3 *h, cudaStream_t s, double *u, const FBC &B, bool after_sweep = false) {
+    if (after_sweep && h->L.p > 1)
+        for (int axis = 0; axis < 3; axis++)
+            if (h->grid.active(axis) && !B.per[axis]) fbc_pass(h, s, u, B, axis, FBC_ZERO_OUTER);
     for (int pass = 0; pass < 2; pass++) {
         for (int axis = 0; axis < 3; axis++) {
             if (!h->d3 && axis == 1) continue;
             if ((pass == 0) != (bool)B.per[axis]) continue;
-            const int n[3] = {L.n0, L.n1, L.n2};
-            const int o0 = axis == 0 ? 1 : 0, o1 = axis == 2 ? 1 : 2;
-            const int acnt = n[o0] + 2, bcnt = n[o1] + 2;
-            const int bx = bxfor(bcnt);
-            k_fbc<<<dim3(cdiv(bcnt, bx), (unsigned)acnt), bx, 0, s>>>(u, L, B, axis, pass, -1, -1, bcnt);
-            h->launches++;
+            fbc_pass(h, s, u, B, axis, pass == 0 ? FBC_PERIODIC : FBC_WALL);
         }
     }
 }
 
-dim3 cgrid(const Lay &L, bool d3, int bx) { return dim3(cdiv(L.n2, bx), d3 ? (unsigned)L.n1 : 1u, (unsigned)L.n0); }
+dim3 cgrid(const FLay &L, bool d3, int bx) {
+    return dim3(cdiv(L.n2, bx), d3 ? (unsigned)L.n1 : 1u, (unsigned)L.n0);
+}
 
 saras_status cn_solve(saras_rk3 *h, cudaStream_t s, int comp, const double *rhs, double coef, double beta,
                       int *iters) {
-    const Lay &L = h->L;
+    const FLay &L = h->L;
     const int bx = bxfor(L.n2);
     const double dt = h->prm.dt;
     const double den_fac = 2.0 * dt * coef * beta;  // 2.0 * dt * nu * beta, left to right
@@ -423,7 +586,7 @@ saras_status cn_solve(saras_rk3 *h, cudaStream_t s, int comp, const double *rhs,
                                                                    den_fac);
         h->launches++;
         std::swap(*cur, *alt);
-        impose(h, s, *cur, B);
+        impose(h, s, *cur, B, true);
         if (h->d3)
             k_cn_resid<true><<<h->nblocks, 256, 0, s>>>(*cur, rhs, L, h->tabs, h->scal, bdc, h->part);
         else
@@ -447,99 +610,134 @@ saras_status cn_solve(saras_rk3 *h, cudaStream_t s, int comp, const double *rhs,
     }
 }
 
+using RhsKernel = void (*)(Fields, FLay, RkTab, RkScal, Stage);
+
+RhsKernel rhs_kernel(bool d3, bool sc, int ds) {
+    // (dimension, scalar, differentiation scheme) -> kernel
+    static const RhsKernel ks[2][2][2] = {
+        {{k_rhs<false, false, 1>, k_rhs<false, false, 2>}, {k_rhs<false, true, 1>, k_rhs<false, true, 2>}},
+        {{k_rhs<true, false, 1>, k_rhs<true, false, 2>}, {k_rhs<true, true, 1>, k_rhs<true, true, 2>}}};
+    return ks[d3 ? 1 : 0][sc ? 1 : 0][ds == 2 ? 1 : 0];
+}
+
+void launch_rhs(saras_rk3 *h, const Stage &sg) {
+    Fields f;
+    for (int d = 0; d < 3; d++) {
+        f.V[d] = h->V[d];
+        f.nse[d] = h->nse[d];
+        f.nl[d] = h->nl[d];
+    }
+    f.P = h->P;
+    f.T = h->T;
+    f.tmpR = h->tmpR;
+    f.nlT = h->nlT;
+    const int bx = bxfor(h->L.n2);
+    rhs_kernel(h->d3, h->sc, h->ds)<<<cgrid(h->L, h->d3, bx), bx, 0, h->stream>>>(f, h->L, h->tabs, h->scal, sg);
+    h->launches++;
+}
+
+// The predictor sweeps, the pressure correction and the boundary conditions
+// shared by both integrators (lsRK3_d3.cc:262-304, eulerCN_d3.cc:237-268).
+saras_status correct_stage(saras_rk3 *h, double beta, double scale, double fac, int *mgc, int *cni) {
+    cudaStream_t s = h->stream;
+    const FLay &L = h->L;
+    const int bx = bxfor(L.n2);
+    const double nu = h->prm.nu, kappa = h->prm.kappa;
+    Level &m0 = h->mg->lv[0];
+    for (int comp = 0; comp < 3; comp++) {
+        if (!h->d3 && comp == 1) continue;
+        SARAS_TRY(cn_solve(h, s, comp, h->nse[comp], nu, beta, cni));
+    }
+    if (h->sc) SARAS_TRY(cn_solve(h, s, 3, h->tmpR, kappa, beta, cni));
+    const dim3 g = cgrid(L, h->d3, bx);
+    using DK = void (*)(const double *, const double *, const double *, double *, FLay, Lay, RkTab, RkScal, double);
+    using CK = void (*)(double *, double *, double *, double *, const double *, FLay, Lay, RkTab, RkScal, double);
+    static const DK dks[2][2] = {{k_divergence<false, 1>, k_divergence<false, 2>},
+                                 {k_divergence<true, 1>, k_divergence<true, 2>}};
+    static const CK cks[2][2] = {{k_correct<false, 1>, k_correct<false, 2>}, {k_correct<true, 1>, k_correct<true, 2>}};
+    const int di = h->d3 ? 1 : 0, si = h->ds == 2 ? 1 : 0;
+    dks[di][si]<<<g, bx, 0, s>>>(h->V[0], h->V[1], h->V[2], m0.rhs, L, m0.lay, h->tabs, h->scal, scale);
+    h->launches++;
+    int nc = 0;
+    saras_status st = mg_solve_resident(h->mg, &nc);
+    if (mgc) *mgc += nc;
+    h->launches += h->mg->last_launches;
+    if (st != SARAS_OK && st != SARAS_NOT_CONVERGED) return st;  // mgSolve itself never fails
+    cks[di][si]<<<g, bx, 0, s>>>(h->V[0], h->V[1], h->V[2], h->P, m0.lhs, L, m0.lay, h->tabs, h->scal, fac);
+    h->launches++;
+    for (int comp = 0; comp < 3; comp++) {
+        if (!h->d3 && comp == 1) continue;
+        impose(h, s, h->V[comp], h->bc[comp]);
+    }
+    impose(h, s, h->P, h->bc[3]);
+    if (h->sc) impose(h, s, h->T, h->bc[4]);
+    return SARAS_OK;
+}
+
+Stage base_stage(const saras_rk3 *h) {
+    Stage sg{};
+    sg.nls = h->prm.nl_scheme;
+    sg.dt = h->prm.dt;
+    for (int d = 0; d < 3; d++) sg.g[d] = h->prm.g_terms[d];
+    return sg;
+}
+
 // lsRK3_d3::timeAdvance (lsRK3_d3.cc:190-305)
-saras_status time_advance(saras_rk3 *h, int *mgc, int *cni) {
+saras_status time_advance_rk3(saras_rk3 *h, int *mgc, int *cni) {
     static const double alph[3] = {4.0 / 15.0, 1.0 / 15.0, 1.0 / 6.0};
     static const double bet[3] = {4.0 / 15.0, 1.0 / 15.0, 1.0 / 6.0};
     static const double gam[3] = {8.0 / 15.0, 5.0 / 12.0, 3.0 / 4.0};
     static const double zet[3] = {0.0, -17.0 / 60.0, -5.0 / 12.0};
-    cudaStream_t s = h->stream;
-    const Lay &L = h->L;
-    const int bx = bxfor(L.n2);
     const double nu = h->prm.nu, kappa = h->prm.kappa, dt = h->prm.dt;
-    Level &m0 = h->mg->lv[0];
     for (int rk = 0; rk < 3; rk++) {
-        Stage sg;
+        Stage sg = base_stage(h);
         sg.rk = rk;
         sg.zeta = zet[rk];
         sg.anu = alph[rk] * nu;
         sg.akap = alph[rk] * kappa;
         sg.ab = alph[rk] + bet[rk];
         sg.gam = gam[rk];
-        sg.dt = dt;
-        for (int d = 0; d < 3; d++) sg.g[d] = h->prm.g_terms[d];
-        Fields f;
-        for (int d = 0; d < 3; d++) {
-            f.V[d] = h->V[d];
-            f.nse[d] = h->nse[d];
-            f.nl[d] = h->nl[d];
-        }
-        f.P = h->P;
-        f.T = h->T;
-        f.tmpR = h->tmpR;
-        f.nlT = h->nlT;
-        const dim3 g = cgrid(L, h->d3, bx);
-        {
-            // (dimension, scalar, non-linear scheme) -> kernel
-            using K = void (*)(Fields, Lay, RkTab, RkScal, Stage);
-            const K ks[2][2][2] = {{{k_rk3_rhs<false, false, 1>, k_rk3_rhs<false, false, 3>},
-                                    {k_rk3_rhs<false, true, 1>, k_rk3_rhs<false, true, 3>}},
-                                   {{k_rk3_rhs<true, false, 1>, k_rk3_rhs<true, false, 3>},
-                                    {k_rk3_rhs<true, true, 1>, k_rk3_rhs<true, true, 3>}}};
-            ks[h->d3 ? 1 : 0][h->sc ? 1 : 0][h->prm.nl_scheme == 3 ? 1 : 0]<<<g, bx, 0, s>>>(f, L, h->tabs, h->scal,
-                                                                                          sg);
-        }
-        h->launches++;
-        for (int comp = 0; comp < 3; comp++) {
-            if (!h->d3 && comp == 1) continue;
-            SARAS_TRY(cn_solve(h, s, comp, h->nse[comp], nu, bet[rk], cni));
-        }
-        if (h->sc) SARAS_TRY(cn_solve(h, s, 3, h->tmpR, kappa, bet[rk], cni));
-        const double scale = 1.0 / ((alph[rk] + bet[rk]) * dt);
-        if (h->d3)
-            k_divergence<true><<<g, bx, 0, s>>>(h->V[0], h->V[1], h->V[2], m0.rhs, L, h->tabs, h->scal, scale);
-        else
-            k_divergence<false><<<g, bx, 0, s>>>(h->V[0], h->V[1], h->V[2], m0.rhs, L, h->tabs, h->scal, scale);
-        h->launches++;
-        int nc = 0;
-        saras_status st = mg_solve_resident(h->mg, &nc);
-        if (mgc) *mgc += nc;
-        h->launches += h->mg->last_launches;
-        if (st != SARAS_OK && st != SARAS_NOT_CONVERGED) return st;  // mgSolve itself never fails
-        const double fac = (alph[rk] + bet[rk]) * dt;
-        if (h->d3)
-            k_correct<true><<<g, bx, 0, s>>>(h->V[0], h->V[1], h->V[2], h->P, m0.lhs, L, h->tabs, h->scal, fac);
-        else
-            k_correct<false><<<g, bx, 0, s>>>(h->V[0], h->V[1], h->V[2], h->P, m0.lhs, L, h->tabs, h->scal, fac);
-        h->launches++;
-        for (int comp = 0; comp < 3; comp++) {
-            if (!h->d3 && comp == 1) continue;
-            impose(h, s, h->V[comp], h->bc[comp]);
-        }
-        impose(h, s, h->P, h->bc[3]);
-        if (h->sc) impose(h, s, h->T, h->bc[4]);
+        launch_rhs(h, sg);
+        SARAS_TRY(correct_stage(h, bet[rk], 1.0 / ((alph[rk] + bet[rk]) * dt), (alph[rk] + bet[rk]) * dt, mgc, cni));
     }
     SARAS_CUDA(cudaGetLastError());
     return SARAS_OK;
 }
 
+// eulerCN_d3::timeAdvance (eulerCN_d3.cc:88-268): Crank-Nicolson weights
+// alpha = beta = 1/2 (eulerCN_d3.cc:62-63).
+saras_status time_advance_euler(saras_rk3 *h, int *mgc, int *cni) {
+    const double alphCN2 = 1.0 / 2.0, betaCN2 = 1.0 / 2.0;
+    const double dt = h->prm.dt;
+    Stage sg = base_stage(h);
+    sg.euler = 1;
+    sg.anu = h->prm.nu * alphCN2;
+    sg.akap = h->prm.kappa * alphCN2;
+    launch_rhs(h, sg);
+    SARAS_TRY(correct_stage(h, betaCN2, 1.0 / dt, dt, mgc, cni));
+    SARAS_CUDA(cudaGetLastError());
+    return SARAS_OK;
+}
+
 saras_status rk3_create(const saras_grid_desc *gd, const saras_rk3_params *p, void *stream, saras_rk3 *h) {
-    if (gd->pad != 1) {
-        set_error("the RK3 stencils use Differentiation Scheme 1 (pad 1)");
+    if (gd->pad != 1 && gd->pad != 2) {
+        set_error("the time step takes Differentiation Scheme 1 (pad 1) or 2 (pad 2)");
         return SARAS_BAD_ARG;
     }
-    if ((p->nl_scheme != 1 && p->nl_scheme != 3) || !(p->dt > 0.0) || !(p->nu >= 0.0) || !(p->kappa >= 0.0) || p->max_iterations < 0) {
-        set_error("invalid RK3 parameters");
+    if (p->nl_scheme < 1 || p->nl_scheme > 3 || p->integration < 0 || p->integration > 2 || !(p->dt > 0.0) ||
+        !(p->nu >= 0.0) || !(p->kappa >= 0.0) || p->max_iterations < 0) {
+        set_error("invalid time-step parameters");
         return SARAS_BAD_ARG;
     }
     h->prm = *p;
     SARAS_TRY(h->grid.build(*gd, p->mg.levels));
     h->d3 = h->grid.dims == 3;
     h->sc = p->with_scalar != 0;
+    h->ds = gd->pad;
     h->stream = (cudaStream_t)stream;
     SARAS_TRY(saras_mg_create(gd, &p->mg, stream, &h->mg));
     const HostGrid &g = h->grid;
-    h->L = make_lay(g.N[0], h->d3 ? g.N[1] : 1, g.N[2]);
+    h->L = make_flay(g.N[0], h->d3 ? g.N[1] : 1, g.N[2], g.pad, h->d3 ? g.pad : 1);
     const int64_t sz = h->L.size;
     for (int d = 0; d < 3; d++) {
         SARAS_TRY(rk_alloc(h, &h->V[d], sz));
@@ -553,9 +751,10 @@ saras_status rk3_create(const saras_grid_desc *gd, const saras_rk3_params *p, vo
     SARAS_TRY(rk_alloc(h, &h->tmpR, sz));
     SARAS_TRY(rk_alloc(h, &h->nlT, sz));
     for (double *q : h->allocs) SARAS_CUDA(cudaMemset(q, 0, (size_t)sz * sizeof(double)));
-    // metric tables: xi_x, xixx, xix2, a2, a1 per axis over the core
+    // metric tables: xi_x, xixx, xix2, a2, a1, dh per axis over the core
+    constexpr int NT = 6;
     const int n[3] = {h->L.n0, h->L.n1, h->L.n2};
-    const int64_t tot = 5 * (int64_t)(n[0] + n[1] + n[2]);
+    const int64_t tot = NT * (int64_t)(n[0] + n[1] + n[2]);
     std::vector<double> host((size_t)tot, 0.0);
     SARAS_TRY(rk_alloc(h, &h->tab, tot));
     int64_t off = 0;
@@ -568,22 +767,43 @@ saras_status rk3_create(const saras_grid_desc *gd, const saras_rk3_params *p, vo
         h->scal.i2ht[d] = 0.5 / g.dxi[d];
         h->scal.i2d[d] = 1.0 / (2.0 * g.dxi[d]);
         h->scal.ih2t[d] = 1.0 / hx2;
-        double *dst[5];
-        for (int q = 0; q < 5; q++) dst[q] = h->tab + off + (int64_t)q * n[d];
+        double *dst[NT];
+        for (int q = 0; q < NT; q++) dst[q] = h->tab + off + (int64_t)q * n[d];
         h->tabs.xi_x[d] = dst[0];
         h->tabs.xixx[d] = dst[1];
         h->tabs.xix2[d] = dst[2];
         h->tabs.a2[d] = dst[3];
         h->tabs.a1[d] = dst[4];
+        h->tabs.dh[d] = dst[5];
         for (int i = 0; i < n[d]; i++) {
             const size_t q = (size_t)(i + p0);
-            const double v[5] = {g.fxi_x[d][q], g.fxixx[d][q], g.fxix2[d][q], h->scal.ih2t[d] * g.fxix2[d][q],
-                                 h->scal.i2ht[d] * g.fxixx[d][q]};
-            for (int qq = 0; qq < 5; qq++) host[(size_t)(off + (int64_t)qq * n[d] + i)] = v[qq];
+            const double v[NT] = {g.fxi_x[d][q],
+                                  g.fxixx[d][q],
+                                  g.fxix2[d][q],
+                                  h->scal.ih2t[d] * g.fxix2[d][q],
+                                  h->scal.i2ht[d] * g.fxixx[d][q],
+                                  g.fx[d][q + 1] - g.fx[d][q]};
+            for (int qq = 0; qq < NT; qq++) host[(size_t)(off + (int64_t)qq * n[d] + i)] = v[qq];
         }
-        off += 5 * (int64_t)n[d];
+        off += NT * (int64_t)n[d];
     }
     SARAS_CUDA(cudaMemcpy(h->tab, host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice));
+    // vfield::vfield / sfield::sfield (vfield.cc:107-130): first-order
+    // upwinding for dScheme 1, omega = "Central Bias"
+    const double omega = p->up_param;
+    if (h->ds == 1) {
+        h->scal.ua = 2.0 - omega;
+        h->scal.ub = 2.0 * (1.0 - omega);
+        h->scal.uc = -omega;
+    } else {
+        h->scal.ua = 1.0 - omega;
+        h->scal.ub = 4.0 - 3.0 * omega;
+        h->scal.uc = 3.0 * (1.0 - omega);
+        h->scal.ud = -omega;
+    }
+    h->scal.pe_limit = p->pe_limit;
+    h->scal.dc_v = p->nu;
+    h->scal.dc_t = p->kappa;
     h->bc[0] = make_fbc(h, p->bc_vx);
     h->bc[1] = make_fbc(h, p->bc_vy);
     h->bc[2] = make_fbc(h, p->bc_vz);
@@ -597,11 +817,12 @@ saras_status rk3_create(const saras_grid_desc *gd, const saras_rk3_params *p, vo
     // timestep::timestep (timestep.cc:115): int(pow(log(Nx*Ny*Nz), 3))
     h->max_iterations = p->max_iterations > 0 ? p->max_iterations
                                               : int(std::pow(std::log(g.N[0] * g.N[1] * g.N[2]), 3));
-    const int py = h->d3 ? 1 : 1;
+    // dense host box of a field: core plus pad (1 on y for the planar case)
+    const int px = h->L.p, py = h->L.py;
     h->bst[2] = 1;
-    h->bst[1] = n[2] + 2;
+    h->bst[1] = n[2] + 2 * px;
     h->bst[0] = h->bst[1] * (n[1] + 2 * py);
-    h->box_elems = h->bst[0] * (n[0] + 2);
+    h->box_elems = h->bst[0] * (n[0] + 2 * px);
     SARAS_TRY(rk_alloc(h, &h->stage, h->box_elems));
     SARAS_CUDA(cudaDeviceSynchronize());
     return SARAS_OK;
@@ -613,24 +834,40 @@ void rk3_free(saras_rk3 *h) {
     if (h->mg) saras_mg_destroy(h->mg);
 }
 
-saras_status box_transfer(saras_rk3 *h, double *field, const double *src_host, double *dst_host,
-                          const int64_t st[3]) {
+// Host box <-> device field.  Fields in the time-step layout move over their
+// whole padded box; the pressure correction lives in the multigrid level
+// layout (one ghost layer), so only its core and first ghost layer move and
+// the host's outer layer is left as it was.
+saras_status box_transfer(saras_rk3 *h, double *field, bool level_layout, const double *src_host,
+                          double *dst_host, const int64_t st[3]) {
     for (int d = 0; d < 3; d++)
         if (st[d] != h->bst[d]) {
-            set_error("RK3 fields must be C-contiguous padded arrays");
+            set_error("time-step fields must be C-contiguous padded arrays");
             return SARAS_BAD_ARG;
         }
     cudaStream_t s = h->stream;
-    const Lay &L = h->L;
-    const int64_t origin = h->bst[0] + h->bst[1] + 1;
+    const FLay &L = h->L;
+    const int64_t origin = L.p * h->bst[0] + L.py * h->bst[1] + L.p;
     const size_t bytes = (size_t)h->box_elems * sizeof(double);
-    const int bx = bxfor(L.n2 + 2);
-    const dim3 g(cdiv(L.n2 + 2, bx), (unsigned)L.n1 + 2, (unsigned)L.n0 + 2);
+    const int qx = level_layout ? 1 : L.p, qy = level_layout ? 1 : L.py;
+    const int bx = bxfor(L.n2 + 2 * qx);
+    const dim3 g(cdiv(L.n2 + 2 * qx, bx), (unsigned)(L.n1 + 2 * qy), (unsigned)(L.n0 + 2 * qx));
+    const Lay &LM = h->mg->lv[0].lay;
     if (src_host) {
         SARAS_CUDA(cudaMemcpyAsync(h->stage, src_host - origin, bytes, cudaMemcpyHostToDevice, s));
-        k_box_in<<<g, bx, 0, s>>>(h->stage + origin, h->bst[0], h->bst[1], field, L, -1, L.n1);
+        if (level_layout)
+            k_box_in<<<g, bx, 0, s>>>(h->stage + origin, h->bst[0], h->bst[1], field, LM, qx, qy);
+        else
+            k_box_in<<<g, bx, 0, s>>>(h->stage + origin, h->bst[0], h->bst[1], field, L, qx, qy);
     } else {
-        k_box_out<<<g, bx, 0, s>>>(field, L, h->stage + origin, h->bst[0], h->bst[1], -1, L.n1);
+        if (level_layout && L.p > 1) {
+            // keep the host's second ghost layer: stage the host box first
+            SARAS_CUDA(cudaMemcpyAsync(h->stage, dst_host - origin, bytes, cudaMemcpyHostToDevice, s));
+        }
+        if (level_layout)
+            k_box_out<<<g, bx, 0, s>>>(field, LM, h->stage + origin, h->bst[0], h->bst[1], qx, qy);
+        else
+            k_box_out<<<g, bx, 0, s>>>(field, L, h->stage + origin, h->bst[0], h->bst[1], qx, qy);
         SARAS_CUDA(cudaMemcpyAsync(dst_host - origin, h->stage, bytes, cudaMemcpyDeviceToHost, s));
     }
     SARAS_CUDA(cudaStreamSynchronize(s));
@@ -666,7 +903,7 @@ saras_status saras_rk3_upload(saras_rk3 *h, const double *vx, const double *vy, 
     double *dst[6] = {h->V[0], h->V[1], h->V[2], h->P, h->T, h->mg->lv[0].lhs};
     for (int q = 0; q < 6; q++) {
         if (!src[q] || (q == 1 && !h->d3) || (q == 4 && !h->sc)) continue;
-        SARAS_TRY(box_transfer(h, dst[q], src[q], nullptr, strides));
+        SARAS_TRY(box_transfer(h, dst[q], q == 5, src[q], nullptr, strides));
     }
     return SARAS_OK;
 }
@@ -678,7 +915,7 @@ saras_status saras_rk3_download(saras_rk3 *h, double *vx, double *vy, double *vz
     double *src[6] = {h->V[0], h->V[1], h->V[2], h->P, h->T, h->mg->lv[0].lhs};
     for (int q = 0; q < 6; q++) {
         if (!dst[q] || (q == 1 && !h->d3) || (q == 4 && !h->sc)) continue;
-        SARAS_TRY(box_transfer(h, src[q], nullptr, dst[q], strides));
+        SARAS_TRY(box_transfer(h, src[q], q == 5, nullptr, dst[q], strides));
     }
     return SARAS_OK;
 }
@@ -688,7 +925,8 @@ saras_status saras_rk3_step(saras_rk3 *h, int32_t nsteps, int32_t *mg_cycles, in
     int mgc = 0, cni = 0;
     h->launches = 0;
     saras_status st = SARAS_OK;
-    for (int n = 0; n < nsteps && st == SARAS_OK; n++) st = time_advance(h, &mgc, &cni);
+    for (int n = 0; n < nsteps && st == SARAS_OK; n++)
+        st = h->prm.integration == 1 ? time_advance_euler(h, &mgc, &cni) : time_advance_rk3(h, &mgc, &cni);
     if (mg_cycles) *mg_cycles = mgc;
     if (cn_iters) *cn_iters = cni;
     return st;

@@ -60,7 +60,8 @@ class Rk3Params(C.Structure):
                 ("cn_tolerance", C.c_double), ("max_iterations", C.c_int32),
                 ("g_terms", C.c_double * 3), ("with_scalar", C.c_int32), ("nl_scheme", C.c_int32),
                 ("bc_vx", FieldBC), ("bc_vy", FieldBC), ("bc_vz", FieldBC), ("bc_t", FieldBC),
-                ("bc_p", FieldBC), ("mg", MgParams)]
+                ("bc_p", FieldBC), ("mg", MgParams), ("pe_limit", C.c_double), ("up_param", C.c_double),
+                ("integration", C.c_int32), ("pad_", C.c_int32)]
 
 
 def grid_desc(n=(16, 16, 16), length=(1.0, 1.0, 1.0), mesh="UUU", beta=(1.0, 1.0, 1.0),
