@@ -1,4 +1,4 @@
-// saras_shim.h -- C++ drop-in for SARAS-CC's multigrid and RK3 classes over
+// saras_shim.h -- C++ drop-in for SARAS-CC's multigrid and time-step classes over
 // the GB300 C ABI (include/saras_gb300.h).
 //
 // A caller of the reference keeps its code: it builds a `parser` from
@@ -9,7 +9,7 @@
 //   grid            lib/grid/grid.h (sizes, pads, periodicity)
 //   plainsf         lib/field/plainsf.h (F(i,j,k) from -pad, row-major, k fastest)
 //   multigrid_d3/_d2 lib/poisson/poisson.h:148-205
-//   lsRK3_d3/_d2    lib/timestep/timestep.h (timeAdvance)
+//   lsRK3_d3/_d2, eulerCN_d3/_d2  lib/timestep/timestep.h (timeAdvance)
 // Blitz++, MPI, yaml-cpp and HDF5 are not needed: fields are std::vector
 // storage with the Blitz layout, and the YAML reader handles the flat
 // "key": value form of the reference's parameters files.
@@ -44,6 +44,7 @@ class parser {
     // Solver
     int dScheme = 1, nlScheme = 1, iScheme = 2;
     double cnTolerance = 1e-6, tStp = 1e-3;
+    double peLimit = 2.0, upParam = 0.8;
     // Multigrid
     int vcCount = 20, preSmooth = 3, postSmooth = 6, resType = 0;
     bool solveFlag = true, printResidual = false;
@@ -120,6 +121,8 @@ class parser {
         dScheme = (int)num("Solver/Differentiation Scheme", dScheme);
         nlScheme = (int)num("Solver/Non-Linear Term", nlScheme);
         iScheme = (int)num("Solver/Integration Scheme", iScheme);
+        peLimit = num("Solver/Peclet Limit", peLimit);
+        upParam = num("Solver/Central Bias", upParam);
         cnTolerance = num("Solver/Solve Tolerance", cnTolerance);
         tStp = num("Solver/Time-Step", tStp);
         vcCount = (int)num("Multigrid/V-Cycle Count", vcCount);
@@ -266,11 +269,14 @@ class multigrid_d2 : public poisson {
 };
 
 // ------------------------------------------------------------------- RK3
-// lsRK3_d3 with the RBC boundary conditions of scalar::initTBCs /
+// The time integrator with the RBC boundary conditions of scalar::initTBCs /
 // hydro::initVBCs / initPBCs for probType 5 (no-slip, hot bottom, cold top).
-class lsRK3_d3 {
+// lsRK3_d3 runs the low-storage RK3 (lsRK3_d3.cc:190-305), eulerCN_d3 the
+// Euler/Crank-Nicolson step (eulerCN_d3.cc:178-268); the differentiation and
+// non-linear schemes, "Peclet Limit" and "Central Bias" come from the parser.
+class timeIntegrator {
   public:
-    lsRK3_d3(const grid &mesh, const double &dt, int mg_precision = SARAS_PREC_FP64_EXACT) : mesh(mesh) {
+    timeIntegrator(const grid &mesh, const double &dt, int integration, int mg_precision) : mesh(mesh) {
         const parser &p = mesh.inputParams;
         saras_rk3_params r{};
         double fb = 1.0;
@@ -281,6 +287,9 @@ class lsRK3_d3 {
         r.cn_tolerance = p.cnTolerance;
         r.with_scalar = 1;
         r.nl_scheme = p.nlScheme;
+        r.pe_limit = p.peLimit;
+        r.up_param = p.upParam;
+        r.integration = integration;
         for (int f = 0; f < 6; f++) {
             r.bc_vx.type[f] = r.bc_vy.type[f] = r.bc_vz.type[f] = SARAS_FBC_DIRICHLET;
             r.bc_p.type[f] = SARAS_FBC_NEUMANN;
@@ -291,12 +300,12 @@ class lsRK3_d3 {
         r.mg.precision = mg_precision;
         check(saras_rk3_create(&mesh.desc, &r, nullptr, &h), "saras_rk3_create");
     }
-    ~lsRK3_d3() { saras_rk3_destroy(h); }
-    lsRK3_d3(const lsRK3_d3 &) = delete;
-    lsRK3_d3 &operator=(const lsRK3_d3 &) = delete;
+    virtual ~timeIntegrator() { saras_rk3_destroy(h); }
+    timeIntegrator(const timeIntegrator &) = delete;
+    timeIntegrator &operator=(const timeIntegrator &) = delete;
 
-    // lsRK3_d3::timeAdvance(V, P, T) (lib/timestep/lsRK3_d3.cc:190-305); the
-    // fields are copied to the device and back around each call.
+    // timeAdvance(V, P, T); the fields are copied to the device and back
+    // around each call.
     void timeAdvance(vfield &V, sfield &P, sfield &T) {
         int64_t st[3];
         P.strides(st);
@@ -316,5 +325,21 @@ class lsRK3_d3 {
     plainsf Pp{mesh};
     bool primed = false;
 };
+
+class lsRK3_d3 : public timeIntegrator {
+  public:
+    lsRK3_d3(const grid &mesh, const double &dt, int mg_precision = SARAS_PREC_FP64_EXACT)
+        : timeIntegrator(mesh, dt, 2, mg_precision) {}
+};
+
+class eulerCN_d3 : public timeIntegrator {
+  public:
+    eulerCN_d3(const grid &mesh, const double &dt, int mg_precision = SARAS_PREC_FP64_EXACT)
+        : timeIntegrator(mesh, dt, 1, mg_precision) {}
+};
+
+// lsRK3_d2 / eulerCN_d2: the same classes over a planar grid
+using lsRK3_d2 = lsRK3_d3;
+using eulerCN_d2 = eulerCN_d3;
 
 }  // namespace saras_shim
