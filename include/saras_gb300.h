@@ -46,7 +46,8 @@ typedef enum saras_status {
     SARAS_TIMEOUT = 5,       /* a bounded device wait gave up */
     SARAS_CUDA_ERR = 6,
     SARAS_NO_DEVICE = 7,
-    SARAS_DIVERGED = 8,      /* CN Jacobi hit maxIterations (reference aborts here) */
+    SARAS_DIVERGED = 8,      /* CN Jacobi hit maxIterations, or the time-series divergence abort
+                              * (the reference exits in both) */
     SARAS_NAN = 9            /* non-finite value met in an input or a residual */
 } saras_status;
 
@@ -209,6 +210,49 @@ saras_status saras_rk3_download(saras_rk3 *h, double *vx, double *vy, double *vz
 saras_status saras_rk3_step(saras_rk3 *h, int32_t nsteps, int32_t *mg_cycles, int32_t *cn_iters);
 saras_status saras_rk3_destroy(saras_rk3 *h);
 int64_t saras_rk3_last_launches(const saras_rk3 *h);
+
+/* ---------------------------------------------------- time loop ---- */
+/* The time loop of scalar_d3/hydro_d3::solvePDE (src/solvers/scalar/
+ * scalar_d3.cc:221-290) on the device-resident fields: timeAdvance, the CFL
+ * time step (vfield::computeTStp, vfield.cc:691-719; capped at the
+ * "Time-Step" the handle was created with), time += dt, a time-series row
+ * every io_count steps (tseries::writeTSData, tseries.cc:200-492), until
+ * |t_max - time| < dt/2.  Probes, solution and restart files are the
+ * caller's.  The next step uses the CFL time step, as the reference's
+ * integrator holds dt by reference. */
+typedef struct saras_run_params {
+    double  t_max;        /* "Final Time" */
+    double  courant;      /* "Courant Number" */
+    int32_t use_cfl;      /* "Use CFL Condition" */
+    int32_t io_count;     /* "I/O Count" */
+    int32_t prob_type;    /* "Problem Type": 9 (open top) counts one wall in Nu */
+    int32_t max_steps;    /* stop after this many steps; 0 = no limit */
+    double  g_axis[3];    /* "Gravity Direction": Nusselt along z unless g_axis[2] == 0 */
+} saras_run_params;
+
+/* One time-series row.  With temperature (tseries.cc:277-492): Re, Nu at
+ * the walls, volume Nu, kinetic and thermal energy per volume; without it
+ * (tseries.cc:200-275): kinetic energy and U_rms.  divergence is the
+ * maximum |div V| over the core.  The sums run over the core in a
+ * different order than the reference's sequential loops, so they agree
+ * with it to rounding (the maxima are exact). */
+typedef struct saras_tseries_row {
+    double time, dt;
+    double re, nu_wall, nu_vol;
+    double ke, te, urms, divergence;
+} saras_tseries_row;
+
+/* The row of the current fields at `time` (no time step). */
+saras_status saras_rk3_tseries(saras_rk3 *h, const saras_run_params *rp, double time, saras_tseries_row *row);
+/* vfield::computeTStp on the current velocity: courant / max(|u|/dx + |v|/dy
+ * + |w|/dz) with the average spacings L/N (exact; not capped). */
+saras_status saras_rk3_cfl_dt(saras_rk3 *h, double courant, double *dt);
+/* Runs the loop from *time (updated).  Row 0 is the state at the start
+ * time.  At most row_cap rows are stored; *n_rows counts the rows produced.
+ * SARAS_DIVERGED when the divergence exceeds 1e3 and grows (tseries.cc:
+ * 208-214), with the rows and steps up to there. */
+saras_status saras_rk3_run(saras_rk3 *h, const saras_run_params *rp, double *time, saras_tseries_row *rows,
+                           int32_t row_cap, int32_t *n_rows, int32_t *n_steps);
 
 /* ------------------------------------------------------------ serving ---- */
 /*

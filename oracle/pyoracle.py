@@ -48,6 +48,11 @@ def load():
                                    vp, vp, C.POINTER(i64), i32, C.POINTER(i32), C.POINTER(i32), dp]
     lib.oracle_field_op.argtypes = [C.POINTER(abi.GridDesc), C.POINTER(abi.Rk3Params), i32, i32, C.c_double,
                                     vp, vp, vp, vp, vp, C.POINTER(i64)]
+    lib.oracle_rk3_loop.argtypes = [C.POINTER(abi.GridDesc), C.POINTER(abi.Rk3Params), C.POINTER(abi.RunParams),
+                                    vp, vp, vp, vp, vp, vp, C.POINTER(i64), dp, C.POINTER(abi.TseriesRow), i32,
+                                    C.POINTER(i32), C.POINTER(i32), dp]
+    lib.oracle_tseries.argtypes = [C.POINTER(abi.GridDesc), C.POINTER(abi.Rk3Params), C.POINTER(abi.RunParams),
+                                   vp, vp, vp, vp, C.POINTER(i64), C.c_double, C.POINTER(abi.TseriesRow), dp]
     _lib = lib
     return lib
 
@@ -140,3 +145,43 @@ def field_op(grid, params, op, f, axis=0, v=(None, None, None), dcoef=1.0):
     if s:
         raise RuntimeError(f"oracle_field_op status {s}")
     return out
+
+
+def rk3_loop(grid, params, run, vx, vy, vz, p, t, pp, time=0.0, cap=4096):
+    """The solvePDE time loop on numpy padded fields (updated in place)."""
+    lib = load()
+    ptrs = []
+    st = None
+    for f in (vx, vy, vz, p, t, pp):
+        if f is None:
+            ptrs.append(C.c_void_p(0))
+            continue
+        ptr, st = abi.field_origin(f, grid)
+        ptrs.append(ptr)
+    rows = (abi.TseriesRow * cap)()
+    tm, nr, ns, dt = C.c_double(time), C.c_int(), C.c_int(), C.c_double()
+    s = lib.oracle_rk3_loop(C.byref(grid), C.byref(params), C.byref(run), *ptrs, st, C.byref(tm), rows, cap,
+                            C.byref(nr), C.byref(ns), C.byref(dt))
+    r = Result()
+    r.status, r.time, r.n_steps, r.dt = s, tm.value, ns.value, dt.value
+    r.rows = [rows[q].as_dict() for q in range(min(nr.value, cap))]
+    return r
+
+
+def tseries(grid, params, run, vx, vy, vz, t, time=0.0):
+    """(time-series row, CFL maximum) of the given fields."""
+    lib = load()
+    ptrs = []
+    st = None
+    for f in (vx, vy, vz, t):
+        if f is None:
+            ptrs.append(C.c_void_p(0))
+            continue
+        ptr, st = abi.field_origin(f, grid)
+        ptrs.append(ptr)
+    row, cm = abi.TseriesRow(), C.c_double()
+    s = lib.oracle_tseries(C.byref(grid), C.byref(params), C.byref(run), *ptrs, st, time, C.byref(row),
+                           C.byref(cm))
+    if s not in (0, 8):  # 8: the divergence abort
+        raise RuntimeError(f"oracle_tseries status {s}")
+    return row.as_dict(), cm.value

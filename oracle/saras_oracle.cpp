@@ -1282,6 +1282,171 @@ struct Rk3 {
         return SARAS_OK;
     }
 
+    /* vfield::computeTStp (vfield.cc:691-719): the maximum over the core of
+     * |u|/avgDx + |v|/avgDy + |w|/avgDz, avgD = L/N; the caller divides the
+     * Courant number by it. */
+    double cfl_max() const {
+        const double ax = g.L[0] / g.N[0], ay = g.L[1] / g.N[1], az = g.L[2] / g.N[2];
+        double m = 0.0;
+        for (int i = 0; i < g.N[0]; i++)
+            for (int j = 0; j < g.N[1]; j++)
+                for (int k = 0; k < g.N[2]; k++) {
+                    double v = std::fabs(Vx(i, j, k)) / ax;
+                    if (d3) v = v + std::fabs(Vy(i, j, k)) / ay;
+                    v = v + std::fabs(Vz(i, j, k)) / az;
+                    if (v > m) m = v;
+                }
+        return m;
+    }
+
+    /* tseries::writeTSData(T) (tseries.cc:277-492) and writeTSData()
+     * (tseries.cc:200-275) on one rank: the sums run sequentially in the
+     * reference's loop order.  Returns SARAS_DIVERGED on the divergence
+     * abort (tseries.cc:208-214). */
+    int tseries(const saras_run_params &rp, double time, double dt, saras_tseries_row &row, double &oldDiv) {
+        const int n0 = g.N[0], n1 = g.N[1], n2 = g.N[2];
+        const bool sc = prm.with_scalar != 0;
+        double divVal = 0.0;
+        for (int i = 0; i < n0; i++)
+            for (int j = 0; j < n1; j++)
+                for (int k = 0; k < n2; k++) {
+                    double dv = 0.0;
+                    dv += d1(Vx, 0, i, j, k);
+                    if (d3) dv += d1(Vy, 1, i, j, k);
+                    dv += d1(Vz, 2, i, j, k);
+                    if (std::fabs(dv) > divVal) divVal = std::fabs(dv);
+                }
+        const double divSlope = divVal - oldDiv;
+        const bool abort = divVal > 1e3 && divSlope > 0;
+        oldDiv = divVal;
+        const double totalVol = d3 ? g.L[0] * g.L[1] * g.L[2] : g.L[0] * g.L[2];
+        auto dvx = [&](int i) { return g.dxi[0] / g.xi_x[0][i]; };
+        auto dvy = [&](int j) { return g.dxi[1] / g.xi_x[1][j]; };
+        auto dvz = [&](int k) { return g.dxi[2] / g.xi_x[2][k]; };
+        row = saras_tseries_row{};
+        row.time = time;
+        row.dt = dt;
+        row.divergence = divVal;
+        if (!sc) {
+            double ke = 0.0;
+            for (int i = 0; i < n0; i++)
+                for (int j = 0; j < n1; j++)
+                    for (int k = 0; k < n2; k++) {
+                        if (d3)
+                            ke += (std::pow(Vx(i, j, k), 2.0) + std::pow(Vy(i, j, k), 2.0) +
+                                   std::pow(Vz(i, j, k), 2.0)) * 0.5 * dvx(i) * dvy(j) * dvz(k);
+                        else
+                            ke += (std::pow(Vx(i, j, k), 2.0) + std::pow(Vz(i, j, k), 2.0)) * 0.5 * dvx(i) * dvz(k);
+                    }
+            ke /= totalVol;
+            row.ke = ke;
+            row.urms = std::sqrt(2.0 * ke);
+            return abort ? SARAS_DIVERGED : SARAS_OK;
+        }
+        /* tseries::tseries (tseries.cc:95-135): on one rank both walls are
+         * ours; wallDn is set by the bottom wall, then by the top wall */
+        const bool zG = !(rp.g_axis[2] == 0);
+        double csArea, wallDn;
+        bool tWall;
+        if (zG) {
+            csArea = d3 ? g.L[0] * g.L[1] : g.L[0];
+            csArea *= rp.prob_type == 9 ? 1 : 2;
+            tWall = rp.prob_type < 9;
+            wallDn = g.xG[2][0];
+            if (tWall) wallDn = g.L[2] - g.xG[2][n2 - 1];
+        } else {
+            csArea = d3 ? g.L[1] * g.L[2] : g.L[2];
+            tWall = true;
+            wallDn = g.xG[0][0];
+            wallDn = g.L[0] - g.xG[0][n0 - 1];
+        }
+        double localDt = 0.0;
+        if (zG) {
+            for (int i = 0; i < n0; i++)
+                for (int j = 0; j < n1; j++) {
+                    const double dArea = d3 ? dvx(i) * dvy(j) : dvx(i);
+                    localDt += (1.0 - std::fabs(T(i, j, 0))) / wallDn * dArea;
+                }
+            if (tWall)
+                for (int i = 0; i < n0; i++)
+                    for (int j = 0; j < n1; j++) {
+                        const double dArea = d3 ? dvx(i) * dvy(j) : dvx(i);
+                        localDt += std::fabs(T(i, j, n2 - 1)) / wallDn * dArea;
+                    }
+        } else {
+            for (int j = 0; j < n1; j++)
+                for (int k = 0; k < n2; k++) {
+                    const double dArea = d3 ? dvy(j) * dvz(k) : dvz(k);
+                    localDt += (1.0 - std::fabs(T(0, j, k))) / wallDn * dArea;
+                }
+            for (int j = 0; j < n1; j++)
+                for (int k = 0; k < n2; k++) {
+                    const double dArea = d3 ? dvy(j) * dvz(k) : dvz(k);
+                    localDt += std::fabs(T(n0 - 1, j, k)) / wallDn * dArea;
+                }
+        }
+        double ke = 0.0, te = 0.0, uzt = 0.0;
+        for (int i = 0; i < n0; i++)
+            for (int j = 0; j < n1; j++)
+                for (int k = 0; k < n2; k++) {
+                    const double dVol = d3 ? dvx(i) * dvy(j) * dvz(k) : dvx(i) * dvz(k);
+                    const double t = T(i, j, k);
+                    const double theta = zG ? t + g.xG[2][k] - 1.0 : t + g.xG[0][i] - 1.0;
+                    if (d3)
+                        ke += (std::pow(Vx(i, j, k), 2.0) + std::pow(Vy(i, j, k), 2.0) +
+                               std::pow(Vz(i, j, k), 2.0)) * 0.5 * dVol;
+                    else
+                        ke += (std::pow(Vx(i, j, k), 2.0) + std::pow(Vz(i, j, k), 2.0)) * 0.5 * dVol;
+                    te += std::pow(theta, 2.0) * 0.5 * dVol;
+                    uzt += (zG ? Vz(i, j, k) : Vx(i, j, k)) * t * dVol;
+                }
+        ke /= totalVol;
+        te /= totalVol;
+        row.nu_vol = 1.0 + (uzt / totalVol) / prm.kappa;
+        row.nu_wall = localDt / csArea;
+        row.re = std::sqrt(2.0 * ke) / prm.nu;
+        row.ke = ke;
+        row.te = te;
+        row.urms = std::sqrt(2.0 * ke);
+        return abort ? SARAS_DIVERGED : SARAS_OK;
+    }
+
+    /* scalar_d3::solvePDE / hydro_d3::solvePDE time loop (scalar_d3.cc:
+     * 221-290) without probes and file output. */
+    int run(const saras_run_params &rp, double &time, saras_tseries_row *rows, int cap, int *nrows, int *nsteps,
+            int *mgc, int *cni) {
+        const double tStp = prm.dt;
+        double dt = prm.dt;
+        double oldDiv = 1.0e10;
+        int nr = 0, steps = 0, s = 0;
+        saras_tseries_row row;
+        s = tseries(rp, time, dt, row, oldDiv);
+        if (nr < cap) rows[nr] = row;
+        nr++;
+        while (!s) {
+            s = prm.integration == 1 ? euler_advance(mgc, cni) : time_advance(mgc, cni);
+            if (s) break;
+            if (rp.use_cfl) {
+                dt = rp.courant / cfl_max();
+                if (dt > tStp) dt = tStp;
+                prm.dt = dt;
+            }
+            steps += 1;
+            time += dt;
+            if (steps % rp.io_count == 0) {
+                s = tseries(rp, time, dt, row, oldDiv);
+                if (nr < cap) rows[nr] = row;
+                nr++;
+                if (s) break;
+            }
+            if (std::fabs(rp.t_max - time) < 0.5 * dt) break;
+            if (rp.max_steps > 0 && steps >= rp.max_steps) break;
+        }
+        if (nrows) *nrows = nr;
+        if (nsteps) *nsteps = steps;
+        return s;
+    }
+
     /* lsRK3_d3::timeAdvance(V, P[, T]) (lib/timestep/lsRK3_d3.cc:94-177,
      * 190-305); lsRK3_d2 skips Vy. */
     int time_advance(int *mgc, int *cni) {
@@ -1508,6 +1673,48 @@ int oracle_field_op(const saras_grid_desc *gd, const saras_rk3_params *prm, int 
         for (int j = 0; j < r.g.N[1]; j++)
             for (int k = 0; k < r.g.N[2]; k++) out[i * strides[0] + j * strides[1] + k * strides[2]] = r.tSF(i, j, k);
     return SARAS_OK;
+}
+
+/* The time loop (Rk3::run) on caller fields, which are updated. */
+int oracle_rk3_loop(const saras_grid_desc *gd, const saras_rk3_params *prm, const saras_run_params *rp, double *vx,
+                    double *vy, double *vz, double *p, double *t, double *pp, const int64_t *strides, double *time,
+                    saras_tseries_row *rows, int cap, int *n_rows, int *n_steps, double *dt_out) {
+    Rk3 r;
+    int s = r.setup(*gd, *prm);
+    if (s) return s;
+    if (rp->io_count < 1) return SARAS_BAD_ARG;
+    copy_in(r.Vx, vx, strides);
+    if (gd->dims == 3) copy_in(r.Vy, vy, strides);
+    copy_in(r.Vz, vz, strides);
+    copy_in(r.P, p, strides);
+    if (prm->with_scalar) copy_in(r.T, t, strides);
+    copy_in(r.Pp, pp, strides);
+    s = r.run(*rp, *time, rows, cap, n_rows, n_steps, nullptr, nullptr);
+    if (dt_out) *dt_out = r.prm.dt;
+    copy_out(r.Vx, vx, strides);
+    if (gd->dims == 3) copy_out(r.Vy, vy, strides);
+    copy_out(r.Vz, vz, strides);
+    copy_out(r.P, p, strides);
+    if (prm->with_scalar) copy_out(r.T, t, strides);
+    copy_out(r.Pp, pp, strides);
+    return s;
+}
+
+/* One time-series row and the CFL maximum of caller fields. */
+int oracle_tseries(const saras_grid_desc *gd, const saras_rk3_params *prm, const saras_run_params *rp,
+                   const double *vx, const double *vy, const double *vz, const double *t, const int64_t *strides,
+                   double time, saras_tseries_row *row, double *cfl_max) {
+    Rk3 r;
+    int s = r.setup(*gd, *prm);
+    if (s) return s;
+    copy_in(r.Vx, vx, strides);
+    if (gd->dims == 3) copy_in(r.Vy, vy, strides);
+    copy_in(r.Vz, vz, strides);
+    if (prm->with_scalar) copy_in(r.T, t, strides);
+    double oldDiv = 1.0e10;
+    s = r.tseries(*rp, time, prm->dt, *row, oldDiv);
+    if (cfl_max) *cfl_max = r.cfl_max();
+    return s;
 }
 
 /* `nsteps` calls of lsRK3 (integration 0 or 2) or eulerCN (integration 1)

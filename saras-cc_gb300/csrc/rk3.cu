@@ -75,6 +75,8 @@ struct RkTab {
     const double *xi_x[3], *xixx[3], *xix2[3];
     const double *a2[3], *a1[3];  // ihx2*xix2, i2hx*xixx (timestep coefficients)
     const double *dh[3];          // x(i+1) - x(i): the upwind Peclet length
+    const double *dv[3];          // dXi / xi_x: cell extent (tseries volumes and areas)
+    const double *xc[3];          // cell-centre coordinate x(i)
 };
 struct RkScal {
     double ih[3], ih2d[3];  // derivative: 1/dXi, pow(1/dXi, 2)
@@ -375,6 +377,102 @@ __global__ void k_max_final(const double *__restrict__ part, int nb, double *__r
     }
     m = warp_max(m);
     if (threadIdx.x == 0) out[0] = m;
+}
+
+// Time-series and CFL reductions of the current fields (tseries::
+// writeTSData, tseries.cc:200-492; vfield::computeTStp, vfield.cc:691-719).
+// Per cell in the reference's operation order; the sums then run per thread,
+// per warp and per block in a fixed order (partials of NTS values per block).
+struct TsPar {
+    int zg;             // gravity along z: Nusselt through the z walls
+    int twall;          // the top (far) wall counts
+    double wall_dn;     // wallDn
+    double avg[3];      // L/N, the CFL spacings
+};
+enum { TS_KE = 0, TS_TE, TS_UZT, TS_DTW, TS_DIV, TS_CFL, NTS };
+
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x < 32) {
+        r = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+    }
+    return r;
+}
+__device__ __forceinline__ double block_max(double v, double *sh) {
+    v = warp_max(v);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x < 32) {
+        r = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+        r = warp_max(r);
+    }
+    return r;
+}
+
+template <bool D3, bool SC, int DS>
+__global__ void k_tseries(const double *__restrict__ vx, const double *__restrict__ vy,
+                          const double *__restrict__ vz, const double *__restrict__ tf, FLay L, RkTab T, RkScal S,
+                          TsPar tp, double *__restrict__ part) {
+    double acc[NTS] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for_core_rows(L, [&](int i, int j, int k) {
+        const int64_t c = L.at(i, j, k);
+        const double u = vx[c], w = vz[c], v = D3 ? vy[c] : 0.0;
+        const double dvx = T.dv[0][i], dvz = T.dv[2][k], dvy = D3 ? T.dv[1][j] : 1.0;
+        const double s2 = D3 ? radd(radd(rmul(u, u), rmul(v, v)), rmul(w, w)) : radd(rmul(u, u), rmul(w, w));
+        if (SC) {
+            const double dvol = D3 ? rmul(rmul(dvx, dvy), dvz) : rmul(dvx, dvz);
+            const double t = tf[c];
+            const double theta = rsub(radd(t, tp.zg ? T.xc[2][k] : T.xc[0][i]), 1.0);
+            acc[TS_KE] += rmul(rmul(s2, 0.5), dvol);
+            acc[TS_TE] += rmul(rmul(rmul(theta, theta), 0.5), dvol);
+            acc[TS_UZT] += rmul(rmul(tp.zg ? w : u, t), dvol);
+            if (tp.zg) {
+                const double da = D3 ? rmul(dvx, dvy) : dvx;
+                if (k == 0) acc[TS_DTW] += rmul(rdiv(rsub(1.0, fabs(t)), tp.wall_dn), da);
+                if (tp.twall && k == L.n2 - 1) acc[TS_DTW] += rmul(rdiv(fabs(t), tp.wall_dn), da);
+            } else {
+                const double da = D3 ? rmul(dvy, dvz) : dvz;
+                if (i == 0) acc[TS_DTW] += rmul(rdiv(rsub(1.0, fabs(t)), tp.wall_dn), da);
+                if (tp.twall && i == L.n0 - 1) acc[TS_DTW] += rmul(rdiv(fabs(t), tp.wall_dn), da);
+            }
+        } else {
+            acc[TS_KE] += D3 ? rmul(rmul(rmul(rmul(s2, 0.5), dvx), dvy), dvz) : rmul(rmul(rmul(s2, 0.5), dvx), dvz);
+        }
+        double d = radd(0.0, d1<DS>(vx, L, T, S, 0, i, c));
+        if (D3) d = radd(d, d1<DS>(vy, L, T, S, 1, j, c));
+        d = radd(d, d1<DS>(vz, L, T, S, 2, k, c));
+        acc[TS_DIV] = fmax(acc[TS_DIV], fabs(d));
+        double cf = rdiv(fabs(u), tp.avg[0]);
+        if (D3) cf = radd(cf, rdiv(fabs(v), tp.avg[1]));
+        cf = radd(cf, rdiv(fabs(w), tp.avg[2]));
+        acc[TS_CFL] = fmax(acc[TS_CFL], cf);
+    });
+    __shared__ double sh[32];
+    for (int q = 0; q < NTS; q++) {
+        const double r = q >= TS_DIV ? block_max(acc[q], sh) : block_sum(acc[q], sh);
+        if (threadIdx.x == 0) part[(int64_t)blockIdx.x * NTS + q] = r;
+    }
+}
+
+// Sums (maxima) of the per-block partials, one block, fixed order.
+__global__ void k_tseries_final(const double *__restrict__ part, int nb, double *__restrict__ out) {
+    __shared__ double sh[32];
+    for (int q = 0; q < NTS; q++) {
+        double a = 0.0;
+        for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+            const double v = part[(int64_t)b * NTS + q];
+            a = q >= TS_DIV ? fmax(a, v) : a + v;
+        }
+        const double r = q >= TS_DIV ? block_max(a, sh) : block_sum(a, sh);
+        if (threadIdx.x == 0) out[q] = r;
+    }
 }
 
 enum { FBC_PERIODIC = 0, FBC_WALL = 1, FBC_ZERO_OUTER = 2 };
@@ -719,6 +817,121 @@ saras_status time_advance_euler(saras_rk3 *h, int *mgc, int *cni) {
     return SARAS_OK;
 }
 
+// The NTS reductions of the current fields into h->red_host.
+saras_status ts_reduce(saras_rk3 *h, const saras_run_params *rp) {
+    const HostGrid &g = h->grid;
+    const FLay &L = h->L;
+    TsPar tp{};
+    tp.zg = !(rp->g_axis[2] == 0);
+    // tseries::tseries (tseries.cc:95-135): on one rank both walls are ours;
+    // wallDn is set by the bottom wall and then by the top wall
+    if (tp.zg) {
+        const int p2 = g.pad;
+        tp.twall = rp->prob_type < 9;
+        tp.wall_dn = g.fx[2][(size_t)p2];
+        if (tp.twall) tp.wall_dn = g.L[2] - g.fx[2][(size_t)(p2 + g.N[2] - 1)];
+    } else {
+        const int p0 = g.pad;
+        tp.twall = 1;
+        tp.wall_dn = g.L[0] - g.fx[0][(size_t)(p0 + g.N[0] - 1)];
+    }
+    for (int d = 0; d < 3; d++) tp.avg[d] = g.L[d] / g.N[d];
+    using TK = void (*)(const double *, const double *, const double *, const double *, FLay, RkTab, RkScal, TsPar,
+                        double *);
+    static const TK ks[2][2][2] = {
+        {{k_tseries<false, false, 1>, k_tseries<false, false, 2>}, {k_tseries<false, true, 1>, k_tseries<false, true, 2>}},
+        {{k_tseries<true, false, 1>, k_tseries<true, false, 2>}, {k_tseries<true, true, 1>, k_tseries<true, true, 2>}}};
+    cudaStream_t s = h->stream;
+    ks[h->d3 ? 1 : 0][h->sc ? 1 : 0][h->ds == 2 ? 1 : 0]<<<h->nblocks, 256, 0, s>>>(
+        h->V[0], h->V[1], h->V[2], h->T, L, h->tabs, h->scal, tp, h->part);
+    k_tseries_final<<<1, 256, 0, s>>>(h->part, h->nblocks, h->red);
+    h->launches += 2;
+    SARAS_CUDA(cudaMemcpyAsync(h->red_host, h->red, NTS * sizeof(double), cudaMemcpyDeviceToHost, s));
+    SARAS_CUDA(cudaStreamSynchronize(s));
+    return SARAS_OK;
+}
+
+// tseries::writeTSData(T) / writeTSData() from the reductions (tseries.cc:
+// 208-214, 245-252, 443-452): the totals per volume, Nusselt numbers,
+// Reynolds number and the divergence abort test.
+saras_status ts_row(saras_rk3 *h, const saras_run_params *rp, double time, double dt, saras_tseries_row *row,
+                    double *old_div) {
+    SARAS_TRY(ts_reduce(h, rp));
+    const HostGrid &g = h->grid;
+    const double *r = h->red_host;
+    const double divVal = r[TS_DIV];
+    const bool abort = divVal > 1e3 && divVal - *old_div > 0;
+    *old_div = divVal;
+    const double totalVol = h->d3 ? g.L[0] * g.L[1] * g.L[2] : g.L[0] * g.L[2];
+    *row = saras_tseries_row{};
+    row->time = time;
+    row->dt = dt;
+    row->divergence = divVal;
+    const double ke = r[TS_KE] / totalVol;
+    row->ke = ke;
+    row->urms = std::sqrt(2.0 * ke);
+    if (h->sc) {
+        const bool zg = !(rp->g_axis[2] == 0);
+        double csArea;
+        if (zg) {
+            csArea = h->d3 ? g.L[0] * g.L[1] : g.L[0];
+            csArea *= rp->prob_type == 9 ? 1 : 2;
+        } else {
+            csArea = h->d3 ? g.L[1] * g.L[2] : g.L[2];
+        }
+        row->te = r[TS_TE] / totalVol;
+        row->nu_vol = 1.0 + (r[TS_UZT] / totalVol) / h->prm.kappa;
+        row->nu_wall = r[TS_DTW] / csArea;
+        row->re = std::sqrt(2.0 * ke) / h->prm.nu;
+    }
+    if (abort) {
+        set_error("divergence exceeds permissible limits (%g)", divVal);
+        return SARAS_DIVERGED;
+    }
+    return SARAS_OK;
+}
+
+saras_status step_once(saras_rk3 *h, int *mgc, int *cni) {
+    return h->prm.integration == 1 ? time_advance_euler(h, mgc, cni) : time_advance_rk3(h, mgc, cni);
+}
+
+// scalar_d3::solvePDE / hydro_d3::solvePDE (scalar_d3.cc:221-290)
+saras_status rk3_run(saras_rk3 *h, const saras_run_params *rp, double *time, saras_tseries_row *rows, int cap,
+                     int *n_rows, int *n_steps) {
+    const double tStp = h->prm.dt;
+    double dt = h->prm.dt;
+    double old_div = 1.0e10;
+    int nr = 0, steps = 0;
+    saras_tseries_row row;
+    saras_status st = ts_row(h, rp, *time, dt, &row, &old_div);
+    if (nr < cap && rows) rows[nr] = row;
+    nr++;
+    while (st == SARAS_OK) {
+        st = step_once(h, nullptr, nullptr);
+        if (st != SARAS_OK) break;
+        if (rp->use_cfl) {
+            st = ts_reduce(h, rp);
+            if (st != SARAS_OK) break;
+            dt = rp->courant / h->red_host[TS_CFL];
+            if (dt > tStp) dt = tStp;
+            h->prm.dt = dt;
+        }
+        steps += 1;
+        *time += dt;
+        if (steps % rp->io_count == 0) {
+            st = ts_row(h, rp, *time, dt, &row, &old_div);
+            if (nr < cap && rows) rows[nr] = row;
+            nr++;
+            if (st != SARAS_OK) break;
+        }
+        if (std::fabs(rp->t_max - *time) < 0.5 * dt) break;
+        if (rp->max_steps > 0 && steps >= rp->max_steps) break;
+    }
+    if (n_rows) *n_rows = nr;
+    if (n_steps) *n_steps = steps;
+    return st;
+}
+
 saras_status rk3_create(const saras_grid_desc *gd, const saras_rk3_params *p, void *stream, saras_rk3 *h) {
     if (gd->pad != 1 && gd->pad != 2) {
         set_error("the time step takes Differentiation Scheme 1 (pad 1) or 2 (pad 2)");
@@ -752,7 +965,7 @@ saras_status rk3_create(const saras_grid_desc *gd, const saras_rk3_params *p, vo
     SARAS_TRY(rk_alloc(h, &h->nlT, sz));
     for (double *q : h->allocs) SARAS_CUDA(cudaMemset(q, 0, (size_t)sz * sizeof(double)));
     // metric tables: xi_x, xixx, xix2, a2, a1, dh per axis over the core
-    constexpr int NT = 6;
+    constexpr int NT = 8;
     const int n[3] = {h->L.n0, h->L.n1, h->L.n2};
     const int64_t tot = NT * (int64_t)(n[0] + n[1] + n[2]);
     std::vector<double> host((size_t)tot, 0.0);
@@ -775,6 +988,8 @@ saras_status rk3_create(const saras_grid_desc *gd, const saras_rk3_params *p, vo
         h->tabs.a2[d] = dst[3];
         h->tabs.a1[d] = dst[4];
         h->tabs.dh[d] = dst[5];
+        h->tabs.dv[d] = dst[6];
+        h->tabs.xc[d] = dst[7];
         for (int i = 0; i < n[d]; i++) {
             const size_t q = (size_t)(i + p0);
             const double v[NT] = {g.fxi_x[d][q],
@@ -782,7 +997,9 @@ saras_status rk3_create(const saras_grid_desc *gd, const saras_rk3_params *p, vo
                                   g.fxix2[d][q],
                                   h->scal.ih2t[d] * g.fxix2[d][q],
                                   h->scal.i2ht[d] * g.fxixx[d][q],
-                                  g.fx[d][q + 1] - g.fx[d][q]};
+                                  g.fx[d][q + 1] - g.fx[d][q],
+                                  g.dxi[d] / g.fxi_x[d][q],
+                                  g.fx[d][q]};
             for (int qq = 0; qq < NT; qq++) host[(size_t)(off + (int64_t)qq * n[d] + i)] = v[qq];
         }
         off += NT * (int64_t)n[d];
@@ -811,9 +1028,9 @@ saras_status rk3_create(const saras_grid_desc *gd, const saras_rk3_params *p, vo
     h->bc[4] = make_fbc(h, p->bc_t);
     const int64_t cells = (int64_t)n[0] * n[1] * n[2];
     h->nblocks = (int)std::max<int64_t>(1, std::min<int64_t>(1216, (cells + 255) / 256));
-    SARAS_TRY(rk_alloc(h, &h->part, h->nblocks));
-    SARAS_TRY(rk_alloc(h, &h->red, 4));
-    SARAS_CUDA(cudaMallocHost((void **)&h->red_host, 4 * sizeof(double)));
+    SARAS_TRY(rk_alloc(h, &h->part, (int64_t)h->nblocks * NTS));
+    SARAS_TRY(rk_alloc(h, &h->red, NTS));
+    SARAS_CUDA(cudaMallocHost((void **)&h->red_host, NTS * sizeof(double)));
     // timestep::timestep (timestep.cc:115): int(pow(log(Nx*Ny*Nz), 3))
     h->max_iterations = p->max_iterations > 0 ? p->max_iterations
                                               : int(std::pow(std::log(g.N[0] * g.N[1] * g.N[2]), 3));
@@ -941,5 +1158,36 @@ saras_status saras_rk3_destroy(saras_rk3 *h) {
 }
 
 int64_t saras_rk3_last_launches(const saras_rk3 *h) { return h ? h->launches : -1; }
+
+saras_status saras_rk3_tseries(saras_rk3 *h, const saras_run_params *rp, double time, saras_tseries_row *row) {
+    if (!h || !rp || !row) return SARAS_BAD_ARG;
+    double old_div = 1.0e10;
+    h->launches = 0;
+    return ts_row(h, rp, time, h->prm.dt, row, &old_div);
+}
+
+saras_status saras_rk3_cfl_dt(saras_rk3 *h, double courant, double *dt) {
+    if (!h || !dt) return SARAS_BAD_ARG;
+    saras_run_params rp{};
+    rp.g_axis[2] = -1.0;
+    h->launches = 0;
+    SARAS_TRY(ts_reduce(h, &rp));
+    *dt = courant / h->red_host[TS_CFL];
+    return SARAS_OK;
+}
+
+saras_status saras_rk3_run(saras_rk3 *h, const saras_run_params *rp, double *time, saras_tseries_row *rows,
+                           int32_t row_cap, int32_t *n_rows, int32_t *n_steps) {
+    if (!h || !rp || !time || row_cap < 0 || rp->io_count < 1 || (rp->use_cfl && !(rp->courant > 0.0))) {
+        set_error("invalid time-loop parameters");
+        return SARAS_BAD_ARG;
+    }
+    h->launches = 0;
+    int nr = 0, ns = 0;
+    saras_status st = rk3_run(h, rp, time, rows, row_cap, &nr, &ns);
+    if (n_rows) *n_rows = nr;
+    if (n_steps) *n_steps = ns;
+    return st;
+}
 
 }  // extern "C"

@@ -64,6 +64,31 @@ class Rk3Params(C.Structure):
                 ("integration", C.c_int32), ("pad_", C.c_int32)]
 
 
+class RunParams(C.Structure):
+    _fields_ = [("t_max", C.c_double), ("courant", C.c_double), ("use_cfl", C.c_int32), ("io_count", C.c_int32),
+                ("prob_type", C.c_int32), ("max_steps", C.c_int32), ("g_axis", C.c_double * 3)]
+
+
+class TseriesRow(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("time", "dt", "re", "nu_wall", "nu_vol", "ke", "te", "urms",
+                                          "divergence")]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def run_params(t_max=1.0, courant=0.2, use_cfl=False, io_count=1, prob_type=5, max_steps=0,
+               g_axis=(0.0, 0.0, -1.0)) -> RunParams:
+    """Time-loop keys of parameters.yaml ("Final Time", "Courant Number",
+    "Use CFL Condition", "I/O Count", "Problem Type", "Gravity Direction")."""
+    r = RunParams()
+    r.t_max, r.courant, r.use_cfl, r.io_count = t_max, courant, int(bool(use_cfl)), io_count
+    r.prob_type, r.max_steps = prob_type, max_steps
+    for d in range(3):
+        r.g_axis[d] = g_axis[d]
+    return r
+
+
 def grid_desc(n=(16, 16, 16), length=(1.0, 1.0, 1.0), mesh="UUU", beta=(1.0, 1.0, 1.0),
               domain="NNN", dims=3, pad=1) -> GridDesc:
     """Grid descriptor from the parameters.yaml Mesh/Program keys."""
@@ -200,6 +225,13 @@ def _bind_rk3(lib):
     lib.saras_rk3_destroy.restype = C.c_int
     lib.saras_rk3_last_launches.argtypes = [vp]
     lib.saras_rk3_last_launches.restype = i64
+    lib.saras_rk3_tseries.argtypes = [vp, C.POINTER(RunParams), C.c_double, C.POINTER(TseriesRow)]
+    lib.saras_rk3_tseries.restype = C.c_int
+    lib.saras_rk3_cfl_dt.argtypes = [vp, C.c_double, C.POINTER(C.c_double)]
+    lib.saras_rk3_cfl_dt.restype = C.c_int
+    lib.saras_rk3_run.argtypes = [vp, C.POINTER(RunParams), C.POINTER(C.c_double), C.POINTER(TseriesRow), i32,
+                                  C.POINTER(i32), C.POINTER(i32)]
+    lib.saras_rk3_run.restype = C.c_int
     _rk3_bound = True
     return lib
 
@@ -373,6 +405,26 @@ class RK3:
 
     def last_launches(self) -> int:
         return self.lib.saras_rk3_last_launches(self.h)
+
+    def tseries(self, run: RunParams, time: float = 0.0) -> dict:
+        """Time-series row of the current fields (tseries::writeTSData)."""
+        row = TseriesRow()
+        check(self.lib.saras_rk3_tseries(self.h, C.byref(run), time, C.byref(row)), "saras_rk3_tseries",
+              allow=(OK, DIVERGED))
+        return row.as_dict()
+
+    def cfl_dt(self, courant: float) -> float:
+        dt = C.c_double()
+        check(self.lib.saras_rk3_cfl_dt(self.h, courant, C.byref(dt)), "saras_rk3_cfl_dt")
+        return dt.value
+
+    def run(self, run: RunParams, time: float = 0.0, cap: int = 4096):
+        """The solvePDE time loop from `time`: (status, end time, steps, rows)."""
+        rows = (TseriesRow * cap)()
+        tm, nr, ns = C.c_double(time), C.c_int32(), C.c_int32()
+        s = self.lib.saras_rk3_run(self.h, C.byref(run), C.byref(tm), rows, cap, C.byref(nr), C.byref(ns))
+        check(s, "saras_rk3_run", allow=(OK, DIVERGED))
+        return s, tm.value, ns.value, [rows[q].as_dict() for q in range(min(nr.value, cap))]
 
     def close(self):
         if self.h:

@@ -56,7 +56,8 @@ def test_struct_layout_matches_c_compiler(tmp_path):
         pytest.skip("no C compiler")
     structs = {"saras_grid_desc": S.GridDesc, "saras_mg_params": S.MgParams, "saras_field_bc": S.FieldBC,
                "saras_rk3_params": S.Rk3Params, "saras_serve_params": S.ServeParams,
-               "saras_serve_stats": S.ServeStats}
+               "saras_serve_stats": S.ServeStats, "saras_run_params": S.RunParams,
+               "saras_tseries_row": S.TseriesRow}
     lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "saras_gb300.h"', "int main(void) {"]
     for cname, py in structs.items():
         lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')

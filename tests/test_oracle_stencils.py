@@ -229,3 +229,69 @@ def test_integrator_amplification_of_shear_mode(integration):
     want = amp * np.sin(2 * math.pi * zc[1:-1])[None, None, :]
     assert np.abs(got - want).max() < 1e-11
     assert np.abs(f["vz"]).max() == 0.0 and np.abs(f["pp"]).max() < 1e-12
+
+
+def _rbc(g, with_scalar=1):
+    """Rayleigh-Benard set-up: no-slip walls, hot bottom and cold top, the
+    reference's Multigrid defaults for the pressure solve."""
+    p = params()
+    p.with_scalar = with_scalar
+    p.nu, p.kappa = 3e-3, 3e-3
+    p.cn_tolerance = 1e-12
+    for d, gv in enumerate((0.0, 0.0, -1.0)):
+        p.g_terms[d] = gv if with_scalar else 0.0
+    p.bc_vx = p.bc_vy = p.bc_vz = S.field_bc([S.FBC_DIRICHLET] * 6, [0.0] * 6)
+    p.bc_t = S.field_bc([S.FBC_NEUMANN] * 4 + [S.FBC_DIRICHLET] * 2, [0, 0, 0, 0, 1.0, 0.0])
+    p.bc_p = S.field_bc([S.FBC_NEUMANN] * 6, [0.0] * 6)
+    p.mg = S.mg_params(vc_count=20, vc_tolerance=1e-6, pre_smooth=3, post_smooth=6, mg_tolerance=1e-2)
+    return p
+
+
+@pytest.mark.parametrize("gk", [dict(n=(8, 8, 16), mesh="UUD", beta=(1, 1, 1.3), domain="PPN"),
+                                dict(n=(16, 1, 16), mesh="UUD", beta=(1, 1, 1.2), domain="PNN", dims=2)],
+                         ids=["3d", "planar"])
+def test_tseries_conductive_state(gk):
+    """tseries::writeTSData on the conductive Rayleigh-Benard state T = 1 - z,
+    u = 0, on a grid symmetric about mid-height: Nu (wall) = Nu (volume) = 1
+    and zero kinetic and thermal energy (theta = T + z - 1 = 0)."""
+    g = S.grid_desc(**gk)
+    p = _rbc(g)
+    x, _, _, _ = O.field_metrics(g, 2)
+    t = along(g, 2, 1.0 - x)
+    z = [S.padded_field(g) for _ in range(3)]
+    row, cfl = O.tseries(g, p, S.run_params(), z[0], z[1], z[2], t)
+    assert abs(row["nu_wall"] - 1.0) < 1e-12 and row["nu_vol"] == 1.0
+    assert row["ke"] == 0.0 and abs(row["te"]) < 1e-28 and row["divergence"] == 0.0 and cfl == 0.0
+
+
+def test_tseries_uniform_flow_energy_and_cfl():
+    # uniform cells: the volumes dXi/xi_x add up to the box exactly
+    g = S.grid_desc(n=(8, 8, 16), length=(2.0, 1.0, 1.0), domain="NNN")
+    p = _rbc(g, with_scalar=0)
+    vx = np.full(S.padded_field(g).shape, 0.3)
+    vz = np.full(vx.shape, -0.4)
+    row, cfl = O.tseries(g, p, S.run_params(), vx, np.zeros_like(vx), vz, None)
+    assert abs(row["ke"] - 0.5 * (0.09 + 0.16)) < 1e-14 and abs(row["urms"] - 0.5) < 1e-14
+    assert row["divergence"] < 1e-12
+    assert cfl == pytest.approx(0.3 / (2.0 / 8) + 0.4 / (1.0 / 16), rel=1e-15)
+
+
+def test_time_loop_fixed_dt_equals_steps():
+    """Without CFL the loop is nsteps calls of timeAdvance: t_max = 4 dt runs
+    four steps and leaves the same fields as four steps."""
+    g = S.grid_desc(n=(8, 8, 8), mesh="UUD", beta=(1, 1, 1.2), domain="NNN")
+    p = _rbc(g)
+    p.dt = 1e-3
+    rng = np.random.default_rng(5)
+    f = {k: S.padded_field(g) for k in ("vx", "vy", "vz", "p", "t", "pp")}
+    for k in ("vx", "vy", "vz"):
+        f[k][...] = rng.uniform(-0.05, 0.05, f[k].shape)
+    f["t"][...] = rng.uniform(0, 1, f["t"].shape)
+    a = {k: v.copy() for k, v in f.items()}
+    r = O.rk3_loop(g, p, S.run_params(t_max=4e-3, io_count=2), a["vx"], a["vy"], a["vz"], a["p"], a["t"], a["pp"])
+    assert r.status == 0 and r.n_steps == 4 and len(r.rows) == 3
+    assert [row["time"] for row in r.rows] == [0.0, 2e-3, 2e-3 + 2e-3]
+    b = {k: v.copy() for k, v in f.items()}
+    O.rk3_run(g, p, b["vx"], b["vy"], b["vz"], b["p"], b["t"], b["pp"], 4)
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
