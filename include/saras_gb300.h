@@ -213,10 +213,10 @@ int64_t saras_rk3_last_launches(const saras_rk3 *h);
 
 /* ---------------------------------------------------- time loop ---- */
 /* The time loop of scalar_d3/hydro_d3::solvePDE (src/solvers/scalar/
- * scalar_d3.cc:221-290) on the device-resident fields: timeAdvance, the CFL
+ * scalar_d3.cc:184-262) on the device-resident fields: timeAdvance, the CFL
  * time step (vfield::computeTStp, vfield.cc:691-719; capped at the
  * "Time-Step" the handle was created with), time += dt, a time-series row
- * every io_count steps (tseries::writeTSData, tseries.cc:200-492), until
+ * every io_count steps (tseries::writeTSData, tseries.cc:209-488), until
  * |t_max - time| < dt/2.  Probes, solution and restart files are the
  * caller's.  The next step uses the CFL time step, as the reference's
  * integrator holds dt by reference. */
@@ -230,9 +230,9 @@ typedef struct saras_run_params {
     double  g_axis[3];    /* "Gravity Direction": Nusselt along z unless g_axis[2] == 0 */
 } saras_run_params;
 
-/* One time-series row.  With temperature (tseries.cc:277-492): Re, Nu at
+/* One time-series row.  With temperature (tseries.cc:291-488): Re, Nu at
  * the walls, volume Nu, kinetic and thermal energy per volume; without it
- * (tseries.cc:200-275): kinetic energy and U_rms.  divergence is the
+ * (tseries.cc:209-289): kinetic energy and U_rms.  divergence is the
  * maximum |div V| over the core.  The sums run over the core in a
  * different order than the reference's sequential loops, so they agree
  * with it to rounding (the maxima are exact). */
@@ -250,7 +250,7 @@ saras_status saras_rk3_cfl_dt(saras_rk3 *h, double courant, double *dt);
 /* Runs the loop from *time (updated).  Row 0 is the state at the start
  * time.  At most row_cap rows are stored; *n_rows counts the rows produced.
  * SARAS_DIVERGED when the divergence exceeds 1e3 and grows (tseries.cc:
- * 208-214), with the rows and steps up to there. */
+* 216-222), with the rows and steps up to there. */
 saras_status saras_rk3_run(saras_rk3 *h, const saras_run_params *rp, double *time, saras_tseries_row *rows,
                            int32_t row_cap, int32_t *n_rows, int32_t *n_steps);
 

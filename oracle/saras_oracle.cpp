@@ -1299,10 +1299,10 @@ struct Rk3 {
         return m;
     }
 
-    /* tseries::writeTSData(T) (tseries.cc:277-492) and writeTSData()
-     * (tseries.cc:200-275) on one rank: the sums run sequentially in the
+    /* tseries::writeTSData(T) (tseries.cc:291-488) and writeTSData()
+     * (tseries.cc:209-289) on one rank: the sums run sequentially in the
      * reference's loop order.  Returns SARAS_DIVERGED on the divergence
-     * abort (tseries.cc:208-214). */
+     * abort (tseries.cc:216-222). */
     int tseries(const saras_run_params &rp, double time, double dt, saras_tseries_row &row, double &oldDiv) {
         const int n0 = g.N[0], n1 = g.N[1], n2 = g.N[2];
         const bool sc = prm.with_scalar != 0;
@@ -1343,7 +1343,7 @@ struct Rk3 {
             row.urms = std::sqrt(2.0 * ke);
             return abort ? SARAS_DIVERGED : SARAS_OK;
         }
-        /* tseries::tseries (tseries.cc:95-135): on one rank both walls are
+        /* tseries::tseries (tseries.cc:105-150): on one rank both walls are
          * ours; wallDn is set by the bottom wall, then by the top wall */
         const bool zG = !(rp.g_axis[2] == 0);
         double csArea, wallDn;
@@ -1412,7 +1412,7 @@ struct Rk3 {
     }
 
     /* scalar_d3::solvePDE / hydro_d3::solvePDE time loop (scalar_d3.cc:
-     * 221-290) without probes and file output. */
+     * 184-262) without probes and file output. */
     int run(const saras_run_params &rp, double &time, saras_tseries_row *rows, int cap, int *nrows, int *nsteps,
             int *mgc, int *cni) {
         const double tStp = prm.dt;

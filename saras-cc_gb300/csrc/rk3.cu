@@ -380,7 +380,7 @@ __global__ void k_max_final(const double *__restrict__ part, int nb, double *__r
 }
 
 // Time-series and CFL reductions of the current fields (tseries::
-// writeTSData, tseries.cc:200-492; vfield::computeTStp, vfield.cc:691-719).
+// writeTSData, tseries.cc:209-488; vfield::computeTStp, vfield.cc:691-719).
 // Per cell in the reference's operation order; the sums then run per thread,
 // per warp and per block in a fixed order (partials of NTS values per block).
 struct TsPar {
@@ -823,7 +823,7 @@ saras_status ts_reduce(saras_rk3 *h, const saras_run_params *rp) {
     const FLay &L = h->L;
     TsPar tp{};
     tp.zg = !(rp->g_axis[2] == 0);
-    // tseries::tseries (tseries.cc:95-135): on one rank both walls are ours;
+    // tseries::tseries (tseries.cc:105-150): on one rank both walls are ours;
     // wallDn is set by the bottom wall and then by the top wall
     if (tp.zg) {
         const int p2 = g.pad;
@@ -852,7 +852,7 @@ saras_status ts_reduce(saras_rk3 *h, const saras_run_params *rp) {
 }
 
 // tseries::writeTSData(T) / writeTSData() from the reductions (tseries.cc:
-// 208-214, 245-252, 443-452): the totals per volume, Nusselt numbers,
+// 216-222, 246, 445-450): the totals per volume, Nusselt numbers,
 // Reynolds number and the divergence abort test.
 saras_status ts_row(saras_rk3 *h, const saras_run_params *rp, double time, double dt, saras_tseries_row *row,
                     double *old_div) {
@@ -895,7 +895,7 @@ saras_status step_once(saras_rk3 *h, int *mgc, int *cni) {
     return h->prm.integration == 1 ? time_advance_euler(h, mgc, cni) : time_advance_rk3(h, mgc, cni);
 }
 
-// scalar_d3::solvePDE / hydro_d3::solvePDE (scalar_d3.cc:221-290)
+// scalar_d3::solvePDE / hydro_d3::solvePDE (scalar_d3.cc:184-262)
 saras_status rk3_run(saras_rk3 *h, const saras_run_params *rp, double *time, saras_tseries_row *rows, int cap,
                      int *n_rows, int *n_steps) {
     const double tStp = h->prm.dt;

@@ -1,7 +1,7 @@
 """GPU time loop (saras_rk3_run / saras_rk3_tseries / saras_rk3_cfl_dt) against
 the oracle's restatement of scalar_d3::solvePDE, vfield::computeTStp and
-tseries::writeTSData (src/solvers/scalar/scalar_d3.cc:221-290,
-lib/field/vfield.cc:691-719, lib/io/tseries.cc:200-492).
+tseries::writeTSData (src/solvers/scalar/scalar_d3.cc:184-262,
+lib/field/vfield.cc:691-719, lib/io/tseries.cc:209-488).
 
 Bars: the CFL time step, the divergence maximum, the step count, the time
 and every field bit for bit (maxima are order-independent; the fields come
