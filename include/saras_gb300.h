@@ -250,7 +250,7 @@ saras_status saras_rk3_cfl_dt(saras_rk3 *h, double courant, double *dt);
 /* Runs the loop from *time (updated).  Row 0 is the state at the start
  * time.  At most row_cap rows are stored; *n_rows counts the rows produced.
  * SARAS_DIVERGED when the divergence exceeds 1e3 and grows (tseries.cc:
-* 216-222), with the rows and steps up to there. */
+ * 216-222), with the rows and steps up to there. */
 saras_status saras_rk3_run(saras_rk3 *h, const saras_run_params *rp, double *time, saras_tseries_row *rows,
                            int32_t row_cap, int32_t *n_rows, int32_t *n_steps);
 
