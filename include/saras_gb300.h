@@ -299,6 +299,18 @@ saras_status saras_serve_create(const saras_serve_params *prm, saras_serve **out
  * its ghost layer. */
 saras_status saras_serve_submit(saras_serve *h, int64_t id, const saras_grid_desc *grid,
                                 const double *rhs, double *lhs);
+/* Queues a time-step request: one timeAdvance (lsRK3 or eulerCN, as
+ * prm->integration says) of the padded host fields vx, vy, vz, p, t, pp,
+ * which are updated in place when the request is returned by
+ * saras_serve_poll (vy is ignored for dims == 2, t when with_scalar == 0).
+ * Each pressure solve of the step runs in the engine's batch, in the MIXED
+ * form with the engine's tolerance, smoothing and outer-iteration cap
+ * (prm->mg is not used): the result equals saras_rk3_step on a handle whose
+ * mg is the MIXED form with those parameters (vc_count = max_cycles).  The
+ * reported cycles are the outer iterations of all its pressure solves. */
+saras_status saras_serve_submit_step(saras_serve *h, int64_t id, const saras_grid_desc *grid,
+                                     const saras_rk3_params *prm, double *vx, double *vy, double *vz,
+                                     double *p, double *t, double *pp);
 /* Admits what fits, runs one batched outer iteration, retires finished
  * requests.  *active / *pending (may be NULL) receive the counts after it. */
 saras_status saras_serve_step(saras_serve *h, int32_t *active, int32_t *pending);

@@ -31,4 +31,13 @@ saras_status mg_load_rhs(saras_mg *h, const double *rhs_box_origin, const int64_
 void mg_store_lhs(saras_mg *h, double *box_origin, const int64_t st[3]);
 int64_t mg_estimate_bytes(const saras_grid_desc *gd, const saras_mg_params *prm);
 
+// rk3.cu: the time step in halves around its pressure solves, for the
+// serving engine, which runs those solves in its batch
+int rk3_stages(const saras_rk3 *h);                          // 3 (lsRK3) or 1 (eulerCN)
+saras_status rk3_stage_begin(saras_rk3 *h, int stage);       // RHS, CN sweeps, divergence into lv[0].rhs
+saras_status rk3_stage_end(saras_rk3 *h, int stage);         // P += Pp, V -= grad Pp, BCs
+saras_mg *rk3_multigrid(saras_rk3 *h);
+int64_t rk3_device_bytes(const saras_rk3 *h);                // the integrator's fields and tables
+int64_t rk3_estimate_bytes(const saras_grid_desc *gd, const saras_rk3_params *prm);  // with its hierarchy
+
 }  // namespace saras

@@ -27,7 +27,7 @@
 
 #include <math_constants.h>
 
-#include "mg_handle.cuh"
+#include "mg_fast.cuh"
 
 namespace saras {
 saras_status mg_solve_resident(saras_mg *h, int32_t *n_cycles);
@@ -594,6 +594,7 @@ struct saras_rk3 {
     int64_t box_elems = 0;
     int max_iterations = 0;
     int64_t launches = 0;
+    int64_t dev_bytes = 0;
     std::vector<double *> allocs;
 };
 
@@ -609,6 +610,7 @@ saras_status rk_alloc(saras_rk3 *h, double **p, int64_t n) {
         return e == cudaErrorMemoryAllocation ? SARAS_OOM : SARAS_CUDA_ERR;
     }
     h->allocs.push_back(*p);
+    h->dev_bytes += std::max<int64_t>(n, 1) * (int64_t)sizeof(double);
     return SARAS_OK;
 }
 
@@ -734,44 +736,6 @@ void launch_rhs(saras_rk3 *h, const Stage &sg) {
     h->launches++;
 }
 
-// The predictor sweeps, the pressure correction and the boundary conditions
-// shared by both integrators (lsRK3_d3.cc:262-304, eulerCN_d3.cc:237-268).
-saras_status correct_stage(saras_rk3 *h, double beta, double scale, double fac, int *mgc, int *cni) {
-    cudaStream_t s = h->stream;
-    const FLay &L = h->L;
-    const int bx = bxfor(L.n2);
-    const double nu = h->prm.nu, kappa = h->prm.kappa;
-    Level &m0 = h->mg->lv[0];
-    for (int comp = 0; comp < 3; comp++) {
-        if (!h->d3 && comp == 1) continue;
-        SARAS_TRY(cn_solve(h, s, comp, h->nse[comp], nu, beta, cni));
-    }
-    if (h->sc) SARAS_TRY(cn_solve(h, s, 3, h->tmpR, kappa, beta, cni));
-    const dim3 g = cgrid(L, h->d3, bx);
-    using DK = void (*)(const double *, const double *, const double *, double *, FLay, Lay, RkTab, RkScal, double);
-    using CK = void (*)(double *, double *, double *, double *, const double *, FLay, Lay, RkTab, RkScal, double);
-    static const DK dks[2][2] = {{k_divergence<false, 1>, k_divergence<false, 2>},
-                                 {k_divergence<true, 1>, k_divergence<true, 2>}};
-    static const CK cks[2][2] = {{k_correct<false, 1>, k_correct<false, 2>}, {k_correct<true, 1>, k_correct<true, 2>}};
-    const int di = h->d3 ? 1 : 0, si = h->ds == 2 ? 1 : 0;
-    dks[di][si]<<<g, bx, 0, s>>>(h->V[0], h->V[1], h->V[2], m0.rhs, L, m0.lay, h->tabs, h->scal, scale);
-    h->launches++;
-    int nc = 0;
-    saras_status st = mg_solve_resident(h->mg, &nc);
-    if (mgc) *mgc += nc;
-    h->launches += h->mg->last_launches;
-    if (st != SARAS_OK && st != SARAS_NOT_CONVERGED) return st;  // mgSolve itself never fails
-    cks[di][si]<<<g, bx, 0, s>>>(h->V[0], h->V[1], h->V[2], h->P, m0.lhs, L, m0.lay, h->tabs, h->scal, fac);
-    h->launches++;
-    for (int comp = 0; comp < 3; comp++) {
-        if (!h->d3 && comp == 1) continue;
-        impose(h, s, h->V[comp], h->bc[comp]);
-    }
-    impose(h, s, h->P, h->bc[3]);
-    if (h->sc) impose(h, s, h->T, h->bc[4]);
-    return SARAS_OK;
-}
-
 Stage base_stage(const saras_rk3 *h) {
     Stage sg{};
     sg.nls = h->prm.nl_scheme;
@@ -780,40 +744,96 @@ Stage base_stage(const saras_rk3 *h) {
     return sg;
 }
 
-// lsRK3_d3::timeAdvance (lsRK3_d3.cc:190-305)
-saras_status time_advance_rk3(saras_rk3 *h, int *mgc, int *cni) {
-    static const double alph[3] = {4.0 / 15.0, 1.0 / 15.0, 1.0 / 6.0};
-    static const double bet[3] = {4.0 / 15.0, 1.0 / 15.0, 1.0 / 6.0};
-    static const double gam[3] = {8.0 / 15.0, 5.0 / 12.0, 3.0 / 4.0};
-    static const double zet[3] = {0.0, -17.0 / 60.0, -5.0 / 12.0};
+// lsRK3 weights (lsRK3_d3.cc:63-66) and the Crank-Nicolson weights of
+// eulerCN (alpha = beta = 1/2, eulerCN_d3.cc:62-63).
+const double RK_ALPH[3] = {4.0 / 15.0, 1.0 / 15.0, 1.0 / 6.0};
+const double RK_BET[3] = {4.0 / 15.0, 1.0 / 15.0, 1.0 / 6.0};
+const double RK_GAM[3] = {8.0 / 15.0, 5.0 / 12.0, 3.0 / 4.0};
+const double RK_ZET[3] = {0.0, -17.0 / 60.0, -5.0 / 12.0};
+const double CN_ALPH = 1.0 / 2.0, CN_BET = 1.0 / 2.0;
+
+// First half of a sub-stage, up to the pressure solve: the right-hand
+// sides, the predictor sweeps and the divergence into the multigrid RHS
+// (lsRK3_d3.cc:199-276, eulerCN_d3.cc:178-244).
+saras_status stage_begin(saras_rk3 *h, int rk, int *cni) {
+    cudaStream_t s = h->stream;
+    const FLay &L = h->L;
+    const int bx = bxfor(L.n2);
     const double nu = h->prm.nu, kappa = h->prm.kappa, dt = h->prm.dt;
-    for (int rk = 0; rk < 3; rk++) {
-        Stage sg = base_stage(h);
+    const bool euler = h->prm.integration == 1;
+    Stage sg = base_stage(h);
+    double beta, scale;
+    if (euler) {
+        sg.euler = 1;
+        sg.anu = nu * CN_ALPH;
+        sg.akap = kappa * CN_ALPH;
+        beta = CN_BET;
+        scale = 1.0 / dt;
+    } else {
         sg.rk = rk;
-        sg.zeta = zet[rk];
-        sg.anu = alph[rk] * nu;
-        sg.akap = alph[rk] * kappa;
-        sg.ab = alph[rk] + bet[rk];
-        sg.gam = gam[rk];
-        launch_rhs(h, sg);
-        SARAS_TRY(correct_stage(h, bet[rk], 1.0 / ((alph[rk] + bet[rk]) * dt), (alph[rk] + bet[rk]) * dt, mgc, cni));
+        sg.zeta = RK_ZET[rk];
+        sg.anu = RK_ALPH[rk] * nu;
+        sg.akap = RK_ALPH[rk] * kappa;
+        sg.ab = RK_ALPH[rk] + RK_BET[rk];
+        sg.gam = RK_GAM[rk];
+        beta = RK_BET[rk];
+        scale = 1.0 / ((RK_ALPH[rk] + RK_BET[rk]) * dt);
     }
+    launch_rhs(h, sg);
+    for (int comp = 0; comp < 3; comp++) {
+        if (!h->d3 && comp == 1) continue;
+        SARAS_TRY(cn_solve(h, s, comp, h->nse[comp], nu, beta, cni));
+    }
+    if (h->sc) SARAS_TRY(cn_solve(h, s, 3, h->tmpR, kappa, beta, cni));
+    Level &m0 = h->mg->lv[0];
+    using DK = void (*)(const double *, const double *, const double *, double *, FLay, Lay, RkTab, RkScal, double);
+    static const DK dks[2][2] = {{k_divergence<false, 1>, k_divergence<false, 2>},
+                                 {k_divergence<true, 1>, k_divergence<true, 2>}};
+    dks[h->d3 ? 1 : 0][h->ds == 2 ? 1 : 0]<<<cgrid(L, h->d3, bx), bx, 0, s>>>(h->V[0], h->V[1], h->V[2], m0.rhs, L,
+                                                                          m0.lay, h->tabs, h->scal, scale);
+    h->launches++;
     SARAS_CUDA(cudaGetLastError());
     return SARAS_OK;
 }
 
-// eulerCN_d3::timeAdvance (eulerCN_d3.cc:88-268): Crank-Nicolson weights
-// alpha = beta = 1/2 (eulerCN_d3.cc:62-63).
-saras_status time_advance_euler(saras_rk3 *h, int *mgc, int *cni) {
-    const double alphCN2 = 1.0 / 2.0, betaCN2 = 1.0 / 2.0;
+// Second half, after the pressure solve left Pp in the multigrid level-0
+// iterate: P += Pp, V -= fac grad Pp and the boundary conditions of V, P
+// and T (lsRK3_d3.cc:278-304, eulerCN_d3.cc:246-268).
+saras_status stage_end(saras_rk3 *h, int rk) {
+    cudaStream_t s = h->stream;
+    const FLay &L = h->L;
+    const int bx = bxfor(L.n2);
     const double dt = h->prm.dt;
-    Stage sg = base_stage(h);
-    sg.euler = 1;
-    sg.anu = h->prm.nu * alphCN2;
-    sg.akap = h->prm.kappa * alphCN2;
-    launch_rhs(h, sg);
-    SARAS_TRY(correct_stage(h, betaCN2, 1.0 / dt, dt, mgc, cni));
+    const double fac = h->prm.integration == 1 ? dt : (RK_ALPH[rk] + RK_BET[rk]) * dt;
+    Level &m0 = h->mg->lv[0];
+    using CK = void (*)(double *, double *, double *, double *, const double *, FLay, Lay, RkTab, RkScal, double);
+    static const CK cks[2][2] = {{k_correct<false, 1>, k_correct<false, 2>}, {k_correct<true, 1>, k_correct<true, 2>}};
+    cks[h->d3 ? 1 : 0][h->ds == 2 ? 1 : 0]<<<cgrid(L, h->d3, bx), bx, 0, s>>>(h->V[0], h->V[1], h->V[2], h->P,
+                                                                          m0.lhs, L, m0.lay, h->tabs, h->scal, fac);
+    h->launches++;
+    for (int comp = 0; comp < 3; comp++) {
+        if (!h->d3 && comp == 1) continue;
+        impose(h, s, h->V[comp], h->bc[comp]);
+    }
+    impose(h, s, h->P, h->bc[3]);
+    if (h->sc) impose(h, s, h->T, h->bc[4]);
     SARAS_CUDA(cudaGetLastError());
+    return SARAS_OK;
+}
+
+// lsRK3_d3::timeAdvance (lsRK3_d3.cc:190-305): three sub-stages; eulerCN_d3::
+// timeAdvance (eulerCN_d3.cc:88-268): one.
+saras_status time_advance(saras_rk3 *h, int *mgc, int *cni) {
+    const int stages = h->prm.integration == 1 ? 1 : 3;
+    for (int rk = 0; rk < stages; rk++) {
+        SARAS_TRY(stage_begin(h, rk, cni));
+        int nc = 0;
+        saras_status st = mg_solve_resident(h->mg, &nc);
+        if (mgc) *mgc += nc;
+        h->launches += h->mg->last_launches;
+        if (st != SARAS_OK && st != SARAS_NOT_CONVERGED) return st;  // mgSolve itself never fails
+        SARAS_TRY(stage_end(h, rk));
+    }
     return SARAS_OK;
 }
 
@@ -891,9 +911,7 @@ saras_status ts_row(saras_rk3 *h, const saras_run_params *rp, double time, doubl
     return SARAS_OK;
 }
 
-saras_status step_once(saras_rk3 *h, int *mgc, int *cni) {
-    return h->prm.integration == 1 ? time_advance_euler(h, mgc, cni) : time_advance_rk3(h, mgc, cni);
-}
+saras_status step_once(saras_rk3 *h, int *mgc, int *cni) { return time_advance(h, mgc, cni); }
 
 // scalar_d3::solvePDE / hydro_d3::solvePDE (scalar_d3.cc:184-262)
 saras_status rk3_run(saras_rk3 *h, const saras_run_params *rp, double *time, saras_tseries_row *rows, int cap,
@@ -1093,6 +1111,24 @@ saras_status box_transfer(saras_rk3 *h, double *field, bool level_layout, const 
 
 }  // namespace
 
+namespace saras {
+
+int rk3_stages(const saras_rk3 *h) { return h->prm.integration == 1 ? 1 : 3; }
+saras_status rk3_stage_begin(saras_rk3 *h, int stage) { return stage_begin(h, stage, nullptr); }
+saras_status rk3_stage_end(saras_rk3 *h, int stage) { return stage_end(h, stage); }
+saras_mg *rk3_multigrid(saras_rk3 *h) { return h->mg; }
+int64_t rk3_device_bytes(const saras_rk3 *h) { return h->dev_bytes; }
+
+int64_t rk3_estimate_bytes(const saras_grid_desc *gd, const saras_rk3_params *prm) {
+    const bool d3 = gd->dims == 3;
+    const FLay L = make_flay(gd->n[0], d3 ? gd->n[1] : 1, gd->n[2], gd->pad, d3 ? gd->pad : 1);
+    const int64_t box = (int64_t)(gd->n[0] + 2 * L.p) * ((d3 ? gd->n[1] : 1) + 2 * L.py) * (gd->n[2] + 2 * L.p);
+    const int64_t tabs = 8 * (int64_t)(gd->n[0] + gd->n[1] + gd->n[2]) + 1216 * NTS + NTS;
+    return (17 * L.size + box + tabs) * (int64_t)sizeof(double) + mg_estimate_bytes(gd, &prm->mg);
+}
+
+}  // namespace saras
+
 extern "C" {
 
 saras_status saras_rk3_create(const saras_grid_desc *grid, const saras_rk3_params *prm, void *stream,
@@ -1143,7 +1179,7 @@ saras_status saras_rk3_step(saras_rk3 *h, int32_t nsteps, int32_t *mg_cycles, in
     h->launches = 0;
     saras_status st = SARAS_OK;
     for (int n = 0; n < nsteps && st == SARAS_OK; n++)
-        st = h->prm.integration == 1 ? time_advance_euler(h, &mgc, &cni) : time_advance_rk3(h, &mgc, &cni);
+        st = time_advance(h, &mgc, &cni);
     if (mg_cycles) *mg_cycles = mgc;
     if (cn_iters) *cn_iters = cni;
     return st;

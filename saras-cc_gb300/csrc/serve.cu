@@ -1,5 +1,5 @@
 // Serving engine: continuous batching of independent multigrid Poisson
-// requests of uneven sizes on one GB300.
+// requests and time-step requests of uneven sizes on one GB300.
 //
 // Every admitted request keeps its MIXED-form hierarchy resident in HBM (a
 // saras_mg handle taken from a per-shape pool and re-pointed at the
@@ -9,6 +9,11 @@
 // block of rows).  A graph is captured once per hierarchy depth; its kernels
 // read the item tables and their lengths from device memory, so admitting or
 // retiring a request only rewrites the tables between launches.
+//
+// A time-step request (one lsRK3 or eulerCN timeAdvance of its fields) runs
+// its right-hand sides, Crank-Nicolson sweeps and corrections on the engine
+// stream between batched iterations, and each of its pressure solves joins
+// the batch as a case on the integrator's own hierarchy.
 //
 // A request's arithmetic never depends on the others or on the schedule:
 // items touch only their own case, the colour sweeps update disjoint cells,
@@ -423,6 +428,14 @@ using Clock = std::chrono::steady_clock;
 struct ServeCase {
     int64_t id = 0;
     saras_mg *mg = nullptr;
+    // time-step request: the integrator, its sub-stage, the caller's fields
+    // (vx, vy, vz, p, t, pp at the core origin) and the V-cycles so far
+    saras_rk3 *rk = nullptr;
+    saras_rk3_params rprm{};
+    int stage = 0;
+    int total_cycles = 0;
+    int32_t step_status = SARAS_OK;
+    double *fields[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     std::string shape;
     int slot = -1;
     int depth = 0;
@@ -497,6 +510,16 @@ saras_mg_params case_params(const saras_serve *h) {
     p.res_type = 0;
     p.precision = SARAS_PREC_MIXED;
     return p;
+}
+
+// A time-step request's integrator: its pressure solves run in the
+// engine's MIXED form, so its multigrid takes the engine's parameters, with
+// the outer-iteration cap of the engine.
+saras_rk3_params step_params(const saras_serve *h, const saras_rk3_params &req) {
+    saras_rk3_params r = req;
+    r.mg = case_params(h);
+    r.mg.vc_count = h->prm.max_cycles;
+    return r;
 }
 
 Bnd bnd_of(const saras_mg *m) {
@@ -762,12 +785,140 @@ saras_status stage_box(saras_serve *h, int64_t elems) {
     return SARAS_OK;
 }
 
+double since(const ServeCase &c) { return std::chrono::duration<double>(Clock::now() - c.t_submit).count(); }
+
+// Starts the pressure solve of the current sub-stage of a time-step case:
+// its RHS is already in lv[0].rhs, the iterate lv[0].lhs holds the previous
+// pressure correction (mgSolve's initial guess), as in saras_rk3_step.
+saras_status start_solve(saras_serve *h, ServeCase &c) {
+    saras_mg *m = c.mg;
+    rhs_norm(m, h->stream);
+    SARAS_CUDA(cudaMemcpyAsync(h->d_fden + c.slot, m->norm_out + 4, sizeof(double), cudaMemcpyDeviceToDevice,
+                               h->stream));
+    mixed_prepare(m, h->stream);
+    SARAS_CUDA(cudaGetLastError());
+    c.cycles = 0;
+    return SARAS_OK;
+}
+
+// Releases a time-step case's integrator and records its outcome.
+void drop_step(saras_serve *h, ServeCase &c, int32_t status) {
+    if (c.rk) {
+        h->bytes_alloc -= rk3_device_bytes(c.rk) + c.mg->dev_bytes;
+        saras_rk3_destroy(c.rk);
+        c.rk = nullptr;
+        c.mg = nullptr;
+    }
+    h->done.push_back(ServeDone{c.id, c.res, c.total_cycles, status, since(c)});
+    h->retired++;
+}
+
+enum AdmitStep { ADMIT_DONE = 0, ADMIT_WAIT = 1 };
+
+// Admission of a time-step request: its integrator (fields and hierarchy)
+// inside the HBM budget, the caller's fields uploaded, the first sub-stage
+// up to its pressure solve, which then joins the batch.
+AdmitStep admit_step(saras_serve *h, ServeCase &c) {
+    const saras_rk3_params rp = step_params(h, c.rprm);
+    const int64_t est = rk3_estimate_bytes(&c.grid, &rp);
+    if (h->bytes_alloc + est > h->prm.hbm_budget_bytes) evict_pooled(h, est);
+    if (h->bytes_alloc + est > h->prm.hbm_budget_bytes) {
+        if (!h->active.empty()) return ADMIT_WAIT;
+        set_error("request %lld needs about %lld bytes, above the HBM budget", (long long)c.id, (long long)est);
+        h->done.push_back(ServeDone{c.id, 0.0, 0, SARAS_BUDGET, since(c)});
+        return ADMIT_DONE;
+    }
+    saras_rk3 *rk = nullptr;
+    saras_status s = saras_rk3_create(&c.grid, &rp, h->stream, &rk);
+    if (s != SARAS_OK) {
+        h->done.push_back(ServeDone{c.id, 0.0, 0, (int32_t)s, since(c)});
+        return ADMIT_DONE;
+    }
+    c.rk = rk;
+    c.mg = rk3_multigrid(rk);
+    h->bytes_alloc += rk3_device_bytes(rk) + c.mg->dev_bytes;
+    const std::array<int, NREG> items = case_items(h, c.mg);
+    if (!fits(h, items)) {
+        h->bytes_alloc -= rk3_device_bytes(rk) + c.mg->dev_bytes;
+        saras_rk3_destroy(rk);
+        c.rk = nullptr;
+        c.mg = nullptr;
+        if (!h->active.empty()) return ADMIT_WAIT;
+        set_error("request %lld has more work items than the tables hold", (long long)c.id);
+        h->done.push_back(ServeDone{c.id, 0.0, 0, SARAS_BUDGET, since(c)});
+        return ADMIT_DONE;
+    }
+    const Box b = box_of(c.grid);
+    s = saras_rk3_upload(rk, c.fields[0], c.fields[1], c.fields[2], c.fields[3], c.fields[4], c.fields[5], b.st);
+    if (s == SARAS_OK) s = rk3_stage_begin(rk, 0);
+    if (s != SARAS_OK) {
+        drop_step(h, c, s);
+        return ADMIT_DONE;
+    }
+    c.items = items;
+    c.slot = h->free_slots.back();
+    h->free_slots.pop_back();
+    c.stage = 0;
+    if (start_solve(h, c) != SARAS_OK) {
+        h->free_slots.push_back(c.slot);
+        drop_step(h, c, SARAS_CUDA_ERR);
+        return ADMIT_DONE;
+    }
+    for (int r = 0; r < NREG; r++) h->used[r] += items[r];
+    h->active.push_back(c);
+    h->admitted++;
+    h->dirty = true;
+    return ADMIT_DONE;
+}
+
+// A time-step case whose pressure solve of this sub-stage has retired:
+// finish the solve, the sub-stage's correction, then either the next
+// sub-stage up to its pressure solve (the case stays in the batch with the
+// same hierarchy and tables) or the download of the fields.  Returns true
+// when the case left the batch.
+bool advance_step(saras_serve *h, size_t idx, int32_t solve_status) {
+    ServeCase &c = h->active[idx];
+    c.total_cycles += c.cycles;
+    saras_status s = SARAS_OK;
+    if (solve_status == SARAS_NAN) {
+        s = SARAS_NAN;
+    } else {
+        if (solve_status == SARAS_NOT_CONVERGED) c.step_status = SARAS_NOT_CONVERGED;  // the step goes on
+        mixed_finish(c.mg, h->stream);
+        s = rk3_stage_end(c.rk, c.stage);
+        if (s == SARAS_OK && c.stage + 1 < rk3_stages(c.rk)) {
+            c.stage++;
+            s = rk3_stage_begin(c.rk, c.stage);
+            if (s == SARAS_OK) s = start_solve(h, c);
+            if (s == SARAS_OK) return false;
+        } else if (s == SARAS_OK) {
+            const Box b = box_of(c.grid);
+            s = saras_rk3_download(c.rk, c.fields[0], c.fields[1], c.fields[2], c.fields[3], c.fields[4],
+                                   c.fields[5], b.st);
+            if (s == SARAS_OK) s = (saras_status)c.step_status;
+        }
+    }
+    ServeCase done = c;
+    h->free_slots.push_back(c.slot);
+    for (int r = 0; r < NREG; r++) h->used[r] -= c.items[r];
+    h->active.erase(h->active.begin() + (long)idx);
+    h->dirty = true;
+    drop_step(h, done, s);
+    return true;
+}
+
 // Admits pending requests in order while slots, the item tables and the HBM
 // budget allow.
 saras_status admit(saras_serve *h) {
     const saras_mg_params p = case_params(h);
     while (!h->pending.empty() && !h->free_slots.empty()) {
         ServeCase &c = h->pending.front();
+        if (c.rk == nullptr && c.fields[0]) {
+            const AdmitStep a = admit_step(h, c);
+            if (a == ADMIT_WAIT) break;
+            h->pending.pop_front();
+            continue;
+        }
         saras_mg *m = take_handle(h, c.shape);
         bool fresh = false;
         if (!m) {
@@ -965,6 +1116,33 @@ saras_status saras_serve_submit(saras_serve *h, int64_t id, const saras_grid_des
     return enqueue(h, id, grid, rhs, lhs, false);
 }
 
+saras_status saras_serve_submit_step(saras_serve *h, int64_t id, const saras_grid_desc *grid,
+                                     const saras_rk3_params *prm, double *vx, double *vy, double *vz, double *p,
+                                     double *t, double *pp) {
+    if (!h || !grid || !prm || !vx || !vz || !p || !pp || (grid->dims == 3 && !vy) || (prm->with_scalar && !t)) {
+        set_error("null argument");
+        return SARAS_BAD_ARG;
+    }
+    HostGrid g;
+    SARAS_TRY(g.build(*grid, 0));
+    if (g.levels < 2 || g.levels > DMAX) {
+        set_error("request depth %d outside 2..%d", g.levels, DMAX);
+        return SARAS_BAD_ARG;
+    }
+    ServeCase c;
+    c.id = id;
+    c.grid = *grid;
+    c.depth = g.levels;
+    c.shape = shape_key(*grid, g.levels);
+    c.rprm = *prm;
+    double *f[6] = {vx, vy, vz, p, t, pp};
+    const Box b = box_of(*grid);
+    for (int q = 0; q < 6; q++) c.fields[q] = f[q] ? f[q] + b.origin : nullptr;
+    c.t_submit = Clock::now();
+    h->pending.push_back(c);
+    return SARAS_OK;
+}
+
 saras_status saras_serve_step(saras_serve *h, int32_t *active, int32_t *pending) {
     if (!h) return SARAS_BAD_ARG;
     SARAS_TRY(admit(h));
@@ -977,6 +1155,10 @@ saras_status saras_serve_step(saras_serve *h, int32_t *active, int32_t *pending)
             const bool bad = !std::isfinite(c.res);
             if (bad || c.res < h->prm.tolerance || c.cycles >= h->prm.max_cycles) {
                 const int32_t st = bad ? SARAS_NAN : (c.res < h->prm.tolerance ? SARAS_OK : SARAS_NOT_CONVERGED);
+                if (c.rk) {
+                    if (!advance_step(h, q, st)) q++;
+                    continue;
+                }
                 SARAS_TRY(retire(h, q, st));
                 continue;
             }
@@ -1111,7 +1293,12 @@ saras_status saras_serve_get_stats(const saras_serve *h, saras_serve_stats *out)
 saras_status saras_serve_destroy(saras_serve *h) {
     if (!h) return SARAS_OK;
     if (h->stream) cudaStreamSynchronize(h->stream);
-    for (ServeCase &c : h->active) saras_mg_destroy(c.mg);
+    for (ServeCase &c : h->active) {
+        if (c.rk)
+            saras_rk3_destroy(c.rk);  // owns its hierarchy
+        else
+            saras_mg_destroy(c.mg);
+    }
     for (auto &kv : h->pool)
         for (saras_mg *m : kv.second) saras_mg_destroy(m);
     drop_graphs(h);

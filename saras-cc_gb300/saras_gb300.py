@@ -466,6 +466,9 @@ def _bind_serve(lib):
     lib.saras_serve_create.restype = C.c_int
     lib.saras_serve_submit.argtypes = [vp, i64, C.POINTER(GridDesc), vp, vp]
     lib.saras_serve_submit.restype = C.c_int
+    lib.saras_serve_submit_step.argtypes = [vp, i64, C.POINTER(GridDesc), C.POINTER(Rk3Params), vp, vp, vp, vp,
+                                            vp, vp]
+    lib.saras_serve_submit_step.restype = C.c_int
     lib.saras_serve_step.argtypes = [vp, C.POINTER(i32), C.POINTER(i32)]
     lib.saras_serve_step.restype = C.c_int
     lib.saras_serve_poll.argtypes = [vp, C.POINTER(i64), dp, C.POINTER(i32), C.POINTER(i32), dp, i32,
@@ -492,7 +495,8 @@ def serve_params(**kw) -> ServeParams:
 
 class Serve:
     """Continuous-batching engine of independent Poisson requests (MIXED
-    form, all admitted requests advanced by one graph launch per step).
+    form, all admitted requests advanced by one graph launch per step) and
+    time-step requests, whose pressure solves join the same batch.
     Request buffers are padded host fields (``padded_field(grid)``) that
     must stay alive until the request is returned by ``poll``."""
 
@@ -511,6 +515,23 @@ class Serve:
         check(self.lib.saras_serve_submit(self.h, rid, C.byref(grid), C.c_void_p(rhs.ctypes.data),
                                           C.c_void_p(lhs.ctypes.data)), "saras_serve_submit")
         self._keep[rid] = (grid, rhs, lhs)
+
+    def submit_step(self, rid: int, grid: GridDesc, params: Rk3Params, fields: dict):
+        """One time step of `fields` (vx, vy, vz, p, t, pp padded boxes,
+        updated in place when the request is polled)."""
+        shape = padded_field(grid).shape
+        ptrs = []
+        for k in ("vx", "vy", "vz", "p", "t", "pp"):
+            a = fields.get(k)
+            if a is None:
+                ptrs.append(C.c_void_p(0))
+                continue
+            if a.dtype != np.float64 or not a.flags.c_contiguous or a.shape != shape:
+                raise ValueError("request fields must be C-contiguous float64 padded boxes of the grid")
+            ptrs.append(C.c_void_p(a.ctypes.data))
+        check(self.lib.saras_serve_submit_step(self.h, rid, C.byref(grid), C.byref(params), *ptrs),
+              "saras_serve_submit_step")
+        self._keep[rid] = (grid, params, fields)
 
     def step(self):
         a, p = C.c_int32(), C.c_int32()
