@@ -354,27 +354,39 @@ def serve_grid(S, size, dims, beta):
     return S.grid_desc(n=size, length=length, mesh="UUD", beta=(1.0, 1.0, beta), domain="NNN", dims=dims)
 
 
-def serve_stream(S, n, rate, seed=7):
+def serve_stream(S, n, rate, seed=7, step_frac=0.0):
     """Seeded request stream: Poisson arrivals, sizes drawn uniformly from
     SERVE_SIZES, z tanh-stretched with beta ~ U[1, 1.5], Neumann walls, RHS
     i.i.d. U[-1,1] made compatible with the all-Neumann operator.  Domain
     lengths follow the cell counts (cells of equal extent before
     stretching): the reference V-cycle diverges on strongly anisotropic
-    cells."""
+    cells.  A fraction `step_frac` are RK3 time-step requests instead: one
+    Rayleigh-Benard step of the same size from the scalar_d3 start."""
     rng = np.random.default_rng(seed)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
     kinds = rng.integers(0, len(SERVE_SIZES), n)
     betas = rng.uniform(1.0, 1.5, n)
+    steps = rng.uniform(0.0, 1.0, n) < step_frac
     reqs = []
     for q in range(n):
         _, size, dims = SERVE_SIZES[kinds[q]]
+        if steps[q]:
+            # Rayleigh-Benard time step (periodic sides, no-slip plates); the
+            # stretching stays at or below 1.3, where the reference pressure
+            # V-cycle converges on this box
+            top = max(size)
+            length = tuple(x / top for x in size) if dims == 3 else (1.0, 1.0, 1.0)
+            g = S.grid_desc(n=size, length=length, mesh="UUD", beta=(1.0, 1.0, 1.0 + 0.6 * (betas[q] - 1.0)),
+                            domain="PPN", dims=dims)
+            reqs.append((g, None))
+            continue
         g = serve_grid(S, size, dims, float(betas[q]))
         ny = 1 if dims == 2 else size[1]
         f = np.random.default_rng([seed, q]).uniform(-1.0, 1.0, (size[0], ny, size[2]))
         rhs = S.padded_field(g)
         rhs[1:1 + size[0], 1:1 + ny, 1:1 + size[2]] = S.project_compatible(g, f)
         reqs.append((g, rhs))
-    return arrivals, kinds, reqs
+    return arrivals, kinds, steps, reqs
 
 
 def run_serving(S, args):
@@ -382,7 +394,8 @@ def run_serving(S, args):
     host buffers): latency = completion seen by the host minus the request's
     scheduled arrival."""
     n, rate = args.serve_requests, args.serve_rate
-    arrivals, kinds, reqs = serve_stream(S, n, rate)
+    arrivals, kinds, steps, reqs = serve_stream(S, n, rate, step_frac=args.serve_step_frac)
+    step_prm = rbc_step_params(S, S.PREC_MIXED)
     eng = S.Serve(S.serve_params(hbm_budget_bytes=40 << 30, max_cases=256, tolerance=SERVE_TOL, max_cycles=400,
                                  **SERVE_MG))
     tune = [serve_grid(S, size, dims, 1.25) for _, size, dims in SERVE_SIZES]
@@ -400,8 +413,12 @@ def run_serving(S, args):
             break
         while nxt < n and arrivals[nxt] <= now:
             g, rhs = reqs[nxt]
-            outs[nxt] = S.padded_field(g)
-            eng.submit(nxt, g, rhs, outs[nxt])
+            if steps[nxt]:
+                outs[nxt] = rbc_fields(S, g, 1000 + nxt)
+                eng.submit_step(nxt, g, step_prm, outs[nxt])
+            else:
+                outs[nxt] = S.padded_field(g)
+                eng.submit(nxt, g, rhs, outs[nxt])
             nxt += 1
         a, p = eng.step()
         t = time.perf_counter() - t0
@@ -420,6 +437,8 @@ def run_serving(S, args):
     cyc = np.array([d["cycles"] for d in done.values()])
     cells = {q: SERVE_SIZES[kinds[q]][1][0] * SERVE_SIZES[kinds[q]][1][1] * SERVE_SIZES[kinds[q]][1][2]
              for q in done}
+    step_lat = [done[q]["latency_s"] * 1e3 for q in done if steps[q]]
+    pois_lat = [done[q]["latency_s"] * 1e3 for q in done if not steps[q]]
     cell_cycles = float(sum(cells[q] * done[q]["cycles"] for q in done))
     model_bytes = float(sum(cells[q] * done[q]["cycles"] * SERVE_BYTES_PER_CELL[SERVE_SIZES[kinds[q]][2]]
                             for q in done))
@@ -431,16 +450,26 @@ def run_serving(S, args):
         statuses[nm] = statuses.get(nm, 0) + 1
     by_size = {}
     for k, (name, _, _) in enumerate(SERVE_SIZES):
-        ls = [done[q]["latency_s"] * 1e3 for q in done if kinds[q] == k]
-        cs = [done[q]["cycles"] for q in done if kinds[q] == k]
+        ls = [done[q]["latency_s"] * 1e3 for q in done if kinds[q] == k and not steps[q]]
+        cs = [done[q]["cycles"] for q in done if kinds[q] == k and not steps[q]]
         if ls:
             by_size[name] = {"count": len(ls), "p50_ms": float(np.percentile(ls, 50)),
                              "p99_ms": float(np.percentile(ls, 99)), "cycles_median": float(np.median(cs))}
+    nstep = int(steps.sum())
     return {
-        "workload": f"{n} Poisson requests, Poisson arrivals {rate}/s (seed 7), sizes uniform over "
+        "workload": f"{n} requests ({n - nstep} Poisson, {nstep} RK3 time steps), Poisson arrivals {rate}/s "
+                    "(seed 7), sizes uniform over "
                     + ", ".join(x[0] for x in SERVE_SIZES) + ", cubic cells before z tanh stretching with beta "
                     "U[1,1.5], Neumann walls, RHS U[-1,1] projected compatible, MIXED form to rel-res 1e-8 (Linf), "
-                    "3/6 RBGS (reference defaults), coarsest tolerance 1e-9, 40 GB HBM budget, 256 case slots",
+                    "3/6 RBGS (reference defaults), coarsest tolerance 1e-9, 40 GB HBM budget, 256 case slots; "
+                    "time-step requests: one RK3 step of Rayleigh-Benard convection (Ra 1e7, Pr 1, dt 1e-4, "
+                    "periodic sides, z beta U[1,1.3], u = 0, T conductive + noise), pressure solves in the batch "
+                    "to the reference's Residual Tolerance 1e-6 / V-Cycle Count 20",
+        "step_requests": nstep,
+        "step_p50_ms": float(np.percentile(step_lat, 50)) if step_lat else None,
+        "step_p99_ms": float(np.percentile(step_lat, 99)) if step_lat else None,
+        "poisson_p50_ms": float(np.percentile(pois_lat, 50)) if pois_lat else None,
+        "poisson_p99_ms": float(np.percentile(pois_lat, 99)) if pois_lat else None,
         "requests": n, "completed": len(done), "statuses": statuses,
         "p50_ms": float(np.percentile(lat, 50)) if len(lat) else None,
         "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,
@@ -511,6 +540,37 @@ def run_c3(args):
     print(json.dumps(out), flush=True)
 
 
+def rbc_step_params(S, prec, dt=1e-4):
+    """Rayleigh-Benard time step, Ra 1e7, Pr 1 ("RBC Type" 2): no-slip
+    walls, hot bottom / cold top, CN tolerance 1e-6, the reference's
+    Multigrid defaults (3/6, coarsest tol 1e-2, 20 cycles, 1e-6)."""
+    nu, ka, fb = S.rbc_coefficients(2, 1e7, 1.0)
+    p = S.Rk3Params()
+    p.nu, p.kappa, p.dt = nu, ka, dt
+    p.cn_tolerance = 1e-6
+    p.max_iterations = 0
+    p.g_terms[0], p.g_terms[1], p.g_terms[2] = 0.0, 0.0, -fb
+    p.with_scalar = 1
+    p.nl_scheme = 1
+    zero = S.field_bc([S.FBC_DIRICHLET] * 6, [0.0] * 6)
+    p.bc_vx, p.bc_vy, p.bc_vz = zero, zero, zero
+    p.bc_t = S.field_bc([S.FBC_NEUMANN] * 4 + [S.FBC_DIRICHLET] * 2, [0, 0, 0, 0, 1.0, 0.0])
+    p.bc_p = S.field_bc([S.FBC_NEUMANN] * 6, [0.0] * 6)
+    p.mg = S.mg_params(vc_count=20, vc_tolerance=1e-6, pre_smooth=3, post_smooth=6, mg_tolerance=1e-2,
+                       precision=prec)
+    return p
+
+
+def rbc_fields(S, g, seed):
+    """scalar_d3 start: u = 0, P = 1, T = conductive profile + noise 1e-3."""
+    rng = np.random.default_rng(seed)
+    f = {k: S.padded_field(g) for k in ("vx", "vy", "vz", "p", "t", "pp")}
+    zc = S.grid_metrics(g, 0, 2)[0]
+    f["t"][...] = (1.0 - zc)[None, None, :] + rng.uniform(-5e-4, 5e-4, f["t"].shape)
+    f["p"][...] = 1.0
+    return f
+
+
 def run_rk3(args):
     """Time steps of 3-D Rayleigh-Benard convection: 256^3, Ra 1e7, Pr 1,
     z tanh-stretched, no-slip isothermal plates, periodic sides, u = 0 and
@@ -524,28 +584,11 @@ def run_rk3(args):
     n = args.rk3_n
     beta = args.rk3_beta
     g = S.grid_desc(n=(n, n, n), mesh="UUD", beta=(1.0, 1.0, beta), domain="PPN")
-    nu, ka, fb = S.rbc_coefficients(2, 1e7, 1.0)
     out = {"config": "rk3", "workload": f"RK3 Rayleigh-Benard {n}^3, Ra 1e7, Pr 1, z tanh beta {beta}, PPN, "
                                         f"dt 1e-4, CN tol 1e-6, MG 3/6 tol 1e-6 coarsest 1e-2, {args.rk3_steps} steps"}
     for name, prec in (("fp64", S.PREC_FP64), ("mixed", S.PREC_MIXED)):
-        p = S.Rk3Params()
-        p.nu, p.kappa, p.dt = nu, ka, 1e-4
-        p.cn_tolerance = 1e-6
-        p.max_iterations = 0
-        p.g_terms[0], p.g_terms[1], p.g_terms[2] = 0.0, 0.0, -fb
-        p.with_scalar = 1
-        p.nl_scheme = 1
-        zero = S.field_bc([S.FBC_DIRICHLET] * 6, [0.0] * 6)
-        p.bc_vx, p.bc_vy, p.bc_vz = zero, zero, zero
-        p.bc_t = S.field_bc([S.FBC_NEUMANN] * 4 + [S.FBC_DIRICHLET] * 2, [0, 0, 0, 0, 1.0, 0.0])
-        p.bc_p = S.field_bc([S.FBC_NEUMANN] * 6, [0.0] * 6)
-        p.mg = S.mg_params(vc_count=20, vc_tolerance=1e-6, pre_smooth=3, post_smooth=6, mg_tolerance=1e-2,
-                           precision=prec)
-        rng = np.random.default_rng(4)
-        f = {k: S.padded_field(g) for k in ("vx", "vy", "vz", "p", "t", "pp")}
-        zc = S.grid_metrics(g, 0, 2)[0]
-        f["t"][...] = (1.0 - zc)[None, None, :] + rng.uniform(-5e-4, 5e-4, f["t"].shape)
-        f["p"][...] = 1.0
+        p = rbc_step_params(S, prec)
+        f = rbc_fields(S, g, 4)
         rk = S.RK3(g, p)
         rk.upload(f["vx"], f["vy"], f["vz"], f["p"], f["t"], f["pp"])
         rk.step(1)  # warm-up
@@ -610,6 +653,8 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=300,
                     help="requests of the serving stream (the full stream is 2000)")
     ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-step-frac", type=float, default=0.1,
+                    help="fraction of serving requests that are RK3 time steps")
     ap.add_argument("--serve-timeout", type=float, default=240.0,
                     help="seconds after which the serving stream stops waiting for requests")
     ap.add_argument("--no-serve", action="store_true")

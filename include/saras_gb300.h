@@ -303,11 +303,16 @@ saras_status saras_serve_submit(saras_serve *h, int64_t id, const saras_grid_des
  * prm->integration says) of the padded host fields vx, vy, vz, p, t, pp,
  * which are updated in place when the request is returned by
  * saras_serve_poll (vy is ignored for dims == 2, t when with_scalar == 0).
- * Each pressure solve of the step runs in the engine's batch, in the MIXED
- * form with the engine's tolerance, smoothing and outer-iteration cap
- * (prm->mg is not used): the result equals saras_rk3_step on a handle whose
- * mg is the MIXED form with those parameters (vc_count = max_cycles).  The
- * reported cycles are the outer iterations of all its pressure solves. */
+ * Each pressure solve of the step runs in the engine's batch in the MIXED
+ * form with the engine's smoothing, SOR and coarsest tolerance, and stops at
+ * the request's own prm->mg.vc_tolerance or after prm->mg.vc_count outer
+ * iterations ("Residual Tolerance", "V-Cycle Count": the pressure RHS of a
+ * collocated step is not exactly compatible with the Neumann operator, so
+ * its residual levels off).  The result equals saras_rk3_step on a handle
+ * whose mg is that MIXED form with those two keys.  The reported cycles are
+ * the outer iterations of all its pressure solves, the status OK, or
+ * NOT_CONVERGED when a solve stopped at its cap (the step still completes,
+ * as in the reference). */
 saras_status saras_serve_submit_step(saras_serve *h, int64_t id, const saras_grid_desc *grid,
                                      const saras_rk3_params *prm, double *vx, double *vy, double *vz,
                                      double *p, double *t, double *pp);

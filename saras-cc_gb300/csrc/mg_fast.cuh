@@ -38,6 +38,9 @@ saras_status rk3_stage_begin(saras_rk3 *h, int stage);       // RHS, CN sweeps, 
 saras_status rk3_stage_end(saras_rk3 *h, int stage);         // P += Pp, V -= grad Pp, BCs
 saras_mg *rk3_multigrid(saras_rk3 *h);
 int64_t rk3_device_bytes(const saras_rk3 *h);                // the integrator's fields and tables
+// re-points a handle at another stretching of the same shape (and new
+// parameters); fields cleared as at creation
+saras_status rk3_retarget(saras_rk3 *h, const saras_grid_desc *gd, const saras_rk3_params *prm);
 int64_t rk3_estimate_bytes(const saras_grid_desc *gd, const saras_rk3_params *prm);  // with its hierarchy
 
 }  // namespace saras

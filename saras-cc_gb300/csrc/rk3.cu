@@ -595,6 +595,7 @@ struct saras_rk3 {
     int max_iterations = 0;
     int64_t launches = 0;
     int64_t dev_bytes = 0;
+    int nfields = 0;  // the first allocations are the fields (cleared on retarget)
     std::vector<double *> allocs;
 };
 
@@ -950,7 +951,7 @@ saras_status rk3_run(saras_rk3 *h, const saras_run_params *rp, double *time, sar
     return st;
 }
 
-saras_status rk3_create(const saras_grid_desc *gd, const saras_rk3_params *p, void *stream, saras_rk3 *h) {
+saras_status check_params(const saras_grid_desc *gd, const saras_rk3_params *p) {
     if (gd->pad != 1 && gd->pad != 2) {
         set_error("the time step takes Differentiation Scheme 1 (pad 1) or 2 (pad 2)");
         return SARAS_BAD_ARG;
@@ -960,34 +961,24 @@ saras_status rk3_create(const saras_grid_desc *gd, const saras_rk3_params *p, vo
         set_error("invalid time-step parameters");
         return SARAS_BAD_ARG;
     }
+    return SARAS_OK;
+}
+
+// Everything of a handle that follows the grid's stretching and the
+// parameters: metric tables (h->tab already allocated), derivative and
+// upwind constants, boundary constants, the CN iteration cap.
+saras_status rk3_configure(saras_rk3 *h, const saras_grid_desc *gd, const saras_rk3_params *p) {
     h->prm = *p;
     SARAS_TRY(h->grid.build(*gd, p->mg.levels));
     h->d3 = h->grid.dims == 3;
     h->sc = p->with_scalar != 0;
     h->ds = gd->pad;
-    h->stream = (cudaStream_t)stream;
-    SARAS_TRY(saras_mg_create(gd, &p->mg, stream, &h->mg));
     const HostGrid &g = h->grid;
-    h->L = make_flay(g.N[0], h->d3 ? g.N[1] : 1, g.N[2], g.pad, h->d3 ? g.pad : 1);
-    const int64_t sz = h->L.size;
-    for (int d = 0; d < 3; d++) {
-        SARAS_TRY(rk_alloc(h, &h->V[d], sz));
-        SARAS_TRY(rk_alloc(h, &h->Vb[d], sz));
-        SARAS_TRY(rk_alloc(h, &h->nse[d], sz));
-        SARAS_TRY(rk_alloc(h, &h->nl[d], sz));
-    }
-    SARAS_TRY(rk_alloc(h, &h->P, sz));
-    SARAS_TRY(rk_alloc(h, &h->T, sz));
-    SARAS_TRY(rk_alloc(h, &h->Tb, sz));
-    SARAS_TRY(rk_alloc(h, &h->tmpR, sz));
-    SARAS_TRY(rk_alloc(h, &h->nlT, sz));
-    for (double *q : h->allocs) SARAS_CUDA(cudaMemset(q, 0, (size_t)sz * sizeof(double)));
-    // metric tables: xi_x, xixx, xix2, a2, a1, dh per axis over the core
+    // metric tables: xi_x, xixx, xix2, a2, a1, dh, dv, xc per axis over the core
     constexpr int NT = 8;
     const int n[3] = {h->L.n0, h->L.n1, h->L.n2};
     const int64_t tot = NT * (int64_t)(n[0] + n[1] + n[2]);
     std::vector<double> host((size_t)tot, 0.0);
-    SARAS_TRY(rk_alloc(h, &h->tab, tot));
     int64_t off = 0;
     for (int d = 0; d < 3; d++) {
         const int p0 = (g.dims == 2 && d == 1) ? 1 : g.pad;
@@ -1026,6 +1017,7 @@ saras_status rk3_create(const saras_grid_desc *gd, const saras_rk3_params *p, vo
     // vfield::vfield / sfield::sfield (vfield.cc:107-130): first-order
     // upwinding for dScheme 1, omega = "Central Bias"
     const double omega = p->up_param;
+    h->scal.ud = 0.0;
     if (h->ds == 1) {
         h->scal.ua = 2.0 - omega;
         h->scal.ub = 2.0 * (1.0 - omega);
@@ -1044,14 +1036,42 @@ saras_status rk3_create(const saras_grid_desc *gd, const saras_rk3_params *p, vo
     h->bc[2] = make_fbc(h, p->bc_vz);
     h->bc[3] = make_fbc(h, p->bc_p);
     h->bc[4] = make_fbc(h, p->bc_t);
+    // timestep::timestep (timestep.cc:115): int(pow(log(Nx*Ny*Nz), 3))
+    h->max_iterations = p->max_iterations > 0 ? p->max_iterations
+                                              : int(std::pow(std::log(g.N[0] * g.N[1] * g.N[2]), 3));
+    return SARAS_OK;
+}
+
+saras_status rk3_create(const saras_grid_desc *gd, const saras_rk3_params *p, void *stream, saras_rk3 *h) {
+    SARAS_TRY(check_params(gd, p));
+    HostGrid g;
+    SARAS_TRY(g.build(*gd, p->mg.levels));
+    const bool d3 = g.dims == 3;
+    h->stream = (cudaStream_t)stream;
+    SARAS_TRY(saras_mg_create(gd, &p->mg, stream, &h->mg));
+    h->L = make_flay(g.N[0], d3 ? g.N[1] : 1, g.N[2], g.pad, d3 ? g.pad : 1);
+    const int64_t sz = h->L.size;
+    for (int d = 0; d < 3; d++) {
+        SARAS_TRY(rk_alloc(h, &h->V[d], sz));
+        SARAS_TRY(rk_alloc(h, &h->Vb[d], sz));
+        SARAS_TRY(rk_alloc(h, &h->nse[d], sz));
+        SARAS_TRY(rk_alloc(h, &h->nl[d], sz));
+    }
+    SARAS_TRY(rk_alloc(h, &h->P, sz));
+    SARAS_TRY(rk_alloc(h, &h->T, sz));
+    SARAS_TRY(rk_alloc(h, &h->Tb, sz));
+    SARAS_TRY(rk_alloc(h, &h->tmpR, sz));
+    SARAS_TRY(rk_alloc(h, &h->nlT, sz));
+    h->nfields = (int)h->allocs.size();
+    for (double *q : h->allocs) SARAS_CUDA(cudaMemset(q, 0, (size_t)sz * sizeof(double)));
+    const int n[3] = {h->L.n0, h->L.n1, h->L.n2};
+    SARAS_TRY(rk_alloc(h, &h->tab, 8 * (int64_t)(n[0] + n[1] + n[2])));
+    SARAS_TRY(rk3_configure(h, gd, p));
     const int64_t cells = (int64_t)n[0] * n[1] * n[2];
     h->nblocks = (int)std::max<int64_t>(1, std::min<int64_t>(1216, (cells + 255) / 256));
     SARAS_TRY(rk_alloc(h, &h->part, (int64_t)h->nblocks * NTS));
     SARAS_TRY(rk_alloc(h, &h->red, NTS));
     SARAS_CUDA(cudaMallocHost((void **)&h->red_host, NTS * sizeof(double)));
-    // timestep::timestep (timestep.cc:115): int(pow(log(Nx*Ny*Nz), 3))
-    h->max_iterations = p->max_iterations > 0 ? p->max_iterations
-                                              : int(std::pow(std::log(g.N[0] * g.N[1] * g.N[2]), 3));
     // dense host box of a field: core plus pad (1 on y for the planar case)
     const int px = h->L.p, py = h->L.py;
     h->bst[2] = 1;
@@ -1118,6 +1138,24 @@ saras_status rk3_stage_begin(saras_rk3 *h, int stage) { return stage_begin(h, st
 saras_status rk3_stage_end(saras_rk3 *h, int stage) { return stage_end(h, stage); }
 saras_mg *rk3_multigrid(saras_rk3 *h) { return h->mg; }
 int64_t rk3_device_bytes(const saras_rk3 *h) { return h->dev_bytes; }
+
+saras_status rk3_retarget(saras_rk3 *h, const saras_grid_desc *gd, const saras_rk3_params *p) {
+    SARAS_TRY(check_params(gd, p));
+    const HostGrid &o = h->grid;
+    bool same = gd->dims == o.dims && gd->pad == o.pad && p->mg.levels == h->prm.mg.levels;
+    for (int d = 0; d < 3; d++) same = same && gd->n[d] == o.N[d] && (gd->periodic[d] != 0) == o.per[d];
+    if (!same) {
+        set_error("a time-step handle is re-pointed only at a grid of its own shape");
+        return SARAS_BAD_ARG;
+    }
+    SARAS_TRY(mg_retarget(h->mg, gd));
+    h->mg->prm.vc_count = p->mg.vc_count;
+    h->mg->prm.vc_tolerance = p->mg.vc_tolerance;
+    SARAS_TRY(rk3_configure(h, gd, p));
+    for (int q = 0; q < h->nfields; q++)
+        SARAS_CUDA(cudaMemsetAsync(h->allocs[(size_t)q], 0, (size_t)h->L.size * sizeof(double), h->stream));
+    return SARAS_OK;
+}
 
 int64_t rk3_estimate_bytes(const saras_grid_desc *gd, const saras_rk3_params *prm) {
     const bool d3 = gd->dims == 3;

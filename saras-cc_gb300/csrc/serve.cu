@@ -434,6 +434,8 @@ struct ServeCase {
     saras_rk3_params rprm{};
     int stage = 0;
     int total_cycles = 0;
+    double tol = 0.0;  // relative residual that ends a solve (engine's, or the step request's)
+    int cap = 0;       // outer iterations per solve
     int32_t step_status = SARAS_OK;
     double *fields[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     std::string shape;
@@ -465,6 +467,7 @@ struct saras_serve {
     std::vector<ServeCase> active;
     std::deque<ServeDone> done;
     std::map<std::string, std::vector<saras_mg *>> pool;
+    std::map<std::string, std::vector<saras_rk3 *>> step_pool;  // idle integrators of time-step requests
     int64_t bytes_alloc = 0;
     std::vector<int> free_slots;
     std::array<int, NREG> used{};
@@ -518,7 +521,8 @@ saras_mg_params case_params(const saras_serve *h) {
 saras_rk3_params step_params(const saras_serve *h, const saras_rk3_params &req) {
     saras_rk3_params r = req;
     r.mg = case_params(h);
-    r.mg.vc_count = h->prm.max_cycles;
+    r.mg.vc_count = req.mg.vc_count;
+    r.mg.vc_tolerance = req.mg.vc_tolerance;
     return r;
 }
 
@@ -746,8 +750,17 @@ saras_mg *take_handle(saras_serve *h, const std::string &key) {
     return m;
 }
 
-// Frees pooled (idle) hierarchies until `need` more bytes fit the budget.
+// Frees pooled (idle) hierarchies and integrators until `need` more bytes
+// fit the budget.
 void evict_pooled(saras_serve *h, int64_t need) {
+    for (auto &kv : h->step_pool) {
+        while (!kv.second.empty() && h->bytes_alloc + need > h->prm.hbm_budget_bytes) {
+            saras_rk3 *rk = kv.second.back();
+            kv.second.pop_back();
+            h->bytes_alloc -= rk3_device_bytes(rk) + rk3_multigrid(rk)->dev_bytes;
+            saras_rk3_destroy(rk);
+        }
+    }
     for (auto &kv : h->pool) {
         while (!kv.second.empty() && h->bytes_alloc + need > h->prm.hbm_budget_bytes) {
             saras_mg *m = kv.second.back();
@@ -801,11 +814,11 @@ saras_status start_solve(saras_serve *h, ServeCase &c) {
     return SARAS_OK;
 }
 
-// Releases a time-step case's integrator and records its outcome.
+// Returns a time-step case's integrator to its pool and records the
+// outcome.
 void drop_step(saras_serve *h, ServeCase &c, int32_t status) {
     if (c.rk) {
-        h->bytes_alloc -= rk3_device_bytes(c.rk) + c.mg->dev_bytes;
-        saras_rk3_destroy(c.rk);
+        h->step_pool[c.shape].push_back(c.rk);
         c.rk = nullptr;
         c.mg = nullptr;
     }
@@ -820,27 +833,41 @@ enum AdmitStep { ADMIT_DONE = 0, ADMIT_WAIT = 1 };
 // up to its pressure solve, which then joins the batch.
 AdmitStep admit_step(saras_serve *h, ServeCase &c) {
     const saras_rk3_params rp = step_params(h, c.rprm);
-    const int64_t est = rk3_estimate_bytes(&c.grid, &rp);
-    if (h->bytes_alloc + est > h->prm.hbm_budget_bytes) evict_pooled(h, est);
-    if (h->bytes_alloc + est > h->prm.hbm_budget_bytes) {
-        if (!h->active.empty()) return ADMIT_WAIT;
-        set_error("request %lld needs about %lld bytes, above the HBM budget", (long long)c.id, (long long)est);
-        h->done.push_back(ServeDone{c.id, 0.0, 0, SARAS_BUDGET, since(c)});
-        return ADMIT_DONE;
-    }
     saras_rk3 *rk = nullptr;
-    saras_status s = saras_rk3_create(&c.grid, &rp, h->stream, &rk);
-    if (s != SARAS_OK) {
-        h->done.push_back(ServeDone{c.id, 0.0, 0, (int32_t)s, since(c)});
-        return ADMIT_DONE;
+    saras_status s = SARAS_OK;
+    auto pit = h->step_pool.find(c.shape);
+    if (pit != h->step_pool.end() && !pit->second.empty()) {
+        rk = pit->second.back();
+        pit->second.pop_back();
+        s = rk3_retarget(rk, &c.grid, &rp);
+        if (s != SARAS_OK) {
+            h->bytes_alloc -= rk3_device_bytes(rk) + rk3_multigrid(rk)->dev_bytes;
+            saras_rk3_destroy(rk);
+            h->done.push_back(ServeDone{c.id, 0.0, 0, (int32_t)s, since(c)});
+            return ADMIT_DONE;
+        }
+    } else {
+        const int64_t est = rk3_estimate_bytes(&c.grid, &rp);
+        if (h->bytes_alloc + est > h->prm.hbm_budget_bytes) evict_pooled(h, est);
+        if (h->bytes_alloc + est > h->prm.hbm_budget_bytes) {
+            if (!h->active.empty()) return ADMIT_WAIT;
+            set_error("request %lld needs about %lld bytes, above the HBM budget", (long long)c.id,
+                      (long long)est);
+            h->done.push_back(ServeDone{c.id, 0.0, 0, SARAS_BUDGET, since(c)});
+            return ADMIT_DONE;
+        }
+        s = saras_rk3_create(&c.grid, &rp, h->stream, &rk);
+        if (s != SARAS_OK) {
+            h->done.push_back(ServeDone{c.id, 0.0, 0, (int32_t)s, since(c)});
+            return ADMIT_DONE;
+        }
+        h->bytes_alloc += rk3_device_bytes(rk) + rk3_multigrid(rk)->dev_bytes;
     }
     c.rk = rk;
     c.mg = rk3_multigrid(rk);
-    h->bytes_alloc += rk3_device_bytes(rk) + c.mg->dev_bytes;
     const std::array<int, NREG> items = case_items(h, c.mg);
     if (!fits(h, items)) {
-        h->bytes_alloc -= rk3_device_bytes(rk) + c.mg->dev_bytes;
-        saras_rk3_destroy(rk);
+        h->step_pool[c.shape].push_back(rk);
         c.rk = nullptr;
         c.mg = nullptr;
         if (!h->active.empty()) return ADMIT_WAIT;
@@ -1026,6 +1053,8 @@ saras_status enqueue(saras_serve *h, int64_t id, const saras_grid_desc *grid, co
     c.in = rhs + b.origin;
     c.out = lhs + b.origin;
     c.internal = internal;
+    c.tol = h->prm.tolerance;
+    c.cap = h->prm.max_cycles;
     c.t_submit = Clock::now();
     h->pending.push_back(c);
     return SARAS_OK;
@@ -1123,6 +1152,10 @@ saras_status saras_serve_submit_step(saras_serve *h, int64_t id, const saras_gri
         set_error("null argument");
         return SARAS_BAD_ARG;
     }
+    if (prm->mg.vc_count < 1 || !(prm->mg.vc_tolerance > 0.0)) {
+        set_error("a time-step request needs vc_count >= 1 and vc_tolerance > 0 for its pressure solves");
+        return SARAS_BAD_ARG;
+    }
     HostGrid g;
     SARAS_TRY(g.build(*grid, 0));
     if (g.levels < 2 || g.levels > DMAX) {
@@ -1135,6 +1168,8 @@ saras_status saras_serve_submit_step(saras_serve *h, int64_t id, const saras_gri
     c.depth = g.levels;
     c.shape = shape_key(*grid, g.levels);
     c.rprm = *prm;
+    c.tol = prm->mg.vc_tolerance;
+    c.cap = prm->mg.vc_count;
     double *f[6] = {vx, vy, vz, p, t, pp};
     const Box b = box_of(*grid);
     for (int q = 0; q < 6; q++) c.fields[q] = f[q] ? f[q] + b.origin : nullptr;
@@ -1153,8 +1188,8 @@ saras_status saras_serve_step(saras_serve *h, int32_t *active, int32_t *pending)
             c.cycles++;
             c.res = h->h_res[c.slot];
             const bool bad = !std::isfinite(c.res);
-            if (bad || c.res < h->prm.tolerance || c.cycles >= h->prm.max_cycles) {
-                const int32_t st = bad ? SARAS_NAN : (c.res < h->prm.tolerance ? SARAS_OK : SARAS_NOT_CONVERGED);
+            if (bad || c.res < c.tol || c.cycles >= c.cap) {
+                const int32_t st = bad ? SARAS_NAN : (c.res < c.tol ? SARAS_OK : SARAS_NOT_CONVERGED);
                 if (c.rk) {
                     if (!advance_step(h, q, st)) q++;
                     continue;
@@ -1285,6 +1320,7 @@ saras_status saras_serve_get_stats(const saras_serve *h, saras_serve_stats *out)
     out->pending = (int32_t)h->pending.size();
     int pooled = 0;
     for (const auto &kv : h->pool) pooled += (int)kv.second.size();
+    for (const auto &kv : h->step_pool) pooled += (int)kv.second.size();
     out->pooled = pooled;
     out->max_active = h->max_active;
     return SARAS_OK;
@@ -1301,6 +1337,8 @@ saras_status saras_serve_destroy(saras_serve *h) {
     }
     for (auto &kv : h->pool)
         for (saras_mg *m : kv.second) saras_mg_destroy(m);
+    for (auto &kv : h->step_pool)
+        for (saras_rk3 *rk : kv.second) saras_rk3_destroy(rk);
     drop_graphs(h);
     cudaFree(h->d_lev);
     cudaFree(h->d_items);

@@ -4,8 +4,9 @@ batch next to Poisson requests.
 
 Bars: a step request's fields are bit-for-bit the same alone, in a mix with
 Poisson and other step requests, and the same as saras_rk3_step on a handle
-whose multigrid is the MIXED form with the engine's parameters; the Poisson
-requests of the mix keep their alone results.
+whose multigrid is the MIXED form with the engine's smoothing and coarsest
+tolerance and the request's own Residual Tolerance and V-Cycle Count; the
+Poisson requests of the mix keep their alone results.
 """
 import numpy as np
 import pytest
@@ -16,8 +17,10 @@ from test_gpu_rk3 import initial_fields, rbc_params
 
 pytestmark = pytest.mark.gpu
 
-TOL, CAP = 1e-6, 40
-ENGINE = dict(tolerance=TOL, max_cycles=CAP, mg_tolerance=1e-2, pre_smooth=3, post_smooth=6, max_cases=16)
+# the engine's form, smoothing and coarsest tolerance; step requests stop
+# their pressure solves at their own Residual Tolerance / V-Cycle Count
+ENGINE = dict(tolerance=1e-9, max_cycles=400, mg_tolerance=1e-9, pre_smooth=3, post_smooth=6, max_cases=16)
+STEP_TOL, STEP_CAP = 1e-6, 20
 STEPS = [
     dict(gk=dict(n=(16, 16, 16), mesh="DDD", beta=(1.1, 1.2, 1.3), domain="NNN"), amp=0.05, pk={}),
     dict(gk=dict(n=(16, 16, 32), mesh="UUD", beta=(1, 1, 1.3), domain="PPN", pad=2), amp=0.05,
@@ -32,14 +35,15 @@ POISSON = [dict(n=(32, 32, 32), mesh="UUD", beta=(1, 1, 1.2), domain="NNN"),
 def _step_request(q):
     c = STEPS[q]
     g = S.grid_desc(**c["gk"])
-    prm = rbc_params(g, **c["pk"])
+    prm = rbc_params(g, vc_tol=STEP_TOL, **c["pk"])
+    prm.mg.vc_count = STEP_CAP
     return g, prm, initial_fields(g, 20 + q, c["amp"])
 
 
 def _alone_handle(q):
     """saras_rk3_step with the engine's multigrid parameters."""
     g, prm, f = _step_request(q)
-    prm.mg = S.mg_params(precision=S.PREC_MIXED, vc_count=CAP, vc_tolerance=TOL, mg_tolerance=1e-2,
+    prm.mg = S.mg_params(precision=S.PREC_MIXED, vc_count=STEP_CAP, vc_tolerance=STEP_TOL, mg_tolerance=1e-9,
                          pre_smooth=3, post_smooth=6)
     rk = S.RK3(g, prm)
     rk.upload(f["vx"], f["vy"], f["vz"], f["p"], f["t"], f["pp"])
@@ -111,3 +115,31 @@ def test_step_request_over_budget():
     done = eng.run()
     eng.close()
     assert done[0]["status"] == S.BUDGET
+
+
+def test_step_request_bad_solve_keys():
+    g, prm, f = _step_request(0)
+    prm.mg.vc_count = 0
+    eng = S.Serve(S.serve_params(**ENGINE))
+    with pytest.raises(S.SarasError):
+        eng.submit_step(3, g, prm, f)
+    eng.close()
+
+
+def test_pooled_integrator_gives_same_results(alone):
+    """A second request of the same shape reuses the first one's integrator
+    (re-pointed at its stretching and parameters): results unchanged."""
+    eng = S.Serve(S.serve_params(**ENGINE))
+    g0, prm0, f0 = _step_request(0)
+    g1 = S.grid_desc(**dict(STEPS[0]["gk"], beta=(1.3, 1.1, 1.2)))
+    prm1 = rbc_params(g1, vc_tol=STEP_TOL)
+    prm1.mg.vc_count = STEP_CAP
+    f1 = initial_fields(g1, 5, 0.05)
+    eng.submit_step(1, g1, prm1, f1)
+    assert eng.run()[0]["id"] == 1
+    assert eng.stats()["pooled"] == 1
+    eng.submit_step(2, g0, prm0, f0)
+    assert eng.run()[0]["id"] == 2
+    eng.close()
+    for k in f0:
+        assert np.array_equal(f0[k], alone[0][k]), k
