@@ -55,6 +55,26 @@ inline Lay make_lay(int n0, int n1, int n2) {
     return l;
 }
 
+// Exact coarsest solve of the MIXED form by fast diagonalisation: per axis
+// the eigenvectors V (row i, column mode), V^-1 (row mode) and eigenvalues
+// of the level's 1-D operator (coarse_fd.cpp).  ok = 0: red-black sweeps.
+constexpr int FD_MAX_CELLS = 4096;
+constexpr int FD_MAX_N = 64;
+struct FDiag {
+    const double *v[3], *vi[3], *lam[3];
+    double lam_tol;  // |eigenvalue sum| at or below this is the null mode
+    int ok;
+};
+inline int64_t fd_elems(const Lay &L) {
+    const int n[3] = {L.n0, L.n1, L.n2};
+    int64_t e = 0;
+    for (int d = 0; d < 3; d++) e += 2 * (int64_t)n[d] * n[d] + n[d];
+    return e;
+}
+inline bool fd_fits(const Lay &L) {
+    return (int64_t)L.n0 * L.n1 * L.n2 <= FD_MAX_CELLS && L.n0 <= FD_MAX_N && L.n1 <= FD_MAX_N && L.n2 <= FD_MAX_N;
+}
+
 // FP64 with explicit rounding: these never contract into fused
 // multiply-adds, which keeps the exact kernels' results bit-identical to the
 // reference's separately rounded operations.

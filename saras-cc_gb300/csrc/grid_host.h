@@ -46,4 +46,12 @@ struct HostGrid {
 // Left null vector of the 1-D all-Neumann finest-level operator.
 void neumann_null_vector(const HostGrid &g, int axis, double *w);
 
+// Eigen-decomposition A = V diag(lam) V^-1 of the 1-D operator
+// cm u(i-1) + cp u(i+1) - 2 a2 u(i) of one axis with its ghost rule folded
+// in (periodic, or the mirrored sign sg_lo / sg_hi: +1 Neumann, -1
+// Dirichlet); V and Vi are n x n row major.  False when the operator is not
+// similar to a symmetric one through a diagonal scaling (coarse_fd.cpp).
+bool coarse_axis_eigen(int n, const double *cm, const double *cp, const double *a2, bool per, int sg_lo, int sg_hi,
+                       double *V, double *Vi, double *lam);
+
 }  // namespace saras

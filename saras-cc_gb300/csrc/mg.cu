@@ -769,7 +769,7 @@ void free_all(saras_mg *h) {
 // exact form's separate residual and smoothed copy, the FP32 error and
 // residual of MIXED's inner levels, and the stored omega/D and D.
 struct LevelArrays {
-    bool u_f, scratch, e_r32, inv_diag, dd;
+    bool u_f, scratch, e_r32, inv_diag, dd, fd;
 };
 
 LevelArrays level_arrays(int precision, int l, int nl) {
@@ -781,6 +781,7 @@ LevelArrays level_arrays(int precision, int l, int nl) {
     a.e_r32 = mixed && !coarsest;
     a.inv_diag = fast || (mixed && coarsest);
     a.dd = fast || (mixed && (l == 0 || coarsest));
+    a.fd = mixed && coarsest;
     return a;
 }
 
@@ -828,6 +829,7 @@ saras_status create(const saras_grid_desc *gd, const saras_mg_params *prm, void 
         }
         if (use.inv_diag) SARAS_TRY(dalloc(h, &v.inv_diag, sz));
         if (use.dd) SARAS_TRY(dalloc(h, &v.dd, sz));
+        if (use.fd && fd_fits(v.lay)) SARAS_TRY(dalloc(h, &v.fd, fd_elems(v.lay)));
     }
     SARAS_TRY(build_tables(h));
     SARAS_TRY(build_walls(h));
@@ -1003,6 +1005,7 @@ int64_t mg_estimate_bytes(const saras_grid_desc *gd, const saras_mg_params *prm)
         if (l == 0) cells0 = (int64_t)L.n0 * L.n1 * L.n2;
         const LevelArrays u = level_arrays(prm->precision, l, g.levels);
         bytes += L.size * (16 * u.u_f + 16 * u.scratch + 8 * u.e_r32 + 8 * u.inv_diag + 8 * u.dd);
+        if (u.fd && fd_fits(L)) bytes += 8 * fd_elems(L);
         bytes += (int64_t)10 * (L.n0 + L.n1 + L.n2) * 12;  // 1-D tables, FP64 and FP32
         if (l == 0) {
             bool walls = false;
@@ -1252,6 +1255,7 @@ saras_status mg_solve_in_scratch(const saras_grid_desc *gd, const saras_mg_param
         }
         if (use.inv_diag) take(&v.inv_diag, sz);
         if (use.dd) take(&v.dd, sz);
+        if (use.fd && fd_fits(v.lay)) take(&v.fd, fd_elems(v.lay));
         const int64_t total = (int64_t)10 * (v.lay.n0 + v.lay.n1 + v.lay.n2);
         take(&v.tab, total);
         take(&v.tab32, total);

@@ -344,6 +344,15 @@ __global__ void k_coarsest_fast(double *ug, const double *__restrict__ fg, const
     if (threadIdx.x == 0) *sweeps_out += sweeps;
 }
 
+// Exact coarsest solve of the MIXED form (fd_solve), one block; dynamic
+// shared memory holds two copies of the coarsest grid.
+__global__ void k_coarsest_fd(double *ug, const double *__restrict__ fg, Lay L, FDiag F) {
+    pdl_enter();
+    extern __shared__ double fds[];
+    const int ncell = L.n0 * L.n1 * L.n2;
+    fd_solve(ug, fg, L, F, fds, fds + ncell);
+}
+
 // u += e over the core (MIXED form update, FP64 accumulate).
 __global__ void k_update64(double *__restrict__ u, const float *__restrict__ e, Lay L) {
     pdl_enter();
@@ -695,6 +704,61 @@ void csum(saras_mg *h, cudaStream_t s, const double *u, int slot) {
 
 namespace saras {
 
+// Tables of the MIXED form's exact coarsest solve: per axis the
+// eigen-decomposition of the coarsest level's 1-D operator (coefficients as
+// build_tables forms them, the handle's ghost rule folded in).  An axis that
+// cannot be decomposed (a stretched periodic axis) leaves the red-black
+// sweeps in place.
+saras_status build_fd(saras_mg *h) {
+    Level &c = h->lv[(size_t)h->nl - 1];
+    c.fdv = FDiag{};
+    if (!c.fd || h->prm.precision != SARAS_PREC_MIXED) return SARAS_OK;
+    const HostGrid &g = h->grid;
+    const int l = h->nl - 1;
+    const int n[3] = {c.lay.n0, c.lay.n1, c.lay.n2};
+    std::vector<double> host((size_t)fd_elems(c.lay), 0.0);
+    FDiag f{};
+    size_t off = 0;
+    double lmax = 0.0;
+    for (int d = 0; d < 3; d++) {
+        const size_t nn = (size_t)n[d] * n[d];
+        double *V = host.data() + off, *Vi = V + nn, *lam = Vi + nn;
+        if (!g.active(d)) {
+            V[0] = 1.0;
+            Vi[0] = 1.0;
+            lam[0] = 0.0;
+        } else {
+            const AxisLevel &a = g.lv[(size_t)l][(size_t)d];
+            const double hx = (1 << l) * g.dxi[d];
+            const double ih2 = 1.0 / std::pow(hx, 2), i2h = 0.5 / hx;
+            std::vector<double> cm((size_t)n[d]), cp((size_t)n[d]), a2((size_t)n[d]);
+            for (int i = 0; i < n[d]; i++) {
+                const double A2 = a.at(a.xix2, i) * ih2, A1 = a.at(a.xixx, i) * i2h;
+                cm[(size_t)i] = A2 - A1;
+                cp[(size_t)i] = A2 + A1;
+                a2[(size_t)i] = A2;
+            }
+            const int sl = h->ghost.kind[2 * d] == SARAS_BC_NEUMANN ? 1 : -1;
+            const int sh = h->ghost.kind[2 * d + 1] == SARAS_BC_NEUMANN ? 1 : -1;
+            if (!coarse_axis_eigen(n[d], cm.data(), cp.data(), a2.data(), h->ghost.per[d] != 0, sl, sh, V, Vi, lam))
+                return SARAS_OK;
+        }
+        double m = 0.0;
+        for (int k = 0; k < n[d]; k++) m = std::max(m, std::fabs(lam[k]));
+        lmax += m;
+        f.v[d] = c.fd + off;
+        f.vi[d] = c.fd + off + nn;
+        f.lam[d] = c.fd + off + 2 * nn;
+        off += 2 * nn + (size_t)n[d];
+    }
+    // pageable source: staged before the call returns, ordered on the stream
+    SARAS_CUDA(cudaMemcpyAsync(c.fd, host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    f.lam_tol = 1e-9 * lmax;
+    f.ok = 1;
+    c.fdv = f;
+    return SARAS_OK;
+}
+
 saras_status fast_setup(saras_mg *h) {
     for (int f = 0; f < 6; f++)
         if (h->prm.bc_kind[f] == SARAS_BC_DIRICHLET_TEST) {
@@ -715,6 +779,9 @@ saras_status fast_setup(saras_mg *h) {
     }
     if (h->prm.precision == SARAS_PREC_MIXED)
         for (int l = 0; l < h->nl; l++) tma_plan(h, h->lv[(size_t)l]);
+    SARAS_TRY(build_fd(h));
+    SARAS_CUDA(cudaFuncSetAttribute(k_coarsest_fd, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    2 * FD_MAX_CELLS * (int)sizeof(double)));
     SARAS_CUDA(cudaFuncSetAttribute(k_coarsest_fast<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     200 * 1024));
     SARAS_CUDA(cudaFuncSetAttribute(k_coarsest_fast<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -782,6 +849,15 @@ void rhs_norm(saras_mg *h, cudaStream_t s) {
 
 void coarsest_fast(saras_mg *h, cudaStream_t s, Level &c) {
     const Lay &C = c.lay;
+    if (h->prm.precision == SARAS_PREC_MIXED && c.fdv.ok) {
+        // the MIXED form solves its coarsest level exactly (fd_solve)
+        const int64_t cells = (int64_t)C.n0 * C.n1 * C.n2;
+        const int threads = cells <= 512 ? 64 : 256;
+        kbegin(h, s, KC_COARSE);
+        launch_pdl(k_coarsest_fd, 1, threads, (size_t)(2 * cells) * sizeof(double), s, c.lhs, c.rhs, C, c.fdv);
+        kend(h, s, KC_COARSE);
+        return;
+    }
     const size_t smem = (size_t)(4 * C.size) * sizeof(double);
     if (smem > 200 * 1024) {  // coarsest grid too large for one block's shared memory
         cudaMemsetAsync(c.lhs, 0, (size_t)C.size * sizeof(double), s);

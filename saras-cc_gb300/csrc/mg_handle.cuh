@@ -44,6 +44,8 @@ struct Level {
     double *inv_diag = nullptr;  // FP64 form: omega / D per cell
     double *dd = nullptr;        // FP64 forms: the diagonal D = 2 sum(xix2*ihx2) per cell
     float *inv_diag32 = nullptr; // MIXED form: omega / D per cell
+    double *fd = nullptr;        // MIXED form, coarsest level: V, V^-1, eigenvalues per axis
+    FDiag fdv{};                 // their device view; fdv.ok = 0: red-black sweeps
     TmaPlan tma{};
 };
 

@@ -36,6 +36,63 @@ constexpr int COARSE_STALL_CHECK = 8;
 __device__ __forceinline__ float sweep_div(float a, float b) { return __fdividef(a, b); }
 __device__ __forceinline__ double sweep_div(double a, double b) { return a / b; }
 
+// out = M applied along axis a of the dense n0 x n1 x n2 block `in`: for
+// every cell, sum over m of M[o][m] * in(index m along a), o the cell's own
+// index along a.  One thread per output cell, a fixed summation order.
+__device__ __forceinline__ void fd_apply(const double *in, double *out, const double *__restrict__ M, int a, int n0,
+                                         int n1, int n2) {
+    const int ncell = n0 * n1 * n2;
+    const int na = a == 0 ? n0 : (a == 1 ? n1 : n2);
+    const int st = a == 0 ? n1 * n2 : (a == 1 ? n2 : 1);
+    for (int q = threadIdx.x; q < ncell; q += blockDim.x) {
+        const int o = (q / st) % na;
+        const int base = q - o * st;
+        const double *row = M + (int64_t)o * na;
+        double s = 0.0;
+        for (int m = 0; m < na; m++) s = fmat(row[m], in[base + m * st], s);
+        out[q] = s;
+    }
+}
+
+// Exact coarsest solve of the MIXED form (one block): u = (Vx (x) Vy (x) Vz)
+// L^-1 (Vx^-1 (x) Vy^-1 (x) Vz^-1) f with the eigenvalue sums L; the null
+// mode of a singular (all-Neumann or periodic) box is dropped, and with it
+// the part of f outside the operator's range.  ug gets zero ghosts, as the
+// sweeps leave them.  sa, sb: two buffers of n0*n1*n2 doubles.
+__device__ __forceinline__ void fd_solve(double *ug, const double *fg, const Lay &L, const FDiag &F, double *sa,
+                                         double *sb) {
+    const int n0 = L.n0, n1 = L.n1, n2 = L.n2, ncell = n0 * n1 * n2;
+    for (int q = threadIdx.x; q < ncell; q += blockDim.x) {
+        const int k = q % n2, rest = q / n2, j = rest % n1, i = rest / n1;
+        sa[q] = fg[L.at(i, j, k)];
+    }
+    __syncthreads();
+    fd_apply(sa, sb, F.vi[2], 2, n0, n1, n2);
+    __syncthreads();
+    fd_apply(sb, sa, F.vi[1], 1, n0, n1, n2);
+    __syncthreads();
+    fd_apply(sa, sb, F.vi[0], 0, n0, n1, n2);
+    __syncthreads();
+    for (int q = threadIdx.x; q < ncell; q += blockDim.x) {
+        const int k = q % n2, rest = q / n2, j = rest % n1, i = rest / n1;
+        const double lam = (F.lam[0][i] + F.lam[1][j]) + F.lam[2][k];
+        sb[q] = fabs(lam) > F.lam_tol ? sb[q] / lam : 0.0;
+    }
+    __syncthreads();
+    fd_apply(sb, sa, F.v[0], 0, n0, n1, n2);
+    __syncthreads();
+    fd_apply(sa, sb, F.v[1], 1, n0, n1, n2);
+    __syncthreads();
+    fd_apply(sb, sa, F.v[2], 2, n0, n1, n2);
+    __syncthreads();
+    for (int64_t q = threadIdx.x; q < L.size; q += blockDim.x) ug[q] = 0.0;
+    __syncthreads();
+    for (int q = threadIdx.x; q < ncell; q += blockDim.x) {
+        const int k = q % n2, rest = q / n2, j = rest % n1, i = rest / n1;
+        ug[L.at(i, j, k)] = sa[q];
+    }
+}
+
 template <class T>
 __device__ __forceinline__ T nb_lo(const T *u, int64_t c, int i, int n, int64_t s, int per, int sg, T uc) {
     if (i > 0) return u[c - s];

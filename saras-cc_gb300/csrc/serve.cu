@@ -57,6 +57,7 @@ struct BLev {
     int top;                  // this level is the case's coarsest (FP64)
     int max_count;            // coarsest iteration limit
     int sweep_only;           // > 0: coarsest too large for one block; plain sweeps
+    FDiag fd;                 // exact coarsest solve (fd.ok), as the single-problem MIXED form
     double tol;
     float w, omc;
     double omc64;
@@ -236,11 +237,17 @@ __global__ void __launch_bounds__(512) kb_restrict(const BItem *__restrict__ ite
 __global__ void kb_coarsest(const BItem *__restrict__ items, const int *__restrict__ count,
                             const BLev *__restrict__ lv) {
     __shared__ unsigned long long shm[32];
+    extern __shared__ double fds[];
     const int n = *count;
     for (int it = blockIdx.x; it < n; it += gridDim.x) {
         const BLev &L = lv[items[it].lev];
         const Lay &Y = L.lay;
         const int ncell = Y.n0 * Y.n1 * Y.n2;
+        if (L.fd.ok) {
+            fd_solve(L.u, L.f, Y, L.fd, fds, fds + FD_MAX_CELLS);
+            __syncthreads();
+            continue;
+        }
         for (int q = threadIdx.x; q < ncell; q += blockDim.x) {
             const int k = q % Y.n2, rest = q / Y.n2, j = rest % Y.n1, i = rest / Y.n1;
             L.u[Y.at(i, j, k)] = 0.0;
@@ -613,6 +620,7 @@ BLev level_desc(const saras_mg *m, int l) {
     d.t64 = Tab3<double>{{v.cm[0], v.cm[1], v.cm[2]}, {v.cp[0], v.cp[1], v.cp[2]}, {v.dg[0], v.dg[1], v.dg[2]}};
     d.b = bnd_of(m);
     d.top = l == m->nl - 1 ? 1 : 0;
+    d.fd = d.top ? v.fdv : FDiag{};
     d.max_count = m->maxCount();
     d.sweep_only = 0;
     if (d.top && (size_t)(4 * v.lay.size) * sizeof(double) > COARSE_SMEM_CAP)
@@ -681,7 +689,8 @@ int64_t issue_batched(saras_serve *h, cudaStream_t s, int depth) {
     sweeps(0, pre);
     for (int l = 0; l + 1 < depth; l++) {
         kb_restrict<<<B, T, 0, s>>>(items(REG_RESTRICT + l), cnt(REG_RESTRICT + l), h->d_lev);
-        kb_coarsest<<<B, COARSE_THREADS, 0, s>>>(items(REG_TOP + l + 1), cnt(REG_TOP + l + 1), h->d_lev);
+        kb_coarsest<<<B, COARSE_THREADS, 2 * FD_MAX_CELLS * sizeof(double), s>>>(items(REG_TOP + l + 1),
+                                                                                  cnt(REG_TOP + l + 1), h->d_lev);
         n += 2;
         if (l + 2 < depth) {
             kb_zero<<<B, T, 0, s>>>(items(REG_SMOOTH + l + 1), cnt(REG_SMOOTH + l + 1), h->d_lev);
@@ -1130,6 +1139,13 @@ saras_status saras_serve_create(const saras_serve_params *prm, saras_serve **out
         set_error("serving engine tables could not be allocated");
         saras_serve_destroy(h);
         return SARAS_OOM;
+    }
+    if (cudaFuncSetAttribute(kb_coarsest, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             2 * FD_MAX_CELLS * (int)sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("serving coarsest-solve kernel configuration failed");
+        saras_serve_destroy(h);
+        return SARAS_CUDA_ERR;
     }
     for (int s = prm->max_cases - 1; s >= 0; s--) h->free_slots.push_back(s);
     *out = h;
