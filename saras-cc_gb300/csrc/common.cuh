@@ -60,6 +60,8 @@ inline Lay make_lay(int n0, int n1, int n2) {
 // of the level's 1-D operator (coarse_fd.cpp).  ok = 0: red-black sweeps.
 constexpr int FD_MAX_CELLS = 4096;
 constexpr int FD_MAX_N = 64;
+constexpr double FD_TOL_MAX = 1e-9;  // coarsest tolerances at or below this take the exact solve
+constexpr int FD_MIN_CELLS = 512;    // ... on coarsest levels of at least this many cells
 struct FDiag {
     const double *v[3], *vi[3], *lam[3];
     double lam_tol;  // |eigenvalue sum| at or below this is the null mode
@@ -72,7 +74,9 @@ inline int64_t fd_elems(const Lay &L) {
     return e;
 }
 inline bool fd_fits(const Lay &L) {
-    return (int64_t)L.n0 * L.n1 * L.n2 <= FD_MAX_CELLS && L.n0 <= FD_MAX_N && L.n1 <= FD_MAX_N && L.n2 <= FD_MAX_N;
+    const int64_t cells = (int64_t)L.n0 * L.n1 * L.n2;
+    return cells >= FD_MIN_CELLS && cells <= FD_MAX_CELLS && L.n0 <= FD_MAX_N && L.n1 <= FD_MAX_N &&
+           L.n2 <= FD_MAX_N;
 }
 
 // FP64 with explicit rounding: these never contract into fused

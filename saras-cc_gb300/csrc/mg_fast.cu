@@ -706,13 +706,19 @@ namespace saras {
 
 // Tables of the MIXED form's exact coarsest solve: per axis the
 // eigen-decomposition of the coarsest level's 1-D operator (coefficients as
-// build_tables forms them, the handle's ghost rule folded in).  An axis that
-// cannot be decomposed (a stretched periodic axis) leaves the red-black
-// sweeps in place.
+// build_tables forms them, the handle's ghost rule folded in).  The exact
+// solve stands in for sweeps run to a tight coarsest tolerance (at most
+// FD_TOL_MAX) on a coarsest level of FD_MIN_CELLS or more cells, where the
+// sweeps cost the most (12x12x6: about ten times the whole rest of the
+// cycle) for the same outer iterations.  A looser tolerance keeps the sweeps,
+// whose early stop damps the injection-prolonged correction (128^3,
+// tolerance 1e-6: 4 outer iterations with the sweeps, 6 with the exact
+// solve); so do small coarsest levels, where sweeps are cheap, and an axis
+// that cannot be decomposed (a stretched periodic axis).
 saras_status build_fd(saras_mg *h) {
     Level &c = h->lv[(size_t)h->nl - 1];
     c.fdv = FDiag{};
-    if (!c.fd || h->prm.precision != SARAS_PREC_MIXED) return SARAS_OK;
+    if (!c.fd || h->prm.precision != SARAS_PREC_MIXED || h->prm.mg_tolerance > FD_TOL_MAX) return SARAS_OK;
     const HostGrid &g = h->grid;
     const int l = h->nl - 1;
     const int n[3] = {c.lay.n0, c.lay.n1, c.lay.n2};

@@ -148,10 +148,11 @@ def test_mixed_converges_to_oracle(name, gk, mk):
 
 def test_mixed_tracks_fp64_cycle_by_cycle():
     """One MIXED outer iteration is the FP64 V-cycle applied to the error
-    equation: the residual histories agree until FP32 rounding shows."""
+    equation: the residual histories agree until FP32 rounding shows (a
+    coarsest tolerance above 1e-9, so both forms sweep the coarsest level)."""
     g = S.grid_desc(n=(32, 32, 32), mesh="UUD", beta=(1, 1, 1.3), domain="NNN")
     rhs = random_rhs(g, 6)
-    kw = dict(vc_count=8, vc_tolerance=1e-30, pre_smooth=2, post_smooth=2, mg_tolerance=1e-12)
+    kw = dict(vc_count=8, vc_tolerance=1e-30, pre_smooth=2, post_smooth=2, mg_tolerance=1e-8)
     h = []
     for prec in (S.PREC_FP64, S.PREC_MIXED):
         mg = S.Multigrid(g, S.mg_params(precision=prec, **kw))
@@ -159,6 +160,35 @@ def test_mixed_tracks_fp64_cycle_by_cycle():
         mg.mg_solve(lhs, rhs)
         h.append(mg.history.copy())
     np.testing.assert_allclose(h[1], h[0], rtol=1e-4)
+
+
+def test_mixed_exact_coarsest_solve():
+    """With a coarsest tolerance of 1e-9 or tighter and a coarsest level of
+    512 cells or more, the MIXED form solves its coarsest level exactly (fast
+    diagonalisation): it takes no more outer iterations than with the sweeps
+    (a 1e-8 coarsest tolerance keeps them) and converges to the oracle's FP64
+    solution to 5e-9."""
+    # 12 x 12 x 6 coarsest levels (at least 512 cells take the exact solve)
+    for gk in (dict(n=(96, 96, 48), length=(1, 1, 0.5), mesh="UUD", beta=(1, 1, 1.25), domain="NNN"),
+               dict(n=(96, 96, 48), length=(1, 1, 0.5), mesh="DUD", beta=(1.2, 1, 1.1), domain="NNN")):
+        g = S.grid_desc(**gk)
+        rhs = random_rhs(g, 8)
+        kw = dict(vc_count=200, vc_tolerance=1e-10, pre_smooth=3, post_smooth=6, mg_tolerance=1e-12)
+        mix = S.padded_field(g)
+        mg = S.Multigrid(g, S.mg_params(precision=S.PREC_MIXED, **kw))
+        assert mg.mg_solve(mix, rhs) == S.OK, gk
+        exact_cycles = mg.cycles
+        mg.close()
+        swp = S.padded_field(g)
+        mg = S.Multigrid(g, S.mg_params(precision=S.PREC_MIXED, **dict(kw, mg_tolerance=1e-8)))
+        assert mg.mg_solve(swp, rhs) == S.OK, gk
+        assert exact_cycles <= mg.cycles, (gk, exact_cycles, mg.cycles)
+        mg.close()
+        orc = S.padded_field(g)
+        r = O.mg_solve(g, S.mg_params(**dict(kw, vc_tolerance=1e-12)), orc, rhs)
+        a, b = demean(core(mix, g)), demean(core(orc, g))
+        # a 1e-10 relative residual bounds the solution error to a few 1e-9
+        assert np.abs(a - b).max() <= 5e-9 * np.abs(b).max(), gk
 
 
 @pytest.mark.parametrize("inner", [4, 16])
