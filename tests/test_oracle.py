@@ -182,3 +182,14 @@ def test_golden_fixtures():
         # fixtures are recorded on x86-64; libm's tanh/pow may differ in the
         # last bit on other hosts
         np.testing.assert_allclose(b, a, rtol=1e-9, atol=1e-14, err_msg=k)
+
+
+@pytest.mark.parametrize("n,dims", [((2, 2, 2), 3), ((3, 5, 7), 3), ((2, 1, 2), 2), ((4, 4, 4), 3),
+                                    ((6, 6, 6), 3), ((64, 8, 16), 3), ((8, 1, 8), 2), ((96, 96, 48), 3)])
+def test_depth_rule_and_rejected_sizes(n, dims):
+    """setVCDepth (grid.cc:678-742) on small, odd and ragged sizes: the
+    product's host-side depth equals the oracle's, and the sizes the
+    reference cannot build a hierarchy for are rejected by both (-1)."""
+    g = S.grid_desc(n=n, domain="NNN", dims=dims)
+    lib = S.load()
+    assert lib.saras_reference_levels(g) == O.num_levels(g)
