@@ -480,6 +480,8 @@ def run_serving(S, args):
         "model_hbm_GBps": model_bytes / makespan / 1e9 if done else None,
         "model_hbm_frac": model_bytes / makespan / 1e9 / hbm if done else None,
         "model_bytes_per_cell_cycle": SERVE_BYTES_PER_CELL,
+        "engine_seconds": {"batched_iterations": st["t_batch_s"], "admissions": st["t_admit_s"],
+                           "retirements": st["t_retire_s"], "time_step_host_phases": st["t_steps_s"]},
         "max_active": st["max_active"], "batched_cycles": st["batched_cycles"], "gpu_launches": st["launches"],
         "device_bytes_resident_peak": st["bytes_allocated"],
         "schedule": {"cells_per_item": chosen.cells_per_item, "threads": chosen.threads,

@@ -287,6 +287,11 @@ typedef struct saras_serve_stats {
     int64_t launches;        /* kernels launched by those graphs */
     int64_t admitted, retired;
     int32_t active, pending, pooled, max_active;
+    /* wall-clock seconds inside saras_serve_step: batched iterations (graph
+     * launch to its residuals on the host), admissions (uploads, hierarchy
+     * set-up), retirements (projection, copy out), and the host-driven parts
+     * of time-step requests (right-hand sides, CN sweeps, corrections) */
+    double t_batch_s, t_admit_s, t_retire_s, t_steps_s;
 } saras_serve_stats;
 
 typedef struct saras_serve saras_serve;

@@ -652,8 +652,11 @@ saras_status build_tables(saras_mg *h, bool async = false) {
             SARAS_CUDA(cudaMemcpyAsync(v.tab, st64, b64, cudaMemcpyHostToDevice, h->stream));
             SARAS_CUDA(cudaMemcpyAsync(v.tab32, st64 + b64, b32, cudaMemcpyHostToDevice, h->stream));
         } else {
-            SARAS_CUDA(cudaMemcpy(v.tab, host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice));
-            SARAS_CUDA(cudaMemcpy(v.tab32, host32.data(), host32.size() * sizeof(float), cudaMemcpyHostToDevice));
+            // pageable sources: staged before the calls return, ordered on the stream
+            SARAS_CUDA(cudaMemcpyAsync(v.tab, host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                       h->stream));
+            SARAS_CUDA(cudaMemcpyAsync(v.tab32, host32.data(), host32.size() * sizeof(float),
+                                       cudaMemcpyHostToDevice, h->stream));
         }
         v.coef = Coef{dp[0][0], dp[0][1], dp[1][0], dp[1][1], dp[2][0], dp[2][1]};
         v.rt = RTab{dp[0][5], dp[0][6], dp[0][7], dp[1][5], dp[1][6], dp[1][7], dp[2][5], dp[2][6], dp[2][7]};
@@ -714,7 +717,7 @@ saras_status build_walls(saras_mg *h) {
         }
     }
     SARAS_TRY(dalloc(h, &h->walls, (int64_t)w.size()));
-    SARAS_CUDA(cudaMemcpy(h->walls, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice));
+    SARAS_CUDA(cudaMemcpyAsync(h->walls, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     h->ghost.wallx = h->walls;
     h->ghost.wally = h->walls + nx;
     h->ghost.wallz = h->walls + nx + ny;
@@ -785,7 +788,28 @@ LevelArrays level_arrays(int precision, int l, int nl) {
     return a;
 }
 
-saras_status create(const saras_grid_desc *gd, const saras_mg_params *prm, void *stream, saras_mg *h) {
+// Pinned staging of the level tables (and exact-solve tables): their
+// uploads are then asynchronous, never waiting for work already queued on
+// the handle's stream.
+saras_status ensure_tab_stage(saras_mg *h) {
+    if (!h->tab_stage) {
+        size_t bytes = 0;
+        for (const Level &v : h->lv) bytes += (size_t)10 * (v.lay.n0 + v.lay.n1 + v.lay.n2) * 12 + 512;
+        const Level &top = h->lv.back();
+        if (top.fd) bytes += (size_t)fd_elems(top.lay) * sizeof(double) + 256;  // exact-solve tables
+        SARAS_CUDA(cudaMallocHost((void **)&h->tab_stage, bytes));
+        h->tab_stage_bytes = bytes;
+    }
+    h->tab_stage_used = 0;
+    return SARAS_OK;
+}
+
+// `wait`: return with the set-up complete on the handle's stream.  Without
+// it the set-up stays queued on that stream (ordered before any later work
+// the caller puts there), so creating a handle never waits for other work
+// already queued on the stream.
+saras_status create(const saras_grid_desc *gd, const saras_mg_params *prm, void *stream, saras_mg *h,
+                    bool wait = true) {
     SARAS_TRY(check_params(*prm));
     h->prm = *prm;
     SARAS_TRY(h->grid.build(*gd, prm->levels));
@@ -814,8 +838,8 @@ saras_status create(const saras_grid_desc *gd, const saras_mg_params *prm, void 
         if (use.u_f) {
             SARAS_TRY(dalloc(h, &v.lhs, sz));
             SARAS_TRY(dalloc(h, &v.rhs, sz));
-            SARAS_CUDA(cudaMemset(v.lhs, 0, (size_t)sz * sizeof(double)));
-            SARAS_CUDA(cudaMemset(v.rhs, 0, (size_t)sz * sizeof(double)));
+            SARAS_CUDA(cudaMemsetAsync(v.lhs, 0, (size_t)sz * sizeof(double), h->stream));
+            SARAS_CUDA(cudaMemsetAsync(v.rhs, 0, (size_t)sz * sizeof(double), h->stream));
         }
         if (use.scratch) {
             SARAS_TRY(dalloc(h, &v.tmp, sz));
@@ -824,14 +848,15 @@ saras_status create(const saras_grid_desc *gd, const saras_mg_params *prm, void 
         if (use.e_r32) {
             SARAS_TRY(dalloc(h, &v.e32, sz));
             SARAS_TRY(dalloc(h, &v.r32, sz));
-            SARAS_CUDA(cudaMemset(v.e32, 0, (size_t)sz * sizeof(float)));
-            SARAS_CUDA(cudaMemset(v.r32, 0, (size_t)sz * sizeof(float)));
+            SARAS_CUDA(cudaMemsetAsync(v.e32, 0, (size_t)sz * sizeof(float), h->stream));
+            SARAS_CUDA(cudaMemsetAsync(v.r32, 0, (size_t)sz * sizeof(float), h->stream));
         }
         if (use.inv_diag) SARAS_TRY(dalloc(h, &v.inv_diag, sz));
         if (use.dd) SARAS_TRY(dalloc(h, &v.dd, sz));
         if (use.fd && fd_fits(v.lay)) SARAS_TRY(dalloc(h, &v.fd, fd_elems(v.lay)));
     }
-    SARAS_TRY(build_tables(h));
+    SARAS_TRY(ensure_tab_stage(h));
+    SARAS_TRY(build_tables(h, true));
     SARAS_TRY(build_walls(h));
     const Lay &L0 = h->lv[0].lay;
     const int64_t cells = (int64_t)L0.n0 * L0.n1 * L0.n2;
@@ -840,8 +865,8 @@ saras_status create(const saras_grid_desc *gd, const saras_mg_params *prm, void 
     SARAS_TRY(dalloc(h, &h->norm_out, 8));
     SARAS_TRY(dalloc(h, &h->coarse_sweeps, 4));
     SARAS_TRY(dalloc(h, &h->mix_scalar, 16));
-    SARAS_CUDA(cudaMemset(h->coarse_sweeps, 0, 4 * sizeof(int)));
-    SARAS_CUDA(cudaMemset(h->norm_out, 0, 8 * sizeof(double)));
+    SARAS_CUDA(cudaMemsetAsync(h->coarse_sweeps, 0, 4 * sizeof(int), h->stream));
+    SARAS_CUDA(cudaMemsetAsync(h->norm_out, 0, 8 * sizeof(double), h->stream));
     SARAS_CUDA(cudaMallocHost((void **)&h->norm_host, 8 * sizeof(double)));
     // Dense padded box of a caller field for the host entry point.
     const int p = h->grid.pad, py = h->d3 ? p : 1;
@@ -855,7 +880,9 @@ saras_status create(const saras_grid_desc *gd, const saras_mg_params *prm, void 
     SARAS_CUDA(cudaFuncSetAttribute(k_coarsest_exact<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)COARSE_SMEM_LIMIT));
     if (prm->precision != SARAS_PREC_FP64_EXACT) SARAS_TRY(fast_setup(h));
-    SARAS_CUDA(cudaDeviceSynchronize());
+    // everything above is ordered on the handle's stream: wait for it alone,
+    // not for other work on the device (a serving batch keeps running)
+    if (wait) SARAS_CUDA(cudaStreamSynchronize(h->stream));
     return SARAS_OK;
 }
 
@@ -1030,16 +1057,27 @@ saras_status mg_retarget(saras_mg *h, const saras_grid_desc *gd) {
     if (g.levels != h->nl || g.dims != h->grid.dims || g.pad != h->grid.pad) return SARAS_BAD_ARG;
     for (int d = 0; d < 3; d++)
         if (g.N[d] != h->grid.N[d] || g.per[d] != h->grid.per[d]) return SARAS_BAD_ARG;
-    if (!h->tab_stage) {
-        size_t bytes = 0;
-        for (const Level &v : h->lv) bytes += (size_t)10 * (v.lay.n0 + v.lay.n1 + v.lay.n2) * 12 + 512;
-        SARAS_CUDA(cudaMallocHost((void **)&h->tab_stage, bytes));
-        h->tab_stage_bytes = bytes;
-    }
-    h->tab_stage_used = 0;
+    SARAS_TRY(ensure_tab_stage(h));
     h->grid = g;
     SARAS_TRY(build_tables(h, true));
     return fast_setup(h);
+}
+
+// saras_mg_create whose set-up stays queued on `stream` (serving
+// admissions: the handle's later work is ordered behind it on that stream).
+saras_status mg_create_queued(const saras_grid_desc *gd, const saras_mg_params *prm, void *stream,
+                              saras_mg **out) {
+    *out = nullptr;
+    saras_mg *h = new saras_mg();
+    saras_status s = create(gd, prm, stream, h, false);
+    if (s != SARAS_OK) {
+        if (h->stream) cudaStreamSynchronize(h->stream);
+        free_all(h);
+        delete h;
+        return s;
+    }
+    *out = h;
+    return SARAS_OK;
 }
 
 // Finest-level fields of a resident handle: zero initial guess and the RHS

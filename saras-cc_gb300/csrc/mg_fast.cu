@@ -14,6 +14,7 @@
 // null-space projection (compensated sums) are FP64.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 #include <math_constants.h>
@@ -757,8 +758,17 @@ saras_status build_fd(saras_mg *h) {
         f.lam[d] = c.fd + off + 2 * nn;
         off += 2 * nn + (size_t)n[d];
     }
-    // pageable source: staged before the call returns, ordered on the stream
-    SARAS_CUDA(cudaMemcpyAsync(c.fd, host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    const size_t bytes = host.size() * sizeof(double);
+    if (h->tab_stage && h->tab_stage_bytes >= h->tab_stage_used + bytes) {
+        // pinned staging of a re-pointed handle: no wait for the stream
+        char *st = h->tab_stage + h->tab_stage_used;
+        std::memcpy(st, host.data(), bytes);
+        h->tab_stage_used += (bytes + 255) / 256 * 256;
+        SARAS_CUDA(cudaMemcpyAsync(c.fd, st, bytes, cudaMemcpyHostToDevice, h->stream));
+    } else {
+        // pageable source: staged before the call returns, ordered on the stream
+        SARAS_CUDA(cudaMemcpyAsync(c.fd, host.data(), bytes, cudaMemcpyHostToDevice, h->stream));
+    }
     f.lam_tol = 1e-9 * lmax;
     f.ok = 1;
     c.fdv = f;

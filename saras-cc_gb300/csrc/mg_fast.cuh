@@ -30,6 +30,8 @@ saras_status mg_retarget(saras_mg *h, const saras_grid_desc *gd);
 saras_status mg_load_rhs(saras_mg *h, const double *rhs_box_origin, const int64_t st[3]);
 void mg_store_lhs(saras_mg *h, double *box_origin, const int64_t st[3]);
 int64_t mg_estimate_bytes(const saras_grid_desc *gd, const saras_mg_params *prm);
+saras_status mg_create_queued(const saras_grid_desc *gd, const saras_mg_params *prm, void *stream,
+                              saras_mg **out);
 
 // rk3.cu: the time step in halves around its pressure solves, for the
 // serving engine, which runs those solves in its batch

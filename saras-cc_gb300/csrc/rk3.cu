@@ -1013,7 +1013,8 @@ saras_status rk3_configure(saras_rk3 *h, const saras_grid_desc *gd, const saras_
         }
         off += NT * (int64_t)n[d];
     }
-    SARAS_CUDA(cudaMemcpy(h->tab, host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice));
+    // pageable source: staged before the call returns, ordered on the stream
+    SARAS_CUDA(cudaMemcpyAsync(h->tab, host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     // vfield::vfield / sfield::sfield (vfield.cc:107-130): first-order
     // upwinding for dScheme 1, omega = "Central Bias"
     const double omega = p->up_param;
@@ -1063,7 +1064,7 @@ saras_status rk3_create(const saras_grid_desc *gd, const saras_rk3_params *p, vo
     SARAS_TRY(rk_alloc(h, &h->tmpR, sz));
     SARAS_TRY(rk_alloc(h, &h->nlT, sz));
     h->nfields = (int)h->allocs.size();
-    for (double *q : h->allocs) SARAS_CUDA(cudaMemset(q, 0, (size_t)sz * sizeof(double)));
+    for (double *q : h->allocs) SARAS_CUDA(cudaMemsetAsync(q, 0, (size_t)sz * sizeof(double), h->stream));
     const int n[3] = {h->L.n0, h->L.n1, h->L.n2};
     SARAS_TRY(rk_alloc(h, &h->tab, 8 * (int64_t)(n[0] + n[1] + n[2])));
     SARAS_TRY(rk3_configure(h, gd, p));
@@ -1079,7 +1080,7 @@ saras_status rk3_create(const saras_grid_desc *gd, const saras_rk3_params *p, vo
     h->bst[0] = h->bst[1] * (n[1] + 2 * py);
     h->box_elems = h->bst[0] * (n[0] + 2 * px);
     SARAS_TRY(rk_alloc(h, &h->stage, h->box_elems));
-    SARAS_CUDA(cudaDeviceSynchronize());
+    SARAS_CUDA(cudaStreamSynchronize(h->stream));
     return SARAS_OK;
 }
 

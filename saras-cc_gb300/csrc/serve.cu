@@ -468,7 +468,22 @@ struct ServeDone {
 
 struct saras_serve {
     saras_serve_params prm{};
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;   // batched iterations, time-step work
+    cudaStream_t adm = nullptr;      // Poisson admissions and retirements
+    cudaStream_t stp = nullptr;      // time-step requests (integrators and their hierarchies)
+    cudaEvent_t ev_adm = nullptr;    // admission work the next batch waits for
+    cudaEvent_t ev_stp = nullptr;    // time-step work the next batch waits for
+    std::vector<ServeCase> incoming; // admitted while a batch ran; join the next one
+    // pinned staging ring for admission uploads (copies from pageable memory
+    // would wait for the admission stream, and so for the running batch)
+    char *pin = nullptr;
+    size_t pin_cap = 0, pin_head = 0;
+    struct PinUse {
+        size_t lo, hi;
+        cudaEvent_t ev;
+    };
+    std::deque<PinUse> pin_busy;
+    std::vector<cudaEvent_t> ev_pool;
     int sms = 152;
     std::deque<ServeCase> pending;
     std::vector<ServeCase> active;
@@ -496,6 +511,7 @@ struct saras_serve {
     // statistics
     int64_t cycles_run = 0, launches = 0, admitted = 0, retired = 0;
     int max_active = 0;
+    double t_batch = 0.0, t_admit = 0.0, t_retire = 0.0, t_steps = 0.0;  // wall seconds by phase
 };
 
 namespace {
@@ -739,7 +755,27 @@ saras_status graph_for(saras_serve *h, int depth, cudaGraphExec_t *out) {
 }
 
 // One batched outer iteration of the active cases; waits for its residuals.
+// Launches one batched outer iteration of the active cases on the engine
+// stream, after the admission work recorded so far.
+saras_status launch_batched(saras_serve *h, int *depth_out) {
+    SARAS_CUDA(cudaEventRecord(h->ev_adm, h->adm));
+    SARAS_CUDA(cudaStreamWaitEvent(h->stream, h->ev_adm, 0));
+    SARAS_CUDA(cudaEventRecord(h->ev_stp, h->stp));
+    SARAS_CUDA(cudaStreamWaitEvent(h->stream, h->ev_stp, 0));
+    if (h->dirty) SARAS_TRY(upload_tables(h));
+    cudaGraphExec_t g;
+    const int depth = active_depth(h);
+    SARAS_TRY(graph_for(h, depth, &g));
+    SARAS_CUDA(cudaGraphLaunch(g, h->stream));
+    *depth_out = depth;
+    return SARAS_OK;
+}
+
 saras_status run_batched(saras_serve *h) {
+    SARAS_CUDA(cudaEventRecord(h->ev_adm, h->adm));
+    SARAS_CUDA(cudaStreamWaitEvent(h->stream, h->ev_adm, 0));
+    SARAS_CUDA(cudaEventRecord(h->ev_stp, h->stp));
+    SARAS_CUDA(cudaStreamWaitEvent(h->stream, h->ev_stp, 0));
     if (h->dirty) SARAS_TRY(upload_tables(h));
     cudaGraphExec_t g;
     const int depth = active_depth(h);
@@ -798,12 +834,68 @@ Box box_of(const saras_grid_desc &g) {
 
 saras_status stage_box(saras_serve *h, int64_t elems) {
     if (elems <= h->box_cap) return SARAS_OK;
-    SARAS_CUDA(cudaStreamSynchronize(h->stream));
+    SARAS_CUDA(cudaStreamSynchronize(h->adm));
     cudaFree(h->d_box);
     h->d_box = nullptr;
     h->box_cap = 0;
     SARAS_CUDA(cudaMalloc((void **)&h->d_box, (size_t)elems * sizeof(double)));
     h->box_cap = elems;
+    return SARAS_OK;
+}
+
+// Nothing resident: a request that does not fit now never will.
+bool idle(const saras_serve *h) { return h->active.empty() && h->incoming.empty(); }
+
+constexpr size_t PIN_BYTES = (size_t)256 << 20;
+
+// Waits for (or retires) the oldest staged uploads until [lo, hi) of the
+// ring is free.
+void pin_wait(saras_serve *h, size_t lo, size_t hi) {
+    auto overlaps = [&]() {
+        for (const auto &u : h->pin_busy)
+            if (u.lo < hi && lo < u.hi) return true;
+        return false;
+    };
+    while (!h->pin_busy.empty() && overlaps()) {
+        cudaEventSynchronize(h->pin_busy.front().ev);
+        h->ev_pool.push_back(h->pin_busy.front().ev);
+        h->pin_busy.pop_front();
+    }
+}
+
+// Host box -> device staging box on the admission stream: through the
+// pinned ring (a host memcpy, then an asynchronous DMA) when it fits,
+// otherwise straight from the caller's pageable memory.
+saras_status upload_box(saras_serve *h, double *dev, const double *host, size_t bytes) {
+    if (!h->pin && h->pin_cap == 0) {
+        if (cudaMallocHost((void **)&h->pin, PIN_BYTES) == cudaSuccess) {
+            h->pin_cap = PIN_BYTES;
+        } else {
+            cudaGetLastError();
+            h->pin = nullptr;
+            h->pin_cap = 1;  // do not retry
+        }
+    }
+    const size_t need = (bytes + 255) / 256 * 256;
+    if (!h->pin || need > h->pin_cap) {
+        SARAS_CUDA(cudaMemcpyAsync(dev, host, bytes, cudaMemcpyHostToDevice, h->adm));
+        return SARAS_OK;
+    }
+    size_t lo = h->pin_head;
+    if (lo + need > h->pin_cap) lo = 0;
+    pin_wait(h, lo, lo + need);
+    std::memcpy(h->pin + lo, host, bytes);
+    SARAS_CUDA(cudaMemcpyAsync(dev, h->pin + lo, bytes, cudaMemcpyHostToDevice, h->adm));
+    cudaEvent_t ev = nullptr;
+    if (!h->ev_pool.empty()) {
+        ev = h->ev_pool.back();
+        h->ev_pool.pop_back();
+    } else {
+        SARAS_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    }
+    SARAS_CUDA(cudaEventRecord(ev, h->adm));
+    h->pin_busy.push_back(saras_serve::PinUse{lo, lo + need, ev});
+    h->pin_head = lo + need;
     return SARAS_OK;
 }
 
@@ -814,10 +906,10 @@ double since(const ServeCase &c) { return std::chrono::duration<double>(Clock::n
 // pressure correction (mgSolve's initial guess), as in saras_rk3_step.
 saras_status start_solve(saras_serve *h, ServeCase &c) {
     saras_mg *m = c.mg;
-    rhs_norm(m, h->stream);
+    rhs_norm(m, m->stream);
     SARAS_CUDA(cudaMemcpyAsync(h->d_fden + c.slot, m->norm_out + 4, sizeof(double), cudaMemcpyDeviceToDevice,
-                               h->stream));
-    mixed_prepare(m, h->stream);
+                               m->stream));
+    mixed_prepare(m, m->stream);
     SARAS_CUDA(cudaGetLastError());
     c.cycles = 0;
     return SARAS_OK;
@@ -840,7 +932,7 @@ enum AdmitStep { ADMIT_DONE = 0, ADMIT_WAIT = 1 };
 // Admission of a time-step request: its integrator (fields and hierarchy)
 // inside the HBM budget, the caller's fields uploaded, the first sub-stage
 // up to its pressure solve, which then joins the batch.
-AdmitStep admit_step(saras_serve *h, ServeCase &c) {
+AdmitStep admit_step(saras_serve *h, ServeCase &c, std::vector<ServeCase> &dst) {
     const saras_rk3_params rp = step_params(h, c.rprm);
     saras_rk3 *rk = nullptr;
     saras_status s = SARAS_OK;
@@ -859,13 +951,13 @@ AdmitStep admit_step(saras_serve *h, ServeCase &c) {
         const int64_t est = rk3_estimate_bytes(&c.grid, &rp);
         if (h->bytes_alloc + est > h->prm.hbm_budget_bytes) evict_pooled(h, est);
         if (h->bytes_alloc + est > h->prm.hbm_budget_bytes) {
-            if (!h->active.empty()) return ADMIT_WAIT;
+            if (!idle(h)) return ADMIT_WAIT;
             set_error("request %lld needs about %lld bytes, above the HBM budget", (long long)c.id,
                       (long long)est);
             h->done.push_back(ServeDone{c.id, 0.0, 0, SARAS_BUDGET, since(c)});
             return ADMIT_DONE;
         }
-        s = saras_rk3_create(&c.grid, &rp, h->stream, &rk);
+        s = saras_rk3_create(&c.grid, &rp, h->stp, &rk);
         if (s != SARAS_OK) {
             h->done.push_back(ServeDone{c.id, 0.0, 0, (int32_t)s, since(c)});
             return ADMIT_DONE;
@@ -879,7 +971,7 @@ AdmitStep admit_step(saras_serve *h, ServeCase &c) {
         h->step_pool[c.shape].push_back(rk);
         c.rk = nullptr;
         c.mg = nullptr;
-        if (!h->active.empty()) return ADMIT_WAIT;
+        if (!idle(h)) return ADMIT_WAIT;
         set_error("request %lld has more work items than the tables hold", (long long)c.id);
         h->done.push_back(ServeDone{c.id, 0.0, 0, SARAS_BUDGET, since(c)});
         return ADMIT_DONE;
@@ -901,7 +993,7 @@ AdmitStep admit_step(saras_serve *h, ServeCase &c) {
         return ADMIT_DONE;
     }
     for (int r = 0; r < NREG; r++) h->used[r] += items[r];
-    h->active.push_back(c);
+    dst.push_back(c);
     h->admitted++;
     h->dirty = true;
     return ADMIT_DONE;
@@ -920,7 +1012,7 @@ bool advance_step(saras_serve *h, size_t idx, int32_t solve_status) {
         s = SARAS_NAN;
     } else {
         if (solve_status == SARAS_NOT_CONVERGED) c.step_status = SARAS_NOT_CONVERGED;  // the step goes on
-        mixed_finish(c.mg, h->stream);
+        mixed_finish(c.mg, c.mg->stream);  // the integrator's stream: ordered before its correction
         s = rk3_stage_end(c.rk, c.stage);
         if (s == SARAS_OK && c.stage + 1 < rk3_stages(c.rk)) {
             c.stage++;
@@ -945,12 +1037,12 @@ bool advance_step(saras_serve *h, size_t idx, int32_t solve_status) {
 
 // Admits pending requests in order while slots, the item tables and the HBM
 // budget allow.
-saras_status admit(saras_serve *h) {
+saras_status admit(saras_serve *h, std::vector<ServeCase> &dst) {
     const saras_mg_params p = case_params(h);
     while (!h->pending.empty() && !h->free_slots.empty()) {
         ServeCase &c = h->pending.front();
         if (c.rk == nullptr && c.fields[0]) {
-            const AdmitStep a = admit_step(h, c);
+            const AdmitStep a = admit_step(h, c, dst);
             if (a == ADMIT_WAIT) break;
             h->pending.pop_front();
             continue;
@@ -961,7 +1053,7 @@ saras_status admit(saras_serve *h) {
             const int64_t est = mg_estimate_bytes(&c.grid, &p);
             if (h->bytes_alloc + est > h->prm.hbm_budget_bytes) evict_pooled(h, est);
             if (h->bytes_alloc + est > h->prm.hbm_budget_bytes) {
-                if (h->active.empty()) {  // can never fit: fail the request rather than wait forever
+                if (idle(h)) {  // can never fit: fail the request rather than wait forever
                     set_error("request %lld needs about %lld bytes, above the HBM budget", (long long)c.id,
                               (long long)est);
                     h->done.push_back(ServeDone{c.id, 0.0, 0, SARAS_BUDGET, 0.0});
@@ -970,7 +1062,7 @@ saras_status admit(saras_serve *h) {
                 }
                 break;  // wait for retirements to free memory
             }
-            saras_status s = saras_mg_create(&c.grid, &p, h->stream, &m);
+            saras_status s = mg_create_queued(&c.grid, &p, h->adm, &m);
             if (s != SARAS_OK) {
                 h->done.push_back(ServeDone{c.id, 0.0, 0, (int32_t)s,
                                             std::chrono::duration<double>(Clock::now() - c.t_submit).count()});
@@ -983,7 +1075,7 @@ saras_status admit(saras_serve *h) {
         const std::array<int, NREG> items = case_items(h, m);
         if (!fits(h, items)) {
             h->pool[c.shape].push_back(m);
-            if (h->active.empty()) {
+            if (idle(h)) {
                 set_error("request %lld has more work items than the tables hold", (long long)c.id);
                 h->done.push_back(ServeDone{c.id, 0.0, 0, SARAS_BUDGET, 0.0});
                 h->pending.pop_front();
@@ -998,21 +1090,20 @@ saras_status admit(saras_serve *h) {
         h->free_slots.pop_back();
         const Box b = box_of(c.grid);
         SARAS_TRY(stage_box(h, b.elems));
-        SARAS_CUDA(cudaMemcpyAsync(h->d_box, c.in - b.origin, (size_t)b.elems * sizeof(double),
-                                   cudaMemcpyHostToDevice, h->stream));
+        SARAS_TRY(upload_box(h, h->d_box, c.in - b.origin, (size_t)b.elems * sizeof(double)));
         SARAS_TRY(mg_load_rhs(m, h->d_box + b.origin, b.st));
-        rhs_norm(m, h->stream);
+        rhs_norm(m, m->stream);
         SARAS_CUDA(cudaMemcpyAsync(h->d_fden + c.slot, m->norm_out + 4, sizeof(double), cudaMemcpyDeviceToDevice,
-                                   h->stream));
-        mixed_prepare(m, h->stream);
+                                   m->stream));
+        mixed_prepare(m, m->stream);
         SARAS_CUDA(cudaGetLastError());
         for (int r = 0; r < NREG; r++) h->used[r] += items[r];
-        h->active.push_back(c);
+        dst.push_back(c);
         h->pending.pop_front();
         h->admitted++;
         h->dirty = true;
     }
-    h->max_active = std::max(h->max_active, (int)h->active.size());
+    h->max_active = std::max(h->max_active, (int)(h->active.size() + h->incoming.size()));
     return SARAS_OK;
 }
 
@@ -1022,17 +1113,17 @@ saras_status retire(saras_serve *h, size_t idx, int32_t status) {
     ServeCase c = h->active[idx];
     saras_mg *m = c.mg;
     if (!c.internal) {
-        mixed_finish(m, h->stream);
+        mixed_finish(m, m->stream);
         const Box b = box_of(c.grid);
         SARAS_TRY(stage_box(h, b.elems));
         // a pad wider than one keeps the caller's outer layers
         if (c.grid.pad > 1)
             SARAS_CUDA(cudaMemcpyAsync(h->d_box, c.out - b.origin, (size_t)b.elems * sizeof(double),
-                                       cudaMemcpyHostToDevice, h->stream));
+                                       cudaMemcpyHostToDevice, m->stream));
         mg_store_lhs(m, h->d_box + b.origin, b.st);
         SARAS_CUDA(cudaMemcpyAsync(c.out - b.origin, h->d_box, (size_t)b.elems * sizeof(double),
-                                   cudaMemcpyDeviceToHost, h->stream));
-        SARAS_CUDA(cudaStreamSynchronize(h->stream));
+                                   cudaMemcpyDeviceToHost, m->stream));
+        SARAS_CUDA(cudaStreamSynchronize(m->stream));
         h->done.push_back(ServeDone{c.id, c.res, c.cycles, status,
                                     std::chrono::duration<double>(Clock::now() - c.t_submit).count()});
         h->retired++;
@@ -1120,6 +1211,10 @@ saras_status saras_serve_create(const saras_serve_params *prm, saras_serve **out
     h->lev_cap = prm->max_cases * DMAX;
     plan_regions(h);
     bool ok = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) == cudaSuccess;
+    ok = ok && cudaStreamCreateWithFlags(&h->adm, cudaStreamNonBlocking) == cudaSuccess;
+    ok = ok && cudaEventCreateWithFlags(&h->ev_adm, cudaEventDisableTiming) == cudaSuccess;
+    ok = ok && cudaStreamCreateWithFlags(&h->stp, cudaStreamNonBlocking) == cudaSuccess;
+    ok = ok && cudaEventCreateWithFlags(&h->ev_stp, cudaEventDisableTiming) == cudaSuccess;
     ok = ok && cudaMalloc((void **)&h->d_lev, (size_t)h->lev_cap * sizeof(BLev)) == cudaSuccess;
     ok = ok && cudaMalloc((void **)&h->d_items, (size_t)h->items_total * sizeof(BItem)) == cudaSuccess;
     ok = ok && cudaMalloc((void **)&h->d_counts, NREG * sizeof(int)) == cudaSuccess;
@@ -1196,9 +1291,30 @@ saras_status saras_serve_submit_step(saras_serve *h, int64_t id, const saras_gri
 
 saras_status saras_serve_step(saras_serve *h, int32_t *active, int32_t *pending) {
     if (!h) return SARAS_BAD_ARG;
-    SARAS_TRY(admit(h));
+    auto secs = [](Clock::time_point a, Clock::time_point b) { return std::chrono::duration<double>(b - a).count(); };
+    auto t0 = Clock::now();
+    if (h->active.empty()) {
+        // nothing to overlap with: admit straight into the batch
+        SARAS_TRY(admit(h, h->active));
+        h->dirty = h->dirty || !h->active.empty();
+    }
+    auto t1 = Clock::now();
+    h->t_admit += secs(t0, t1);
     if (!h->active.empty()) {
-        SARAS_TRY(run_batched(h));
+        // the batch runs on the engine stream while the requests that arrived
+        // meanwhile are admitted on the admission stream; they join the next
+        // batch, so the iterations of every request keep their arithmetic
+        int depth = 0;
+        SARAS_TRY(launch_batched(h, &depth));
+        t0 = Clock::now();
+        SARAS_TRY(admit(h, h->incoming));
+        t1 = Clock::now();
+        h->t_admit += secs(t0, t1);
+        SARAS_CUDA(cudaStreamSynchronize(h->stream));
+        t0 = Clock::now();
+        h->t_batch += secs(t1, t0);
+        h->cycles_run++;
+        h->launches += h->graph_launches[depth];
         for (size_t q = 0; q < h->active.size();) {
             ServeCase &c = h->active[q];
             c.cycles++;
@@ -1207,13 +1323,23 @@ saras_status saras_serve_step(saras_serve *h, int32_t *active, int32_t *pending)
             if (bad || c.res < c.tol || c.cycles >= c.cap) {
                 const int32_t st = bad ? SARAS_NAN : (c.res < c.tol ? SARAS_OK : SARAS_NOT_CONVERGED);
                 if (c.rk) {
-                    if (!advance_step(h, q, st)) q++;
+                    const auto a0 = Clock::now();
+                    const bool left = advance_step(h, q, st);
+                    h->t_steps += secs(a0, Clock::now());
+                    if (!left) q++;
                     continue;
                 }
+                const auto r0 = Clock::now();
                 SARAS_TRY(retire(h, q, st));
+                h->t_retire += secs(r0, Clock::now());
                 continue;
             }
             q++;
+        }
+        if (!h->incoming.empty()) {
+            for (ServeCase &c : h->incoming) h->active.push_back(c);
+            h->incoming.clear();
+            h->dirty = true;
         }
     }
     if (active) *active = (int32_t)h->active.size();
@@ -1262,7 +1388,7 @@ saras_status saras_serve_autotune(saras_serve *h, const saras_grid_desc *grids, 
         }
         SARAS_TRY(enqueue(h, -1 - q, &grids[q], rhs[(size_t)q].data(), lhs[(size_t)q].data(), true));
     }
-    saras_status st = admit(h);
+    saras_status st = admit(h, h->active);
     while (!h->pending.empty()) h->pending.pop_front();  // what did not fit is not tuned for
     if (st == SARAS_OK && h->active.empty()) {
         set_error("no autotune request fits the engine's budget");
@@ -1339,12 +1465,20 @@ saras_status saras_serve_get_stats(const saras_serve *h, saras_serve_stats *out)
     for (const auto &kv : h->step_pool) pooled += (int)kv.second.size();
     out->pooled = pooled;
     out->max_active = h->max_active;
+    out->t_batch_s = h->t_batch;
+    out->t_admit_s = h->t_admit;
+    out->t_retire_s = h->t_retire;
+    out->t_steps_s = h->t_steps;
     return SARAS_OK;
 }
 
 saras_status saras_serve_destroy(saras_serve *h) {
     if (!h) return SARAS_OK;
     if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->adm) cudaStreamSynchronize(h->adm);
+    if (h->stp) cudaStreamSynchronize(h->stp);
+    for (ServeCase &c : h->incoming) h->active.push_back(c);
+    h->incoming.clear();
     for (ServeCase &c : h->active) {
         if (c.rk)
             saras_rk3_destroy(c.rk);  // owns its hierarchy
@@ -1368,6 +1502,13 @@ saras_status saras_serve_destroy(saras_serve *h) {
     if (h->h_items) cudaFreeHost(h->h_items);
     if (h->h_counts) cudaFreeHost(h->h_counts);
     if (h->stream) cudaStreamDestroy(h->stream);
+    if (h->adm) cudaStreamDestroy(h->adm);
+    if (h->ev_adm) cudaEventDestroy(h->ev_adm);
+    if (h->stp) cudaStreamDestroy(h->stp);
+    if (h->ev_stp) cudaEventDestroy(h->ev_stp);
+    for (auto &u : h->pin_busy) cudaEventDestroy(u.ev);
+    for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
+    if (h->pin) cudaFreeHost(h->pin);
     delete h;
     return SARAS_OK;
 }

@@ -449,7 +449,9 @@ class ServeParams(C.Structure):
 class ServeStats(C.Structure):
     _fields_ = [("bytes_allocated", C.c_int64), ("batched_cycles", C.c_int64), ("launches", C.c_int64),
                 ("admitted", C.c_int64), ("retired", C.c_int64), ("active", C.c_int32),
-                ("pending", C.c_int32), ("pooled", C.c_int32), ("max_active", C.c_int32)]
+                ("pending", C.c_int32), ("pooled", C.c_int32), ("max_active", C.c_int32),
+                ("t_batch_s", C.c_double), ("t_admit_s", C.c_double), ("t_retire_s", C.c_double),
+                ("t_steps_s", C.c_double)]
 
 
 _serve_bound = False
