@@ -650,7 +650,19 @@ void prolong_add(saras_mg *h, cudaStream_t s, int l, bool mixed) {
 }
 
 void smooth(saras_mg *h, cudaStream_t s, int l, int count, bool mixed) {
-    for (int n = 0; n < count; n++) {
+    int n = 0;
+    Level &v = h->lv[(size_t)l];
+    if (mixed && v.tma.fok) {
+        // pairs of iterations through the fused kernel, e32 -> e32b -> e32;
+        // an odd last one takes the colour sweeps below
+        for (; n + 2 <= count; n += 2)
+            for (int half = 0; half < 2; half++) {
+                kbegin(h, s, l == 0 ? KC_SMOOTH0 : -1);
+                tma_fused(h, s, v, half == 0);
+                kend(h, s, l == 0 ? KC_SMOOTH0 : -1);
+            }
+    }
+    for (; n < count; n++) {
         if (mixed) {
             colour32(h, s, l, 0);
             colour32(h, s, l, 1);
@@ -915,8 +927,19 @@ double kernel_bytes(const saras_mg *h, int kclass) {
     const bool mixed = h->prm.precision == SARAS_PREC_MIXED;
     const double sz = mixed ? 4.0 : 8.0;
     switch (kclass) {
-    case KC_SMOOTH0:  // one colour = half of an RBGS iteration's 3 N s
-        return 1.5 * n * sz;
+    case KC_SMOOTH0: {
+        // an RBGS iteration reads e and r and writes e (3 N s): a fused
+        // launch is a whole iteration, a colour launch half of one; the
+        // average over a V-cycle's launch mix (smooth() pairs iterations)
+        const bool fused = mixed && h->lv[0].tma.fok;
+        int f = 0, k = 0;
+        for (int c : {h->prm.pre_smooth, h->prm.post_smooth}) {
+            const int fc = fused ? c / 2 * 2 : 0;
+            f += fc;
+            k += c - fc;
+        }
+        return f + 2 * k > 0 ? (f + k) * 3.0 * n * sz / (f + 2 * k) : 0.0;
+    }
     case KC_RESTRICT:  // read u, f; write the coarse rhs
         return (2.0 + 0.125) * n * sz;
     case KC_PROLONG:  // read coarse, read and write fine

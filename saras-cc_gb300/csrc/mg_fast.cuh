@@ -24,6 +24,8 @@ void coarsest_fast(saras_mg *h, cudaStream_t s, Level &c);
 // mg_tma.cu: TMA-staged FP32 colour sweep of the large 3-D levels
 void tma_plan(saras_mg *h, Level &v);
 bool tma_colour(saras_mg *h, cudaStream_t s, Level &v, int colour);
+bool tma_fused(saras_mg *h, cudaStream_t s, Level &v, bool to_b);
+bool fused_sweep_fits(const Lay &L, bool d3);
 
 // mg.cu: handle reuse by the serving engine
 saras_status mg_retarget(saras_mg *h, const saras_grid_desc *gd);

@@ -13,10 +13,14 @@ namespace saras {
 
 // TMA plan of a level's FP32 colour sweep (mg_tma.cu): tensor maps of e
 // (tile with one halo row each side, tile alone) and r, tile rows and planes
-// per block.
+// per block.  The fused red-black iteration (fok) adds maps of e (tile rows,
+// two halo rows) for both buffers of its ping-pong pair and of r (tile rows,
+// one halo row), with its own tile rows and plane chunk.
 struct TmaPlan {
     CUtensorMap eld, est, rld;
     int tj = 0, chunk = 0, ok = 0;
+    CUtensorMap fa, fa2, fb, fb2, fr, fr1;
+    int ftj = 0, fchunk = 0, fok = 0;
 };
 
 // Per-level device state.  FP64 arrays serve the FP64_EXACT and FP64 forms
@@ -26,6 +30,7 @@ struct Level {
     Lay lay;
     double *lhs = nullptr, *rhs = nullptr, *tmp = nullptr, *smd = nullptr;
     float *e32 = nullptr, *r32 = nullptr;
+    float *e32b = nullptr;  // second buffer of the fused red-black iteration's ping-pong
     double *tab = nullptr;  // all 1-D tables of the level in one allocation
     Coef coef{};
     RTab rt{};

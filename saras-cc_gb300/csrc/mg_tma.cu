@@ -274,6 +274,264 @@ __global__ void __launch_bounds__(TMA_WS_THREADS) k_rbgs_tma(const __grid_consta
     if (lane == 0) bulk_wait_all();
 }
 
+// ---- One whole red-black iteration per launch, out of place ----
+//
+// k_rbgs_tma moves e and r through HBM once per colour.  k_rbgs_fused runs
+// both colours of an iteration in one pass: a block reads its tile of e
+// (from the source buffer) and of r once, updates the first colour, then the
+// second, and stores the tile into the destination buffer.  The second
+// colour of a cell needs the first colour's new values around it, also those
+// of the neighbouring tiles and chunks, which other blocks produce at times
+// nobody orders; so the block recomputes the first colour itself on one halo
+// row each side of its tile and one halo plane each side of its chunk, from
+// the source buffer, which no block writes during the launch (two halo rows
+// and planes of e, one of r).  The arithmetic per cell is strip4's, so one
+// launch gives the bits of k_rbgs_tma's colour-0 launch followed by its
+// colour-1 launch.
+//
+// Tiles: tj rows (FU_TILE cells) by the whole row; the block marches through
+// planes i0-1 .. i1 of its chunk.  Per plane step q, every consumer thread:
+//   R(q):   first colour on plane q, tile rows and halo rows;
+//   barrier (consumer threads): R(q) and K(q-2) complete everywhere;
+//   thread 0: TMA store of plane q-2, release of e(q-3) and r(q-2);
+//   K(q-1): second colour on plane q-1, tile rows.
+// R(q) reads the second colour on planes q-1..q+1 (old values) and K(q-1)
+// the first colour on planes q-2..q (new values).  Between two barriers
+// threads run K(q-1) and R(q+1), which update disjoint cells; a strip is
+// written back whole, its cells of the other colour unchanged (the bits a
+// concurrent reader expects).  A producer lane streams e planes through a
+// ring of FU_ESLOTS slots and r planes through FU_RSLOTS slots, two steps
+// ahead of their first use.
+constexpr int FU_CONSUMERS = 12;
+constexpr int FU_NT = 32 * FU_CONSUMERS;
+constexpr int FU_THREADS = FU_NT + 32;
+constexpr int FU_ESLOTS = 6, FU_RSLOTS = 4;
+constexpr int FU_TILE = 4096;
+constexpr int64_t FU_MIN_CELLS = int64_t(1) << 22;
+constexpr size_t FU_HEAD = 1024;  // mbarriers and the tile's y coefficients
+
+__device__ __forceinline__ void consumer_sync() { asm volatile("bar.sync 1, %0;" ::"r"(FU_NT) : "memory"); }
+__device__ __forceinline__ int wrap(int a, int n) { return ((a % n) + n) % n; }
+
+// Colour cells of the strip at row[k0 .. k0+3] (a tile row of e in shared
+// memory); xmr / xpr: the same row on the planes below and above, rrow: the
+// row of r.  Mirrors at non-periodic walls as k_rbgs_tma forms them.
+__device__ __forceinline__ void fu_strip(float *row, const float *xmr, const float *xpr, const float *rrow, int n2,
+                                         int k0, bool xlo, bool xhi, bool ylo, bool yhi, const Bnd &b, int par,
+                                         int li, int ri, bool lneg, bool rneg, float cmx, float cpx, float dx,
+                                         float cmy, float cpy, float dy, const float (&zc)[3][4], float w,
+                                         float omc) {
+    const float4 cur = lds4(row + k0);
+    const float4 xm = xlo ? mirror4(cur, b.sg_lo[0]) : lds4(xmr + k0);
+    const float4 xp = xhi ? mirror4(cur, b.sg_hi[0]) : lds4(xpr + k0);
+    const float4 ym = ylo ? mirror4(cur, b.sg_lo[1]) : lds4(row - n2 + k0);
+    const float4 yp = yhi ? mirror4(cur, b.sg_hi[1]) : lds4(row + n2 + k0);
+    const float4 fr = lds4(rrow + k0);
+    const float lv = row[li], rv = row[ri];
+    const float left = lneg ? -lv : lv, right = rneg ? -rv : rv;
+    float o[4] = {cur.x, cur.y, cur.z, cur.w};
+    if (par == 0)
+        strip4<0>(o, cur, xm, xp, ym, yp, fr, left, right, cmx, cpx, dx, cmy, cpy, dy, zc, w, omc);
+    else
+        strip4<1>(o, cur, xm, xp, ym, yp, fr, left, right, cmx, cpx, dx, cmy, cpy, dy, zc, w, omc);
+    *reinterpret_cast<float4 *>(row + k0) = make_float4(o[0], o[1], o[2], o[3]);
+}
+
+// esrc / esrc2: source e with boxes of tj rows and of two rows; edst:
+// destination e, tj rows; rld / rld1: r with tj rows and one row.
+__global__ void __launch_bounds__(FU_THREADS, 1)
+    k_rbgs_fused(const __grid_constant__ CUtensorMap esrc, const __grid_constant__ CUtensorMap esrc2,
+                 const __grid_constant__ CUtensorMap edst, const __grid_constant__ CUtensorMap rld,
+                 const __grid_constant__ CUtensorMap rld1, Lay L, Tab3<float> t, Bnd b, float w, float omc, int tj,
+                 int chunk, int *err) {
+    pdl_enter();
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ int s_fail;
+    const int n0 = L.n0, n1 = L.n1, n2 = L.n2;
+    const int e_slot = (tj + 4) * n2, r_slot = (tj + 2) * n2;
+    uint64_t *efull = reinterpret_cast<uint64_t *>(smem), *eempty = efull + FU_ESLOTS;
+    uint64_t *rfull = eempty + FU_ESLOTS, *rempty = rfull + FU_RSLOTS;
+    float *sy = reinterpret_cast<float *>(smem + 256);  // cm, cp, dg of y for rows j0-1 .. j0+tj
+    float *es = reinterpret_cast<float *>(smem + FU_HEAD);
+    float *rs = es + FU_ESLOTS * e_slot;
+    const int j0 = (int)blockIdx.x * tj;
+    const int i0 = (int)blockIdx.y * chunk;
+    const int i1 = min(n0, i0 + chunk);
+    if (i0 >= i1) return;
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < FU_ESLOTS; q++) {
+            mbar_init(&efull[q], 1);
+            mbar_init(&eempty[q], 1);
+        }
+        for (int q = 0; q < FU_RSLOTS; q++) {
+            mbar_init(&rfull[q], 1);
+            mbar_init(&rempty[q], 1);
+        }
+        mbar_init_fence();
+        s_fail = 0;
+    }
+    __syncthreads();
+    // e planes i0-2 .. i1+1 and r planes i0-1 .. i1; plane p of e sits in
+    // slot (p - P0) % FU_ESLOTS, of r in (p - Q0) % FU_RSLOTS.  Periodic
+    // axes wrap the plane and halo-row coordinates; at walls the halo rows
+    // and planes are the ghost layer or out of range (TMA fills zeros) and
+    // are never read.
+    const int P0 = i0 - 2, Q0 = i0 - 1;
+    auto pco = [&](int p) { return (b.per[0] ? wrap(p, n0) : p) + 1; };
+    auto rco = [&](int j) { return (b.per[1] ? wrap(j, n1) : j) + 1; };
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp == 0) {
+        // ---- producer ----
+        if (lane == 0) {
+            const uint32_t eb = (uint32_t)(e_slot * sizeof(float)), rb = (uint32_t)(r_slot * sizeof(float));
+            int ne = 0, nr = 0;
+            bool fail = false;
+            for (int P = P0; P <= i1 + 1 && !fail; P++) {
+                const int u = P - P0, s = u % FU_ESLOTS;
+                if (u >= FU_ESLOTS && !mbar_wait(&eempty[s], (uint32_t)((u / FU_ESLOTS - 1) & 1))) {
+                    fail = true;
+                    break;
+                }
+                mbar_expect_tx(&efull[s], eb);
+                float *d = es + s * e_slot;
+                tma_load3(d, &esrc2, &efull[s], KOFF, rco(j0 - 2), pco(P));
+                tma_load3(d + 2 * n2, &esrc, &efull[s], KOFF, j0 + 1, pco(P));
+                tma_load3(d + (tj + 2) * n2, &esrc2, &efull[s], KOFF, rco(j0 + tj), pco(P));
+                ne++;
+                const int Q = P - 1;
+                if (Q < Q0 || Q > i1) continue;
+                const int v = Q - Q0, sr = v % FU_RSLOTS;
+                if (v >= FU_RSLOTS && !mbar_wait(&rempty[sr], (uint32_t)((v / FU_RSLOTS - 1) & 1))) {
+                    fail = true;
+                    break;
+                }
+                mbar_expect_tx(&rfull[sr], rb);
+                float *d2 = rs + sr * r_slot;
+                tma_load3(d2, &rld1, &rfull[sr], KOFF, rco(j0 - 1), pco(Q));
+                tma_load3(d2 + n2, &rld, &rfull[sr], KOFF, j0 + 1, pco(Q));
+                tma_load3(d2 + (tj + 1) * n2, &rld1, &rfull[sr], KOFF, rco(j0 + tj), pco(Q));
+                nr++;
+            }
+            if (fail) {
+                s_fail = 1;
+                atomicExch(err, 1);
+            }
+            // nothing may be in flight when the block exits: wait (bounded)
+            // for the last planes issued to land
+            for (int x = max(0, ne - FU_ESLOTS); x < ne; x++)
+                mbar_wait(&efull[x % FU_ESLOTS], (uint32_t)((x / FU_ESLOTS) & 1));
+            for (int x = max(0, nr - FU_RSLOTS); x < nr; x++)
+                mbar_wait(&rfull[x % FU_RSLOTS], (uint32_t)((x / FU_RSLOTS) & 1));
+        }
+        return;
+    }
+    // ---- consumers ----
+    // Thread ct owns the 4-cell strip at k0 of every rstep-th row it visits:
+    // its z coefficients and z-wall handling stay in registers.
+    const int ct = threadIdx.x - 32;
+    const int s4 = n2 >> 2;
+    const int k0 = (ct % s4) * 4, ro = ct / s4, rstep = FU_NT / s4;
+    float zc[3][4];
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        zc[0][c] = t.cm[2][k0 + c];
+        zc[1][c] = t.cp[2][k0 + c];
+        zc[2][c] = t.dg[2][k0 + c];
+    }
+    const int li = k0 > 0 ? k0 - 1 : (b.per[2] ? n2 - 1 : k0);
+    const bool lneg = k0 == 0 && !b.per[2] && b.sg_lo[2] < 0;
+    const int ri = k0 + 4 < n2 ? k0 + 4 : (b.per[2] ? 0 : k0 + 3);
+    const bool rneg = k0 + 4 >= n2 && !b.per[2] && b.sg_hi[2] < 0;
+    const int ny = tj + 2;
+    for (int x = ct; x < ny; x += FU_NT) {
+        const int j = j0 - 1 + x;
+        const int jw = b.per[1] ? wrap(j, n1) : min(max(j, 0), n1 - 1);
+        sy[x] = t.cm[1][jw];
+        sy[ny + x] = t.cp[1][jw];
+        sy[2 * ny + x] = t.dg[1][jw];
+    }
+    consumer_sync();
+    auto eptr = [&](int p) { return es + ((p - P0) % FU_ESLOTS) * e_slot; };
+    auto rptr = [&](int p) { return rs + ((p - Q0) % FU_RSLOTS) * r_slot; };
+    auto wait_e = [&](int p) {
+        const int u = p - P0;
+        if (!s_fail && !mbar_wait(&efull[u % FU_ESLOTS], (uint32_t)((u / FU_ESLOTS) & 1))) {
+            s_fail = 1;
+            atomicExch(err, 1);
+        }
+    };
+    auto wait_r = [&](int p) {
+        const int u = p - Q0;
+        if (!s_fail && !mbar_wait(&rfull[u % FU_RSLOTS], (uint32_t)((u / FU_RSLOTS) & 1))) {
+            s_fail = 1;
+            atomicExch(err, 1);
+        }
+    };
+    const bool px = b.per[0] != 0, py = b.per[1] != 0;
+    wait_e(P0);
+    wait_e(P0 + 1);
+    // every consumer thread runs every step and barrier, failed or not
+    for (int q = i0 - 1; q <= i1; q++) {
+        wait_e(q + 1);
+        wait_r(q);
+        if (px || (q >= 0 && q < n0)) {
+            // R(q)
+            const int qi = px ? wrap(q, n0) : q;
+            float *pc = eptr(q);
+            const float *pm = eptr(q - 1), *pp = eptr(q + 1), *rr = rptr(q);
+            const float cmx = t.cm[0][qi], cpx = t.cp[0][qi], dx = t.dg[0][qi];
+            const bool xlo = !px && qi == 0, xhi = !px && qi == n0 - 1;
+            for (int x = ro; x < ny; x += rstep) {
+                const int j = j0 - 1 + x;
+                if (!py && (j < 0 || j >= n1)) continue;
+                const int jw = py ? wrap(j, n1) : j;
+                const int off = (x + 1) * n2;
+                fu_strip(pc + off, pm + off, pp + off, rr + x * n2, n2, k0, xlo, xhi, !py && jw == 0,
+                         !py && jw == n1 - 1, b, (qi + jw) & 1, li, ri, lneg, rneg, cmx, cpx, dx, sy[x], sy[ny + x],
+                         sy[2 * ny + x], zc, w, omc);
+            }
+        }
+        // this thread's writes (R(q), K(q-2)) before the async proxy reads them
+        fence_async_smem();
+        consumer_sync();
+        if (ct == 0 && !s_fail) {
+            if (q - 2 >= i0) {
+                tma_store3(&edst, eptr(q - 2) + 2 * n2, KOFF, j0 + 1, q - 1);
+                bulk_commit();
+            }
+            if (q - 3 >= P0) {
+                if (q - 3 >= i0) bulk_wait_read1();  // the store of plane q-3 has read its slot
+                mbar_arrive(&eempty[(q - 3 - P0) % FU_ESLOTS]);
+            }
+            if (q - 2 >= Q0) mbar_arrive(&rempty[(q - 2 - Q0) % FU_RSLOTS]);
+        }
+        const int p = q - 1;
+        if (p >= i0) {
+            // K(p)
+            float *pc = eptr(p);
+            const float *pm = eptr(p - 1), *pp = eptr(p + 1), *rr = rptr(p);
+            const float cmx = t.cm[0][p], cpx = t.cp[0][p], dx = t.dg[0][p];
+            const bool xlo = !px && p == 0, xhi = !px && p == n0 - 1;
+            for (int x = ro; x < tj; x += rstep) {
+                const int j = j0 + x;
+                const int off = (x + 2) * n2;
+                fu_strip(pc + off, pm + off, pp + off, rr + (x + 1) * n2, n2, k0, xlo, xhi, !py && j == 0,
+                         !py && j == n1 - 1, b, (1 + p + j) & 1, li, ri, lneg, rneg, cmx, cpx, dx, sy[x + 1],
+                         sy[ny + x + 1], sy[2 * ny + x + 1], zc, w, omc);
+            }
+        }
+    }
+    fence_async_smem();
+    consumer_sync();
+    if (ct == 0) {
+        if (!s_fail) {
+            tma_store3(&edst, eptr(i1 - 1) + 2 * n2, KOFF, j0 + 1, i1);
+            bulk_commit();
+        }
+        bulk_wait_all();
+    }
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
     static bool tried = false;
@@ -307,15 +565,80 @@ size_t tma_smem(int tj, int n2) {
     return (size_t)TMA_SLOTS * ((size_t)(tj + 2) * n2 + (size_t)tj * n2) * sizeof(float) + 2 * TMA_SLOTS * 8;
 }
 
+size_t fused_smem(int tj, int n2) {
+    return FU_HEAD + ((size_t)FU_ESLOTS * (tj + 4) + (size_t)FU_RSLOTS * (tj + 2)) * n2 * sizeof(float);
+}
+
+Tab3<float> sweep_tab(const Level &v) {
+    return Tab3<float>{{v.cm32[0], v.cm32[1], v.cm32[2]}, {v.cp32[0], v.cp32[1], v.cp32[2]},
+                       {v.dg32[0], v.dg32[1], v.dg32[2]}};
+}
+
+Bnd sweep_bnd(const saras_mg *h) {
+    Bnd b;
+    for (int d = 0; d < 3; d++) {
+        b.per[d] = h->ghost.per[d];
+        b.sg_lo[d] = h->ghost.kind[2 * d] == SARAS_BC_NEUMANN ? 1 : -1;
+        b.sg_hi[d] = h->ghost.kind[2 * d + 1] == SARAS_BC_NEUMANN ? 1 : -1;
+    }
+    return b;
+}
+
+// The fused iteration's plan: tile rows, plane chunk (all blocks resident
+// in one wave) and the six tensor maps.
+void fused_plan(Level &v, int sms) {
+    const Lay &L = v.lay;
+    const int tj = FU_TILE / L.n2;
+    TmaPlan &m = v.tma;
+    if (fused_smem(tj, L.n2) > 200 * 1024 || !encode3(&m.fa, v.e32, L, tj) || !encode3(&m.fa2, v.e32, L, 2) ||
+        !encode3(&m.fb, v.e32b, L, tj) || !encode3(&m.fb2, v.e32b, L, 2) || !encode3(&m.fr, v.r32, L, tj) ||
+        !encode3(&m.fr1, v.r32, L, 1))
+        return;
+    if (cudaFuncSetAttribute(k_rbgs_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    // the block must fit an SM (registers and shared memory) or the level
+    // keeps the colour sweeps
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rbgs_fused, FU_THREADS, fused_smem(tj, L.n2)) !=
+            cudaSuccess ||
+        per_sm < 1) {
+        cudaGetLastError();
+        return;
+    }
+    // one wave: the chunks of every tile column fill the resident blocks
+    const int nch = std::max(1, per_sm * sms / (L.n1 / tj));
+    const int chunk = std::max(8, (L.n0 + nch - 1) / nch);
+    m.ftj = tj;
+    m.fchunk = chunk;
+    m.fok = 1;
+}
+
 }  // namespace
 
-// Plans the TMA sweep of one level: tile rows, plane chunk and the three
+// Levels that take the fused red-black iteration (and hold a second e
+// buffer for it): 3-D, rows of 128 or 256 cells, FU_TILE-cell tiles that
+// divide the level's rows, at least FU_MIN_CELLS cells.
+bool fused_sweep_fits(const Lay &L, bool d3) {
+    if (!d3 || L.n2 < 128 || L.n2 > 256 || FU_TILE % L.n2 != 0 || FU_NT % (L.n2 / 4) != 0) return false;
+    const int tj = FU_TILE / L.n2;
+    return L.n1 % tj == 0 && L.n0 >= 16 && (int64_t)L.n0 * L.n1 * L.n2 >= FU_MIN_CELLS;
+}
+
+// Plans the TMA sweeps of one level: the fused iteration's (levels with a
+// second e buffer) and the colour sweep's tile rows, plane chunk and three
 // tensor maps (e with halo rows, e without, r).  Levels that do not qualify
 // keep the vector sweep.
 void tma_plan(saras_mg *h, Level &v) {
     v.tma.ok = 0;
+    v.tma.fok = 0;
     const Lay &L = v.lay;
     if (!h->d3 || !v.e32 || !v.r32) return;
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (v.e32b && fused_sweep_fits(L, h->d3)) fused_plan(v, sms);
     // rows of 32..256 cells (a power of two); tiles of 2048 cells shared by
     // the consumer warps row-wise
     if (L.n2 < 32 || L.n2 > 256 || 1024 % L.n2 != 0 || (int64_t)L.n0 * L.n1 * L.n2 < (1 << 20)) return;
@@ -324,9 +647,6 @@ void tma_plan(saras_mg *h, Level &v) {
     if (L.n1 % tj != 0 || tj % TMA_CONSUMERS != 0 || tj + 2 > 256) return;
     const size_t smem = tma_smem(tj, L.n2);
     if (smem > 200 * 1024) return;
-    int dev = 0, sms = 152;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int per_sm = std::max(1, (int)((227 * 1024) / smem));
     const int jt = L.n1 / tj;
     const int nchunks = std::max(1, per_sm * sms / jt);  // one wave
@@ -349,18 +669,26 @@ bool tma_colour(saras_mg *h, cudaStream_t s, Level &v, int colour) {
     if (!v.tma.ok) return false;
     const Lay &L = v.lay;
     const dim3 grid((unsigned)(L.n1 / v.tma.tj), (unsigned)((L.n0 + v.tma.chunk - 1) / v.tma.chunk));
-    const Tab3<float> t{{v.cm32[0], v.cm32[1], v.cm32[2]}, {v.cp32[0], v.cp32[1], v.cp32[2]},
-                        {v.dg32[0], v.dg32[1], v.dg32[2]}};
-    Bnd b;
-    for (int d = 0; d < 3; d++) {
-        b.per[d] = h->ghost.per[d];
-        b.sg_lo[d] = h->ghost.kind[2 * d] == SARAS_BC_NEUMANN ? 1 : -1;
-        b.sg_hi[d] = h->ghost.kind[2 * d + 1] == SARAS_BC_NEUMANN ? 1 : -1;
-    }
+    const Tab3<float> t = sweep_tab(v);
+    const Bnd b = sweep_bnd(h);
     int *err = reinterpret_cast<int *>(h->norm_out + 7);
     launch_pdl(k_rbgs_tma, grid, dim3(TMA_WS_THREADS), tma_smem(v.tma.tj, L.n2), s, v.tma.eld, v.tma.est, v.tma.rld,
                (const float *)v.e32, L, t, b, colour, (float)h->prm.sor_param, (float)(1.0 - h->prm.sor_param),
                v.tma.tj, v.tma.chunk, err);
+    return true;
+}
+
+// One red-black iteration through the fused kernel, e32 -> e32b (to_b) or
+// e32b -> e32; false when the level has no fused plan.
+bool tma_fused(saras_mg *h, cudaStream_t s, Level &v, bool to_b) {
+    if (!v.tma.fok) return false;
+    const Lay &L = v.lay;
+    const TmaPlan &m = v.tma;
+    const dim3 grid((unsigned)(L.n1 / m.ftj), (unsigned)((L.n0 + m.fchunk - 1) / m.fchunk));
+    int *err = reinterpret_cast<int *>(h->norm_out + 7);
+    launch_pdl(k_rbgs_fused, grid, dim3(FU_THREADS), fused_smem(m.ftj, L.n2), s, to_b ? m.fa : m.fb,
+               to_b ? m.fa2 : m.fb2, to_b ? m.fb : m.fa, m.fr, m.fr1, L, sweep_tab(v), sweep_bnd(h),
+               (float)h->prm.sor_param, (float)(1.0 - h->prm.sor_param), m.ftj, m.fchunk, err);
     return true;
 }
 

@@ -3,9 +3,11 @@
 Bars: bit-identical to the batched item kernels of the serving engine, which
 sweep cell by cell with the same arithmetic (so the MIXED solve of a level
 large enough for the TMA path equals the served solve bit for bit,
-periodic axes included), and the converged MIXED solution agrees with the
-oracle's FP64 solve to 1e-9 relative (constant component removed) once both
-reach 1e-11.
+periodic axes included, and so does a solve whose finest level takes the
+fused red-black iteration, which recomputes the first colour on halo rows
+and planes instead of reading it back from HBM), and the converged MIXED
+solution agrees with the oracle's FP64 solve to 1e-9 relative (constant
+component removed) once both reach 1e-11.
 """
 import numpy as np
 import pytest
@@ -17,23 +19,35 @@ from helpers import core, demean, random_rhs
 pytestmark = pytest.mark.gpu
 
 MG = dict(mg_tolerance=1e-9, pre_smooth=3, post_smooth=6)
+# the last three grids' finest levels (4M cells, rows of 256 or 128 cells,
+# cells of equal extent on all axes: red-black point smoothing converges
+# slowly on anisotropic cells)
+# take the fused red-black iteration for pairs of smoothing iterations: with
+# 3 / 6 sweeps one pair plus a colour-sweep iteration before the descent and
+# three pairs after it; with 2 / 2 pairs only
 GRIDS = [
-    ("128c_uud", dict(n=(128, 128, 128), mesh="UUD", beta=(1, 1, 1.2), domain="NNN")),
+    ("128c_uud", dict(n=(128, 128, 128), mesh="UUD", beta=(1, 1, 1.2), domain="NNN"), MG),
     ("128x128x64_ppn", dict(n=(128, 128, 64), length=(1.0, 1.0, 0.5), mesh="UUD", beta=(1, 1, 1.1),
-                            domain="PPN")),
+                            domain="PPN"), MG),
+    ("fused_128x128x256_uud", dict(n=(128, 128, 256), length=(1.0, 1.0, 2.0), mesh="UUD", beta=(1, 1, 1.2),
+                                   domain="NNN"), MG),
+    ("fused_256x128x128_ppn", dict(n=(256, 128, 128), length=(2.0, 1.0, 1.0), mesh="UUU", domain="PPN"), MG),
+    ("fused_128x128x256_uud_2x2", dict(n=(128, 128, 256), length=(1.0, 1.0, 2.0), mesh="UUD", beta=(1, 1, 1.2),
+                                       domain="NNN"), dict(mg_tolerance=1e-9, pre_smooth=2, post_smooth=2)),
 ]
+DDD = dict(n=(128, 128, 256), length=(1.0, 1.0, 2.0), mesh="DDD", beta=(1.05, 1.05, 1.1), domain="NNN")
 
 
-@pytest.mark.parametrize("name,gk", GRIDS, ids=[g[0] for g in GRIDS])
-def test_tma_sweep_matches_cellwise_kernels(name, gk):
+@pytest.mark.parametrize("name,gk,mgk", GRIDS, ids=[g[0] for g in GRIDS])
+def test_tma_sweep_matches_cellwise_kernels(name, gk, mgk):
     g = S.grid_desc(**gk)
     rhs = random_rhs(g, 21)
     single = S.padded_field(g)
-    mg = S.Multigrid(g, S.mg_params(precision=S.PREC_MIXED, vc_count=100, vc_tolerance=1e-8, **MG))
+    mg = S.Multigrid(g, S.mg_params(precision=S.PREC_MIXED, vc_count=100, vc_tolerance=1e-8, **mgk))
     assert mg.mg_solve(single, rhs) == S.OK
     cycles = mg.cycles
     mg.close()
-    eng = S.Serve(S.serve_params(tolerance=1e-8, max_cycles=100, max_cases=4, **MG))
+    eng = S.Serve(S.serve_params(tolerance=1e-8, max_cycles=100, max_cases=4, **mgk))
     served = S.padded_field(g)
     eng.submit(1, g, rhs, served)
     done = eng.run()
@@ -42,15 +56,29 @@ def test_tma_sweep_matches_cellwise_kernels(name, gk):
     assert np.array_equal(served, single)
 
 
-def test_tma_mixed_solve_matches_oracle():
-    g = S.grid_desc(**GRIDS[0][1])
+# the fused iteration's wall mirrors are checked against the oracle with
+# Dirichlet (odd) and Neumann (even) walls
+ORACLE_CASES = [
+    ("128c_uud", GRIDS[0][1], MG),
+    ("fused_128x128x256_uud", GRIDS[2][1], MG),
+    ("fused_ddd_dirichlet_z", DDD, dict(MG, bc_kind=[0, 0, 0, 0, 1, 1])),
+    ("fused_ddd_dirichlet_xy", DDD, dict(MG, bc_kind=[1, 1, 1, 1, 0, 0])),
+]
+
+
+@pytest.mark.parametrize("name,gk,mgk", ORACLE_CASES, ids=[c[0] for c in ORACLE_CASES])
+def test_tma_mixed_solve_matches_oracle(name, gk, mgk):
+    g = S.grid_desc(**gk)
     rhs = random_rhs(g, 22)
     mix = S.padded_field(g)
-    mg = S.Multigrid(g, S.mg_params(precision=S.PREC_MIXED, vc_count=100, vc_tolerance=1e-11, **MG))
+    mg = S.Multigrid(g, S.mg_params(precision=S.PREC_MIXED, vc_count=100, vc_tolerance=1e-11, **mgk))
     assert mg.mg_solve(mix, rhs) == S.OK and mg.history[-1] < 1e-11
     mg.close()
     orc = S.padded_field(g)
-    r = O.mg_solve(g, S.mg_params(vc_count=100, vc_tolerance=1e-12, **MG), orc, rhs)
+    # the converged solution does not depend on the smoothing counts: the
+    # oracle smooths 3 / 6 to reach 1e-12 within its cycle cap
+    r = O.mg_solve(g, S.mg_params(vc_count=100, vc_tolerance=1e-12, **dict(mgk, pre_smooth=3, post_smooth=6)),
+                   orc, rhs)
     assert r.history[-1] < 1e-12
     a, b = demean(core(mix, g)), demean(core(orc, g))
     assert np.abs(a - b).max() <= 1e-9 * np.abs(b).max()
