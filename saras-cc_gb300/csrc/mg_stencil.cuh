@@ -350,6 +350,96 @@ __device__ __forceinline__ void resid_row8(const T *__restrict__ u, const T *__r
     }
 }
 
+// f - A u on the 4-cell row segment (i, j, k0 .. k0+3): resid_row8's
+// arithmetic on half the cells (a kernel with half the registers per thread).
+template <class T, bool D3>
+__device__ __forceinline__ void resid_row4(const T *__restrict__ u, const T *__restrict__ f, const Lay &L,
+                                           const Tab3<T> &t, const Bnd &b, int i, int j, int k0,
+                                           const T *__restrict__ dd, T (&r)[4]) {
+    const int64_t c0 = L.at(i, j, k0);
+    T cur[4], xm[4], xp[4], ym[4], yp[4], fr[4];
+    auto mirror = [](const T (&c)[4], int sg, T (&o)[4]) {
+#pragma unroll
+        for (int q = 0; q < 4; q++) o[q] = sg > 0 ? c[q] : -c[q];
+    };
+    ld4(u + c0, cur);
+    if (i > 0) ld4(u + c0 - L.s0, xm);
+    else if (b.per[0]) ld4(u + c0 + (int64_t)(L.n0 - 1) * L.s0, xm);
+    else mirror(cur, b.sg_lo[0], xm);
+    if (i < L.n0 - 1) ld4(u + c0 + L.s0, xp);
+    else if (b.per[0]) ld4(u + c0 - (int64_t)(L.n0 - 1) * L.s0, xp);
+    else mirror(cur, b.sg_hi[0], xp);
+    if (D3) {
+        if (j > 0) ld4(u + c0 - L.s1, ym);
+        else if (b.per[1]) ld4(u + c0 + (int64_t)(L.n1 - 1) * L.s1, ym);
+        else mirror(cur, b.sg_lo[1], ym);
+        if (j < L.n1 - 1) ld4(u + c0 + L.s1, yp);
+        else if (b.per[1]) ld4(u + c0 - (int64_t)(L.n1 - 1) * L.s1, yp);
+        else mirror(cur, b.sg_hi[1], yp);
+    }
+    ld4(f + c0, fr);
+    const T left = k0 > 0 ? __ldg(u + c0 - 1) : (b.per[2] ? __ldg(u + c0 + L.n2 - 1) : (b.sg_lo[2] > 0 ? cur[0] : -cur[0]));
+    const T right = k0 + 4 < L.n2 ? __ldg(u + c0 + 4)
+                                  : (b.per[2] ? __ldg(u + c0 + 4 - L.n2) : (b.sg_hi[2] > 0 ? cur[3] : -cur[3]));
+    T dv[4];
+    if (dd) ld4(dd + c0, dv);
+    const T cmx = t.cm[0][i], cpx = t.cp[0][i];
+    T cmy = T(0), cpy = T(0);
+    if (D3) {
+        cmy = t.cm[1][j];
+        cpy = t.cp[1][j];
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const int k = k0 + q;
+        const T zm = q > 0 ? cur[q - 1] : left;
+        const T zp = q < 3 ? cur[q + 1] : right;
+        T sm = cmx * xm[q];
+        sm = fmat(cpx, xp[q], sm);
+        if (D3) {
+            sm = fmat(cmy, ym[q], sm);
+            sm = fmat(cpy, yp[q], sm);
+        }
+        sm = fmat(t.cm[2][k], zm, sm);
+        sm = fmat(t.cp[2][k], zp, sm);
+        const T d = dd ? dv[q] : diag<T, D3>(t, i, j, k);
+        r[q] = fr[q] - fmat(-d, cur[q], sm);
+    }
+}
+
+// The two coarse cells (i, j, kc0, kc0+1) of the fused residual and
+// restriction: restrict4's arithmetic from 4-cell fine rows.
+template <class T, bool D3>
+__device__ __forceinline__ void restrict2(const T *__restrict__ u, const T *__restrict__ f, const Lay &Lf,
+                                          const Tab3<T> &t, const Bnd &b, const WTab<T> &w,
+                                          const T *__restrict__ dd, int i, int j, int kc0, T (&out)[2]) {
+    if (D3) {
+        T sy[2][2];
+#pragma unroll
+        for (int a = 0; a < 2; a++) {
+            T sz[2][2];
+#pragma unroll
+            for (int bb = 0; bb < 2; bb++) {
+                T r[4];
+                resid_row4<T, true>(u, f, Lf, t, b, 2 * i + a, 2 * j + bb, 2 * kc0, dd, r);
+#pragma unroll
+                for (int q = 0; q < 2; q++)
+                    sz[bb][q] = fmat(w.w1[2][kc0 + q], r[2 * q + 1], w.w0[2][kc0 + q] * r[2 * q]);
+            }
+#pragma unroll
+            for (int q = 0; q < 2; q++) sy[a][q] = fmat(w.w1[1][j], sz[1][q], w.w0[1][j] * sz[0][q]);
+        }
+#pragma unroll
+        for (int q = 0; q < 2; q++) out[q] = fmat(w.w1[0][i], sy[1][q], w.w0[0][i] * sy[0][q]);
+    } else {
+        T r0[4], r1[4];
+        resid_row4<T, false>(u, f, Lf, t, b, 2 * i, 0, 2 * kc0, dd, r0);
+        resid_row4<T, false>(u, f, Lf, t, b, 2 * i + 1, 0, 2 * kc0, dd, r1);
+#pragma unroll
+        for (int q = 0; q < 2; q++) out[q] = ((r0[2 * q] + r0[2 * q + 1]) + (r1[2 * q] + r1[2 * q + 1])) * T(0.25);
+    }
+}
+
 // The four coarse cells (i, j, kc0 .. kc0+3) of the fused residual and
 // restriction: residuals of their 2x2x2 children from 8-cell fine rows,
 // weighted by the coarsen factors v_abc / vTot (poisson_d3.cc:494-508) per
