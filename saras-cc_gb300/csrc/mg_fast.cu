@@ -295,6 +295,64 @@ __global__ void k_rhs_norm_final(const double *__restrict__ part, int nb, int rt
     if (threadIdx.x == 0) out[0] = rtype == 0 ? m : sm;
 }
 
+// A coarsest-level cell with its neighbours and folded coefficients, in the
+// order offdiag applies them (x-, x+, y-, y+, z-, z+).  A wall neighbour is
+// the cell itself (the mirror of its own value), its coefficient negated at a
+// Dirichlet wall; a periodic neighbour wraps.
+struct CCell {
+    int c, nb[6];
+    double cf[6];
+};
+
+template <bool D3>
+__device__ __forceinline__ CCell ccell(const Lay &L, const Tab3<double> &t, const Bnd &b, int i, int j, int k) {
+    CCell x;
+    x.c = (int)L.at(i, j, k);
+    const int ax[3] = {i, j, k}, nn[3] = {L.n0, L.n1, L.n2};
+    const int st[3] = {(int)L.s0, (int)L.s1, 1};
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const int lo = 2 * d, hi = 2 * d + 1;
+        const double cm = D3 || d != 1 ? t.cm[d][ax[d]] : 0.0, cp = D3 || d != 1 ? t.cp[d][ax[d]] : 0.0;
+        if (ax[d] > 0) {
+            x.nb[lo] = x.c - st[d];
+            x.cf[lo] = cm;
+        } else if (b.per[d]) {
+            x.nb[lo] = x.c + (nn[d] - 1) * st[d];
+            x.cf[lo] = cm;
+        } else {
+            x.nb[lo] = x.c;
+            x.cf[lo] = b.sg_lo[d] > 0 ? cm : -cm;
+        }
+        if (ax[d] < nn[d] - 1) {
+            x.nb[hi] = x.c + st[d];
+            x.cf[hi] = cp;
+        } else if (b.per[d]) {
+            x.nb[hi] = x.c - (nn[d] - 1) * st[d];
+            x.cf[hi] = cp;
+        } else {
+            x.nb[hi] = x.c;
+            x.cf[hi] = b.sg_hi[d] > 0 ? cp : -cp;
+        }
+    }
+    return x;
+}
+
+// offdiag<double, D3> of a prepared cell: the same products and sums, in the
+// same order.
+template <bool D3>
+__device__ __forceinline__ double ccell_offdiag(const double *u, const CCell &x) {
+    double s = x.cf[0] * u[x.nb[0]];
+    s = fmat(x.cf[1], u[x.nb[1]], s);
+    if (D3) {
+        s = fmat(x.cf[2], u[x.nb[2]], s);
+        s = fmat(x.cf[3], u[x.nb[3]], s);
+    }
+    s = fmat(x.cf[4], u[x.nb[4]], s);
+    s = fmat(x.cf[5], u[x.nb[5]], s);
+    return s;
+}
+
 // Coarsest level of the FP64 and MIXED forms: SOR red-black sweeps with
 // omega/D stored per cell and the boundary folded into the stencil, run to
 // the absolute tolerance or the iteration cap of poisson_d3.cc:249-432, by
@@ -319,6 +377,85 @@ __global__ void k_coarsest_fast(double *ug, const double *__restrict__ fg, const
     const int ncell = L.n0 * L.n1 * L.n2;
     int iter = 0, sweeps = 0;
     double stall_ref = __longlong_as_double(0x7ff0000000000000ll);  // +infinity
+    if (ncol <= (int)blockDim.x && ncell <= 2 * (int)blockDim.x) {
+        // Every thread owns at most one cell of each colour and two residual
+        // cells: their indices, neighbours and coefficients are formed once
+        // and kept in registers, and a sweep is shared-memory loads and the
+        // FMA chain.  A wall neighbour is the cell itself with the
+        // coefficient negated at a Dirichlet wall (cf * -u and -cf * u are
+        // the same bits), so the arithmetic is offdiag's and resid's.
+        CCell col[2], res[2];
+        bool has_col[2], has_res[2];
+        double wdc[2], fcol[2], ddr[2], fres[2];
+#pragma unroll
+        for (int colour = 0; colour < 2; colour++) {
+            const int q = threadIdx.x;
+            has_col[colour] = false;
+            if (q < ncol) {
+                const int kk = q % half, rest = q / half, j = rest % L.n1, i = rest / L.n1;
+                const int k = 2 * kk + ((i + j + colour) & 1);
+                if (k < L.n2) {
+                    col[colour] = ccell<D3>(L, t, b, i, j, k);
+                    wdc[colour] = wd[col[colour].c];
+                    fcol[colour] = f[col[colour].c];
+                    has_col[colour] = true;
+                }
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < 2; r++) {
+            const int q = threadIdx.x + r * blockDim.x;
+            has_res[r] = q < ncell;
+            if (has_res[r]) {
+                const int k = q % L.n2, rest = q / L.n2, j = rest % L.n1, i = rest / L.n1;
+                res[r] = ccell<D3>(L, t, b, i, j, k);
+                ddr[r] = dd[res[r].c];
+                fres[r] = f[res[r].c];
+            }
+        }
+        for (;;) {
+#pragma unroll
+            for (int colour = 0; colour < 2; colour++) {
+                if (has_col[colour]) {
+                    const CCell &x = col[colour];
+                    const double uc = u[x.c];
+                    const double sv = ccell_offdiag<D3>(u, x) - fcol[colour];
+                    u[x.c] = fmat(sv, wdc[colour], omc * uc);
+                }
+                __syncthreads();
+            }
+            unsigned long long m = 0ull;
+#pragma unroll
+            for (int r = 0; r < 2; r++) {
+                if (!has_res[r]) continue;
+                const CCell &x = res[r];
+                const double rv = fres[r] - fmat(-ddr[r], u[x.c], ccell_offdiag<D3>(u, x));
+                const unsigned long long bits = (unsigned long long)__double_as_longlong(rv) & 0x7fffffffffffffffull;
+                m = bits > m ? bits : m;
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                const unsigned long long w2 = __shfl_xor_sync(0xffffffffu, m, o);
+                m = w2 > m ? w2 : m;
+            }
+            if ((threadIdx.x & 31) == 0) shm[threadIdx.x >> 5] = m;
+            __syncthreads();
+            unsigned long long mm = 0ull;
+            for (int q = 0; q < (int)(blockDim.x >> 5); q++) mm = shm[q] > mm ? shm[q] : mm;
+            __syncthreads();
+            sweeps++;
+            const double rn = __longlong_as_double((long long)mm);
+            if (rn < tol) break;
+            if (stall_check > 0 && iter % stall_check == 0) {
+                if (rn > 0.999 * stall_ref) break;
+                stall_ref = rn;
+            }
+            iter++;
+            if (iter > max_count) break;
+        }
+        for (int64_t q = threadIdx.x; q < L.size; q += blockDim.x) ug[q] = u[q];
+        if (threadIdx.x == 0) *sweeps_out += sweeps;
+        return;
+    }
     for (;;) {
         for (int colour = 0; colour < 2; colour++) {
             for (int q = threadIdx.x; q < ncol; q += blockDim.x) {
@@ -916,7 +1053,11 @@ void coarsest_fast(saras_mg *h, cudaStream_t s, Level &c) {
         return;
     }
     const int64_t cells = (int64_t)C.n0 * C.n1 * C.n2;
-    const int threads = cells <= 512 ? 32 : (cells <= 4096 ? 128 : 256);
+    // up to 512 cells: one thread per cell of a colour (k_coarsest_fast's
+    // register-cached sweeps); larger grids loop over their cells
+    const int64_t ncol = (int64_t)C.n0 * C.n1 * ((C.n2 + 1) / 2);
+    const int threads = ncol <= 256 ? (int)std::max<int64_t>(32, (ncol + 31) / 32 * 32)
+                                    : (cells <= 4096 ? 128 : 256);
     const Bnd b = bnd(h);
     // the MIXED form also stops a stagnating coarsest solve; the FP64 form
     // keeps mgSolve's tolerance-or-cap rule
