@@ -413,6 +413,15 @@ __global__ void k_coarsest_fast(double *ug, const double *__restrict__ fg, const
                 fres[r] = f[res[r].c];
             }
         }
+        // one warp (up to 64 cells): warp barriers, and the shuffle maximum
+        // is already in every lane
+        const bool one_warp = blockDim.x == 32;
+        auto sync = [&]() {
+            if (one_warp)
+                __syncwarp();
+            else
+                __syncthreads();
+        };
         for (;;) {
 #pragma unroll
             for (int colour = 0; colour < 2; colour++) {
@@ -422,7 +431,7 @@ __global__ void k_coarsest_fast(double *ug, const double *__restrict__ fg, const
                     const double sv = ccell_offdiag<D3>(u, x) - fcol[colour];
                     u[x.c] = fmat(sv, wdc[colour], omc * uc);
                 }
-                __syncthreads();
+                sync();
             }
             unsigned long long m = 0ull;
 #pragma unroll
@@ -437,11 +446,14 @@ __global__ void k_coarsest_fast(double *ug, const double *__restrict__ fg, const
                 const unsigned long long w2 = __shfl_xor_sync(0xffffffffu, m, o);
                 m = w2 > m ? w2 : m;
             }
-            if ((threadIdx.x & 31) == 0) shm[threadIdx.x >> 5] = m;
-            __syncthreads();
-            unsigned long long mm = 0ull;
-            for (int q = 0; q < (int)(blockDim.x >> 5); q++) mm = shm[q] > mm ? shm[q] : mm;
-            __syncthreads();
+            unsigned long long mm = m;
+            if (!one_warp) {
+                if ((threadIdx.x & 31) == 0) shm[threadIdx.x >> 5] = m;
+                __syncthreads();
+                mm = 0ull;
+                for (int q = 0; q < (int)(blockDim.x >> 5); q++) mm = shm[q] > mm ? shm[q] : mm;
+                __syncthreads();
+            }
             sweeps++;
             const double rn = __longlong_as_double((long long)mm);
             if (rn < tol) break;
