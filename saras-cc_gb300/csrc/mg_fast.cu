@@ -353,6 +353,108 @@ __device__ __forceinline__ double ccell_offdiag(const double *u, const CCell &x)
     return s;
 }
 
+// The coarsest SOR red-black sweeps of k_coarsest_fast when every thread of
+// the block owns at most one cell of each colour and two residual cells
+// (n0 * n1 * ceil(n2/2) <= blockDim, cells <= 2 blockDim): u (zero), f, wd
+// (omega/D) and dd (D) in shared memory; returns the sweeps run.
+template <bool D3>
+__device__ int coarsest_cached(double *u, const double *f, const double *wd, const double *dd, const Lay &L,
+                               const Tab3<double> &t, const Bnd &b, double omc, double tol, int max_count,
+                               int stall_check, unsigned long long *shm) {
+    const int half = (L.n2 + 1) / 2;
+    const int ncol = L.n0 * L.n1 * half;
+    const int ncell = L.n0 * L.n1 * L.n2;
+    int iter = 0, sweeps = 0;
+    double stall_ref = __longlong_as_double(0x7ff0000000000000ll);  // +infinity
+    // Every thread owns at most one cell of each colour and two residual
+    // cells: their indices, neighbours and coefficients are formed once
+    // and kept in registers, and a sweep is shared-memory loads and the
+    // FMA chain.  A wall neighbour is the cell itself with the
+    // coefficient negated at a Dirichlet wall (cf * -u and -cf * u are
+    // the same bits), so the arithmetic is offdiag's and resid's.
+    CCell col[2], res[2];
+    bool has_col[2], has_res[2];
+    double wdc[2], fcol[2], ddr[2], fres[2];
+#pragma unroll
+    for (int colour = 0; colour < 2; colour++) {
+        const int q = threadIdx.x;
+        has_col[colour] = false;
+        if (q < ncol) {
+            const int kk = q % half, rest = q / half, j = rest % L.n1, i = rest / L.n1;
+            const int k = 2 * kk + ((i + j + colour) & 1);
+            if (k < L.n2) {
+                col[colour] = ccell<D3>(L, t, b, i, j, k);
+                wdc[colour] = wd[col[colour].c];
+                fcol[colour] = f[col[colour].c];
+                has_col[colour] = true;
+            }
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < 2; r++) {
+        const int q = threadIdx.x + r * blockDim.x;
+        has_res[r] = q < ncell;
+        if (has_res[r]) {
+            const int k = q % L.n2, rest = q / L.n2, j = rest % L.n1, i = rest / L.n1;
+            res[r] = ccell<D3>(L, t, b, i, j, k);
+            ddr[r] = dd[res[r].c];
+            fres[r] = f[res[r].c];
+        }
+    }
+    // one warp (up to 64 cells): warp barriers, and the shuffle maximum
+    // is already in every lane
+    const bool one_warp = blockDim.x == 32;
+    auto sync = [&]() {
+        if (one_warp)
+            __syncwarp();
+        else
+            __syncthreads();
+    };
+    for (;;) {
+#pragma unroll
+        for (int colour = 0; colour < 2; colour++) {
+            if (has_col[colour]) {
+                const CCell &x = col[colour];
+                const double uc = u[x.c];
+                const double sv = ccell_offdiag<D3>(u, x) - fcol[colour];
+                u[x.c] = fmat(sv, wdc[colour], omc * uc);
+            }
+            sync();
+        }
+        unsigned long long m = 0ull;
+#pragma unroll
+        for (int r = 0; r < 2; r++) {
+            if (!has_res[r]) continue;
+            const CCell &x = res[r];
+            const double rv = fres[r] - fmat(-ddr[r], u[x.c], ccell_offdiag<D3>(u, x));
+            const unsigned long long bits = (unsigned long long)__double_as_longlong(rv) & 0x7fffffffffffffffull;
+            m = bits > m ? bits : m;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long w2 = __shfl_xor_sync(0xffffffffu, m, o);
+            m = w2 > m ? w2 : m;
+        }
+        unsigned long long mm = m;
+        if (!one_warp) {
+            if ((threadIdx.x & 31) == 0) shm[threadIdx.x >> 5] = m;
+            __syncthreads();
+            mm = 0ull;
+            for (int q = 0; q < (int)(blockDim.x >> 5); q++) mm = shm[q] > mm ? shm[q] : mm;
+            __syncthreads();
+        }
+        sweeps++;
+        const double rn = __longlong_as_double((long long)mm);
+        if (rn < tol) break;
+        if (stall_check > 0 && iter % stall_check == 0) {
+            if (rn > 0.999 * stall_ref) break;
+            stall_ref = rn;
+        }
+        iter++;
+        if (iter > max_count) break;
+    }
+    return sweeps;
+}
+
 // Coarsest level of the FP64 and MIXED forms: SOR red-black sweeps with
 // omega/D stored per cell and the boundary folded into the stencil, run to
 // the absolute tolerance or the iteration cap of poisson_d3.cc:249-432, by
@@ -378,92 +480,7 @@ __global__ void k_coarsest_fast(double *ug, const double *__restrict__ fg, const
     int iter = 0, sweeps = 0;
     double stall_ref = __longlong_as_double(0x7ff0000000000000ll);  // +infinity
     if (ncol <= (int)blockDim.x && ncell <= 2 * (int)blockDim.x) {
-        // Every thread owns at most one cell of each colour and two residual
-        // cells: their indices, neighbours and coefficients are formed once
-        // and kept in registers, and a sweep is shared-memory loads and the
-        // FMA chain.  A wall neighbour is the cell itself with the
-        // coefficient negated at a Dirichlet wall (cf * -u and -cf * u are
-        // the same bits), so the arithmetic is offdiag's and resid's.
-        CCell col[2], res[2];
-        bool has_col[2], has_res[2];
-        double wdc[2], fcol[2], ddr[2], fres[2];
-#pragma unroll
-        for (int colour = 0; colour < 2; colour++) {
-            const int q = threadIdx.x;
-            has_col[colour] = false;
-            if (q < ncol) {
-                const int kk = q % half, rest = q / half, j = rest % L.n1, i = rest / L.n1;
-                const int k = 2 * kk + ((i + j + colour) & 1);
-                if (k < L.n2) {
-                    col[colour] = ccell<D3>(L, t, b, i, j, k);
-                    wdc[colour] = wd[col[colour].c];
-                    fcol[colour] = f[col[colour].c];
-                    has_col[colour] = true;
-                }
-            }
-        }
-#pragma unroll
-        for (int r = 0; r < 2; r++) {
-            const int q = threadIdx.x + r * blockDim.x;
-            has_res[r] = q < ncell;
-            if (has_res[r]) {
-                const int k = q % L.n2, rest = q / L.n2, j = rest % L.n1, i = rest / L.n1;
-                res[r] = ccell<D3>(L, t, b, i, j, k);
-                ddr[r] = dd[res[r].c];
-                fres[r] = f[res[r].c];
-            }
-        }
-        // one warp (up to 64 cells): warp barriers, and the shuffle maximum
-        // is already in every lane
-        const bool one_warp = blockDim.x == 32;
-        auto sync = [&]() {
-            if (one_warp)
-                __syncwarp();
-            else
-                __syncthreads();
-        };
-        for (;;) {
-#pragma unroll
-            for (int colour = 0; colour < 2; colour++) {
-                if (has_col[colour]) {
-                    const CCell &x = col[colour];
-                    const double uc = u[x.c];
-                    const double sv = ccell_offdiag<D3>(u, x) - fcol[colour];
-                    u[x.c] = fmat(sv, wdc[colour], omc * uc);
-                }
-                sync();
-            }
-            unsigned long long m = 0ull;
-#pragma unroll
-            for (int r = 0; r < 2; r++) {
-                if (!has_res[r]) continue;
-                const CCell &x = res[r];
-                const double rv = fres[r] - fmat(-ddr[r], u[x.c], ccell_offdiag<D3>(u, x));
-                const unsigned long long bits = (unsigned long long)__double_as_longlong(rv) & 0x7fffffffffffffffull;
-                m = bits > m ? bits : m;
-            }
-            for (int o = 16; o > 0; o >>= 1) {
-                const unsigned long long w2 = __shfl_xor_sync(0xffffffffu, m, o);
-                m = w2 > m ? w2 : m;
-            }
-            unsigned long long mm = m;
-            if (!one_warp) {
-                if ((threadIdx.x & 31) == 0) shm[threadIdx.x >> 5] = m;
-                __syncthreads();
-                mm = 0ull;
-                for (int q = 0; q < (int)(blockDim.x >> 5); q++) mm = shm[q] > mm ? shm[q] : mm;
-                __syncthreads();
-            }
-            sweeps++;
-            const double rn = __longlong_as_double((long long)mm);
-            if (rn < tol) break;
-            if (stall_check > 0 && iter % stall_check == 0) {
-                if (rn > 0.999 * stall_ref) break;
-                stall_ref = rn;
-            }
-            iter++;
-            if (iter > max_count) break;
-        }
+        const int sweeps = coarsest_cached<D3>(u, f, wd, dd, L, t, b, omc, tol, max_count, stall_check, shm);
         for (int64_t q = threadIdx.x; q < L.size; q += blockDim.x) ug[q] = u[q];
         if (threadIdx.x == 0) *sweeps_out += sweeps;
         return;
@@ -512,6 +529,139 @@ __global__ void k_coarsest_fast(double *ug, const double *__restrict__ fg, const
     }
     for (int64_t q = threadIdx.x; q < L.size; q += blockDim.x) ug[q] = u[q];
     if (threadIdx.x == 0) *sweeps_out += sweeps;
+}
+
+// ---- the bottom of the MIXED V-cycle in one block ----
+//
+// Below some size a level's kernels are launch latency: a colour sweep of
+// 16^3 cells lasts a few microseconds.  k_bottom runs everything a V-cycle
+// does from the first level it holds down to the coarsest and back up to
+// that level again (pre-smoothing, residual and restriction, the coarsest
+// solve, prolongation and correction, post-smoothing) in one block, each
+// level's e and r and the coarsest u, f, omega/D and D in shared memory,
+// the steps separated by block barriers.  Each step has the arithmetic of
+// the kernel it replaces (k_rbgs32, k_resid_restrict, k_coarsest_fast,
+// k_prolong_add), cell for cell, so the V-cycle's bits do not change.
+constexpr int BOT_MAX = 4;  // FP32 levels above the coarsest
+constexpr int BOT_THREADS = 256;
+
+struct BotArgs {
+    int nb;  // FP32 levels held: lb .. lb + nb - 1, then the coarsest
+    Lay L[BOT_MAX];
+    Tab3<float> t[BOT_MAX];
+    WTab<float> w[BOT_MAX + 1];  // restriction weights of levels lb+1 .. the coarsest (index m+1)
+    Lay Lc;
+    Tab3<double> tc;
+    const double *wdc, *ddc;  // the coarsest level's omega/D and D
+    const float *r_top;       // r of level lb, formed by the restriction before
+    float *e_top;             // e of level lb, read by the prolongation after
+    Bnd b;
+    float w32, omc32;
+    double omc64, tol;
+    int max_count, stall, pre, post;
+    int *sweeps_out;
+    unsigned off[2 * BOT_MAX + 4];  // shared-memory byte offsets: e, r per level; u, f, wd, dd
+};
+
+template <bool D3>
+__device__ void bot_smooth(float *e, const float *r, const Lay &L, const Tab3<float> &t, const Bnd &b, int count,
+                           float w, float omc) {
+    const int half = (L.n2 + 1) / 2, ncol = L.n0 * L.n1 * half;
+    for (int n = 0; n < count; n++)
+        for (int colour = 0; colour < 2; colour++) {
+            for (int q = threadIdx.x; q < ncol; q += blockDim.x) {
+                const int kk = q % half, rest = q / half, j = rest % L.n1, i = rest / L.n1;
+                const int k = 2 * kk + ((i + j + colour) & 1);
+                if (k >= L.n2) continue;
+                const int64_t c = L.at(i, j, k);
+                const float uc = e[c];
+                const float sv = offdiag<float, D3>(e, L, t, b, i, j, k, c, uc) - r[c];
+                e[c] = fmat(omc, uc, sweep_div(w * sv, diag<float, D3>(t, i, j, k)));
+            }
+            __syncthreads();
+        }
+}
+
+template <class TO, bool D3>
+__device__ void bot_restrict(const float *e, const float *r, const Lay &Lf, const Tab3<float> &t, const Bnd &b,
+                             const WTab<float> &w, TO *rc, const Lay &Lc) {
+    const int ncell = Lc.n0 * Lc.n1 * Lc.n2;
+    for (int q = threadIdx.x; q < ncell; q += blockDim.x) {
+        const int k = q % Lc.n2, rest = q / Lc.n2, j = rest % Lc.n1, i = rest / Lc.n1;
+        const int i2 = 2 * i, j2 = 2 * j, k2 = 2 * k;
+        float sy[2];
+        for (int a = 0; a < 2; a++) {
+            float sz[2];
+            for (int bb = 0; bb < 2; bb++) {
+                const float r0 = resid<float, D3>(e, r, Lf, t, b, i2 + a, j2 + bb, k2);
+                const float r1 = resid<float, D3>(e, r, Lf, t, b, i2 + a, j2 + bb, k2 + 1);
+                sz[bb] = fmat(w.w1[2][k], r1, w.w0[2][k] * r0);
+            }
+            sy[a] = fmat(w.w1[1][j], sz[1], w.w0[1][j] * sz[0]);
+        }
+        rc[Lc.at(i, j, k)] = (TO)fmat(w.w1[0][i], sy[1], w.w0[0][i] * sy[0]);
+    }
+}
+
+template <class TC>
+__device__ void bot_prolong(float *ef, const TC *ec, const Lay &Lf, const Lay &Lc) {
+    const int ncell = Lf.n0 * Lf.n1 * Lf.n2;
+    for (int q = threadIdx.x; q < ncell; q += blockDim.x) {
+        const int k = q % Lf.n2, rest = q / Lf.n2, j = rest % Lf.n1, i = rest / Lf.n1;
+        const int64_t c = Lf.at(i, j, k);
+        ef[c] = ef[c] + (float)ec[Lc.at(i >> 1, j >> 1, k >> 1)];
+    }
+}
+
+template <bool D3>
+__global__ void __launch_bounds__(BOT_THREADS) k_bottom(const __grid_constant__ BotArgs a) {
+    pdl_enter();
+    extern __shared__ __align__(16) unsigned char bsm[];
+    __shared__ unsigned long long shm[32];
+    float *e[BOT_MAX], *r[BOT_MAX];
+    for (int m = 0; m < a.nb; m++) {
+        e[m] = reinterpret_cast<float *>(bsm + a.off[2 * m]);
+        r[m] = reinterpret_cast<float *>(bsm + a.off[2 * m + 1]);
+    }
+    double *u = reinterpret_cast<double *>(bsm + a.off[2 * BOT_MAX]);
+    double *f = reinterpret_cast<double *>(bsm + a.off[2 * BOT_MAX + 1]);
+    double *wd = reinterpret_cast<double *>(bsm + a.off[2 * BOT_MAX + 2]);
+    double *dd = reinterpret_cast<double *>(bsm + a.off[2 * BOT_MAX + 3]);
+    // every e starts from zero (the restriction into a level clears it);
+    // ghosts stay zero and are never read
+    for (int64_t q = threadIdx.x; q < a.L[0].size; q += blockDim.x) {
+        e[0][q] = 0.f;
+        r[0][q] = a.r_top[q];
+    }
+    for (int m = 1; m < a.nb; m++)
+        for (int64_t q = threadIdx.x; q < a.L[m].size; q += blockDim.x) e[m][q] = r[m][q] = 0.f;
+    for (int64_t q = threadIdx.x; q < a.Lc.size; q += blockDim.x) {
+        u[q] = 0.0;
+        f[q] = 0.0;
+        wd[q] = a.wdc[q];
+        dd[q] = a.ddc[q];
+    }
+    __syncthreads();
+    for (int m = 0; m < a.nb; m++) {
+        bot_smooth<D3>(e[m], r[m], a.L[m], a.t[m], a.b, a.pre, a.w32, a.omc32);
+        if (m + 1 < a.nb)
+            bot_restrict<float, D3>(e[m], r[m], a.L[m], a.t[m], a.b, a.w[m + 1], r[m + 1], a.L[m + 1]);
+        else
+            bot_restrict<double, D3>(e[m], r[m], a.L[m], a.t[m], a.b, a.w[m + 1], f, a.Lc);
+        __syncthreads();
+    }
+    const int sweeps = coarsest_cached<D3>(u, f, wd, dd, a.Lc, a.tc, a.b, a.omc64, a.tol, a.max_count, a.stall, shm);
+    __syncthreads();
+    for (int m = a.nb - 1; m >= 0; m--) {
+        if (m == a.nb - 1)
+            bot_prolong<double>(e[m], u, a.L[m], a.Lc);
+        else
+            bot_prolong<float>(e[m], e[m + 1], a.L[m], a.L[m + 1]);
+        __syncthreads();
+        bot_smooth<D3>(e[m], r[m], a.L[m], a.t[m], a.b, a.post, a.w32, a.omc32);
+    }
+    for (int64_t q = threadIdx.x; q < a.L[0].size; q += blockDim.x) a.e_top[q] = e[0][q];
+    if (threadIdx.x == 0) *a.sweeps_out += sweeps;
 }
 
 // Exact coarsest solve of the MIXED form (fd_solve), one block; dynamic
@@ -959,6 +1109,8 @@ saras_status build_fd(saras_mg *h) {
     return SARAS_OK;
 }
 
+void bottom_plan(saras_mg *h);
+
 saras_status fast_setup(saras_mg *h) {
     for (int f = 0; f < 6; f++)
         if (h->prm.bc_kind[f] == SARAS_BC_DIRICHLET_TEST) {
@@ -980,6 +1132,7 @@ saras_status fast_setup(saras_mg *h) {
     if (h->prm.precision == SARAS_PREC_MIXED)
         for (int l = 0; l < h->nl; l++) tma_plan(h, h->lv[(size_t)l]);
     SARAS_TRY(build_fd(h));
+    bottom_plan(h);
     SARAS_CUDA(cudaFuncSetAttribute(k_coarsest_fd, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     2 * FD_MAX_CELLS * (int)sizeof(double)));
     SARAS_CUDA(cudaFuncSetAttribute(k_coarsest_fast<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -990,11 +1143,108 @@ saras_status fast_setup(saras_mg *h) {
     return SARAS_OK;
 }
 
+// The MIXED form's single-block bottom (k_bottom): the FP32 levels above
+// the coarsest whose colour sweeps are one cell per thread, as long as
+// their e and r and the coarsest level's FP64 arrays fit BOT_SMEM bytes of
+// shared memory.  Needs a 3-D hierarchy and a coarsest level swept in
+// registers (no exact solve).  At 256^3 it holds 8^3 and 4^3 and replaces
+// eleven launches per V-cycle (about 1% of the solve).
+constexpr size_t BOT_SMEM = 160 * 1024;
+
+void bottom_plan(saras_mg *h) {
+    h->bottom = -1;
+    h->bottom_smem = 0;
+    if (h->prm.precision != SARAS_PREC_MIXED || !h->d3 || h->nl < 3 || !h->prm.solve_flag) return;
+    const int top = h->nl - 1;
+    const Level &c = h->lv[(size_t)top];
+    if (c.fdv.ok) return;
+    const Lay &C = c.lay;
+    if ((int64_t)C.n0 * C.n1 * ((C.n2 + 1) / 2) > BOT_THREADS) return;
+    auto al = [](size_t x) { return (x + 15) / 16 * 16; };
+    size_t total = 4 * al((size_t)C.size * sizeof(double));
+    int lb = top;
+    while (lb - 1 >= 1 && top - (lb - 1) <= BOT_MAX) {
+        // a level joins while its colour sweep is one cell per thread: one
+        // block is slower than a multi-block launch on anything larger
+        // (16^3: 93 us per V-cycle in the block against 52 us in launches)
+        const Lay &L = h->lv[(size_t)lb - 1].lay;
+        if ((int64_t)L.n0 * L.n1 * ((L.n2 + 1) / 2) > BOT_THREADS) break;
+        const size_t add = 2 * al((size_t)L.size * sizeof(float));
+        if (total + add > BOT_SMEM) break;
+        total += add;
+        lb--;
+    }
+    if (lb >= top) return;
+    if (cudaFuncSetAttribute(k_bottom<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BOT_SMEM) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    h->bottom = lb;
+    h->bottom_smem = total;
+}
+
+void bottom(saras_mg *h, cudaStream_t s) {
+    const int lb = h->bottom, top = h->nl - 1;
+    BotArgs a{};
+    a.nb = top - lb;
+    auto al = [](size_t x) { return (unsigned)((x + 15) / 16 * 16); };
+    unsigned off = 0;
+    for (int m = 0; m < a.nb; m++) {
+        const Level &v = h->lv[(size_t)(lb + m)];
+        a.L[m] = v.lay;
+        a.t[m] = tab32(v);
+        a.w[m + 1] = wt32(h->lv[(size_t)(lb + m + 1)]);
+        a.off[2 * m] = off;
+        off += al((size_t)v.lay.size * sizeof(float));
+        a.off[2 * m + 1] = off;
+        off += al((size_t)v.lay.size * sizeof(float));
+    }
+    const Level &c = h->lv[(size_t)top];
+    for (int q = 0; q < 4; q++) {
+        a.off[2 * BOT_MAX + q] = off;
+        off += al((size_t)c.lay.size * sizeof(double));
+    }
+    a.Lc = c.lay;
+    a.tc = tab64(c);
+    a.wdc = c.inv_diag;
+    a.ddc = c.dd;
+    a.r_top = h->lv[(size_t)lb].r32;
+    a.e_top = h->lv[(size_t)lb].e32;
+    a.b = bnd(h);
+    a.w32 = (float)h->prm.sor_param;
+    a.omc32 = (float)(1.0 - h->prm.sor_param);
+    a.omc64 = 1.0 - h->prm.sor_param;
+    a.tol = h->prm.mg_tolerance;
+    a.max_count = h->maxCount();
+    a.stall = COARSE_STALL_CHECK;
+    a.pre = h->prm.pre_smooth;
+    a.post = h->prm.post_smooth;
+    a.sweeps_out = h->coarse_sweeps;
+    kbegin(h, s, KC_COARSE);
+    launch_pdl(k_bottom<true>, 1, BOT_THREADS, (size_t)off, s, a);
+    kend(h, s, KC_COARSE);
+}
+
 // One V-cycle over the whole hierarchy: u (FP64 form) or e (MIXED form) at
 // the finest level is smoothed from its current value.
 void vcycle_fast(saras_mg *h, cudaStream_t s, bool mixed) {
     const int top = h->nl - 1;
     smooth(h, s, 0, h->prm.pre_smooth, mixed);
+    const int lb = mixed ? h->bottom : -1;
+    if (lb > 0) {
+        // down to level lb, the bottom in one block, up from level lb
+        for (int l = 0; l < lb; l++) {
+            residual_restrict(h, s, l, mixed);
+            if (l + 1 < lb) smooth(h, s, l + 1, h->prm.pre_smooth, mixed);
+        }
+        bottom(h, s);
+        for (int l = lb; l > 0; l--) {
+            prolong_add(h, s, l, mixed);
+            smooth(h, s, l - 1, h->prm.post_smooth, mixed);
+        }
+        return;
+    }
     for (int l = 0; l < top; l++) {
         residual_restrict(h, s, l, mixed);
         if (l + 1 == top)

@@ -83,6 +83,10 @@ struct saras_mg {
     // graph of one V-cycle (plus the norm and its host copy)
     cudaGraphExec_t graph = nullptr;
     bool use_graph = true;
+    // MIXED form: first level of the V-cycle's bottom run by one block in
+    // shared memory (k_bottom, with the coarsest solve), -1 for none
+    int bottom = -1;
+    size_t bottom_smem = 0;
     int64_t launches_cycle = 0;
     int64_t last_launches = 0;
     int64_t dev_bytes = 0;
