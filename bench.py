@@ -307,6 +307,12 @@ def run_gb300(args):
         mix.close()
         f64.close()
         serving = run_serving(S, args)
+        if args.serve_step_frac > 0:
+            # the Poisson-only half of the stream: the same arrivals, sizes and
+            # RHS draws without time-step requests
+            p = run_serving(S, args, 0.0)
+            serving["poisson_only"] = {k: p[k] for k in ("requests", "completed", "statuses", "throughput_req_per_s",
+                                                         "p50_ms", "p99_ms", "mean_ms", "makespan_s")}
     # CPU baseline: the oracle's full FP64 solve of the same workload once
     # (about 20 s on 16 Grace cores, inside the 10-30 s sample bound)
     sys.path.insert(0, str(ROOT / "oracle"))
@@ -399,12 +405,14 @@ def serve_stream(S, n, rate, seed=7, step_frac=0.0):
     return arrivals, kinds, steps, reqs
 
 
-def run_serving(S, args):
+def run_serving(S, args, step_frac=None):
     """Continuous-batching stream through the serving engine (host API,
     host buffers): latency = completion seen by the host minus the request's
     scheduled arrival."""
     n, rate = args.serve_requests, args.serve_rate
-    arrivals, kinds, steps, reqs = serve_stream(S, n, rate, step_frac=args.serve_step_frac)
+    if step_frac is None:
+        step_frac = args.serve_step_frac
+    arrivals, kinds, steps, reqs = serve_stream(S, n, rate, step_frac=step_frac)
     step_prm = rbc_step_params(S, S.PREC_MIXED)
     eng = S.Serve(S.serve_params(hbm_budget_bytes=40 << 30, max_cases=256, tolerance=SERVE_TOL, max_cycles=400,
                                  **SERVE_MG))
