@@ -34,6 +34,9 @@ GRIDS = [
     ("fused_256x128x128_ppn", dict(n=(256, 128, 128), length=(2.0, 1.0, 1.0), mesh="UUU", domain="PPN"), MG),
     ("fused_128x128x256_uud_2x2", dict(n=(128, 128, 256), length=(1.0, 1.0, 2.0), mesh="UUD", beta=(1, 1, 1.2),
                                        domain="NNN"), dict(mg_tolerance=1e-9, pre_smooth=2, post_smooth=2)),
+    # every axis periodic: the fused iteration's wraps in x, y and z (rows
+    # read across the row's ends) and the single-block bottom on a periodic box
+    ("fused_128x128x256_ppp", dict(n=(128, 128, 256), length=(1.0, 1.0, 2.0), mesh="UUU", domain="PPP"), MG),
 ]
 DDD = dict(n=(128, 128, 256), length=(1.0, 1.0, 2.0), mesh="DDD", beta=(1.05, 1.05, 1.1), domain="NNN")
 
@@ -63,6 +66,11 @@ ORACLE_CASES = [
     ("fused_128x128x256_uud", GRIDS[2][1], MG),
     ("fused_ddd_dirichlet_z", DDD, dict(MG, bc_kind=[0, 0, 0, 0, 1, 1])),
     ("fused_ddd_dirichlet_xy", DDD, dict(MG, bc_kind=[1, 1, 1, 1, 0, 0])),
+    # 128^3 reaches 8^3 above a 4^3 coarsest level: the single-block bottom
+    # (smoothing, restriction, coarsest solve, prolongation) with Dirichlet
+    # walls on every face
+    ("bottom_128c_dirichlet", dict(n=(128, 128, 128), mesh="UUD", beta=(1, 1, 1.2), domain="NNN"),
+     dict(MG, bc_kind=[1, 1, 1, 1, 1, 1])),
 ]
 
 
