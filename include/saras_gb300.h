@@ -99,7 +99,10 @@ typedef struct saras_mg_params {
     int32_t precision;     /* SARAS_PREC_* */
     int32_t levels;        /* 0: reference depth from setVCDepth; >0: that many levels */
     int32_t inner_cycles;  /* MIXED form: FP32 V-cycles per FP64 defect correction (>= 1;
-                              1 repeats the FP64 form cycle by cycle); ignored by the others */
+                              1 repeats the FP64 form cycle by cycle); negative: adaptive, at most
+                              -inner_cycles per correction and, once the residual is within reach,
+                              the V-cycles the last correction's contraction says are left (plus
+                              one); ignored by the others */
 } saras_mg_params;
 
 typedef struct saras_mg saras_mg;
@@ -140,6 +143,10 @@ saras_status saras_mg_kernel_stats(saras_mg *h, int32_t kclass, int64_t *launche
                                    double *total_ms, double *bytes_per_launch);
 /* Total kernel launches issued by the last solve. */
 int64_t saras_mg_last_launches(const saras_mg *h);
+
+/* No reference counterpart.  V-cycles the last solve ran (the MIXED form:
+ * FP32 V-cycles over all its outer iterations). */
+int64_t saras_mg_last_vcycles(const saras_mg *h);
 
 /* Host restatement of the per-level grid metrics the multigrid uses:
  * x (cell centres), xixx and xix2 for `axis` at `level`, each over indices

@@ -726,7 +726,7 @@ saras_status build_walls(saras_mg *h) {
 
 saras_status check_params(const saras_mg_params &p) {
     if (p.vc_count < 1 || p.pre_smooth < 0 || p.post_smooth < 0 || p.res_type < 0 || p.res_type > 2 ||
-        p.precision < 0 || p.precision > 2 || p.levels < 0 || p.inner_cycles < 0 ||
+        p.precision < 0 || p.precision > 2 || p.levels < 0 || p.inner_cycles < -4096 ||
         !(p.sor_param > 0.0 && p.sor_param < 2.0)) {
         set_error("invalid multigrid parameters");
         return SARAS_BAD_ARG;
@@ -764,6 +764,8 @@ void free_all(saras_mg *h) {
     if (h->norm_host) cudaFreeHost(h->norm_host);
     if (h->tab_stage) cudaFreeHost(h->tab_stage);
     if (h->graph) cudaGraphExecDestroy(h->graph);
+    if (h->graph_v) cudaGraphExecDestroy(h->graph_v);
+    if (h->graph_tail) cudaGraphExecDestroy(h->graph_tail);
     for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
     if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
 }
@@ -942,25 +944,88 @@ saras_status ensure_graph(saras_mg *h) {
     return SARAS_OK;
 }
 
+// A MIXED outer iteration of n < the full count of V-cycles (adaptive inner
+// counts): its head, n replays of a one-V-cycle graph and its tail with the
+// norm's host copy.  The two graphs are captured on first use; with kernel
+// timing on, or without graphs, the pieces are issued directly.
+saras_status short_iteration(saras_mg *h, cudaStream_t s, int n) {
+    const bool graphs = h->use_graph && !h->timing;
+    if (graphs && !h->graph_v) {
+        for (int q = 0; q < 2; q++) {
+            cudaGraph_t g = nullptr;
+            SARAS_CUDA(cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeThreadLocal));
+            h->capturing = true;
+            h->issued = 0;
+            if (q == 0) {
+                vcycle_fast(h, h->cap_stream, true);
+            } else {
+                mixed_tail(h, h->cap_stream);
+                cudaMemcpyAsync(h->norm_host, h->norm_out, 8 * sizeof(double), cudaMemcpyDeviceToHost,
+                                h->cap_stream);
+            }
+            h->capturing = false;
+            SARAS_CUDA(cudaStreamEndCapture(h->cap_stream, &g));
+            cudaGraphExec_t ge = nullptr;
+            const cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+            cudaGraphDestroy(g);
+            SARAS_CUDA(e);
+            (q == 0 ? h->graph_v : h->graph_tail) = ge;
+            (q == 0 ? h->launches_v : h->launches_tail) = h->issued;
+        }
+    }
+    mixed_head(h, s);
+    h->last_launches += 1;
+    if (graphs) {
+        for (int q = 0; q < n; q++) SARAS_CUDA(cudaGraphLaunch(h->graph_v, s));
+        SARAS_CUDA(cudaGraphLaunch(h->graph_tail, s));
+        h->last_launches += n * h->launches_v + h->launches_tail;
+    } else {
+        h->issued = 0;
+        for (int q = 0; q < n; q++) vcycle_fast(h, s, true);
+        mixed_tail(h, s);
+        cudaMemcpyAsync(h->norm_host, h->norm_out, 8 * sizeof(double), cudaMemcpyDeviceToHost, s);
+        h->last_launches += h->issued;
+    }
+    return SARAS_OK;
+}
+
 // poisson::mgSolve on level-0 arrays already filled by the caller path.
 saras_status solve_loop(saras_mg *h, double *res_hist, int32_t hist_cap, int32_t *n_cycles) {
     cudaStream_t s = h->stream;
+    h->inner_now = 0;
     SARAS_TRY(ensure_graph(h));
     int cyc = 0;
     double r = 0.0;
+    // MIXED form with a negative inner_cycles: outer iterations of up to
+    // -inner_cycles V-cycles; once the residual is within reach, the next
+    // iteration runs the V-cycles the last one's contraction says the
+    // tolerance still needs (plus one) instead of the full count
+    const bool mixed = h->prm.precision == SARAS_PREC_MIXED;
+    const bool adapt = mixed && h->prm.inner_cycles < 0;
+    const int full = mixed ? (adapt ? -h->prm.inner_cycles : std::max(1, h->prm.inner_cycles)) : 1;
+    int n_next = full;
+    double r_prev = -1.0;
+    h->last_vcycles = 0;
     for (int c = 0; c < h->prm.vc_count; c++) {
         if (h->prm.precision != SARAS_PREC_FP64_EXACT && c == 0) rhs_norm(h, s);
-        if (h->prm.precision == SARAS_PREC_MIXED && c == 0) {
+        if (mixed && c == 0) {
             // the defect-correction loop starts from the residual of the guess
             mixed_prepare(h, s);
         }
-        if (h->graph) {
+        const int n_this = n_next;
+        if (adapt && n_this < full) {
+            h->inner_now = n_this;
+            const saras_status st = short_iteration(h, s, n_this);
+            h->inner_now = 0;
+            SARAS_TRY(st);
+        } else if (h->graph) {
             SARAS_CUDA(cudaGraphLaunch(h->graph, s));
             h->last_launches += h->launches_cycle;
         } else {
             issue_cycle(h, s);
             h->last_launches += h->issued;
         }
+        h->last_vcycles += n_this;
         SARAS_CUDA(cudaStreamSynchronize(s));
         harvest_timing(h);
         r = h->norm_host[0];
@@ -980,6 +1045,15 @@ saras_status solve_loop(saras_mg *h, double *res_hist, int32_t hist_cap, int32_t
             return SARAS_NAN;
         }
         if (!h->prm.test_poisson && r < h->prm.vc_tolerance) break;
+        if (adapt) {
+            n_next = full;
+            if (r_prev > 0.0 && r > 0.0 && r < r_prev) {
+                const double rho = std::pow(r / r_prev, 1.0 / n_this);
+                const double need = std::log(h->prm.vc_tolerance / r) / std::log(rho);
+                if (need >= 0.0 && need + 1.0 < full) n_next = std::max(1, (int)std::ceil(need) + 1);
+            }
+            r_prev = r;
+        }
     }
     if (h->prm.precision == SARAS_PREC_MIXED)
         mixed_finish(h, s);
@@ -1231,6 +1305,8 @@ saras_status saras_mg_kernel_stats(saras_mg *h, int32_t kclass, int64_t *launche
 }
 
 int64_t saras_mg_last_launches(const saras_mg *h) { return h ? h->last_launches : -1; }
+
+int64_t saras_mg_last_vcycles(const saras_mg *h) { return h ? h->last_vcycles : -1; }
 
 }  // extern "C"
 

@@ -1263,21 +1263,41 @@ void vcycle_fast(saras_mg *h, cudaStream_t s, bool mixed) {
 // e = 0, the others from the current e), then the FP64 update and residual.
 void fast_cycle(saras_mg *h, cudaStream_t s) {
     const bool mixed = h->prm.precision == SARAS_PREC_MIXED;
-    if (mixed) {
-        // error equation at the finest level starts from zero
-        Level &v0 = h->lv[0];
-        cudaMemsetAsync(v0.e32, 0, (size_t)v0.lay.size * sizeof(float), s);
+    if (!mixed) {
+        vcycle_fast(h, s, false);
+        resid_norm(h, s, false);
+        return;
     }
-    const int inner = mixed ? std::max(1, h->prm.inner_cycles) : 1;
-    for (int q = 0; q < inner; q++) vcycle_fast(h, s, mixed);
-    if (mixed) {
-        Level &v0 = h->lv[0];
-        const Lay &L = v0.lay;
-        const int bx = bxfor(L.n2);
-        kbegin(h, s, -1);
-        launch_pdl(k_update64, dim3(cdiv(L.n2, bx), (unsigned)L.n1, (unsigned)L.n0), bx, 0, s, v0.lhs, v0.e32, L);
-    }
-    resid_norm(h, s, mixed);
+    mixed_head(h, s);
+    const int inner = mixed_inner(h);
+    for (int q = 0; q < inner; q++) vcycle_fast(h, s, true);
+    mixed_tail(h, s);
+}
+
+// FP32 V-cycles of the current outer iteration: inner_cycles, or with a
+// negative inner_cycles (adaptive) the count the solve loop chose, at most
+// -inner_cycles.
+int mixed_inner(const saras_mg *h) {
+    const int n = h->prm.inner_cycles;
+    if (n > 0) return n;
+    return h->inner_now > 0 ? h->inner_now : std::max(1, -n);
+}
+
+// The error equation at the finest level starts from zero.
+void mixed_head(saras_mg *h, cudaStream_t s) {
+    Level &v0 = h->lv[0];
+    cudaMemsetAsync(v0.e32, 0, (size_t)v0.lay.size * sizeof(float), s);
+}
+
+// u += e (FP64), then the FP64 residual, its norm and the FP32 residual the
+// next outer iteration starts from.
+void mixed_tail(saras_mg *h, cudaStream_t s) {
+    Level &v0 = h->lv[0];
+    const Lay &L = v0.lay;
+    const int bx = bxfor(L.n2);
+    kbegin(h, s, -1);
+    launch_pdl(k_update64, dim3(cdiv(L.n2, bx), (unsigned)L.n1, (unsigned)L.n0), bx, 0, s, v0.lhs, v0.e32, L);
+    resid_norm(h, s, true);
 }
 
 void mixed_prepare(saras_mg *h, cudaStream_t s) {

@@ -14,6 +14,11 @@ void harvest_timing(saras_mg *h);
 // mg_fast.cu
 saras_status fast_setup(saras_mg *h);          // per-cell inverse diagonals, checks
 void fast_cycle(saras_mg *h, cudaStream_t s);  // one V-cycle / outer iteration + norm
+// the MIXED outer iteration in pieces (adaptive inner counts)
+void vcycle_fast(saras_mg *h, cudaStream_t s, bool mixed);
+void mixed_head(saras_mg *h, cudaStream_t s);
+void mixed_tail(saras_mg *h, cudaStream_t s);
+int mixed_inner(const saras_mg *h);
 void mixed_prepare(saras_mg *h, cudaStream_t s);
 void mixed_finish(saras_mg *h, cudaStream_t s);
 void final_ghosts(saras_mg *h, cudaStream_t s);

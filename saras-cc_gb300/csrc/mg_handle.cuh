@@ -83,6 +83,14 @@ struct saras_mg {
     // graph of one V-cycle (plus the norm and its host copy)
     cudaGraphExec_t graph = nullptr;
     bool use_graph = true;
+    // MIXED form with adaptive inner counts: V-cycles of the current outer
+    // iteration (0: the full count), graphs of one V-cycle and of the outer
+    // iteration's tail for shortened iterations, and the V-cycles of the
+    // last solve
+    int inner_now = 0;
+    cudaGraphExec_t graph_v = nullptr, graph_tail = nullptr;
+    int64_t launches_v = 0, launches_tail = 0;
+    int64_t last_vcycles = 0;
     // MIXED form: first level of the V-cycle's bottom run by one block in
     // shared memory (k_bottom, with the coarsest solve), -1 for none
     int bottom = -1;

@@ -189,6 +189,8 @@ def load():
     lib.saras_mg_kernel_stats.restype = C.c_int
     lib.saras_mg_last_launches.argtypes = [vp]
     lib.saras_mg_last_launches.restype = i64
+    lib.saras_mg_last_vcycles.argtypes = [vp]
+    lib.saras_mg_last_vcycles.restype = i64
     lib.saras_grid_metrics.argtypes = [C.POINTER(GridDesc), i32, i32, i32, dp, dp, dp, C.POINTER(i32)]
     lib.saras_grid_metrics.restype = C.c_int
     lib.saras_reference_levels.argtypes = [C.POINTER(GridDesc)]
@@ -340,6 +342,11 @@ class Multigrid:
 
     def last_launches(self) -> int:
         return self.lib.saras_mg_last_launches(self.h)
+
+    def last_vcycles(self) -> int:
+        """V-cycles of the last solve (MIXED: FP32 V-cycles of all outer
+        iterations)."""
+        return self.lib.saras_mg_last_vcycles(self.h)
 
     def device_bytes(self) -> int:
         return self.lib.saras_mg_device_bytes(self.h)

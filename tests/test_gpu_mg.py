@@ -284,3 +284,30 @@ def test_bad_arguments():
     bad = np.zeros((18, 18, 20))  # not the padded box of this grid
     with pytest.raises(S.SarasError):
         mg.mg_solve(bad, bad)
+
+
+def test_mixed_adaptive_inner_cycles():
+    """A negative inner_cycles runs outer iterations of up to -inner_cycles
+    FP32 V-cycles and sizes the last one by the measured contraction: it
+    converges, runs no more V-cycles than the fixed count, agrees with the
+    fixed-count solution to the tolerance, and the captured-graph path and
+    the direct launches (kernel timing on) give the same bits."""
+    g = S.grid_desc(n=(128, 128, 128), mesh="UUD", beta=(1, 1, 1.2), domain="NNN")
+    rhs = random_rhs(g, 31)
+    tol = 1e-10
+    out = {}
+    for name, inner, timing in (("fixed", 16, False), ("adapt", -16, False), ("adapt_direct", -16, True)):
+        mg = S.Multigrid(g, S.mg_params(precision=S.PREC_MIXED, vc_count=200, vc_tolerance=tol, mg_tolerance=1e-6,
+                                        pre_smooth=2, post_smooth=2, inner_cycles=inner))
+        mg.set_kernel_timing(timing)
+        lhs = S.padded_field(g)
+        assert mg.mg_solve(lhs, rhs) == S.OK
+        out[name] = (lhs, mg.last_vcycles(), mg.cycles, mg.history[-1])
+        mg.close()
+    lf, vf, cf, rf = out["fixed"]
+    la, va, ca, ra = out["adapt"]
+    assert vf == 16 * cf
+    assert ra < tol and va <= vf
+    a, b = demean(core(la, g)), demean(core(lf, g))
+    assert np.abs(a - b).max() <= 1e-8 * np.abs(b).max()
+    assert np.array_equal(out["adapt_direct"][0], la) and out["adapt_direct"][1] == va
