@@ -44,6 +44,13 @@ struct Lay {
     }
 };
 
+// Row-split position of cell (i, j, k) (the MIXED form's finest level, see
+// Level::rs): each row holds its red cells ((i + j + k) even), then its
+// black cells, each in k order.
+__host__ __device__ __forceinline__ int64_t rs_at(const Lay &L, int i, int j, int k) {
+    return L.at(i, j, 0) + (k >> 1) + (int64_t)(((i + j + k) & 1) * (L.n2 >> 1));
+}
+
 inline Lay make_lay(int n0, int n1, int n2) {
     Lay l;
     l.n0 = n0;

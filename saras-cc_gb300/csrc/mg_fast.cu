@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(128, 4) k_resid_restrict8(const T *__restrict_
 // (fine n_z a multiple of 8): the arithmetic of k_resid_restrict8 at 80
 // registers instead of 128, so three blocks of eight warps per SM hide the
 // loads' latency (256^3 -> 128^3: 52 us per launch against 73).
-template <bool D3>
+template <bool D3, bool RS>
 __global__ void __launch_bounds__(256, 3) k_resid_restrict4(const float *__restrict__ u, const float *__restrict__ f,
                                                          Lay Lf, Tab3<float> t, Bnd b, WTab<float> w,
                                                          float *__restrict__ rc, Lay Lc, float *__restrict__ ezero) {
@@ -157,7 +157,7 @@ __global__ void __launch_bounds__(256, 3) k_resid_restrict4(const float *__restr
     const int i = blockIdx.z;
     if (kc0 >= Lc.n2 || j >= Lc.n1) return;
     float out[2];
-    restrict2<float, D3>(u, f, Lf, t, b, w, (const float *)nullptr, i, j, kc0, out);
+    restrict2<float, D3, RS>(u, f, Lf, t, b, w, (const float *)nullptr, i, j, kc0, out);
     const int64_t q = Lc.at(i, j, kc0);
     *reinterpret_cast<float2 *>(rc + q) = make_float2(out[0], out[1]);
     if (ezero) *reinterpret_cast<float2 *>(ezero + q) = make_float2(0.f, 0.f);  // the coarse error starts from zero
@@ -184,6 +184,24 @@ __global__ void k_prolong_add8(T *__restrict__ f, const T *__restrict__ c, Lay L
     const int j = (int)(blockIdx.y * blockDim.y + threadIdx.y), i = blockIdx.z;
     if (k0 >= Lf.n2 || j >= Lf.n1) return;
     prolong8(f, c, Lf, Lc, d3, i, j, k0);
+}
+
+// k_prolong_add8 into a row-split FP32 level (3-D): fine cells k0 .. k0+7 of
+// a row are its red and black halves at k0/2 .. k0/2+3, and both take the
+// coarse cells (i/2, j/2, k0/2 .. k0/2+3), cell for cell what k_prolong_add8
+// adds.
+__global__ void k_prolong_add8_rs(float *__restrict__ f, const float *__restrict__ c, Lay Lf, Lay Lc) {
+    pdl_enter();
+    const int k0 = 8 * (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = (int)(blockIdx.y * blockDim.y + threadIdx.y), i = blockIdx.z;
+    if (k0 >= Lf.n2 || j >= Lf.n1) return;
+    const int h = k0 >> 1, H = Lf.n2 >> 1;
+    float *row = f + Lf.at(i, j, 0);
+    const float4 w = __ldg(reinterpret_cast<const float4 *>(c + Lc.at(i >> 1, j >> 1, h)));
+    float4 *rd = reinterpret_cast<float4 *>(row + h), *bk = reinterpret_cast<float4 *>(row + H + h);
+    const float4 a = *rd, d = *bk;
+    *rd = make_float4(a.x + w.x, a.y + w.y, a.z + w.z, a.w + w.w);
+    *bk = make_float4(d.x + w.x, d.y + w.y, d.z + w.z, d.w + w.w);
 }
 
 __device__ __forceinline__ double warp_max(double v) {
@@ -225,12 +243,12 @@ __device__ __forceinline__ void block_store(double (&v)[NV], const bool (&is_max
 template <bool D3, bool MIX>
 __global__ void k_resid_norm64(const double *__restrict__ u, const double *__restrict__ f,
                                const double *__restrict__ dd, Lay L, Tab3<double> t, Bnd b, int rtype,
-                               double *__restrict__ part, float *__restrict__ r32) {
+                               double *__restrict__ part, float *__restrict__ r32, int rs) {
     unsigned long long mbits = 0ull;
     double v[4] = {0.0, 0.0, 0.0, 0.0};
     for_core_rows(L, [&](int i, int j, int k) {
         const double r = resid<double, D3>(u, f, L, t, b, i, j, k, dd);
-        if (MIX) r32[L.at(i, j, k)] = (float)r;
+        if (MIX) r32[rs ? rs_at(L, i, j, k) : L.at(i, j, k)] = (float)r;
         if (rtype == 0) {
             const unsigned long long bits = (unsigned long long)__double_as_longlong(r) & 0x7fffffffffffffffull;
             mbits = bits > mbits ? bits : mbits;
@@ -674,13 +692,13 @@ __global__ void k_coarsest_fd(double *ug, const double *__restrict__ fg, Lay L, 
 }
 
 // u += e over the core (MIXED form update, FP64 accumulate).
-__global__ void k_update64(double *__restrict__ u, const float *__restrict__ e, Lay L) {
+__global__ void k_update64(double *__restrict__ u, const float *__restrict__ e, Lay L, int rs) {
     pdl_enter();
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y, i = blockIdx.z;
     if (k >= L.n2) return;
     const int64_t q = L.at(i, j, k);
-    u[q] = u[q] + (double)e[q];
+    u[q] = u[q] + (double)e[rs ? rs_at(L, i, j, k) : q];
 }
 
 __device__ __forceinline__ void two_sum(double a, double b, double &s, double &c) {
@@ -916,11 +934,11 @@ void residual_restrict(saras_mg *h, cudaStream_t s, int l, bool mixed) {
             const int pairs = Lc.n2 / 2, bx2 = std::min(pairs, 64), by2 = h->d3 ? std::max(1, 256 / bx2) : 1;
             const dim3 g2(cdiv(pairs, bx2), h->d3 ? cdiv(Lc.n1, by2) : 1u, (unsigned)Lc.n0);
             if (h->d3)
-                launch_pdl(k_resid_restrict4<true>, g2, dim3(bx2, by2), 0, s, f.e32, f.r32, f.lay, tab32(f), b,
-                           wt32(c), c.r32, Lc, z32);
+                launch_pdl(f.rs ? k_resid_restrict4<true, true> : k_resid_restrict4<true, false>, g2, dim3(bx2, by2),
+                           0, s, f.e32, f.r32, f.lay, tab32(f), b, wt32(c), c.r32, Lc, z32);
             else
-                launch_pdl(k_resid_restrict4<false>, g2, dim3(bx2, by2), 0, s, f.e32, f.r32, f.lay, tab32(f), b,
-                           wt32(c), c.r32, Lc, z32);
+                launch_pdl(k_resid_restrict4<false, false>, g2, dim3(bx2, by2), 0, s, f.e32, f.r32, f.lay, tab32(f),
+                           b, wt32(c), c.r32, Lc, z32);
         }
     } else if (!mixed) {
         if (h->d3)
@@ -960,6 +978,8 @@ void prolong_add(saras_mg *h, cudaStream_t s, int l, bool mixed) {
         const dim3 g8(cdiv(strips, bx8), cdiv(L.n1, by), (unsigned)L.n0);
         if (!mixed)
             launch_pdl(k_prolong_add8<double>, g8, dim3(bx8, by), 0, s, f.lhs, c.lhs, L, c.lay, h->d3 ? 1 : 0);
+        else if (f.rs)
+            launch_pdl(k_prolong_add8_rs, g8, dim3(bx8, by), 0, s, f.e32, c.e32, L, c.lay);
         else
             launch_pdl(k_prolong_add8<float>, g8, dim3(bx8, by), 0, s, f.e32, c.e32, L, c.lay, h->d3 ? 1 : 0);
     } else if (!mixed)
@@ -1002,17 +1022,17 @@ void resid_norm(saras_mg *h, cudaStream_t s, bool mixed) {
     if (h->d3) {
         if (mixed)
             k_resid_norm64<true, true><<<h->norm_blocks, 256, 0, s>>>(v.lhs, v.rhs, v.dd, v.lay, tab64(v), b,
-                                                                      h->prm.res_type, h->norm_part, v.r32);
+                                                                      h->prm.res_type, h->norm_part, v.r32, v.rs);
         else
             k_resid_norm64<true, false><<<h->norm_blocks, 256, 0, s>>>(v.lhs, v.rhs, v.dd, v.lay, tab64(v), b,
-                                                                       h->prm.res_type, h->norm_part, nullptr);
+                                                                       h->prm.res_type, h->norm_part, nullptr, 0);
     } else {
         if (mixed)
             k_resid_norm64<false, true><<<h->norm_blocks, 256, 0, s>>>(v.lhs, v.rhs, v.dd, v.lay, tab64(v), b,
-                                                                       h->prm.res_type, h->norm_part, v.r32);
+                                                                       h->prm.res_type, h->norm_part, v.r32, v.rs);
         else
             k_resid_norm64<false, false><<<h->norm_blocks, 256, 0, s>>>(v.lhs, v.rhs, v.dd, v.lay, tab64(v), b,
-                                                                        h->prm.res_type, h->norm_part, nullptr);
+                                                                        h->prm.res_type, h->norm_part, nullptr, 0);
     }
     kend(h, s, KC_NORM);
     norm_final(h, s);
@@ -1131,6 +1151,16 @@ saras_status fast_setup(saras_mg *h) {
     }
     if (h->prm.precision == SARAS_PREC_MIXED)
         for (int l = 0; l < h->nl; l++) tma_plan(h, h->lv[(size_t)l]);
+    // the finest level's FP32 arrays are row-split when every smoothing
+    // iteration there is a fused pair (even counts): its only other readers
+    // and writers (FP64 residual, update, restriction, prolongation) follow
+    {
+        Level &v0 = h->lv[0];
+        v0.rs = !h->no_rowsplit && h->prm.precision == SARAS_PREC_MIXED && h->d3 && v0.tma.fok &&
+                        h->prm.pre_smooth % 2 == 0 && h->prm.post_smooth % 2 == 0
+                    ? 1
+                    : 0;
+    }
     SARAS_TRY(build_fd(h));
     bottom_plan(h);
     SARAS_CUDA(cudaFuncSetAttribute(k_coarsest_fd, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1296,7 +1326,8 @@ void mixed_tail(saras_mg *h, cudaStream_t s) {
     const Lay &L = v0.lay;
     const int bx = bxfor(L.n2);
     kbegin(h, s, -1);
-    launch_pdl(k_update64, dim3(cdiv(L.n2, bx), (unsigned)L.n1, (unsigned)L.n0), bx, 0, s, v0.lhs, v0.e32, L);
+    launch_pdl(k_update64, dim3(cdiv(L.n2, bx), (unsigned)L.n1, (unsigned)L.n0), bx, 0, s, v0.lhs, v0.e32, L,
+               v0.rs);
     resid_norm(h, s, true);
 }
 

@@ -52,6 +52,12 @@ struct Level {
     double *fd = nullptr;        // MIXED form, coarsest level: V, V^-1, eigenvalues per axis
     FDiag fdv{};                 // their device view; fdv.ok = 0: red-black sweeps
     TmaPlan tma{};
+    // MIXED form, finest level with the fused iteration and even smoothing
+    // counts: e32, e32b and r32 are row-split, each row holding its red
+    // cells, then its black cells (rs_at); the kernels that touch them
+    // (fused sweep, FP64 residual, update, restriction from and
+    // prolongation into the level) follow it
+    int rs = 0;
 };
 
 enum KClass { KC_SMOOTH0 = 0, KC_RESTRICT = 1, KC_PROLONG = 2, KC_NORM = 3, KC_COARSE = 4, KC_COUNT = 5 };
@@ -95,6 +101,9 @@ struct saras_mg {
     // shared memory (k_bottom, with the coarsest solve), -1 for none
     int bottom = -1;
     size_t bottom_smem = 0;
+    // the serving engine's hierarchies: its batched kernels address the
+    // FP32 arrays in the plain layout, so the finest level is never row-split
+    bool no_rowsplit = false;
     int64_t launches_cycle = 0;
     int64_t last_launches = 0;
     int64_t dev_bytes = 0;

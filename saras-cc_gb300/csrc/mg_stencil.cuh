@@ -352,35 +352,64 @@ __device__ __forceinline__ void resid_row8(const T *__restrict__ u, const T *__r
 
 // f - A u on the 4-cell row segment (i, j, k0 .. k0+3): resid_row8's
 // arithmetic on half the cells (a kernel with half the registers per thread).
-template <class T, bool D3>
+template <class T, bool D3, bool RS = false>
 __device__ __forceinline__ void resid_row4(const T *__restrict__ u, const T *__restrict__ f, const Lay &L,
                                            const Tab3<T> &t, const Bnd &b, int i, int j, int k0,
                                            const T *__restrict__ dd, T (&r)[4]) {
-    const int64_t c0 = L.at(i, j, k0);
+    const int64_t c0 = RS ? L.at(i, j, 0) : L.at(i, j, k0);
     T cur[4], xm[4], xp[4], ym[4], yp[4], fr[4];
     auto mirror = [](const T (&c)[4], int sg, T (&o)[4]) {
 #pragma unroll
         for (int q = 0; q < 4; q++) o[q] = sg > 0 ? c[q] : -c[q];
     };
-    ld4(u + c0, cur);
-    if (i > 0) ld4(u + c0 - L.s0, xm);
-    else if (b.per[0]) ld4(u + c0 + (int64_t)(L.n0 - 1) * L.s0, xm);
+    // RS: c0 is the row's start; cells k0 .. k0+3 of a row of parity pr are
+    // its red and black halves at k0/2, k0/2 + 1, interleaved
+    const int pr = (i + j) & 1, h = k0 >> 1, H = L.n2 >> 1;
+    auto ld = [&](const T *p, int par, T (&o)[4]) {
+        if (!RS) {
+            ld4(p, o);
+            return;
+        }
+        T rd[2], bk[2];
+        if constexpr (RS && sizeof(T) == 4) {
+            // h is even: 8-byte aligned pairs
+            const float2 a = __ldg(reinterpret_cast<const float2 *>(p + h));
+            const float2 c = __ldg(reinterpret_cast<const float2 *>(p + H + h));
+            rd[0] = a.x; rd[1] = a.y; bk[0] = c.x; bk[1] = c.y;
+        } else {
+            rd[0] = __ldg(p + h);
+            rd[1] = __ldg(p + h + 1);
+            bk[0] = __ldg(p + H + h);
+            bk[1] = __ldg(p + H + h + 1);
+        }
+        if (par == 0) {
+            o[0] = rd[0]; o[1] = bk[0]; o[2] = rd[1]; o[3] = bk[1];
+        } else {
+            o[0] = bk[0]; o[1] = rd[0]; o[2] = bk[1]; o[3] = rd[1];
+        }
+    };
+    // position of cell k of this row (RS) or its offset from c0
+    auto at_k = [&](int k) -> int64_t { return RS ? (k >> 1) + (int64_t)(((pr + k) & 1) * H) : k - k0; };
+    ld(u + c0, pr, cur);
+    if (i > 0) ld(u + c0 - L.s0, 1 - pr, xm);
+    else if (b.per[0]) ld(u + c0 + (int64_t)(L.n0 - 1) * L.s0, 1 - pr, xm);
     else mirror(cur, b.sg_lo[0], xm);
-    if (i < L.n0 - 1) ld4(u + c0 + L.s0, xp);
-    else if (b.per[0]) ld4(u + c0 - (int64_t)(L.n0 - 1) * L.s0, xp);
+    if (i < L.n0 - 1) ld(u + c0 + L.s0, 1 - pr, xp);
+    else if (b.per[0]) ld(u + c0 - (int64_t)(L.n0 - 1) * L.s0, 1 - pr, xp);
     else mirror(cur, b.sg_hi[0], xp);
     if (D3) {
-        if (j > 0) ld4(u + c0 - L.s1, ym);
-        else if (b.per[1]) ld4(u + c0 + (int64_t)(L.n1 - 1) * L.s1, ym);
+        if (j > 0) ld(u + c0 - L.s1, 1 - pr, ym);
+        else if (b.per[1]) ld(u + c0 + (int64_t)(L.n1 - 1) * L.s1, 1 - pr, ym);
         else mirror(cur, b.sg_lo[1], ym);
-        if (j < L.n1 - 1) ld4(u + c0 + L.s1, yp);
-        else if (b.per[1]) ld4(u + c0 - (int64_t)(L.n1 - 1) * L.s1, yp);
+        if (j < L.n1 - 1) ld(u + c0 + L.s1, 1 - pr, yp);
+        else if (b.per[1]) ld(u + c0 - (int64_t)(L.n1 - 1) * L.s1, 1 - pr, yp);
         else mirror(cur, b.sg_hi[1], yp);
     }
-    ld4(f + c0, fr);
-    const T left = k0 > 0 ? __ldg(u + c0 - 1) : (b.per[2] ? __ldg(u + c0 + L.n2 - 1) : (b.sg_lo[2] > 0 ? cur[0] : -cur[0]));
-    const T right = k0 + 4 < L.n2 ? __ldg(u + c0 + 4)
-                                  : (b.per[2] ? __ldg(u + c0 + 4 - L.n2) : (b.sg_hi[2] > 0 ? cur[3] : -cur[3]));
+    ld(f + c0, pr, fr);
+    const T left = k0 > 0 ? __ldg(u + c0 + at_k(k0 - 1))
+                          : (b.per[2] ? __ldg(u + c0 + at_k(L.n2 - 1)) : (b.sg_lo[2] > 0 ? cur[0] : -cur[0]));
+    const T right = k0 + 4 < L.n2 ? __ldg(u + c0 + at_k(k0 + 4))
+                                  : (b.per[2] ? __ldg(u + c0 + at_k(0)) : (b.sg_hi[2] > 0 ? cur[3] : -cur[3]));
     T dv[4];
     if (dd) ld4(dd + c0, dv);
     const T cmx = t.cm[0][i], cpx = t.cp[0][i];
@@ -409,7 +438,7 @@ __device__ __forceinline__ void resid_row4(const T *__restrict__ u, const T *__r
 
 // The two coarse cells (i, j, kc0, kc0+1) of the fused residual and
 // restriction: restrict4's arithmetic from 4-cell fine rows.
-template <class T, bool D3>
+template <class T, bool D3, bool RS = false>
 __device__ __forceinline__ void restrict2(const T *__restrict__ u, const T *__restrict__ f, const Lay &Lf,
                                           const Tab3<T> &t, const Bnd &b, const WTab<T> &w,
                                           const T *__restrict__ dd, int i, int j, int kc0, T (&out)[2]) {
@@ -421,7 +450,7 @@ __device__ __forceinline__ void restrict2(const T *__restrict__ u, const T *__re
 #pragma unroll
             for (int bb = 0; bb < 2; bb++) {
                 T r[4];
-                resid_row4<T, true>(u, f, Lf, t, b, 2 * i + a, 2 * j + bb, 2 * kc0, dd, r);
+                resid_row4<T, true, RS>(u, f, Lf, t, b, 2 * i + a, 2 * j + bb, 2 * kc0, dd, r);
 #pragma unroll
                 for (int q = 0; q < 2; q++)
                     sz[bb][q] = fmat(w.w1[2][kc0 + q], r[2 * q + 1], w.w0[2][kc0 + q] * r[2 * q]);
@@ -433,8 +462,8 @@ __device__ __forceinline__ void restrict2(const T *__restrict__ u, const T *__re
         for (int q = 0; q < 2; q++) out[q] = fmat(w.w1[0][i], sy[1][q], w.w0[0][i] * sy[0][q]);
     } else {
         T r0[4], r1[4];
-        resid_row4<T, false>(u, f, Lf, t, b, 2 * i, 0, 2 * kc0, dd, r0);
-        resid_row4<T, false>(u, f, Lf, t, b, 2 * i + 1, 0, 2 * kc0, dd, r1);
+        resid_row4<T, false, RS>(u, f, Lf, t, b, 2 * i, 0, 2 * kc0, dd, r0);
+        resid_row4<T, false, RS>(u, f, Lf, t, b, 2 * i + 1, 0, 2 * kc0, dd, r1);
 #pragma unroll
         for (int q = 0; q < 2; q++) out[q] = ((r0[2 * q] + r0[2 * q + 1]) + (r1[2 * q] + r1[2 * q + 1])) * T(0.25);
     }

@@ -337,8 +337,73 @@ __device__ __forceinline__ void fu_strip(float *row, const float *xmr, const flo
     *reinterpret_cast<float4 *>(row + k0) = make_float4(o[0], o[1], o[2], o[3]);
 }
 
+// Row-split rows (each row: its red cells, then its black cells, in k
+// order): the four cells of one colour at compact positions m .. m+3 of the
+// half `own` (0 red, H black) of `row`, own k = 2 (m + q) + o.  Every x and y
+// neighbour is the other colour at the same compact positions of the
+// neighbouring rows' other half; the z neighbours are the other half of the
+// same row at m .. m+3 shifted by one (left of it for o = 0, right for
+// o = 1), with the row's wrap or wall mirror at its ends.  strip4's
+// arithmetic, cell for cell, on four cells of one colour.
+template <int o>
+__device__ __forceinline__ void fu_strip_rs(float *row, const float *xmr, const float *xpr, const float *rrow, int n2,
+                                            int H, int own, int m, bool xlo, bool xhi, bool ylo, bool yhi,
+                                            const Bnd &b, float cmx, float cpx, float dx, float cmy, float cpy,
+                                            float dy, const float (&zc)[3][4], float w, float omc) {
+    const int oth = H - own;
+    const float4 cur4 = lds4(row + own + m);
+    const float4 xm4 = xlo ? mirror4(cur4, b.sg_lo[0]) : lds4(xmr + oth + m);
+    const float4 xp4 = xhi ? mirror4(cur4, b.sg_hi[0]) : lds4(xpr + oth + m);
+    const float4 ym4 = ylo ? mirror4(cur4, b.sg_lo[1]) : lds4(row - n2 + oth + m);
+    const float4 yp4 = yhi ? mirror4(cur4, b.sg_hi[1]) : lds4(row + n2 + oth + m);
+    const float4 f4 = lds4(rrow + own + m);
+    const float4 a4 = lds4(row + oth + m);
+    const float c[4] = {cur4.x, cur4.y, cur4.z, cur4.w};
+    const float xm[4] = {xm4.x, xm4.y, xm4.z, xm4.w}, xp[4] = {xp4.x, xp4.y, xp4.z, xp4.w};
+    const float ym[4] = {ym4.x, ym4.y, ym4.z, ym4.w}, yp[4] = {yp4.x, yp4.y, yp4.z, yp4.w};
+    const float f[4] = {f4.x, f4.y, f4.z, f4.w};
+    float zm[4], zp[4];
+    if (o == 1) {
+        float right;
+        if (m + 4 < H)
+            right = row[oth + m + 4];
+        else if (b.per[2])
+            right = row[oth];
+        else
+            right = b.sg_hi[2] > 0 ? c[3] : -c[3];
+        zm[0] = a4.x; zm[1] = a4.y; zm[2] = a4.z; zm[3] = a4.w;
+        zp[0] = a4.y; zp[1] = a4.z; zp[2] = a4.w; zp[3] = right;
+    } else {
+        float left;
+        if (m > 0)
+            left = row[oth + m - 1];
+        else if (b.per[2])
+            left = row[oth + H - 1];
+        else
+            left = b.sg_lo[2] > 0 ? c[0] : -c[0];
+        zm[0] = left; zm[1] = a4.x; zm[2] = a4.y; zm[3] = a4.z;
+        zp[0] = a4.x; zp[1] = a4.y; zp[2] = a4.z; zp[3] = a4.w;
+    }
+    float u[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        float sm = cmx * xm[q];
+        sm = fmat(cpx, xp[q], sm);
+        sm = fmat(cmy, ym[q], sm);
+        sm = fmat(cpy, yp[q], sm);
+        sm = fmat(zc[0][q], zm[q], sm);
+        sm = fmat(zc[1][q], zp[q], sm);
+        sm = sm - f[q];
+        float d = dx + zc[2][q];
+        d += dy;
+        u[q] = fmat(omc, c[q], sweep_div(w * sm, d + d));
+    }
+    *reinterpret_cast<float4 *>(row + own + m) = make_float4(u[0], u[1], u[2], u[3]);
+}
+
 // esrc / esrc2: source e with boxes of tj rows and of two rows; edst:
 // destination e, tj rows; rld / rld1: r with tj rows and one row.
+template <bool RS>
 __global__ void __launch_bounds__(FU_THREADS, 1)
     k_rbgs_fused(const __grid_constant__ CUtensorMap esrc, const __grid_constant__ CUtensorMap esrc2,
                  const __grid_constant__ CUtensorMap edst, const __grid_constant__ CUtensorMap rld,
@@ -429,15 +494,22 @@ __global__ void __launch_bounds__(FU_THREADS, 1)
     // Thread ct owns the 4-cell strip at k0 of every rstep-th row it visits:
     // its z coefficients and z-wall handling stay in registers.
     const int ct = threadIdx.x - 32;
-    const int s4 = n2 >> 2;
+    // strips of four cells: of the row (both colours), or with RS of one
+    // row half (one colour); a thread keeps its strip's z coefficients (for
+    // RS those of both colour offsets o)
+    const int H = n2 >> 1;
+    const int s4 = RS ? (H >> 2) : (n2 >> 2);
     const int k0 = (ct % s4) * 4, ro = ct / s4, rstep = FU_NT / s4;
-    float zc[3][4];
+    float zc[2][3][4];
 #pragma unroll
-    for (int c = 0; c < 4; c++) {
-        zc[0][c] = t.cm[2][k0 + c];
-        zc[1][c] = t.cp[2][k0 + c];
-        zc[2][c] = t.dg[2][k0 + c];
-    }
+    for (int oo = 0; oo < (RS ? 2 : 1); oo++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            const int k = RS ? 2 * (k0 + c) + oo : k0 + c;
+            zc[oo][0][c] = t.cm[2][k];
+            zc[oo][1][c] = t.cp[2][k];
+            zc[oo][2][c] = t.dg[2][k];
+        }
     const int li = k0 > 0 ? k0 - 1 : (b.per[2] ? n2 - 1 : k0);
     const bool lneg = k0 == 0 && !b.per[2] && b.sg_lo[2] < 0;
     const int ri = k0 + 4 < n2 ? k0 + 4 : (b.per[2] ? 0 : k0 + 3);
@@ -486,9 +558,20 @@ __global__ void __launch_bounds__(FU_THREADS, 1)
                 if (!py && (j < 0 || j >= n1)) continue;
                 const int jw = py ? wrap(j, n1) : j;
                 const int off = (x + 1) * n2;
-                fu_strip(pc + off, pm + off, pp + off, rr + x * n2, n2, k0, xlo, xhi, !py && jw == 0,
-                         !py && jw == n1 - 1, b, (qi + jw) & 1, li, ri, lneg, rneg, cmx, cpx, dx, sy[x], sy[ny + x],
-                         sy[2 * ny + x], zc, w, omc);
+                if (RS) {
+                    // red: own half 0, k = 2m + parity
+                    const bool ylo = !py && jw == 0, yhi = !py && jw == n1 - 1;
+                    if (((qi + jw) & 1) == 0)
+                        fu_strip_rs<0>(pc + off, pm + off, pp + off, rr + x * n2, n2, H, 0, k0, xlo, xhi, ylo, yhi,
+                                       b, cmx, cpx, dx, sy[x], sy[ny + x], sy[2 * ny + x], zc[0], w, omc);
+                    else
+                        fu_strip_rs<1>(pc + off, pm + off, pp + off, rr + x * n2, n2, H, 0, k0, xlo, xhi, ylo, yhi,
+                                       b, cmx, cpx, dx, sy[x], sy[ny + x], sy[2 * ny + x], zc[1], w, omc);
+                } else {
+                    fu_strip(pc + off, pm + off, pp + off, rr + x * n2, n2, k0, xlo, xhi, !py && jw == 0,
+                             !py && jw == n1 - 1, b, (qi + jw) & 1, li, ri, lneg, rneg, cmx, cpx, dx, sy[x],
+                             sy[ny + x], sy[2 * ny + x], zc[0], w, omc);
+                }
             }
         }
         // this thread's writes (R(q), K(q-2)) before the async proxy reads them
@@ -515,9 +598,22 @@ __global__ void __launch_bounds__(FU_THREADS, 1)
             for (int x = ro; x < tj; x += rstep) {
                 const int j = j0 + x;
                 const int off = (x + 2) * n2;
-                fu_strip(pc + off, pm + off, pp + off, rr + (x + 1) * n2, n2, k0, xlo, xhi, !py && j == 0,
-                         !py && j == n1 - 1, b, (1 + p + j) & 1, li, ri, lneg, rneg, cmx, cpx, dx, sy[x + 1],
-                         sy[ny + x + 1], sy[2 * ny + x + 1], zc, w, omc);
+                if (RS) {
+                    // black: own half H, k = 2m + 1 - parity
+                    const bool ylo = !py && j == 0, yhi = !py && j == n1 - 1;
+                    if (((p + j) & 1) == 1)
+                        fu_strip_rs<0>(pc + off, pm + off, pp + off, rr + (x + 1) * n2, n2, H, H, k0, xlo, xhi, ylo,
+                                       yhi, b, cmx, cpx, dx, sy[x + 1], sy[ny + x + 1], sy[2 * ny + x + 1], zc[0], w,
+                                       omc);
+                    else
+                        fu_strip_rs<1>(pc + off, pm + off, pp + off, rr + (x + 1) * n2, n2, H, H, k0, xlo, xhi, ylo,
+                                       yhi, b, cmx, cpx, dx, sy[x + 1], sy[ny + x + 1], sy[2 * ny + x + 1], zc[1], w,
+                                       omc);
+                } else {
+                    fu_strip(pc + off, pm + off, pp + off, rr + (x + 1) * n2, n2, k0, xlo, xhi, !py && j == 0,
+                             !py && j == n1 - 1, b, (1 + p + j) & 1, li, ri, lneg, rneg, cmx, cpx, dx, sy[x + 1],
+                             sy[ny + x + 1], sy[2 * ny + x + 1], zc[0], w, omc);
+                }
             }
         }
     }
@@ -594,14 +690,15 @@ void fused_plan(Level &v, int sms) {
         !encode3(&m.fb, v.e32b, L, tj) || !encode3(&m.fb2, v.e32b, L, 2) || !encode3(&m.fr, v.r32, L, tj) ||
         !encode3(&m.fr1, v.r32, L, 1))
         return;
-    if (cudaFuncSetAttribute(k_rbgs_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess) {
+    if (cudaFuncSetAttribute(k_rbgs_fused<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess ||
+        cudaFuncSetAttribute(k_rbgs_fused<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess) {
         cudaGetLastError();
         return;
     }
     // the block must fit an SM (registers and shared memory) or the level
     // keeps the colour sweeps
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rbgs_fused, FU_THREADS, fused_smem(tj, L.n2)) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rbgs_fused<true>, FU_THREADS, fused_smem(tj, L.n2)) !=
             cudaSuccess ||
         per_sm < 1) {
         cudaGetLastError();
@@ -621,7 +718,9 @@ void fused_plan(Level &v, int sms) {
 // buffer for it): 3-D, rows of 128 or 256 cells, FU_TILE-cell tiles that
 // divide the level's rows, at least FU_MIN_CELLS cells.
 bool fused_sweep_fits(const Lay &L, bool d3) {
-    if (!d3 || L.n2 < 128 || L.n2 > 256 || FU_TILE % L.n2 != 0 || FU_NT % (L.n2 / 4) != 0) return false;
+    if (!d3 || L.n2 < 128 || L.n2 > 256 || FU_TILE % L.n2 != 0 || FU_NT % (L.n2 / 4) != 0 ||
+        FU_NT % (L.n2 / 8) != 0)
+        return false;
     const int tj = FU_TILE / L.n2;
     return L.n1 % tj == 0 && L.n0 >= 16 && (int64_t)L.n0 * L.n1 * L.n2 >= FU_MIN_CELLS;
 }
@@ -686,7 +785,8 @@ bool tma_fused(saras_mg *h, cudaStream_t s, Level &v, bool to_b) {
     const TmaPlan &m = v.tma;
     const dim3 grid((unsigned)(L.n1 / m.ftj), (unsigned)((L.n0 + m.fchunk - 1) / m.fchunk));
     int *err = reinterpret_cast<int *>(h->norm_out + 7);
-    launch_pdl(k_rbgs_fused, grid, dim3(FU_THREADS), fused_smem(m.ftj, L.n2), s, to_b ? m.fa : m.fb,
+    launch_pdl(v.rs ? k_rbgs_fused<true> : k_rbgs_fused<false>, grid, dim3(FU_THREADS), fused_smem(m.ftj, L.n2), s,
+               to_b ? m.fa : m.fb,
                to_b ? m.fa2 : m.fb2, to_b ? m.fb : m.fa, m.fr, m.fr1, L, sweep_tab(v), sweep_bnd(h),
                (float)h->prm.sor_param, (float)(1.0 - h->prm.sor_param), m.ftj, m.fchunk, err);
     return true;

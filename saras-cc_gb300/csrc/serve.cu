@@ -962,6 +962,8 @@ AdmitStep admit_step(saras_serve *h, ServeCase &c, std::vector<ServeCase> &dst) 
             h->done.push_back(ServeDone{c.id, 0.0, 0, (int32_t)s, since(c)});
             return ADMIT_DONE;
         }
+        rk3_multigrid(rk)->no_rowsplit = true;
+        rk3_multigrid(rk)->lv[0].rs = 0;
         h->bytes_alloc += rk3_device_bytes(rk) + rk3_multigrid(rk)->dev_bytes;
     }
     c.rk = rk;
@@ -1063,6 +1065,10 @@ saras_status admit(saras_serve *h, std::vector<ServeCase> &dst) {
                 break;  // wait for retirements to free memory
             }
             saras_status s = mg_create_queued(&c.grid, &p, h->adm, &m);
+            if (s == SARAS_OK) {
+                m->no_rowsplit = true;
+                m->lv[0].rs = 0;
+            }
             if (s != SARAS_OK) {
                 h->done.push_back(ServeDone{c.id, 0.0, 0, (int32_t)s,
                                             std::chrono::duration<double>(Clock::now() - c.t_submit).count()});

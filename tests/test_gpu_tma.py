@@ -37,6 +37,10 @@ GRIDS = [
     # every axis periodic: the fused iteration's wraps in x, y and z (rows
     # read across the row's ends) and the single-block bottom on a periodic box
     ("fused_128x128x256_ppp", dict(n=(128, 128, 256), length=(1.0, 1.0, 2.0), mesh="UUU", domain="PPP"), MG),
+    # even smoothing counts: the finest level is stored row-split (each row's
+    # red cells, then its black cells) for the fused iteration
+    ("rowsplit_128x128x256_ppp_2x2", dict(n=(128, 128, 256), length=(1.0, 1.0, 2.0), mesh="UUU", domain="PPP"),
+     dict(mg_tolerance=1e-9, pre_smooth=2, post_smooth=2)),
 ]
 DDD = dict(n=(128, 128, 256), length=(1.0, 1.0, 2.0), mesh="DDD", beta=(1.05, 1.05, 1.1), domain="NNN")
 
@@ -71,6 +75,9 @@ ORACLE_CASES = [
     # walls on every face
     ("bottom_128c_dirichlet", dict(n=(128, 128, 128), mesh="UUD", beta=(1, 1, 1.2), domain="NNN"),
      dict(MG, bc_kind=[1, 1, 1, 1, 1, 1])),
+    # the row-split finest level with Dirichlet z walls
+    ("rowsplit_dirichlet_z_2x2", GRIDS[4][1], dict(mg_tolerance=1e-9, pre_smooth=2, post_smooth=2,
+                                                   bc_kind=[0, 0, 0, 0, 1, 1])),
 ]
 
 
