@@ -302,15 +302,28 @@ __global__ void __launch_bounds__(TMA_WS_THREADS) k_rbgs_tma(const __grid_consta
 // concurrent reader expects).  A producer lane streams e planes through a
 // ring of FU_ESLOTS slots and r planes through FU_RSLOTS slots, two steps
 // ahead of their first use.
-constexpr int FU_CONSUMERS = 12;
-constexpr int FU_NT = 32 * FU_CONSUMERS;
-constexpr int FU_THREADS = FU_NT + 32;
+//
+// Consumer warps: 12 on the plain layout; 9 on the row-split layout, whose
+// strips carry fewer instructions, so that its per-step barrier waits on
+// fewer warps (9 warps give every thread two of the 18 rows of R at 256-cell
+// rows).
+template <bool RS>
+__host__ __device__ constexpr int fu_nt() {
+    return 32 * (RS ? 9 : 12);
+}
+template <bool RS>
+__host__ __device__ constexpr int fu_threads() {
+    return fu_nt<RS>() + 32;
+}
 constexpr int FU_ESLOTS = 6, FU_RSLOTS = 4;
 constexpr int FU_TILE = 4096;
 constexpr int64_t FU_MIN_CELLS = int64_t(1) << 22;
 constexpr size_t FU_HEAD = 1024;  // mbarriers and the tile's y coefficients
 
-__device__ __forceinline__ void consumer_sync() { asm volatile("bar.sync 1, %0;" ::"r"(FU_NT) : "memory"); }
+template <int NT>
+__device__ __forceinline__ void consumer_sync() {
+    asm volatile("bar.sync 1, %0;" ::"r"(NT) : "memory");
+}
 __device__ __forceinline__ int wrap(int a, int n) { return ((a % n) + n) % n; }
 
 // Colour cells of the strip at row[k0 .. k0+3] (a tile row of e in shared
@@ -322,10 +335,16 @@ __device__ __forceinline__ void fu_strip(float *row, const float *xmr, const flo
                                          float cmy, float cpy, float dy, const float (&zc)[3][4], float w,
                                          float omc) {
     const float4 cur = lds4(row + k0);
-    const float4 xm = xlo ? mirror4(cur, b.sg_lo[0]) : lds4(xmr + k0);
-    const float4 xp = xhi ? mirror4(cur, b.sg_hi[0]) : lds4(xpr + k0);
-    const float4 ym = ylo ? mirror4(cur, b.sg_lo[1]) : lds4(row - n2 + k0);
-    const float4 yp = yhi ? mirror4(cur, b.sg_hi[1]) : lds4(row + n2 + k0);
+    // the neighbour rows always exist in the slots (halo rows, ghost or
+    // out-of-range planes), so they are loaded unconditionally and replaced
+    // by mirrors only on a wall (rare, and the same for a whole warp)
+    float4 xm = lds4(xmr + k0), xp = lds4(xpr + k0), ym = lds4(row - n2 + k0), yp = lds4(row + n2 + k0);
+    if (xlo | xhi | ylo | yhi) {
+        if (xlo) xm = mirror4(cur, b.sg_lo[0]);
+        if (xhi) xp = mirror4(cur, b.sg_hi[0]);
+        if (ylo) ym = mirror4(cur, b.sg_lo[1]);
+        if (yhi) yp = mirror4(cur, b.sg_hi[1]);
+    }
     const float4 fr = lds4(rrow + k0);
     const float lv = row[li], rv = row[ri];
     const float left = lneg ? -lv : lv, right = rneg ? -rv : rv;
@@ -352,10 +371,15 @@ __device__ __forceinline__ void fu_strip_rs(float *row, const float *xmr, const 
                                             float dy, const float (&zc)[3][4], float w, float omc) {
     const int oth = H - own;
     const float4 cur4 = lds4(row + own + m);
-    const float4 xm4 = xlo ? mirror4(cur4, b.sg_lo[0]) : lds4(xmr + oth + m);
-    const float4 xp4 = xhi ? mirror4(cur4, b.sg_hi[0]) : lds4(xpr + oth + m);
-    const float4 ym4 = ylo ? mirror4(cur4, b.sg_lo[1]) : lds4(row - n2 + oth + m);
-    const float4 yp4 = yhi ? mirror4(cur4, b.sg_hi[1]) : lds4(row + n2 + oth + m);
+    // neighbour rows always exist in the slots; mirrors replace them on walls
+    float4 xm4 = lds4(xmr + oth + m), xp4 = lds4(xpr + oth + m);
+    float4 ym4 = lds4(row - n2 + oth + m), yp4 = lds4(row + n2 + oth + m);
+    if (xlo | xhi | ylo | yhi) {
+        if (xlo) xm4 = mirror4(cur4, b.sg_lo[0]);
+        if (xhi) xp4 = mirror4(cur4, b.sg_hi[0]);
+        if (ylo) ym4 = mirror4(cur4, b.sg_lo[1]);
+        if (yhi) yp4 = mirror4(cur4, b.sg_hi[1]);
+    }
     const float4 f4 = lds4(rrow + own + m);
     const float4 a4 = lds4(row + oth + m);
     const float c[4] = {cur4.x, cur4.y, cur4.z, cur4.w};
@@ -404,11 +428,12 @@ __device__ __forceinline__ void fu_strip_rs(float *row, const float *xmr, const 
 // esrc / esrc2: source e with boxes of tj rows and of two rows; edst:
 // destination e, tj rows; rld / rld1: r with tj rows and one row.
 template <bool RS>
-__global__ void __launch_bounds__(FU_THREADS, 1)
+__global__ void __launch_bounds__(fu_threads<RS>(), 1)
     k_rbgs_fused(const __grid_constant__ CUtensorMap esrc, const __grid_constant__ CUtensorMap esrc2,
                  const __grid_constant__ CUtensorMap edst, const __grid_constant__ CUtensorMap rld,
                  const __grid_constant__ CUtensorMap rld1, Lay L, Tab3<float> t, Bnd b, float w, float omc, int tj,
                  int chunk, int *err) {
+    constexpr int NT = fu_nt<RS>();
     pdl_enter();
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ int s_fail;
@@ -499,7 +524,7 @@ __global__ void __launch_bounds__(FU_THREADS, 1)
     // RS those of both colour offsets o)
     const int H = n2 >> 1;
     const int s4 = RS ? (H >> 2) : (n2 >> 2);
-    const int k0 = (ct % s4) * 4, ro = ct / s4, rstep = FU_NT / s4;
+    const int k0 = (ct % s4) * 4, ro = ct / s4, rstep = NT / s4;
     float zc[2][3][4];
 #pragma unroll
     for (int oo = 0; oo < (RS ? 2 : 1); oo++)
@@ -515,14 +540,14 @@ __global__ void __launch_bounds__(FU_THREADS, 1)
     const int ri = k0 + 4 < n2 ? k0 + 4 : (b.per[2] ? 0 : k0 + 3);
     const bool rneg = k0 + 4 >= n2 && !b.per[2] && b.sg_hi[2] < 0;
     const int ny = tj + 2;
-    for (int x = ct; x < ny; x += FU_NT) {
+    for (int x = ct; x < ny; x += NT) {
         const int j = j0 - 1 + x;
         const int jw = b.per[1] ? wrap(j, n1) : min(max(j, 0), n1 - 1);
         sy[x] = t.cm[1][jw];
         sy[ny + x] = t.cp[1][jw];
         sy[2 * ny + x] = t.dg[1][jw];
     }
-    consumer_sync();
+    consumer_sync<NT>();
     auto eptr = [&](int p) { return es + ((p - P0) % FU_ESLOTS) * e_slot; };
     auto rptr = [&](int p) { return rs + ((p - Q0) % FU_RSLOTS) * r_slot; };
     auto wait_e = [&](int p) {
@@ -576,7 +601,7 @@ __global__ void __launch_bounds__(FU_THREADS, 1)
         }
         // this thread's writes (R(q), K(q-2)) before the async proxy reads them
         fence_async_smem();
-        consumer_sync();
+        consumer_sync<NT>();
         if (ct == 0 && !s_fail) {
             if (q - 2 >= i0) {
                 tma_store3(&edst, eptr(q - 2) + 2 * n2, KOFF, j0 + 1, q - 1);
@@ -618,7 +643,7 @@ __global__ void __launch_bounds__(FU_THREADS, 1)
         }
     }
     fence_async_smem();
-    consumer_sync();
+    consumer_sync<NT>();
     if (ct == 0) {
         if (!s_fail) {
             tma_store3(&edst, eptr(i1 - 1) + 2 * n2, KOFF, j0 + 1, i1);
@@ -697,13 +722,16 @@ void fused_plan(Level &v, int sms) {
     }
     // the block must fit an SM (registers and shared memory) or the level
     // keeps the colour sweeps
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rbgs_fused<true>, FU_THREADS, fused_smem(tj, L.n2)) !=
-            cudaSuccess ||
-        per_sm < 1) {
+    int per_sm = 0, per_sm_rs = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rbgs_fused<false>, fu_threads<false>(),
+                                                      fused_smem(tj, L.n2)) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_rs, k_rbgs_fused<true>, fu_threads<true>(),
+                                                      fused_smem(tj, L.n2)) != cudaSuccess ||
+        per_sm < 1 || per_sm_rs < 1) {
         cudaGetLastError();
         return;
     }
+    per_sm = std::min(per_sm, per_sm_rs);
     // one wave: the chunks of every tile column fill the resident blocks
     const int nch = std::max(1, per_sm * sms / (L.n1 / tj));
     const int chunk = std::max(8, (L.n0 + nch - 1) / nch);
@@ -718,8 +746,10 @@ void fused_plan(Level &v, int sms) {
 // buffer for it): 3-D, rows of 128 or 256 cells, FU_TILE-cell tiles that
 // divide the level's rows, at least FU_MIN_CELLS cells.
 bool fused_sweep_fits(const Lay &L, bool d3) {
-    if (!d3 || L.n2 < 128 || L.n2 > 256 || FU_TILE % L.n2 != 0 || FU_NT % (L.n2 / 4) != 0 ||
-        FU_NT % (L.n2 / 8) != 0)
+    // every consumer thread owns one strip of each row it visits: strips of
+    // four cells of the row (plain layout) or of a row half (row-split)
+    if (!d3 || L.n2 < 128 || L.n2 > 256 || FU_TILE % L.n2 != 0 || fu_nt<false>() % (L.n2 / 4) != 0 ||
+        fu_nt<true>() % (L.n2 / 8) != 0)
         return false;
     const int tj = FU_TILE / L.n2;
     return L.n1 % tj == 0 && L.n0 >= 16 && (int64_t)L.n0 * L.n1 * L.n2 >= FU_MIN_CELLS;
@@ -785,9 +815,9 @@ bool tma_fused(saras_mg *h, cudaStream_t s, Level &v, bool to_b) {
     const TmaPlan &m = v.tma;
     const dim3 grid((unsigned)(L.n1 / m.ftj), (unsigned)((L.n0 + m.fchunk - 1) / m.fchunk));
     int *err = reinterpret_cast<int *>(h->norm_out + 7);
-    launch_pdl(v.rs ? k_rbgs_fused<true> : k_rbgs_fused<false>, grid, dim3(FU_THREADS), fused_smem(m.ftj, L.n2), s,
-               to_b ? m.fa : m.fb,
-               to_b ? m.fa2 : m.fb2, to_b ? m.fb : m.fa, m.fr, m.fr1, L, sweep_tab(v), sweep_bnd(h),
+    const dim3 block((unsigned)(v.rs ? fu_threads<true>() : fu_threads<false>()));
+    launch_pdl(v.rs ? k_rbgs_fused<true> : k_rbgs_fused<false>, grid, block, fused_smem(m.ftj, L.n2), s,
+               to_b ? m.fa : m.fb, to_b ? m.fa2 : m.fb2, to_b ? m.fb : m.fa, m.fr, m.fr1, L, sweep_tab(v), sweep_bnd(h),
                (float)h->prm.sor_param, (float)(1.0 - h->prm.sor_param), m.ftj, m.fchunk, err);
     return true;
 }
