@@ -560,8 +560,16 @@ __global__ void k_coarsest_fast(double *ug, const double *__restrict__ fg, const
 // the steps separated by block barriers.  Each step has the arithmetic of
 // the kernel it replaces (k_rbgs32, k_resid_restrict, k_coarsest_fast,
 // k_prolong_add), cell for cell, so the V-cycle's bits do not change.
+//
+// Inside the block everything is latency, so the block keeps every operand
+// in shared memory: the levels' coefficient and restriction-weight tables
+// and the coarsest level's tables are copied in, each level's colour cells
+// are listed once as packed (i, j, k/2) (before the wait on the previous
+// kernel), and a thread forms all of its cells of a sweep (at most BOT_CPT)
+// before it writes any of them back.
 constexpr int BOT_MAX = 4;  // FP32 levels above the coarsest
-constexpr int BOT_THREADS = 256;
+constexpr int BOT_THREADS = 512;
+constexpr int BOT_CPT = 4;  // colour cells per thread and sweep
 
 struct BotArgs {
     int nb;  // FP32 levels held: lb .. lb + nb - 1, then the coarsest
@@ -578,24 +586,97 @@ struct BotArgs {
     double omc64, tol;
     int max_count, stall, pre, post;
     int *sweeps_out;
-    unsigned off[2 * BOT_MAX + 4];  // shared-memory byte offsets: e, r per level; u, f, wd, dd
+    // shared-memory byte offsets: e, r per level; u, f, wd, dd; the tables
+    // of each level (coefficients, then the next level's restriction
+    // weights), the coarsest level's tables; each level's colour-cell list
+    unsigned off[2 * BOT_MAX + 4];
+    unsigned toff[BOT_MAX], tcoff, loff[BOT_MAX];
 };
+
+// Asynchronous global -> shared copies (cp.async): a thread issues all of
+// its copies back to back and waits once, so the block's set-up is one
+// round trip to L2 however many arrays it gathers.
+__device__ __forceinline__ void cpa(void *dst, const float *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(__cvta_generic_to_global(src))
+                 : "memory");
+}
+__device__ __forceinline__ void cpa(void *dst, const double *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(__cvta_generic_to_global(src))
+                 : "memory");
+}
+__device__ __forceinline__ void cpa_wait() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Shared-memory copies of a level's tables (every thread issues a share of
+// the copies); the pointers go to the shared struct `s` (thread 0).
+template <class T>
+__device__ void bot_tab(const Tab3<T> &g, const Lay &L, T *p, Tab3<T> *s) {
+    const int n[3] = {L.n0, L.n1, L.n2};
+    for (int d = 0; d < 3; d++) {
+        if (threadIdx.x == 0) {
+            s->cm[d] = p;
+            s->cp[d] = p + n[d];
+            s->dg[d] = p + 2 * n[d];
+        }
+        for (int q = threadIdx.x; q < n[d]; q += blockDim.x) {
+            cpa(p + q, g.cm[d] + q);
+            cpa(p + n[d] + q, g.cp[d] + q);
+            cpa(p + 2 * n[d] + q, g.dg[d] + q);
+        }
+        p += 3 * n[d];
+    }
+}
+__device__ void bot_wtab(const WTab<float> &g, const Lay &Lc, float *p, WTab<float> *s) {
+    const int n[3] = {Lc.n0, Lc.n1, Lc.n2};
+    for (int d = 0; d < 3; d++) {
+        if (threadIdx.x == 0) {
+            s->w0[d] = p;
+            s->w1[d] = p + n[d];
+        }
+        for (int q = threadIdx.x; q < n[d]; q += blockDim.x) {
+            cpa(p + q, g.w0[d] + q);
+            cpa(p + n[d] + q, g.w1[d] + q);
+        }
+        p += 2 * n[d];
+    }
+}
+
+// Colour column q of a level (q < n0 n1 ceil(n2/2)) as (i << 20 | j << 10 | k/2).
+__device__ __forceinline__ unsigned bot_pack(const Lay &L, int q) {
+    const int half = (L.n2 + 1) / 2;
+    const int kk = q % half, rest = q / half, j = rest % L.n1, i = rest / L.n1;
+    return ((unsigned)i << 20) | ((unsigned)j << 10) | (unsigned)kk;
+}
 
 template <bool D3>
 __device__ void bot_smooth(float *e, const float *r, const Lay &L, const Tab3<float> &t, const Bnd &b, int count,
-                           float w, float omc) {
+                           float w, float omc, const unsigned *lst) {
     const int half = (L.n2 + 1) / 2, ncol = L.n0 * L.n1 * half;
     for (int n = 0; n < count; n++)
         for (int colour = 0; colour < 2; colour++) {
-            for (int q = threadIdx.x; q < ncol; q += blockDim.x) {
-                const int kk = q % half, rest = q / half, j = rest % L.n1, i = rest / L.n1;
-                const int k = 2 * kk + ((i + j + colour) & 1);
+            // the sweep's cells read only cells of the other colour: all
+            // of a thread's cells are formed before any is written
+            float nv[BOT_CPT];
+            int cc[BOT_CPT];
+#pragma unroll
+            for (int m = 0; m < BOT_CPT; m++) {
+                cc[m] = -1;
+                const int q = threadIdx.x + m * blockDim.x;
+                if (q >= ncol) continue;
+                const unsigned pk = lst[q];
+                const int i = (int)(pk >> 20), j = (int)((pk >> 10) & 1023u);
+                const int k = 2 * (int)(pk & 1023u) + ((i + j + colour) & 1);
                 if (k >= L.n2) continue;
                 const int64_t c = L.at(i, j, k);
                 const float uc = e[c];
                 const float sv = offdiag<float, D3>(e, L, t, b, i, j, k, c, uc) - r[c];
-                e[c] = fmat(omc, uc, sweep_div(w * sv, diag<float, D3>(t, i, j, k)));
+                nv[m] = fmat(omc, uc, sweep_div(w * sv, diag<float, D3>(t, i, j, k)));
+                cc[m] = (int)c;
             }
+#pragma unroll
+            for (int m = 0; m < BOT_CPT; m++)
+                if (cc[m] >= 0) e[cc[m]] = nv[m];
             __syncthreads();
         }
 }
@@ -621,64 +702,107 @@ __device__ void bot_restrict(const float *e, const float *r, const Lay &Lf, cons
     }
 }
 
+// e_fine += e_coarse of the parent cell, by coarse cells: the eight children
+// are read before any is written.
 template <class TC>
 __device__ void bot_prolong(float *ef, const TC *ec, const Lay &Lf, const Lay &Lc) {
-    const int ncell = Lf.n0 * Lf.n1 * Lf.n2;
+    const int ncell = Lc.n0 * Lc.n1 * Lc.n2;
     for (int q = threadIdx.x; q < ncell; q += blockDim.x) {
-        const int k = q % Lf.n2, rest = q / Lf.n2, j = rest % Lf.n1, i = rest / Lf.n1;
-        const int64_t c = Lf.at(i, j, k);
-        ef[c] = ef[c] + (float)ec[Lc.at(i >> 1, j >> 1, k >> 1)];
+        const int k = q % Lc.n2, rest = q / Lc.n2, j = rest % Lc.n1, i = rest / Lc.n1;
+        const float v = (float)ec[Lc.at(i, j, k)];
+        float o[8];
+        int cc[8];
+#pragma unroll
+        for (int x = 0; x < 8; x++) {
+            const int fi = 2 * i + (x >> 2), fj = 2 * j + ((x >> 1) & 1), fk = 2 * k + (x & 1);
+            cc[x] = -1;
+            if (fi < Lf.n0 && fj < Lf.n1 && fk < Lf.n2) {
+                cc[x] = (int)Lf.at(fi, fj, fk);
+                o[x] = ef[cc[x]] + v;
+            }
+        }
+#pragma unroll
+        for (int x = 0; x < 8; x++)
+            if (cc[x] >= 0) ef[cc[x]] = o[x];
     }
 }
 
 template <bool D3>
 __global__ void __launch_bounds__(BOT_THREADS) k_bottom(const __grid_constant__ BotArgs a) {
-    pdl_enter();
     extern __shared__ __align__(16) unsigned char bsm[];
     __shared__ unsigned long long shm[32];
-    float *e[BOT_MAX], *r[BOT_MAX];
-    for (int m = 0; m < a.nb; m++) {
-        e[m] = reinterpret_cast<float *>(bsm + a.off[2 * m]);
-        r[m] = reinterpret_cast<float *>(bsm + a.off[2 * m + 1]);
-    }
+    // the levels' table pointers (the same for every thread) live in shared
+    // memory, and the arrays' addresses are formed from the offsets where
+    // they are used: nothing per level sits in per-thread local memory
+    __shared__ Tab3<float> st[BOT_MAX];
+    __shared__ WTab<float> sw[BOT_MAX];
+    __shared__ Tab3<double> stc;
+    auto E = [&](int m) { return reinterpret_cast<float *>(bsm + a.off[2 * m]); };
+    auto R = [&](int m) { return reinterpret_cast<float *>(bsm + a.off[2 * m + 1]); };
+    auto LST = [&](int m) { return reinterpret_cast<unsigned *>(bsm + a.loff[m]); };
     double *u = reinterpret_cast<double *>(bsm + a.off[2 * BOT_MAX]);
     double *f = reinterpret_cast<double *>(bsm + a.off[2 * BOT_MAX + 1]);
     double *wd = reinterpret_cast<double *>(bsm + a.off[2 * BOT_MAX + 2]);
     double *dd = reinterpret_cast<double *>(bsm + a.off[2 * BOT_MAX + 3]);
-    // every e starts from zero (the restriction into a level clears it);
-    // ghosts stay zero and are never read
-    for (int64_t q = threadIdx.x; q < a.L[0].size; q += blockDim.x) {
-        e[0][q] = 0.f;
-        r[0][q] = a.r_top[q];
+    // on-chip set-up before the wait on the previous kernels: cell lists
+    // and zeroed arrays (every e starts from zero; the restriction into a
+    // level clears it; ghosts stay zero and are never read)
+    for (int m = 0; m < a.nb; m++) {
+        unsigned *l = LST(m);
+        const int ncol = a.L[m].n0 * a.L[m].n1 * ((a.L[m].n2 + 1) / 2);
+        for (int q = threadIdx.x; q < ncol; q += blockDim.x) l[q] = bot_pack(a.L[m], q);
+        float *em = E(m), *rm = R(m);
+        for (int64_t q = threadIdx.x; q < a.L[m].size; q += blockDim.x) {
+            em[q] = 0.f;
+            if (m > 0) rm[q] = 0.f;
+        }
     }
-    for (int m = 1; m < a.nb; m++)
-        for (int64_t q = threadIdx.x; q < a.L[m].size; q += blockDim.x) e[m][q] = r[m][q] = 0.f;
     for (int64_t q = threadIdx.x; q < a.Lc.size; q += blockDim.x) {
         u[q] = 0.0;
         f[q] = 0.0;
-        wd[q] = a.wdc[q];
-        dd[q] = a.ddc[q];
     }
+    // global memory only after the wait (earlier kernels may still run
+    // before it)
+    pdl_enter();
+    for (int m = 0; m < a.nb; m++) {
+        float *tp = reinterpret_cast<float *>(bsm + a.toff[m]);
+        bot_tab<float>(a.t[m], a.L[m], tp, &st[m]);
+        const Lay &Ln = m + 1 < a.nb ? a.L[m + 1] : a.Lc;
+        bot_wtab(a.w[m + 1], Ln, tp + 3 * (a.L[m].n0 + a.L[m].n1 + a.L[m].n2), &sw[m]);
+    }
+    bot_tab<double>(a.tc, a.Lc, reinterpret_cast<double *>(bsm + a.tcoff), &stc);
+    for (int64_t q = threadIdx.x; q < a.Lc.size; q += blockDim.x) {
+        cpa(wd + q, a.wdc + q);
+        cpa(dd + q, a.ddc + q);
+    }
+    {
+        float *r0 = R(0);
+        for (int64_t q = threadIdx.x; q < a.L[0].size; q += blockDim.x) cpa(r0 + q, a.r_top + q);
+    }
+    cpa_wait();
     __syncthreads();
     for (int m = 0; m < a.nb; m++) {
-        bot_smooth<D3>(e[m], r[m], a.L[m], a.t[m], a.b, a.pre, a.w32, a.omc32);
+        bot_smooth<D3>(E(m), R(m), a.L[m], st[m], a.b, a.pre, a.w32, a.omc32, LST(m));
         if (m + 1 < a.nb)
-            bot_restrict<float, D3>(e[m], r[m], a.L[m], a.t[m], a.b, a.w[m + 1], r[m + 1], a.L[m + 1]);
+            bot_restrict<float, D3>(E(m), R(m), a.L[m], st[m], a.b, sw[m], R(m + 1), a.L[m + 1]);
         else
-            bot_restrict<double, D3>(e[m], r[m], a.L[m], a.t[m], a.b, a.w[m + 1], f, a.Lc);
+            bot_restrict<double, D3>(E(m), R(m), a.L[m], st[m], a.b, sw[m], f, a.Lc);
         __syncthreads();
     }
-    const int sweeps = coarsest_cached<D3>(u, f, wd, dd, a.Lc, a.tc, a.b, a.omc64, a.tol, a.max_count, a.stall, shm);
+    const int sweeps = coarsest_cached<D3>(u, f, wd, dd, a.Lc, stc, a.b, a.omc64, a.tol, a.max_count, a.stall, shm);
     __syncthreads();
     for (int m = a.nb - 1; m >= 0; m--) {
         if (m == a.nb - 1)
-            bot_prolong<double>(e[m], u, a.L[m], a.Lc);
+            bot_prolong<double>(E(m), u, a.L[m], a.Lc);
         else
-            bot_prolong<float>(e[m], e[m + 1], a.L[m], a.L[m + 1]);
+            bot_prolong<float>(E(m), E(m + 1), a.L[m], a.L[m + 1]);
         __syncthreads();
-        bot_smooth<D3>(e[m], r[m], a.L[m], a.t[m], a.b, a.post, a.w32, a.omc32);
+        bot_smooth<D3>(E(m), R(m), a.L[m], st[m], a.b, a.post, a.w32, a.omc32, LST(m));
     }
-    for (int64_t q = threadIdx.x; q < a.L[0].size; q += blockDim.x) a.e_top[q] = e[0][q];
+    {
+        const float *e0 = E(0);
+        for (int64_t q = threadIdx.x; q < a.L[0].size; q += blockDim.x) a.e_top[q] = e0[q];
+    }
     if (threadIdx.x == 0) *a.sweeps_out += sweeps;
 }
 
@@ -1174,12 +1298,41 @@ saras_status fast_setup(saras_mg *h) {
 }
 
 // The MIXED form's single-block bottom (k_bottom): the FP32 levels above
-// the coarsest whose colour sweeps are one cell per thread, as long as
-// their e and r and the coarsest level's FP64 arrays fit BOT_SMEM bytes of
-// shared memory.  Needs a 3-D hierarchy and a coarsest level swept in
-// registers (no exact solve).  At 256^3 it holds 8^3 and 4^3 and replaces
-// eleven launches per V-cycle (about 1% of the solve).
+// the coarsest whose colour sweeps are at most BOT_CPT cells per thread, as
+// long as everything the block keeps fits BOT_SMEM bytes of shared memory.
+// Needs a 3-D hierarchy and a coarsest level swept in registers (no exact
+// solve).  At 256^3 it holds 16^3, 8^3 and 4^3 and replaces twenty-one
+// launches per V-cycle.
 constexpr size_t BOT_SMEM = 160 * 1024;
+
+int64_t bot_ncol(const Lay &L) { return (int64_t)L.n0 * L.n1 * ((L.n2 + 1) / 2); }
+
+// k_bottom's shared memory when it holds levels lb .. the coarsest: the
+// offsets go to `a`, the bytes are returned.
+size_t bot_layout(const saras_mg *h, int lb, BotArgs *a) {
+    const int top = h->nl - 1;
+    auto al = [](size_t x) { return (x + 15) / 16 * 16; };
+    size_t off = 0;
+    for (int m = 0; m < top - lb; m++) {
+        const Lay &L = h->lv[(size_t)(lb + m)].lay, &Ln = h->lv[(size_t)(lb + m + 1)].lay;
+        a->off[2 * m] = (unsigned)off;
+        off += al((size_t)L.size * sizeof(float));
+        a->off[2 * m + 1] = (unsigned)off;
+        off += al((size_t)L.size * sizeof(float));
+        a->toff[m] = (unsigned)off;
+        off += al((size_t)(3 * (L.n0 + L.n1 + L.n2) + 2 * (Ln.n0 + Ln.n1 + Ln.n2)) * sizeof(float));
+        a->loff[m] = (unsigned)off;
+        off += al((size_t)bot_ncol(L) * sizeof(unsigned));
+    }
+    const Lay &C = h->lv[(size_t)top].lay;
+    for (int q = 0; q < 4; q++) {
+        a->off[2 * BOT_MAX + q] = (unsigned)off;
+        off += al((size_t)C.size * sizeof(double));
+    }
+    a->tcoff = (unsigned)off;
+    off += al((size_t)3 * (C.n0 + C.n1 + C.n2) * sizeof(double));
+    return off;
+}
 
 void bottom_plan(saras_mg *h) {
     h->bottom = -1;
@@ -1189,19 +1342,20 @@ void bottom_plan(saras_mg *h) {
     const Level &c = h->lv[(size_t)top];
     if (c.fdv.ok) return;
     const Lay &C = c.lay;
-    if ((int64_t)C.n0 * C.n1 * ((C.n2 + 1) / 2) > BOT_THREADS) return;
-    auto al = [](size_t x) { return (x + 15) / 16 * 16; };
-    size_t total = 4 * al((size_t)C.size * sizeof(double));
+    // the coarsest solve keeps one cell of each colour and two residual
+    // cells per thread in registers
+    if (bot_ncol(C) > BOT_THREADS || (int64_t)C.n0 * C.n1 * C.n2 > 2 * BOT_THREADS) return;
+    BotArgs tmp{};
     int lb = top;
     while (lb - 1 >= 1 && top - (lb - 1) <= BOT_MAX) {
-        // a level joins while its colour sweep is one cell per thread: one
-        // block is slower than a multi-block launch on anything larger
-        // (16^3: 93 us per V-cycle in the block against 52 us in launches)
-        const Lay &L = h->lv[(size_t)lb - 1].lay;
-        if ((int64_t)L.n0 * L.n1 * ((L.n2 + 1) / 2) > BOT_THREADS) break;
-        const size_t add = 2 * al((size_t)L.size * sizeof(float));
-        if (total + add > BOT_SMEM) break;
-        total += add;
+        // a level joins while its colour sweep is at most BOT_CPT cells per
+        // thread (the packed cell lists need i < 4096, j < 1024, k < 2048),
+        // each of its cells has its parent on the next level, and the
+        // block's shared memory stays within BOT_SMEM
+        const Lay &L = h->lv[(size_t)lb - 1].lay, &Ln = h->lv[(size_t)lb].lay;
+        if (bot_ncol(L) > (int64_t)BOT_CPT * BOT_THREADS || L.n0 >= 4096 || L.n1 >= 1024 || L.n2 >= 2048) break;
+        if (L.n0 > 2 * Ln.n0 || L.n1 > 2 * Ln.n1 || L.n2 > 2 * Ln.n2) break;
+        if (bot_layout(h, lb - 1, &tmp) > BOT_SMEM) break;
         lb--;
     }
     if (lb >= top) return;
@@ -1211,30 +1365,21 @@ void bottom_plan(saras_mg *h) {
         return;
     }
     h->bottom = lb;
-    h->bottom_smem = total;
+    h->bottom_smem = bot_layout(h, lb, &tmp);
 }
 
 void bottom(saras_mg *h, cudaStream_t s) {
     const int lb = h->bottom, top = h->nl - 1;
     BotArgs a{};
     a.nb = top - lb;
-    auto al = [](size_t x) { return (unsigned)((x + 15) / 16 * 16); };
-    unsigned off = 0;
+    const size_t smem = bot_layout(h, lb, &a);
     for (int m = 0; m < a.nb; m++) {
         const Level &v = h->lv[(size_t)(lb + m)];
         a.L[m] = v.lay;
         a.t[m] = tab32(v);
         a.w[m + 1] = wt32(h->lv[(size_t)(lb + m + 1)]);
-        a.off[2 * m] = off;
-        off += al((size_t)v.lay.size * sizeof(float));
-        a.off[2 * m + 1] = off;
-        off += al((size_t)v.lay.size * sizeof(float));
     }
     const Level &c = h->lv[(size_t)top];
-    for (int q = 0; q < 4; q++) {
-        a.off[2 * BOT_MAX + q] = off;
-        off += al((size_t)c.lay.size * sizeof(double));
-    }
     a.Lc = c.lay;
     a.tc = tab64(c);
     a.wdc = c.inv_diag;
@@ -1252,7 +1397,7 @@ void bottom(saras_mg *h, cudaStream_t s) {
     a.post = h->prm.post_smooth;
     a.sweeps_out = h->coarse_sweeps;
     kbegin(h, s, KC_COARSE);
-    launch_pdl(k_bottom<true>, 1, BOT_THREADS, (size_t)off, s, a);
+    launch_pdl(k_bottom<true>, 1, BOT_THREADS, smem, s, a);
     kend(h, s, KC_COARSE);
 }
 
