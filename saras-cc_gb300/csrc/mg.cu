@@ -853,7 +853,7 @@ saras_status create(const saras_grid_desc *gd, const saras_mg_params *prm, void 
             SARAS_TRY(dalloc(h, &v.r32, sz));
             SARAS_CUDA(cudaMemsetAsync(v.e32, 0, (size_t)sz * sizeof(float), h->stream));
             SARAS_CUDA(cudaMemsetAsync(v.r32, 0, (size_t)sz * sizeof(float), h->stream));
-            if (fused_sweep_fits(v.lay, h->d3)) SARAS_TRY(dalloc(h, &v.e32b, sz));
+            if (fused_sweep_fits(v.lay, h->d3) || pair_sweep_fits(v.lay, h->d3)) SARAS_TRY(dalloc(h, &v.e32b, sz));
         }
         if (use.inv_diag) SARAS_TRY(dalloc(h, &v.inv_diag, sz));
         if (use.dd) SARAS_TRY(dalloc(h, &v.dd, sz));
@@ -1108,7 +1108,8 @@ int64_t mg_estimate_bytes(const saras_grid_desc *gd, const saras_mg_params *prm)
         if (l == 0) cells0 = (int64_t)L.n0 * L.n1 * L.n2;
         const LevelArrays u = level_arrays(prm->precision, l, g.levels);
         bytes += L.size * (16 * u.u_f + 16 * u.scratch + 8 * u.e_r32 + 8 * u.inv_diag + 8 * u.dd);
-        if (u.e_r32 && fused_sweep_fits(L, d3)) bytes += 4 * L.size;  // the fused sweep's second e buffer
+        if (u.e_r32 && (fused_sweep_fits(L, d3) || pair_sweep_fits(L, d3)))
+            bytes += 4 * L.size;  // the fused iterations' second e buffer
         if (u.fd && fd_fits(L)) bytes += 8 * fd_elems(L);
         bytes += (int64_t)10 * (L.n0 + L.n1 + L.n2) * 12;  // 1-D tables, FP64 and FP32
         if (l == 0) {

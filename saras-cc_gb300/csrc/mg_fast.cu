@@ -1017,6 +1017,198 @@ void colour32(saras_mg *h, cudaStream_t s, int l, int colour) {
     kend(h, s, l == 0 ? KC_SMOOTH0 : -1);
 }
 
+// ---- one whole FP32 red-black iteration on a small 3-D level ----
+//
+// On the levels between the finest ones and the single-block bottom (rows
+// of at most 64 cells, 64^3 and 32^3 at 256^3) a colour launch costs about
+// the same whatever its size, so k_rbgs_pair runs both colours of an
+// iteration in one launch, the way k_rbgs_fused does on the large levels: a
+// block stages its tile (SP_TI planes x SP_TJ rows x the whole row) with two
+// halo cells of e and one of r, and the tables, in shared memory, updates
+// the first colour on the tile and one halo cell around it, meets at a block
+// barrier, updates the second colour on the tile and stores the tile to the
+// other buffer of a ping-pong pair (no block writes what another reads).
+// Every cell's arithmetic is offdiag's and diag's in their order, so the
+// launch gives the bits of the two colour launches.
+// Tiles of 2 planes x 2 rows: the levels are L2-resident and each launch is
+// latency, so many small blocks (1024 at 64^3) beat fewer large ones in
+// spite of the recomputed halo (256^3 solve: 2x2 tiles 111.6 ms, 2x4 112.6,
+// 4x8 117.7, the two colour launches 112.7).
+constexpr int SP_TI = 2, SP_TJ = 2, SP_THREADS = 256;
+constexpr int SP_EI = SP_TI + 4, SP_EJ = SP_TJ + 4, SP_RI = SP_TI + 2, SP_RJ = SP_TJ + 2;
+constexpr int SP_MAXN2 = 64;  // longest row
+// per thread at SP_MAXN2: e and r vectors staged, first- and second-colour cells
+constexpr int SP_EV = (SP_EI * SP_EJ * (SP_MAXN2 / 4) + SP_THREADS - 1) / SP_THREADS;
+constexpr int SP_RV = (SP_RI * SP_RJ * (SP_MAXN2 / 4) + SP_THREADS - 1) / SP_THREADS;
+constexpr int SP_RC = (SP_RI * SP_RJ * (SP_MAXN2 / 2) + SP_THREADS - 1) / SP_THREADS;
+constexpr int SP_KC = (SP_TI * SP_TJ * (SP_MAXN2 / 2) + SP_THREADS - 1) / SP_THREADS;
+static_assert(SP_RI + SP_RJ + SP_MAXN2 <= SP_THREADS, "one table entry per thread");
+
+__device__ __forceinline__ int wrapi(int a, int n) { return ((a % n) + n) % n; }
+
+size_t pair_smem(int n2) {
+    return ((size_t)(SP_EI * SP_EJ + SP_RI * SP_RJ) * n2 + 3 * (SP_RI + SP_RJ) + 3 * (size_t)n2) * sizeof(float);
+}
+
+// One colour cell at position c of the e tile (plane offset ti and row
+// offset tj in the tables' index, k its own index): offdiag, then diag.
+__device__ __forceinline__ float pair_cell(const float *es, int c, int n2, int iw, int jw, int k, int n0, int n1,
+                                           const Bnd &b, const float *tx, const float *ty, const float *tz, int ti,
+                                           int tj, float f, float w, float omc) {
+    constexpr int RS1 = 1;
+    const int sj = n2, si = SP_EJ * n2;
+    const float uc = es[c];
+    const float xm = iw > 0 || b.per[0] ? es[c - si] : (b.sg_lo[0] > 0 ? uc : -uc);
+    const float xp = iw < n0 - 1 || b.per[0] ? es[c + si] : (b.sg_hi[0] > 0 ? uc : -uc);
+    const float zm = k > 0 ? es[c - RS1] : (b.per[2] ? es[c + n2 - 1] : (b.sg_lo[2] > 0 ? uc : -uc));
+    const float zp = k < n2 - 1 ? es[c + RS1] : (b.per[2] ? es[c - (n2 - 1)] : (b.sg_hi[2] > 0 ? uc : -uc));
+    const float ym = jw > 0 || b.per[1] ? es[c - sj] : (b.sg_lo[1] > 0 ? uc : -uc);
+    const float yp = jw < n1 - 1 || b.per[1] ? es[c + sj] : (b.sg_hi[1] > 0 ? uc : -uc);
+    const int nx = SP_RI, ny = SP_RJ;
+    float sm = tx[ti] * xm;
+    sm = fmat(tx[nx + ti], xp, sm);
+    sm = fmat(ty[tj], ym, sm);
+    sm = fmat(ty[ny + tj], yp, sm);
+    sm = fmat(tz[k], zm, sm);
+    sm = fmat(tz[n2 + k], zp, sm);
+    const float sv = sm - f;
+    float d = tx[2 * nx + ti] + tz[2 * n2 + k];
+    d += ty[2 * ny + tj];
+    return fmat(omc, uc, sweep_div(w * sv, d + d));
+}
+
+__global__ void __launch_bounds__(SP_THREADS) k_rbgs_pair(const float *__restrict__ src, float *__restrict__ dst,
+                                                          const float *__restrict__ r, Lay L, Tab3<float> t, Bnd b,
+                                                          float w, float omc) {
+    extern __shared__ __align__(16) float sp[];
+    const int n0 = L.n0, n1 = L.n1, n2 = L.n2, n4 = n2 >> 2, h2 = n2 >> 1;
+    float *es = sp;                             // planes i0-2 .. i0+TI+1, rows j0-2 .. j0+TJ+1
+    float *rs = es + SP_EI * SP_EJ * n2;        // planes i0-1 .. i0+TI, rows j0-1 .. j0+TJ
+    float *tx = rs + SP_RI * SP_RJ * n2;        // cm, cp, dg of planes i0-1 .. i0+TI
+    float *ty = tx + 3 * SP_RI;                 // ... of rows j0-1 .. j0+TJ
+    float *tz = ty + 3 * SP_RJ;                 // ... of k
+    const int i0 = (int)blockIdx.y * SP_TI, j0 = (int)blockIdx.x * SP_TJ;
+    const bool px = b.per[0] != 0, py = b.per[1] != 0;
+    pdl_enter();
+    // Staging: a thread issues all of its loads (at most SP_EV e vectors,
+    // SP_RV r vectors and one table entry) before it stores any, so the
+    // block waits for one round trip to L2.  Planes and rows outside a wall
+    // are not loaded (the stencil mirrors); on a periodic axis they are the
+    // wrapped ones.
+    {
+        float4 ev[SP_EV], rv[SP_RV];
+        int eo[SP_EV], ro[SP_RV];
+#pragma unroll
+        for (int m = 0; m < SP_EV; m++) {
+            const int x = threadIdx.x + m * SP_THREADS;
+            eo[m] = -1;
+            if (x >= SP_EI * SP_EJ * n4) continue;
+            const int k4 = x % n4, row = x / n4, jj = row % SP_EJ, ii = row / SP_EJ;
+            int ig = i0 - 2 + ii, jg = j0 - 2 + jj;
+            if (px) ig = wrapi(ig, n0); else if (ig < 0 || ig >= n0) continue;
+            if (py) jg = wrapi(jg, n1); else if (jg < 0 || jg >= n1) continue;
+            ev[m] = __ldg(reinterpret_cast<const float4 *>(src + L.at(ig, jg, 4 * k4)));
+            eo[m] = row * n2 + 4 * k4;
+        }
+#pragma unroll
+        for (int m = 0; m < SP_RV; m++) {
+            const int x = threadIdx.x + m * SP_THREADS;
+            ro[m] = -1;
+            if (x >= SP_RI * SP_RJ * n4) continue;
+            const int k4 = x % n4, row = x / n4, jj = row % SP_RJ, ii = row / SP_RJ;
+            int ig = i0 - 1 + ii, jg = j0 - 1 + jj;
+            if (px) ig = wrapi(ig, n0); else if (ig < 0 || ig >= n0) continue;
+            if (py) jg = wrapi(jg, n1); else if (jg < 0 || jg >= n1) continue;
+            rv[m] = __ldg(reinterpret_cast<const float4 *>(r + L.at(ig, jg, 4 * k4)));
+            ro[m] = row * n2 + 4 * k4;
+        }
+        // tables: entry x < SP_RI + SP_RJ + n2 (at most SP_THREADS)
+        const int x = threadIdx.x;
+        float tv[3];
+        float *dt = nullptr;
+        int st = 0;
+        if (x < SP_RI) {
+            const int q = px ? wrapi(i0 - 1 + x, n0) : min(max(i0 - 1 + x, 0), n0 - 1);
+            tv[0] = __ldg(t.cm[0] + q), tv[1] = __ldg(t.cp[0] + q), tv[2] = __ldg(t.dg[0] + q);
+            dt = tx + x, st = SP_RI;
+        } else if (x < SP_RI + SP_RJ) {
+            const int q = py ? wrapi(j0 - 1 + x - SP_RI, n1) : min(max(j0 - 1 + x - SP_RI, 0), n1 - 1);
+            tv[0] = __ldg(t.cm[1] + q), tv[1] = __ldg(t.cp[1] + q), tv[2] = __ldg(t.dg[1] + q);
+            dt = ty + (x - SP_RI), st = SP_RJ;
+        } else if (x < SP_RI + SP_RJ + n2) {
+            const int q = x - SP_RI - SP_RJ;
+            tv[0] = __ldg(t.cm[2] + q), tv[1] = __ldg(t.cp[2] + q), tv[2] = __ldg(t.dg[2] + q);
+            dt = tz + q, st = n2;
+        }
+#pragma unroll
+        for (int m = 0; m < SP_EV; m++)
+            if (eo[m] >= 0) *reinterpret_cast<float4 *>(es + eo[m]) = ev[m];
+#pragma unroll
+        for (int m = 0; m < SP_RV; m++)
+            if (ro[m] >= 0) *reinterpret_cast<float4 *>(rs + ro[m]) = rv[m];
+        if (dt) {
+            dt[0] = tv[0];
+            dt[st] = tv[1];
+            dt[2 * st] = tv[2];
+        }
+    }
+    __syncthreads();
+    // first colour ((i + j + k) even) on the tile and one halo cell around
+    // it; a colour's cells read only the other colour, so a thread forms all
+    // of its cells before it writes any
+    {
+        float nv[SP_RC];
+        int co[SP_RC];
+#pragma unroll
+        for (int m = 0; m < SP_RC; m++) {
+            const int x = threadIdx.x + m * SP_THREADS;
+            co[m] = -1;
+            if (x >= SP_RI * SP_RJ * h2) continue;
+            const int kk = x % h2, row = x / h2, jj = row % SP_RJ, ii = row / SP_RJ;
+            int iw = i0 - 1 + ii, jw = j0 - 1 + jj;
+            if (px) iw = wrapi(iw, n0); else if (iw < 0 || iw >= n0) continue;
+            if (py) jw = wrapi(jw, n1); else if (jw < 0 || jw >= n1) continue;
+            const int k = 2 * kk + ((iw + jw) & 1);
+            if (k >= n2) continue;
+            const int c = ((ii + 1) * SP_EJ + (jj + 1)) * n2 + k;
+            nv[m] = pair_cell(es, c, n2, iw, jw, k, n0, n1, b, tx, ty, tz, ii, jj, rs[row * n2 + k], w, omc);
+            co[m] = c;
+        }
+#pragma unroll
+        for (int m = 0; m < SP_RC; m++)
+            if (co[m] >= 0) es[co[m]] = nv[m];
+    }
+    __syncthreads();
+    // second colour on the tile
+    {
+        float nv[SP_KC];
+        int co[SP_KC];
+#pragma unroll
+        for (int m = 0; m < SP_KC; m++) {
+            const int x = threadIdx.x + m * SP_THREADS;
+            co[m] = -1;
+            if (x >= SP_TI * SP_TJ * h2) continue;
+            const int kk = x % h2, row = x / h2, jj = row % SP_TJ, ii = row / SP_TJ;
+            const int iw = i0 + ii, jw = j0 + jj;
+            const int k = 2 * kk + 1 - ((iw + jw) & 1);
+            if (k >= n2) continue;
+            const int c = ((ii + 2) * SP_EJ + (jj + 2)) * n2 + k;
+            nv[m] = pair_cell(es, c, n2, iw, jw, k, n0, n1, b, tx, ty, tz, ii + 1, jj + 1,
+                              rs[((ii + 1) * SP_RJ + (jj + 1)) * n2 + k], w, omc);
+            co[m] = c;
+        }
+#pragma unroll
+        for (int m = 0; m < SP_KC; m++)
+            if (co[m] >= 0) es[co[m]] = nv[m];
+    }
+    __syncthreads();
+    for (int x = threadIdx.x; x < SP_TI * SP_TJ * n4; x += blockDim.x) {
+        const int k4 = x % n4, row = x / n4, jj = row % SP_TJ, ii = row / SP_TJ;
+        *reinterpret_cast<float4 *>(dst + L.at(i0 + ii, j0 + jj, 4 * k4)) =
+            *reinterpret_cast<const float4 *>(es + ((ii + 2) * SP_EJ + (jj + 2)) * n2 + 4 * k4);
+    }
+}
+
 // Coarsest level: the FP64_EXACT single-block solve (or smoothing), shared
 // by all forms; declared in mg.cu.
 }  // namespace
@@ -1025,6 +1217,14 @@ namespace saras {
 void coarsest_level(saras_mg *h, cudaStream_t s);
 void norm_final(saras_mg *h, cudaStream_t s);
 void ghost_all_level(saras_mg *h, cudaStream_t s, int l, bool zeroBC);
+
+// Levels that take k_rbgs_pair (and hold a second e buffer for it): 3-D,
+// rows of 8 to 64 cells in whole float4s, planes and rows that divide into
+// tiles, not a level of the large fused iteration.
+bool pair_sweep_fits(const Lay &L, bool d3) {
+    return d3 && L.n2 >= 8 && L.n2 <= SP_MAXN2 && L.n2 % 4 == 0 && L.n0 % SP_TI == 0 && L.n1 % SP_TJ == 0 &&
+           !fused_sweep_fits(L, d3);
+}
 }  // namespace saras
 
 namespace {
@@ -1125,6 +1325,17 @@ void smooth(saras_mg *h, cudaStream_t s, int l, int count, bool mixed) {
             for (int half = 0; half < 2; half++) {
                 kbegin(h, s, l == 0 ? KC_SMOOTH0 : -1);
                 tma_fused(h, s, v, half == 0);
+                kend(h, s, l == 0 ? KC_SMOOTH0 : -1);
+            }
+    } else if (mixed && v.e32b && pair_sweep_fits(v.lay, h->d3)) {
+        const Lay &L = v.lay;
+        const dim3 grid((unsigned)(L.n1 / SP_TJ), (unsigned)(L.n0 / SP_TI));
+        const float w = (float)h->prm.sor_param, omc = (float)(1.0 - h->prm.sor_param);
+        for (; n + 2 <= count; n += 2)
+            for (int half = 0; half < 2; half++) {
+                kbegin(h, s, l == 0 ? KC_SMOOTH0 : -1);
+                launch_pdl(k_rbgs_pair, grid, SP_THREADS, pair_smem(L.n2), s, half == 0 ? v.e32 : v.e32b,
+                           half == 0 ? v.e32b : v.e32, v.r32, L, tab32(v), bnd(h), w, omc);
                 kend(h, s, l == 0 ? KC_SMOOTH0 : -1);
             }
     }
@@ -1553,7 +1764,7 @@ double kernel_bytes(const saras_mg *h, int kclass) {
         // an RBGS iteration reads e and r and writes e (3 N s): a fused
         // launch is a whole iteration, a colour launch half of one; the
         // average over a V-cycle's launch mix (smooth() pairs iterations)
-        const bool fused = mixed && h->lv[0].tma.fok;
+        const bool fused = mixed && (h->lv[0].tma.fok || (h->lv[0].e32b && pair_sweep_fits(h->lv[0].lay, h->d3)));
         int f = 0, k = 0;
         for (int c : {h->prm.pre_smooth, h->prm.post_smooth}) {
             const int fc = fused ? c / 2 * 2 : 0;

@@ -31,6 +31,7 @@ void tma_plan(saras_mg *h, Level &v);
 bool tma_colour(saras_mg *h, cudaStream_t s, Level &v, int colour);
 bool tma_fused(saras_mg *h, cudaStream_t s, Level &v, bool to_b);
 bool fused_sweep_fits(const Lay &L, bool d3);
+bool pair_sweep_fits(const Lay &L, bool d3);  // mg_fast.cu: levels of k_rbgs_pair
 
 // mg.cu: handle reuse by the serving engine
 saras_status mg_retarget(saras_mg *h, const saras_grid_desc *gd);
