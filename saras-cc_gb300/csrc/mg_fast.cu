@@ -650,8 +650,9 @@ __device__ __forceinline__ unsigned bot_pack(const Lay &L, int q) {
 }
 
 template <bool D3>
-__device__ void bot_smooth(float *e, const float *r, const Lay &L, const Tab3<float> &t, const Bnd &b, int count,
+__device__ void bot_smooth(float *e, const float *r, const Lay &L, const Tab3<float> &ts, const Bnd &b, int count,
                            float w, float omc, const unsigned *lst) {
+    const Tab3<float> t = ts;  // the table pointers in registers for the whole sweep
     const int half = (L.n2 + 1) / 2, ncol = L.n0 * L.n1 * half;
     for (int n = 0; n < count; n++)
         for (int colour = 0; colour < 2; colour++) {
@@ -682,8 +683,10 @@ __device__ void bot_smooth(float *e, const float *r, const Lay &L, const Tab3<fl
 }
 
 template <class TO, bool D3>
-__device__ void bot_restrict(const float *e, const float *r, const Lay &Lf, const Tab3<float> &t, const Bnd &b,
-                             const WTab<float> &w, TO *rc, const Lay &Lc) {
+__device__ void bot_restrict(const float *e, const float *r, const Lay &Lf, const Tab3<float> &ts, const Bnd &b,
+                             const WTab<float> &ws, TO *rc, const Lay &Lc) {
+    const Tab3<float> t = ts;  // the table pointers in registers
+    const WTab<float> w = ws;
     const int ncell = Lc.n0 * Lc.n1 * Lc.n2;
     for (int q = threadIdx.x; q < ncell; q += blockDim.x) {
         const int k = q % Lc.n2, rest = q / Lc.n2, j = rest % Lc.n1, i = rest / Lc.n1;
