@@ -61,7 +61,7 @@ def workload(S):
 
 # MIXED form: FP32 V-cycles per FP64 defect correction; negative = adaptive,
 # at most |INNER| per correction and the last one sized to what is left
-INNER = int(os.environ.get("SARAS_BENCH_INNER", "-32"))
+INNER = int(os.environ.get("SARAS_BENCH_INNER", "-64"))
 
 
 def mg_kw(S, precision, cycles=2000):
