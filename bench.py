@@ -49,11 +49,14 @@ TOL = 1e-10
 CPU_SAMPLE_CYCLES = 2
 
 
-def workload(S):
+def workload(S, project=None):
+    """The 256^3 grid and its padded RHS.  `project` makes the RHS compatible
+    (the product's projection by default; the reference arm passes the
+    oracle's, bit-identical, so that it never loads the product library)."""
     g = S.grid_desc(n=(N, N, N), mesh="UUD", beta=(1.0, 1.0, 1.3), domain="NNN")
     rng = np.random.default_rng(1)
     f = rng.uniform(-1.0, 1.0, (N, N, N))
-    f = S.project_compatible(g, f)
+    f = (project or S.project_compatible)(g, f)
     rhs = S.padded_field(g)
     rhs[1:-1, 1:-1, 1:-1] = f
     return g, rhs
@@ -171,11 +174,13 @@ def run_reference(args):
     rank, ws, dist = dist_init()
     if rank != 0:
         return
+    # the CPU restatement alone: saras_gb300 supplies ctypes struct layouts
+    # and numpy helpers; its CUDA library is never loaded on this arm
     import saras_gb300 as S
-    g, rhs = workload(S)
-    levels = S.load().saras_reference_levels(g)
     sys.path.insert(0, str(ROOT / "oracle"))
     import pyoracle as O
+    g, rhs = workload(S, O.project_compatible)
+    levels = O.num_levels(g)
     nt = O.max_threads()
     O.set_threads(nt)
     # warm-up steps: short samples; timed steps: the full solve to the

@@ -358,9 +358,13 @@ saras_status saras_serve_destroy(saras_serve *h);
  * already hold the free HBM, and a time step must not fail half-way for want
  * of memory.  The first call on a device does the set-up (it looks up the
  * scratch's address with that device current); make that first call before
- * any stream capture.  Nothing in the scratch has to start at zero.  Every
- * call on a device uses the same scratch, so calls that overlap in time (on
- * different streams or host threads) race; the caller serialises them.
+ * any stream capture.  The looked-up address is kept for the life of the
+ * process, so the entry point must not be used again on a device after
+ * cudaDeviceReset.  Nothing in the scratch has to start at zero.  The call
+ * returns once its work on `stream` has finished (it synchronises the
+ * stream), so a later call on any stream finds the scratch free.  Every call
+ * on a device uses the same scratch, so calls that overlap in time (from
+ * different host threads) race; the caller serialises them.
  * Arguments as saras_mg_create (grid, params, stream) plus
  * saras_mg_solve_dev (device fields, strides, residual history).
  */

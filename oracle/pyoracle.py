@@ -83,6 +83,35 @@ def grid_metrics(grid, level, axis, levels=0):
     return x[:m].copy(), a[:m].copy(), b[:m].copy()
 
 
+def null_vector(grid, axis):
+    """Left null vector of the 1-D all-Neumann finest-level operator along
+    `axis` (normalised to max |w| = 1), from the oracle's level-0 metrics:
+    the column balance of the stretched second-difference operator of
+    poisson_d3.cc:96-246 with Neumann ghosts (ghost = interior) gives the
+    flux recurrence w[j+1] (c2 - c1)[j+1] = w[j] (c2 + c1)[j]."""
+    n = grid.n[axis]
+    _, xixx, xix2 = grid_metrics(grid, 0, axis)
+    h = 1.0 / n
+    ih2, i2h = 1.0 / (h * h), 0.5 / h
+    c2 = xix2[1:n + 1] * ih2
+    c1 = xixx[1:n + 1] * i2h
+    lo, up = c2 - c1, c2 + c1
+    w = np.zeros(n)
+    w[0] = 1.0
+    for j in range(n - 1):
+        w[j + 1] = w[j] * up[j] / lo[j + 1]
+    return w / np.abs(w).max()
+
+
+def project_compatible(grid, f):
+    """f minus its component along the separable left null vector of the
+    all-Neumann operator, (w.f / w.1): a compatible right-hand side; plain
+    mean subtraction on uniform axes."""
+    ws = [null_vector(grid, d) if (grid.dims == 3 or d != 1) else np.ones(1) for d in range(3)]
+    w = ws[0][:, None, None] * ws[1][None, :, None] * ws[2][None, None, :]
+    return f - (w * f).sum() / w.sum()
+
+
 def field_metrics(grid, axis):
     lib = load()
     m = grid.n[axis] + 2 * grid.pad

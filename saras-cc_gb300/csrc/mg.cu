@@ -347,7 +347,9 @@ namespace saras {
 void kbegin(saras_mg *h, cudaStream_t s, int kc) {
     h->issued++;
     if (!h->timing || kc < 0) return;
-    if (h->graph && !h->capturing) return;  // only the graph's launches are timed in graph mode
+    // in graph mode the graph's own event-record nodes time its launches;
+    // a sequence issued directly beside it records marks of its own
+    if (h->graph && !h->capturing && !h->timing_direct) return;
     if (h->ev_used + 2 > h->ev_pool.size()) {
         if (h->capturing) {  // no event creation inside a capture: stop timing this class
             return;
@@ -372,12 +374,12 @@ void kend(saras_mg *h, cudaStream_t s, int kc) {
     h->mark_open = false;
 }
 
-// Adds the elapsed times of the bracketed launches of the last sequence.
-// With a captured graph the event-record nodes are part of the graph and the
-// marks stay valid for every replay.
-void harvest_timing(saras_mg *h) {
+// Adds the elapsed times of the bracketed launches of the last sequence:
+// a replay of the captured graph (its event-record nodes, whose marks stay
+// valid for every replay) or a sequence issued directly (its own marks,
+// recorded on events past the graph's).
+void harvest_timing(saras_mg *h, bool from_graph) {
     if (!h->timing) return;
-    const bool from_graph = h->graph != nullptr;
     auto &marks = from_graph ? h->graph_marks : h->ev_marks;
     for (auto &m : marks) {
         float ms = 0.f;
@@ -387,7 +389,7 @@ void harvest_timing(saras_mg *h) {
     }
     if (!from_graph) {
         h->ev_marks.clear();
-        h->ev_used = 0;
+        h->ev_used = h->graph ? h->ev_base : 0;
     }
     cudaGetLastError();  // a failed elapsed-time query must not surface as a solve error
 }
@@ -904,6 +906,8 @@ saras_status ensure_graph(saras_mg *h) {
     if (h->graph && h->graph_timing != h->timing) {
         cudaGraphExecDestroy(h->graph);
         h->graph = nullptr;
+        h->graph_marks.clear();
+        h->ev_base = 0;
     }
     if (h->graph || !h->use_graph) return SARAS_OK;
     if (h->timing) {
@@ -933,6 +937,7 @@ saras_status ensure_graph(saras_mg *h) {
     h->launches_cycle = h->issued;
     h->graph_marks = h->ev_marks;
     h->ev_marks.clear();
+    h->ev_base = h->ev_used;
     h->graph_timing = h->timing;
     e = cudaGraphInstantiate(&h->graph, g, 0);
     cudaGraphDestroy(g);
@@ -981,8 +986,10 @@ saras_status short_iteration(saras_mg *h, cudaStream_t s, int n) {
         h->last_launches += n * h->launches_v + h->launches_tail;
     } else {
         h->issued = 0;
+        h->timing_direct = true;
         for (int q = 0; q < n; q++) vcycle_fast(h, s, true);
         mixed_tail(h, s);
+        h->timing_direct = false;
         cudaMemcpyAsync(h->norm_host, h->norm_out, 8 * sizeof(double), cudaMemcpyDeviceToHost, s);
         h->last_launches += h->issued;
     }
@@ -1013,7 +1020,10 @@ saras_status solve_loop(saras_mg *h, double *res_hist, int32_t hist_cap, int32_t
             mixed_prepare(h, s);
         }
         const int n_this = n_next;
+        // whether this iteration's kernel-timing marks are the graph's
+        bool from_graph = h->graph != nullptr;
         if (adapt && n_this < full) {
+            from_graph = false;
             h->inner_now = n_this;
             const saras_status st = short_iteration(h, s, n_this);
             h->inner_now = 0;
@@ -1027,7 +1037,7 @@ saras_status solve_loop(saras_mg *h, double *res_hist, int32_t hist_cap, int32_t
         }
         h->last_vcycles += n_this;
         SARAS_CUDA(cudaStreamSynchronize(s));
-        harvest_timing(h);
+        harvest_timing(h, from_graph);
         r = h->norm_host[0];
         cyc++;
         int tma_err = 0;
@@ -1370,7 +1380,7 @@ saras_status mg_solve_in_scratch(const saras_grid_desc *gd, const saras_mg_param
         if (use.e_r32) {
             take(&v.e32, sz);
             take(&v.r32, sz);
-            if (fused_sweep_fits(v.lay, h.d3)) take(&v.e32b, sz);
+            if (fused_sweep_fits(v.lay, h.d3) || pair_sweep_fits(v.lay, h.d3)) take(&v.e32b, sz);
         }
         if (use.inv_diag) take(&v.inv_diag, sz);
         if (use.dd) take(&v.dd, sz);
@@ -1402,12 +1412,16 @@ saras_status mg_solve_in_scratch(const saras_grid_desc *gd, const saras_mg_param
     SARAS_CUDA(cudaMemsetAsync(h.coarse_sweeps, 0, 4 * sizeof(int), stream));
     saras_status s = build_tables(&h, true);  // pageable sources: staged at the call, ordered on the stream
     h.tab_stage = nullptr;
-    h.norm_host = nullptr;
-    SARAS_TRY(s);
     h.norm_host = norm_host;
-    s = fast_setup(&h);
+    if (s == SARAS_OK) s = fast_setup(&h);
     if (s == SARAS_OK) s = solve_common(&h, lhs, rhs, st, res_hist, hist_cap, n_cycles);
+    // whatever the outcome, work queued on the stream (the finishing kernels
+    // and the gather) may still read the scratch: the call returns only once
+    // it is done, so that the next call, on any stream, may reuse the scratch
+    const cudaError_t e = cudaStreamSynchronize(stream);
     h.norm_host = nullptr;
+    if (e != cudaSuccess && (s == SARAS_OK || s == SARAS_NOT_CONVERGED))
+        return cuda_fail(e, "cudaStreamSynchronize", __FILE__, __LINE__);
     return s;
 }
 

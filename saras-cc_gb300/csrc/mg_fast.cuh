@@ -9,7 +9,7 @@ namespace saras {
 // Kernel-class event timing (mg.cu)
 void kbegin(saras_mg *h, cudaStream_t s, int kc);
 void kend(saras_mg *h, cudaStream_t s, int kc);
-void harvest_timing(saras_mg *h);
+void harvest_timing(saras_mg *h, bool from_graph);
 
 // mg_fast.cu
 saras_status fast_setup(saras_mg *h);          // per-cell inverse diagonals, checks

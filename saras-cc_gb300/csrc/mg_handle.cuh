@@ -115,6 +115,10 @@ struct saras_mg {
     std::vector<std::pair<int, size_t>> graph_marks;  // marks baked into the graph
     bool graph_timing = false;
     bool capturing = false;
+    // a sequence issued directly while a timed graph exists (a shortened
+    // MIXED iteration): its launches record their own marks
+    bool timing_direct = false;
+    size_t ev_base = 0;  // events [0, ev_base) are the graph's event-record nodes
     bool mark_open = false;
     int64_t kc_launches[saras::KC_COUNT] = {0, 0, 0, 0, 0};
     double kc_ms[saras::KC_COUNT] = {0, 0, 0, 0, 0};

@@ -291,7 +291,13 @@ def test_mixed_adaptive_inner_cycles():
     FP32 V-cycles and sizes the last one by the measured contraction: it
     converges, runs no more V-cycles than the fixed count, agrees with the
     fixed-count solution to the tolerance, and the captured-graph path and
-    the direct launches (kernel timing on) give the same bits."""
+    the direct launches (kernel timing on) give the same bits.  With kernel
+    timing on, the per-class launch counts follow the V-cycles actually run
+    (shortened iterations included): one finest residual-restriction and
+    one prolongation per V-cycle, finest smoothing launches that carry
+    (pre + post) iterations of 3 N 4 bytes per V-cycle, and bracketed kernel
+    times that add up to less than the solve's own time."""
+    import time
     g = S.grid_desc(n=(128, 128, 128), mesh="UUD", beta=(1, 1, 1.2), domain="NNN")
     rhs = random_rhs(g, 31)
     tol = 1e-10
@@ -301,8 +307,18 @@ def test_mixed_adaptive_inner_cycles():
                                         pre_smooth=2, post_smooth=2, inner_cycles=inner))
         mg.set_kernel_timing(timing)
         lhs = S.padded_field(g)
+        t0 = time.perf_counter()
         assert mg.mg_solve(lhs, rhs) == S.OK
+        wall_ms = (time.perf_counter() - t0) * 1e3
         out[name] = (lhs, mg.last_vcycles(), mg.cycles, mg.history[-1])
+        if timing:
+            ks = [mg.kernel_stats(k) for k in range(5)]
+            v = mg.last_vcycles()
+            assert v < 16 * mg.cycles  # a shortened iteration ran
+            assert ks[1][0] == v and ks[2][0] == v, (ks, v)
+            n_cells = 128 ** 3
+            np.testing.assert_allclose(ks[0][0] * ks[0][2], v * 4 * 3 * n_cells * 4, rtol=1e-12)
+            assert sum(k[1] for k in ks) <= wall_ms
         mg.close()
     lf, vf, cf, rf = out["fixed"]
     la, va, ca, ra = out["adapt"]

@@ -193,3 +193,21 @@ def test_depth_rule_and_rejected_sizes(n, dims):
     g = S.grid_desc(n=n, domain="NNN", dims=dims)
     lib = S.load()
     assert lib.saras_reference_levels(g) == O.num_levels(g)
+
+
+@pytest.mark.parametrize("gk", [
+    dict(n=(256, 256, 256), mesh="UUD", beta=(1, 1, 1.3), domain="NNN"),
+    dict(n=(32, 16, 64), mesh="SDU", beta=(1.2, 1.4, 1.0), domain="NNN"),
+    dict(n=(64, 1, 32), mesh="DUS", beta=(1.1, 1.0, 1.3), domain="NNN", dims=2),
+])
+def test_oracle_null_vector_equals_product(gk):
+    """The oracle's left null vector and compatible projection (numpy, from
+    the oracle's metrics) are bit-identical to the product's host
+    restatement, so the CPU baseline solves exactly the GPU's right-hand side
+    without loading the product library."""
+    g = S.grid_desc(**gk)
+    for d in (0, 2) if g.dims == 2 else (0, 1, 2):
+        assert np.array_equal(O.null_vector(g, d), S.null_vector(g, d)), d
+    ny = 1 if g.dims == 2 else g.n[1]
+    f = np.random.default_rng(4).uniform(-1, 1, (g.n[0], ny, g.n[2]))
+    assert np.array_equal(O.project_compatible(g, f), S.project_compatible(g, f))

@@ -3,7 +3,8 @@ memory (its scratch is a file-scope __device__ array), called through the C
 ABI and compared with the handle-based entry point saras_mg_solve_dev on the
 same inputs, for two calls in a row.  Tolerance: 1e-12 relative in the
 solution and the residual history (the two run the same kernels in the same
-order, so they normally agree bit for bit)."""
+order, so they normally agree bit for bit).  The second call must leave the
+device's free memory unchanged: the entry point allocates nothing."""
 import ctypes as C
 
 import numpy as np
@@ -18,6 +19,9 @@ RTOL = 1e-12
 CASES = [
     ("fp64_3d", dict(n=(32, 32, 32), mesh="UUD", beta=(1, 1, 1.2), domain="NNN"), S.PREC_FP64),
     ("mixed_2d", dict(n=(64, 1, 64), mesh="UUD", beta=(1, 1, 1.1), domain="NNN", dims=2), S.PREC_MIXED),
+    # 3-D MIXED: the paired red-black iterations (second e buffer), the
+    # single-block bottom and adaptive inner counts, all in the scratch
+    ("mixed_3d", dict(n=(64, 64, 64), mesh="UUD", beta=(1, 1, 1.2), domain="NNN"), S.PREC_MIXED),
     ("fp64_dirichlet", dict(n=(16, 16, 32), mesh="UUD", beta=(1, 1, 1.3), domain="PPN"), S.PREC_FP64),
 ]
 
@@ -34,7 +38,7 @@ def _entry():
 def _params(precision, gk):
     bc = [0, 0, 0, 0, 1, 1] if gk.get("domain") == "PPN" else [0] * 6
     return S.mg_params(precision=precision, vc_count=80, vc_tolerance=1e-10, mg_tolerance=1e-6, pre_smooth=2,
-                       post_smooth=2, bc_kind=bc)
+                       post_smooth=2, bc_kind=bc, inner_cycles=-8 if precision == S.PREC_MIXED else 1)
 
 
 @pytest.mark.parametrize("name,gk,prec", CASES, ids=[c[0] for c in CASES])
@@ -54,15 +58,19 @@ def test_static_scratch_solve_matches_handle_solve(name, gk, prec):
     ref, ref_hist = ref_d.cpu().numpy(), mg.history.copy()
     mg.close()
     lib, f = _entry()
-    for _ in range(2):
+    for call in range(2):
         out_d = torch.zeros_like(rhs_d)
         hist = np.zeros(512)
         n = C.c_int32()
+        torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info()[0]
         s = f(C.byref(g), C.byref(prm), None, C.c_void_p(out_d.data_ptr() + off),
               C.c_void_p(rhs_d.data_ptr() + off), (C.c_int64 * 3)(*st),
               hist.ctypes.data_as(C.POINTER(C.c_double)), 512, C.byref(n))
         assert s == S.OK, lib.saras_last_error()
         torch.cuda.synchronize()
+        if call == 1:  # the first call may load kernels; the second allocates nothing
+            assert torch.cuda.mem_get_info()[0] == free_before
         out = out_d.cpu().numpy()
         assert n.value == len(ref_hist) and ref_hist[-1] < 1e-10
         assert np.abs(hist[:n.value] - ref_hist).max() <= RTOL * np.abs(ref_hist).max()
