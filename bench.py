@@ -222,6 +222,57 @@ def time_solves(mg, lhs_d, rhs_d, st, off, steps, torch, stream):
     return ev0.elapsed_time(ev1) / steps, cycles
 
 
+def origin_offset(g, st):
+    p = g.pad
+    py = 1 if g.dims == 2 else p
+    return p * st[0] + py * st[1] + p * st[2]
+
+
+def dev_solve(S, torch, g, rhs, prm, stream, warm=1, reps=1):
+    """Device-resident solves of one configuration from a zero initial guess:
+    ms per solve (CUDA events on the solve stream), V-cycles (outer
+    iterations), FP32 V-cycles, residual history and the padded solution."""
+    mg = S.Multigrid(g, prm, stream=stream.cuda_stream)
+    rhs_d = torch.from_numpy(rhs).cuda()
+    lhs_d = torch.zeros_like(rhs_d)
+    st = [x // 8 for x in rhs.strides]
+    off = origin_offset(g, st)
+    for _ in range(warm):
+        lhs_d.zero_()
+        mg.mg_solve_dev(lhs_d.data_ptr() + 8 * off, rhs_d.data_ptr() + 8 * off, st)
+    ms, cyc = time_solves(mg, lhs_d, rhs_d, st, off, reps, torch, stream)
+    out = {"ms": ms, "cycles": int(np.median(cyc)), "vcycles": int(mg.last_vcycles()), "levels": mg.levels,
+           "final_residual": float(mg.history[-1]) if len(mg.history) else None}
+    hist = mg.history.copy()
+    sol = lhs_d.cpu().numpy()
+    mg.close()
+    del rhs_d, lhs_d
+    return out, hist, sol
+
+
+def core_of(a, g):
+    if g.dims == 2:
+        return a[1:-1, 1, 1:-1]
+    p = g.pad
+    return a[p:-p, p:-p, p:-p]
+
+
+def rel_err(a, b, singular=True):
+    """max |a - b| / max |b| over the core; the constant null-space component
+    is removed first on all-Neumann problems."""
+    if singular:
+        a, b = a - a.mean(), b - b.mean()
+    return float(np.abs(a - b).max() / np.abs(b).max())
+
+
+# FP64 instructions (add, multiply, fused multiply-add: one each) per cell
+# one colour launch of the FP64 form's finest sweep updates (k_rbgs_v8 with
+# the stored omega/D: one multiply and five fused multiply-adds for the
+# neighbour sum, the subtraction of f, then (1 - omega) u + (omega/D) s as a
+# multiply and a fused multiply-add)
+FP64_SWEEP_OPS_PER_CELL = 9
+
+
 def run_gb300(args):
     import torch
     rank, ws, dist = dist_init()
@@ -257,7 +308,8 @@ def run_gb300(args):
     wall_mix = (time.perf_counter() - t_wall) * 1e3 / args.steps
     if dist:
         dist.barrier()
-    sol_mix = lhs_d[1:-1, 1:-1, 1:-1].double().cpu().numpy()
+    sol_mix = lhs_d.cpu().numpy()
+    hist_mix = mix.history.copy()
     launches = mix.last_launches()
     vcycles_mix = mix.last_vcycles()
     # ---- the same solves again with every finest-level launch bracketed by
@@ -271,30 +323,47 @@ def run_gb300(args):
     if dist:
         dist.barrier()
     ms_f64, cyc_f64 = time_solves(f64, lhs_d, rhs_d, st, off, args.steps, torch, stream)
-    sol_f64 = lhs_d[1:-1, 1:-1, 1:-1].double().cpu().numpy()
-    a = sol_mix - sol_mix.mean()
-    b = sol_f64 - sol_f64.mean()
-    err = float(np.abs(a - b).max() / np.abs(b).max())
+    sol_f64 = lhs_d.cpu().numpy()
+    f64.set_kernel_timing(True)
+    time_solves(f64, lhs_d, rhs_d, st, off, 1, torch, stream)
+    kstats64 = {k: f64.kernel_stats(k) for k in range(5)}
+    f64.set_kernel_timing(False)
 
     # ---- end to end through the host entry point, pinned host buffers ----
-    # every step solves from a zero initial guess: each gets its own zeroed
-    # pinned box, prepared before the timed region (a host memset of the
-    # 137 MB box between solves would be timed with the GPU idle)
+    # Every step solves from a zero initial guess.  Two pinned boxes take
+    # turns, as a caller's fields would: while the GPU solves into one, a
+    # host thread clears the other, used by the next step (the clearing
+    # overlaps the solve; the thread is joined before the next call).
     h_rhs = torch.from_numpy(rhs).pin_memory()
     h_np_rhs = h_rhs.numpy()
-    h_lhs = [torch.zeros_like(h_rhs).pin_memory() for _ in range(args.steps)]
+    h_lhs = [torch.zeros_like(h_rhs).pin_memory() for _ in range(2)]
     h_np_lhs = [x.numpy() for x in h_lhs]
     # one untimed call through the same entry point: the handle allocates its
-    # device copies of the host boxes on first use
+    # device copies of the host boxes on first use; a second one with the
+    # copies bracketed by events gives their durations
     mix.mg_solve(h_np_lhs[0], h_np_rhs)
-    h_np_lhs[0][...] = 0.0
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    h_np_lhs[0].fill(0.0)
+    mix.set_kernel_timing(True)
+    mix.mg_solve(h_np_lhs[0], h_np_rhs)
+    copy_stats = {"h2d": mix.kernel_stats(5), "d2h": mix.kernel_stats(6)}
+    mix.set_kernel_timing(False)
+    h_np_lhs[0].fill(0.0)
     torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clearer = None
     ev0.record(stream)
     for q in range(args.steps):
-        mix.mg_solve(h_np_lhs[q], h_np_rhs)
+        if clearer is not None:
+            clearer.join()
+            clearer = None
+        if q >= 1 and q + 1 < args.steps:
+            clearer = threading.Thread(target=h_np_lhs[(q + 1) % 2].fill, args=(0.0,))
+            clearer.start()
+        mix.mg_solve(h_np_lhs[q % 2], h_np_rhs)
     ev1.record(stream)
     torch.cuda.synchronize()
+    if clearer is not None:
+        clearer.join()
     e2e_ms = ev0.elapsed_time(ev1) / args.steps
     field_bytes = rhs.nbytes
 
@@ -303,6 +372,15 @@ def run_gb300(args):
     e2e_ms = max_over_ranks(e2e_ms, dist, dev)
     if rank != 0:
         return
+    del h_rhs, h_lhs, h_np_lhs
+    mix.close()
+    f64.close()
+    del rhs_d, lhs_d
+
+    # ---- the plain reference-order FP64 GPU form, once: bit-identical to
+    # the oracle's solve below ----
+    ex, hist_exact, sol_exact = dev_solve(S, torch, g, rhs, S.mg_params(**mg_kw(S, S.PREC_FP64_EXACT)), stream,
+                                          warm=0, reps=1)
 
     # roofline of the dominant kernel class (largest total time)
     names = ["rbgs_sweep_finest", "resid_restrict_finest", "prolong_correct_finest", "resid_norm_update",
@@ -316,27 +394,55 @@ def run_gb300(args):
     tf = ROOT / "profiles" / "traffic.json"
     if tf.exists():
         traffic = json.loads(tf.read_text()).get(names[dom])
+    # FP64 form: its finest sweep against the FP64 instruction rate measured
+    # here, and against HBM
+    fma_rate, addmul_rate = S.measure_fp64_rate(sptr)
+    n64, t64, b64 = kstats64[0]
+    avg64 = t64 / max(1, n64) / 1e3
+    ops64 = FP64_SWEEP_OPS_PER_CELL * N ** 3 / 2
+    roofline_fp64 = {
+        "bound": "fp64", "kernel": "rbgs_sweep_finest (FP64 form, one colour per launch)",
+        "achieved": ops64 / avg64 / 1e12, "peak": fma_rate / 1e12, "unit": "T FP64 instructions/s",
+        "frac": ops64 / avg64 / fma_rate, "peak_source": "measured in this run (saras_measure_fp64_rate: "
+                                                            "independent FP64 FMA chains over every SM)",
+        "addmul_peak": addmul_rate / 1e12, "avg_launch_us": avg64 * 1e6, "launches": n64,
+        "fp64_instructions_per_launch": ops64, "algorithmic_bytes_per_launch": b64,
+        "hbm_frac": b64 / avg64 / 1e9 / hbm,
+        "kernel_ms_per_solve": {names[k]: kstats64[k][1] for k in range(5)}}
+
     serving = None
     if not args.no_serve:
-        del rhs_d, lhs_d, h_rhs, h_lhs
-        mix.close()
-        f64.close()
         serving = run_serving(S, args)
         if args.serve_step_frac > 0:
             # the Poisson-only half of the stream: the same arrivals, sizes and
             # RHS draws without time-step requests
             p = run_serving(S, args, 0.0)
             serving["poisson_only"] = {k: p[k] for k in ("requests", "completed", "statuses", "throughput_req_per_s",
-                                                         "p50_ms", "p99_ms", "mean_ms", "makespan_s")}
+                                                         "p50_ms", "p99_ms", "mean_ms", "makespan_s",
+                                                         "model_hbm_frac")}
     # CPU baseline: the oracle's full FP64 solve of the same workload once
-    # (about 20 s on 16 Grace cores, inside the 10-30 s sample bound)
+    # (about 20 s on 16 Grace cores, inside the 10-30 s sample bound); its
+    # solution and history are the parity reference of the three GPU forms
     sys.path.insert(0, str(ROOT / "oracle"))
     import pyoracle as O
     nt = O.max_threads()
     O.set_threads(nt)
-    cpu_full = O.mg_solve(g, S.mg_params(**dict(mg_kw(S, S.PREC_FP64_EXACT, 2000), vc_tolerance=TOL)),
-                          S.padded_field(g), rhs)
+    orc = S.padded_field(g)
+    cpu_full = O.mg_solve(g, S.mg_params(**dict(mg_kw(S, S.PREC_FP64_EXACT, 2000), vc_tolerance=TOL)), orc, rhs)
     cpu_ms = cpu_full.seconds * 1e3
+    oc = core_of(orc, g)
+    parity = {
+        "oracle_cycles": cpu_full.cycles, "oracle_final_residual": float(cpu_full.history[-1]),
+        "fp64_exact_cycles": ex["cycles"],
+        "fp64_exact_bitwise": bool(np.array_equal(sol_exact, orc) and np.array_equal(hist_exact, cpu_full.history)),
+        "mixed_vs_oracle_rel_err": rel_err(core_of(sol_mix, g), oc),
+        "fp64_vs_oracle_rel_err": rel_err(core_of(sol_f64, g), oc),
+        "mixed_vs_fp64_rel_err": rel_err(core_of(sol_mix, g), core_of(sol_f64, g)),
+        "mixed_final_residual": float(hist_mix[-1]),
+        "norm": "max |u - v| / max |v| over the core, constant null-space component removed",
+    }
+    del sol_mix, sol_f64, sol_exact, orc
+    extra = None if args.no_extra else extra_configs(S, O, torch, stream, args)
     clocks = clk.summary()
     out = {
         "metric": METRIC, "value": ms_mix, "unit": "ms", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
@@ -346,23 +452,95 @@ def run_gb300(args):
         "mixed_inner_vcycles": INNER if INNER > 0 else f"adaptive, up to {-INNER}",
         "mixed_vcycles": int(vcycles_mix),
         "fp64_ms": ms_f64, "fp64_cycles": int(np.median(cyc_f64)),
-        "speedup_mixed_vs_fp64": ms_f64 / ms_mix, "mixed_vs_fp64_rel_err": err,
+        "fp64_exact_ms": ex["ms"], "fp64_exact_cycles": ex["cycles"],
+        "speedup_mixed_vs_fp64": ms_f64 / ms_mix, "speedup_mixed_vs_fp64_exact": ex["ms"] / ms_mix,
+        "parity": parity,
         "wall_ms_per_step": wall_mix, "ms_per_step_with_kernel_events": ms_mix_events,
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": 2 * field_bytes,
                 "d2h_bytes_per_step": field_bytes},
+        "e2e_copies_ms": {k: v[1] for k, v in copy_stats.items()},
+        "e2e_copy_GBps": {k: v[0] * v[2] / v[1] / 1e6 if v[1] > 0 else None for k, v in copy_stats.items()},
         "gpu_launches": int(launches) * args.steps,
         "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": hbm,
                      "unit": "GB/s", "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
                      "peak_source": src, "avg_launch_us": avg_s * 1e6, "launches": n_l,
                      "algorithmic_bytes_per_launch": byts},
+        "roofline_fp64": roofline_fp64,
         "kernel_ms": {names[k]: kstats[k][1] / args.steps for k in range(5)},
+        "kernel_launches_per_solve": {names[k]: kstats[k][0] / args.steps for k in range(5)},
         "cpu_baseline": {"value": cpu_ms, "unit": "ms", "cores": nt, "kind": "port",
                          "sample": f"the full {N}^3 FP64 mgSolve to rel-res {TOL:g} ({cpu_full.cycles} V-cycles; "
                                    f"oracle restatement, OpenMP {nt} threads), once"},
         "clocks": clocks,
         "serving": serving,
+        "configs": extra,
     }
     print(json.dumps(out), flush=True)
+
+
+def c1_block(S, O, torch, stream):
+    """2-D PLANAR 256^2, uniform, Neumann, f = cos(2 pi x) cos(2 pi z), 2/2
+    RBGS, coarsest solved to 1e-12, to rel-res 1e-10: GPU FP64_EXACT (bit
+    for bit against the oracle) and MIXED, the oracle's own time, and the
+    deviation from the manufactured solution -f/(8 pi^2)."""
+    n = 256
+    g = S.grid_desc(n=(n, 1, n), domain="NNN", dims=2)
+    x = O.grid_metrics(g, 0, 0)[0][1:-1]
+    z = O.grid_metrics(g, 0, 2)[0][1:-1]
+    f = np.cos(2 * math.pi * x)[:, None] * np.cos(2 * math.pi * z)[None, :]
+    rhs = S.padded_field(g)
+    rhs[1:-1, 1, 1:-1] = f
+    kw = dict(vc_count=400, vc_tolerance=TOL, solve_flag=1, mg_tolerance=1e-12, pre_smooth=2, post_smooth=2)
+    ex, hex_, sex = dev_solve(S, torch, g, rhs, S.mg_params(precision=S.PREC_FP64_EXACT, **kw), stream, 1, 5)
+    mx, _, smx = dev_solve(S, torch, g, rhs, S.mg_params(precision=S.PREC_MIXED, inner_cycles=INNER, **kw),
+                           stream, 1, 5)
+    orc = S.padded_field(g)
+    r = O.mg_solve(g, S.mg_params(**kw), orc, rhs)
+    exact = -f / (8 * math.pi ** 2)
+    u = core_of(sex, g)
+    return {"workload": "2-D 256^2 uniform, Neumann, cos(2 pi x) cos(2 pi z), 2/2 RBGS, coarsest tol 1e-12, "
+                        "to rel-res 1e-10", "levels": ex["levels"],
+            "fp64_exact_ms": ex["ms"], "fp64_exact_cycles": ex["cycles"],
+            "mixed_ms": mx["ms"], "mixed_cycles": mx["cycles"], "mixed_vcycles": mx["vcycles"],
+            "oracle_ms": r.seconds * 1e3, "oracle_cycles": r.cycles,
+            "fp64_exact_bitwise": bool(np.array_equal(sex, orc) and np.array_equal(hex_, r.history)),
+            "mixed_vs_oracle_rel_err": rel_err(core_of(smx, g), core_of(orc, g)),
+            "error_vs_manufactured": float(np.abs((u - u.mean()) - (exact - exact.mean())).max())}
+
+
+def c2_levels_block(S, O, torch, stream, levels=8, cycles=6):
+    """The headline 256^3 workload with an 8-level hierarchy (setVCDepth
+    gives 7; the eighth level is 2^3 cells).  The reference V-cycle diverges
+    on it: the first `cycles` V-cycles of the reference-order GPU form and
+    of the oracle, residual histories compared bit for bit."""
+    g, rhs = workload(S)
+    kw = dict(mg_kw(S, S.PREC_FP64_EXACT, cycles), vc_tolerance=1e-30, levels=levels)
+    r, hist, sol = dev_solve(S, torch, g, rhs, S.mg_params(**kw), stream, warm=0, reps=1)
+    orc = S.padded_field(g)
+    o = O.mg_solve(g, S.mg_params(**kw), orc, rhs)
+    return {"workload": f"the headline {N}^3 workload with {levels} levels (setVCDepth gives {O.num_levels(g)}), "
+                        f"FP64_EXACT form, {cycles} V-cycles",
+            "gpu_history": [float(x) for x in hist], "oracle_history": [float(x) for x in o.history],
+            "bitwise": bool(np.array_equal(hist, o.history) and np.array_equal(sol, orc)),
+            "growth_per_cycle": float((hist[-1] / hist[1]) ** (1.0 / max(1, len(hist) - 2))) if len(hist) > 2
+            else None,
+            "note": "the reference V-cycle diverges with a 2^3 coarsest level (oracle and GPU alike); the "
+                    "headline runs the reference depth"}
+
+
+def extra_configs(S, O, torch, stream, args):
+    """The benchmark's other configurations, each once (outside the timed
+    region of the headline)."""
+    out = {}
+    t0 = time.perf_counter()
+    out["c1_2d_256"] = c1_block(S, O, torch, stream)
+    # 8 levels at 256^3 leave a 2^3 coarsest level; smaller test sizes take
+    # one level more than the reference's depth rule instead
+    out["c2_8_levels"] = c2_levels_block(S, O, torch, stream, min(8, int(math.log2(N))))
+    out["c3_512"] = c3_block(S, torch, stream, args.c3_n, reps=1)
+    out["c4_rk3"] = c4_block(S, torch, args.rk3_n, args.c4_steps, args.rk3_beta)
+    out["seconds"] = time.perf_counter() - t0
+    return out
 
 
 SERVE_SIZES = [("2D 512^2", (512, 1, 512), 2), ("64^3", (64, 64, 64), 3), ("96x96x48", (96, 96, 48), 3),
@@ -540,40 +718,38 @@ def blob_rhs(S, g, count=16, sigma=0.05, seed=3):
     return rhs
 
 
-def run_c3(args):
+def c3_block(S, torch, stream, n=512, reps=1):
     """512^3 MIXED against FP64: mesh DDD (tanh beta 1.2 on every axis),
     periodic x and y, Dirichlet walls in z, RHS of 16 Gaussian blobs
     (sigma 0.05), to rel-res 1e-10.  3/6 smoothing (the reference defaults):
     the 2/2 V-cycle diverges on this stretching."""
-    import torch
-    import saras_gb300 as S
-    n = args.c3_n
     g = S.grid_desc(n=(n, n, n), mesh="DDD", beta=(1.2, 1.2, 1.2), domain="PPN")
     rhs = blob_rhs(S, g)
-    stream = torch.cuda.current_stream()
-    rhs_d = torch.from_numpy(rhs).cuda()
-    lhs_d = torch.zeros_like(rhs_d)
-    st = [x // 8 for x in rhs.strides]
-    off = st[0] + st[1] + st[2]
     kw = dict(vc_count=2000, vc_tolerance=TOL, mg_tolerance=1e-9, pre_smooth=3, post_smooth=6,
               bc_kind=[0, 0, 0, 0, 1, 1])
-    out = {"config": "c3", "workload": f"Poisson {n}^3, mesh DDD beta 1.2, periodic x/y, Dirichlet z, 16 Gaussian "
-                                       "blobs sigma 0.05 (seed 3), 3/6 RBGS, coarsest tol 1e-9, to rel-res 1e-10"}
+    out = {"workload": f"Poisson {n}^3, mesh DDD beta 1.2, periodic x/y, Dirichlet z, 16 Gaussian blobs sigma "
+                       "0.05 (seed 3), 3/6 RBGS, coarsest tol 1e-9, to rel-res 1e-10; one solve per form"}
     sols = {}
     for name, prec, inner in (("mixed", S.PREC_MIXED, 8), ("fp64", S.PREC_FP64, 1)):
-        mg = S.Multigrid(g, S.mg_params(precision=prec, inner_cycles=inner, **kw), stream=stream.cuda_stream)
-        lhs_d.zero_()
-        mg.mg_solve_dev(lhs_d.data_ptr() + 8 * off, rhs_d.data_ptr() + 8 * off, st)  # warm-up
-        ms, cyc = time_solves(mg, lhs_d, rhs_d, st, off, args.steps, torch, stream)
-        out[f"{name}_ms"] = ms
-        out[f"{name}_cycles"] = int(np.median(cyc))
-        out[f"{name}_final_residual"] = float(mg.history[-1])
-        sols[name] = lhs_d[1:-1, 1:-1, 1:-1].cpu().numpy()
-        mg.close()
-    out["mixed_vcycles"] = out["mixed_cycles"] * 8
+        r, _, sol = dev_solve(S, torch, g, rhs, S.mg_params(precision=prec, inner_cycles=inner, **kw), stream,
+                              warm=0, reps=reps)
+        out[f"{name}_ms"] = r["ms"]
+        out[f"{name}_cycles"] = r["cycles"]
+        out[f"{name}_vcycles"] = r["vcycles"]
+        out[f"{name}_final_residual"] = r["final_residual"]
+        out["levels"] = r["levels"]
+        sols[name] = core_of(sol, g)
+        del sol
     out["speedup_mixed_vs_fp64"] = out["fp64_ms"] / out["mixed_ms"]
-    out["mixed_vs_fp64_rel_err"] = float(np.abs(sols["mixed"] - sols["fp64"]).max() / np.abs(sols["fp64"]).max())
-    print(json.dumps(out), flush=True)
+    out["mixed_vs_fp64_rel_err"] = rel_err(sols["mixed"], sols["fp64"], singular=False)
+    return out
+
+
+def run_c3(args):
+    import torch
+    import saras_gb300 as S
+    out = c3_block(S, torch, torch.cuda.current_stream(), args.c3_n, reps=args.steps)
+    print(json.dumps(dict(config="c3", **out)), flush=True)
 
 
 def rbc_step_params(S, prec, dt=1e-4):
@@ -607,8 +783,8 @@ def rbc_fields(S, g, seed):
     return f
 
 
-def run_rk3(args):
-    """Time steps of 3-D Rayleigh-Benard convection: 256^3, Ra 1e7, Pr 1,
+def c4_block(S, torch, n=256, steps=100, beta=1.3):
+    """Time steps of 3-D Rayleigh-Benard convection: n^3, Ra 1e7, Pr 1,
     z tanh-stretched, no-slip isothermal plates, periodic sides, u = 0 and
     T = conductive profile + seeded noise 1e-3; CN Jacobi to 1e-6 and the
     reference's Multigrid defaults (3/6, coarsest tol 1e-2, 20 cycles,
@@ -616,33 +792,36 @@ def run_rk3(args):
     pressure solves.  The stretching defaults to beta 1.3: at 1.5 the
     reference pressure V-cycle diverges in the first sub-step on this machine
     (the CPU restatement does the same)."""
-    import saras_gb300 as S
-    n = args.rk3_n
-    beta = args.rk3_beta
     g = S.grid_desc(n=(n, n, n), mesh="UUD", beta=(1.0, 1.0, beta), domain="PPN")
-    out = {"config": "rk3", "workload": f"RK3 Rayleigh-Benard {n}^3, Ra 1e7, Pr 1, z tanh beta {beta}, PPN, "
-                                        f"dt 1e-4, CN tol 1e-6, MG 3/6 tol 1e-6 coarsest 1e-2, {args.rk3_steps} steps"}
+    out = {"workload": f"RK3 Rayleigh-Benard {n}^3, Ra 1e7, Pr 1, z tanh beta {beta}, PPN, dt 1e-4, CN tol 1e-6, "
+                       f"MG 3/6 tol 1e-6 coarsest 1e-2, {steps} steps after one warm-up step"}
     for name, prec in (("fp64", S.PREC_FP64), ("mixed", S.PREC_MIXED)):
         p = rbc_step_params(S, prec)
         f = rbc_fields(S, g, 4)
         rk = S.RK3(g, p)
         rk.upload(f["vx"], f["vy"], f["vz"], f["p"], f["t"], f["pp"])
         rk.step(1)  # warm-up
-        import torch
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        mgc, cni = rk.step(args.rk3_steps)
+        mgc, cni = rk.step(steps)
         torch.cuda.synchronize()
-        dt = (time.perf_counter() - t0) * 1e3 / args.rk3_steps
+        dt = (time.perf_counter() - t0) * 1e3 / steps
         rk.download(f["vx"], f["vy"], f["vz"], f["p"], f["t"], f["pp"])
         rk.close()
         out[f"{name}_ms_per_step"] = dt
-        out[f"{name}_mg_cycles_per_step"] = mgc / args.rk3_steps
-        out[f"{name}_cn_iters_per_step"] = cni / args.rk3_steps
+        out[f"{name}_mg_cycles_per_step"] = mgc / steps
+        out[f"{name}_cn_iters_per_step"] = cni / steps
         out[f"{name}_max_w"] = float(np.abs(f["vz"][1:-1, 1:-1, 1:-1]).max())
         out[f"{name}_t_mean"] = float(f["t"][1:-1, 1:-1, 1:-1].mean())
     out["speedup_mixed_vs_fp64"] = out["fp64_ms_per_step"] / out["mixed_ms_per_step"]
-    print(json.dumps(out), flush=True)
+    return out
+
+
+def run_rk3(args):
+    import torch
+    import saras_gb300 as S
+    out = c4_block(S, torch, args.rk3_n, args.rk3_steps, args.rk3_beta)
+    print(json.dumps(dict(config="rk3", **out)), flush=True)
 
 
 def run_serve_only(args):
@@ -686,14 +865,17 @@ def main():
     ap.add_argument("--profile", type=int, default=0,
                     help="profiler mode: run this many fixed V-cycles per form and exit")
     ap.add_argument("--forms", default="mixed,fp64")
-    ap.add_argument("--serve-requests", type=int, default=300,
-                    help="requests of the serving stream (the full stream is 2000)")
+    ap.add_argument("--serve-requests", type=int, default=2000,
+                    help="requests of the serving stream")
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-step-frac", type=float, default=0.1,
                     help="fraction of serving requests that are RK3 time steps")
     ap.add_argument("--serve-timeout", type=float, default=240.0,
                     help="seconds after which the serving stream stops waiting for requests")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the other configurations (2-D 256^2, 8 levels, 512^3, RK3 steps) in the line")
+    ap.add_argument("--c4-steps", type=int, default=100, help="RK3 steps per form in the line's RK3 block")
     ap.add_argument("--serve-no-tune", action="store_true", help="keep the default schedule (no autotune)")
     ap.add_argument("--serve-only", action="store_true")
     ap.add_argument("--config", choices=["mg256", "c3", "rk3"], default="mg256",

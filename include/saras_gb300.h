@@ -137,7 +137,8 @@ int64_t saras_mg_device_bytes(const saras_mg *h);
 /* Kernel timing: when enabled, launches of each kernel class are bracketed
  * with CUDA events on the solve stream.  Class ids: 0 smoothing sweep at the
  * finest level, 1 residual+restriction, 2 prolongation+correction,
- * 3 residual norm, 4 coarsest solve. */
+ * 3 residual norm, 4 coarsest solve; and the copies of saras_mg_solve's host
+ * boxes: 5 host->device (two per call), 6 device->host (one per call). */
 saras_status saras_mg_set_kernel_timing(saras_mg *h, int32_t enable);
 saras_status saras_mg_kernel_stats(saras_mg *h, int32_t kclass, int64_t *launches,
                                    double *total_ms, double *bytes_per_launch);
@@ -147,6 +148,13 @@ int64_t saras_mg_last_launches(const saras_mg *h);
 /* No reference counterpart.  V-cycles the last solve ran (the MIXED form:
  * FP32 V-cycles over all its outer iterations). */
 int64_t saras_mg_last_vcycles(const saras_mg *h);
+
+/* No reference counterpart (measurement).  The FP64 instruction rate of the
+ * current device, the denominator of the FP64 form's arithmetic roofline:
+ * full-occupancy kernels of independent dependency chains, timed with CUDA
+ * events on `stream`.  *fma_per_s: fused multiply-adds per second;
+ * *addmul_per_s: separately rounded adds and multiplies per second. */
+saras_status saras_measure_fp64_rate(void *stream, double *fma_per_s, double *addmul_per_s);
 
 /* Host restatement of the per-level grid metrics the multigrid uses:
  * x (cell centres), xixx and xix2 for `axis` at `level`, each over indices
@@ -322,9 +330,10 @@ saras_status saras_serve_submit(saras_serve *h, int64_t id, const saras_grid_des
  * collocated step is not exactly compatible with the Neumann operator, so
  * its residual levels off).  The result equals saras_rk3_step on a handle
  * whose mg is that MIXED form with those two keys.  The reported cycles are
- * the outer iterations of all its pressure solves, the status OK, or
- * NOT_CONVERGED when a solve stopped at its cap (the step still completes,
- * as in the reference). */
+ * the outer iterations of all its pressure solves and the status OK also
+ * when a pressure solve stopped at its V-Cycle Count above the tolerance:
+ * mgSolve simply returns after vcCount cycles and the step completes
+ * (poisson.cc:182-188); the residual polled is the last solve's. */
 saras_status saras_serve_submit_step(saras_serve *h, int64_t id, const saras_grid_desc *grid,
                                      const saras_rk3_params *prm, double *vx, double *vy, double *vz,
                                      double *p, double *t, double *pp);

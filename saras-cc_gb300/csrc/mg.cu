@@ -769,6 +769,8 @@ void free_all(saras_mg *h) {
     if (h->graph_v) cudaGraphExecDestroy(h->graph_v);
     if (h->graph_tail) cudaGraphExecDestroy(h->graph_tail);
     for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
+    for (cudaEvent_t e : h->copy_ev)
+        if (e) cudaEventDestroy(e);
     if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
 }
 
@@ -1274,13 +1276,30 @@ saras_status saras_mg_solve(saras_mg *h, double *lhs, const double *rhs, const i
         SARAS_TRY(dalloc(h, &h->stage_lhs, h->stage_elems));
         SARAS_TRY(dalloc(h, &h->stage_rhs, h->stage_elems));
     }
+    // with kernel timing on, the copies are bracketed by events too
+    const bool tc = h->timing;
+    if (tc && !h->copy_ev[0])
+        for (int q = 0; q < 4; q++) SARAS_CUDA(cudaEventCreate(&h->copy_ev[q]));
+    if (tc) SARAS_CUDA(cudaEventRecord(h->copy_ev[0], s));
     SARAS_CUDA(cudaMemcpyAsync(h->stage_lhs, lhs - origin, bytes, cudaMemcpyHostToDevice, s));
     SARAS_CUDA(cudaMemcpyAsync(h->stage_rhs, rhs - origin, bytes, cudaMemcpyHostToDevice, s));
+    if (tc) SARAS_CUDA(cudaEventRecord(h->copy_ev[1], s));
     saras_status st = solve_common(h, h->stage_lhs + origin, h->stage_rhs + origin, h->stage_st, res_hist,
                                    hist_cap, n_cycles);
     if (st != SARAS_OK && st != SARAS_NOT_CONVERGED) return st;
+    if (tc) SARAS_CUDA(cudaEventRecord(h->copy_ev[2], s));
     SARAS_CUDA(cudaMemcpyAsync(lhs - origin, h->stage_lhs, bytes, cudaMemcpyDeviceToHost, s));
+    if (tc) SARAS_CUDA(cudaEventRecord(h->copy_ev[3], s));
     SARAS_CUDA(cudaStreamSynchronize(s));
+    if (tc) {
+        float a = 0.f, b = 0.f;
+        SARAS_CUDA(cudaEventElapsedTime(&a, h->copy_ev[0], h->copy_ev[1]));
+        SARAS_CUDA(cudaEventElapsedTime(&b, h->copy_ev[2], h->copy_ev[3]));
+        h->kc_ms[KC_H2D] += a;
+        h->kc_launches[KC_H2D] += 2;
+        h->kc_ms[KC_D2H] += b;
+        h->kc_launches[KC_D2H] += 1;
+    }
     return st;
 }
 

@@ -1782,6 +1782,9 @@ double kernel_bytes(const saras_mg *h, int kclass) {
         return (0.125 + 2.0) * n * sz;
     case KC_NORM:  // read u, f (FP64); MIXED also writes r in FP32
         return mixed ? 20.0 * n : 16.0 * n;
+    case KC_H2D:  // one dense padded box of the caller per copy
+    case KC_D2H:
+        return (double)h->stage_elems * sizeof(double);
     default:
         return 0.0;
     }

@@ -60,7 +60,18 @@ struct Level {
     int rs = 0;
 };
 
-enum KClass { KC_SMOOTH0 = 0, KC_RESTRICT = 1, KC_PROLONG = 2, KC_NORM = 3, KC_COARSE = 4, KC_COUNT = 5 };
+// kernel classes timed with events (KC_H2D / KC_D2H: the host entry point's
+// copies of the caller's boxes)
+enum KClass {
+    KC_SMOOTH0 = 0,
+    KC_RESTRICT = 1,
+    KC_PROLONG = 2,
+    KC_NORM = 3,
+    KC_COARSE = 4,
+    KC_H2D = 5,
+    KC_D2H = 6,
+    KC_COUNT = 7
+};
 
 }  // namespace saras
 
@@ -120,9 +131,10 @@ struct saras_mg {
     bool timing_direct = false;
     size_t ev_base = 0;  // events [0, ev_base) are the graph's event-record nodes
     bool mark_open = false;
-    int64_t kc_launches[saras::KC_COUNT] = {0, 0, 0, 0, 0};
-    double kc_ms[saras::KC_COUNT] = {0, 0, 0, 0, 0};
-    double kc_bytes[saras::KC_COUNT] = {0, 0, 0, 0, 0};
+    int64_t kc_launches[saras::KC_COUNT] = {};
+    double kc_ms[saras::KC_COUNT] = {};
+    double kc_bytes[saras::KC_COUNT] = {};
+    cudaEvent_t copy_ev[4] = {nullptr, nullptr, nullptr, nullptr};  // host entry point's copies
     int64_t issued = 0;  // launches issued while recording the current sequence
     int maxCount() const;  // coarsest-level iteration limit (poisson.cc:430-436)
     // pinned staging of table refills (serving retargets)

@@ -1013,7 +1013,10 @@ bool advance_step(saras_serve *h, size_t idx, int32_t solve_status) {
     if (solve_status == SARAS_NAN) {
         s = SARAS_NAN;
     } else {
-        if (solve_status == SARAS_NOT_CONVERGED) c.step_status = SARAS_NOT_CONVERGED;  // the step goes on
+        // a pressure solve that stopped at its V-Cycle Count above the
+        // tolerance is not a failure: mgSolve returns after vcCount cycles
+        // (poisson.cc:182-188) and timeAdvance goes on; the request's
+        // residual reports where the last solve stopped
         mixed_finish(c.mg, c.mg->stream);  // the integrator's stream: ordered before its correction
         s = rk3_stage_end(c.rk, c.stage);
         if (s == SARAS_OK && c.stage + 1 < rk3_stages(c.rk)) {

@@ -191,6 +191,8 @@ def load():
     lib.saras_mg_last_launches.restype = i64
     lib.saras_mg_last_vcycles.argtypes = [vp]
     lib.saras_mg_last_vcycles.restype = i64
+    lib.saras_measure_fp64_rate.argtypes = [vp, dp, dp]
+    lib.saras_measure_fp64_rate.restype = C.c_int
     lib.saras_grid_metrics.argtypes = [C.POINTER(GridDesc), i32, i32, i32, dp, dp, dp, C.POINTER(i32)]
     lib.saras_grid_metrics.restype = C.c_int
     lib.saras_reference_levels.argtypes = [C.POINTER(GridDesc)]
@@ -273,6 +275,15 @@ def null_vector(grid: GridDesc, axis: int) -> np.ndarray:
     check(lib.saras_neumann_null_vector(C.byref(grid), axis, w.ctypes.data_as(C.POINTER(C.c_double))),
           "saras_neumann_null_vector")
     return w
+
+
+def measure_fp64_rate(stream: int | None = None):
+    """(FP64 fused multiply-adds per second, separately rounded FP64 adds and
+    multiplies per second) of the current device."""
+    lib = load()
+    a, b = C.c_double(), C.c_double()
+    check(lib.saras_measure_fp64_rate(C.c_void_p(stream or 0), C.byref(a), C.byref(b)), "saras_measure_fp64_rate")
+    return a.value, b.value
 
 
 def project_compatible(grid: GridDesc, f: np.ndarray) -> np.ndarray:

@@ -5,9 +5,9 @@ Bars: FP64_EXACT is bit-for-bit (solution with ghost layer, residual
 history) for the L-infinity residual type, and within 1e-13 relative for the
 L1/L2 types whose sums the GPU takes in a different order.  The FP64 form
 agrees with the oracle to 1e-11 relative after the same number of V-cycles.
-The MIXED form reaches the requested residual and matches the oracle's
-converged solution to 1e-9 relative (constant null-space component removed
-for all-Neumann problems).
+The MIXED form run to the oracle's tolerance (rel-res 1e-12) matches its
+solution to 1e-10 relative (constant null-space component removed for
+all-Neumann problems).
 """
 import numpy as np
 import pytest
@@ -144,9 +144,9 @@ def test_mixed_converges_to_oracle(name, gk, mk):
     base = dict(vc_count=120, pre_smooth=2, post_smooth=2, mg_tolerance=1e-12)
     base.update(mk)
     mix = S.padded_field(g)
-    mg = S.Multigrid(g, S.mg_params(precision=S.PREC_MIXED, vc_tolerance=1e-10, **base))
+    mg = S.Multigrid(g, S.mg_params(precision=S.PREC_MIXED, vc_tolerance=1e-12, **base))
     st = mg.mg_solve(mix, rhs)
-    assert st == S.OK and mg.history[-1] < 1e-10
+    assert st == S.OK and mg.history[-1] < 1e-12
     orc = S.padded_field(g)
     r = O.mg_solve(g, S.mg_params(vc_tolerance=1e-12, **base), orc, rhs)
     assert r.status == 0
@@ -154,7 +154,7 @@ def test_mixed_converges_to_oracle(name, gk, mk):
     if singular:
         a, b = demean(a), demean(b)
     err = np.abs(a - b).max() / np.abs(b).max()
-    assert err < 1e-9, err
+    assert err < 1e-10, err
 
 
 def test_mixed_tracks_fp64_cycle_by_cycle():

@@ -88,7 +88,9 @@ def test_steps_same_in_the_mix(alone):
     fields, pois, done, st = _serve([0, 1, 2], [0, 1])
     assert st["max_active"] == 5
     for q in range(len(STEPS)):
-        assert done[100 + q]["status"] in (S.OK, S.NOT_CONVERGED), done[100 + q]
+        # a pressure solve stopped at its V-Cycle Count is no failure (mgSolve
+        # returns after vcCount cycles, poisson.cc:182-188)
+        assert done[100 + q]["status"] == S.OK, done[100 + q]
         assert done[100 + q]["cycles"] >= 1
         for k in fields[q]:
             assert np.array_equal(fields[q][k], alone[q][k]), (q, k)
