@@ -142,6 +142,16 @@ int64_t saras_mg_device_bytes(const saras_mg *h);
 saras_status saras_mg_set_kernel_timing(saras_mg *h, int32_t enable);
 saras_status saras_mg_kernel_stats(saras_mg *h, int32_t kclass, int64_t *launches,
                                    double *total_ms, double *bytes_per_launch);
+/* No reference counterpart (fault handling).  Bound, in polls, of the
+ * mbarrier waits of the TMA-staged FP32 sweeps (MIXED form, large 3-D
+ * levels); 0 restores the default of 2^24 polls.  A wait that runs out ends
+ * that sweep: the kernel records the error, stops issuing copies, waits
+ * (with the default bound) for the loads and stores it issued and returns;
+ * the solve then returns SARAS_TIMEOUT after the V-cycle, and the handle
+ * stays usable (the next solve starts with the error cleared).  Setting a
+ * new bound re-captures the handle's CUDA graphs on their next use. */
+saras_status saras_mg_set_wait_limit(saras_mg *h, int64_t polls);
+
 /* Total kernel launches issued by the last solve. */
 int64_t saras_mg_last_launches(const saras_mg *h);
 

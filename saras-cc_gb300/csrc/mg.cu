@@ -1002,6 +1002,9 @@ saras_status short_iteration(saras_mg *h, cudaStream_t s, int n) {
 saras_status solve_loop(saras_mg *h, double *res_hist, int32_t hist_cap, int32_t *n_cycles) {
     cudaStream_t s = h->stream;
     h->inner_now = 0;
+    // the TMA sweeps' error word starts clear: an earlier solve whose wait
+    // ran out leaves the handle usable
+    SARAS_CUDA(cudaMemsetAsync(h->norm_out + 7, 0, sizeof(double), s));
     SARAS_TRY(ensure_graph(h));
     int cyc = 0;
     double r = 0.0;
@@ -1331,6 +1334,24 @@ saras_status saras_mg_kernel_stats(saras_mg *h, int32_t kclass, int64_t *launche
     if (launches) *launches = h->kc_launches[kclass];
     if (total_ms) *total_ms = h->kc_ms[kclass];
     if (bytes_per_launch) *bytes_per_launch = kernel_bytes(h, kclass);
+    return SARAS_OK;
+}
+
+saras_status saras_mg_set_wait_limit(saras_mg *h, int64_t polls) {
+    if (!h || polls < 0 || polls > 0xffffffffLL) {
+        set_error("invalid argument");
+        return SARAS_BAD_ARG;
+    }
+    if ((unsigned)polls == h->wait_limit) return SARAS_OK;
+    // the captured graphs hold the old bound: capture them again on next use
+    SARAS_CUDA(cudaStreamSynchronize(h->stream));
+    if (h->graph) cudaGraphExecDestroy(h->graph);
+    if (h->graph_v) cudaGraphExecDestroy(h->graph_v);
+    if (h->graph_tail) cudaGraphExecDestroy(h->graph_tail);
+    h->graph = h->graph_v = h->graph_tail = nullptr;
+    h->graph_marks.clear();
+    h->ev_base = 0;
+    h->wait_limit = (unsigned)polls;
     return SARAS_OK;
 }
 

@@ -118,6 +118,8 @@ struct saras_mg {
     int64_t launches_cycle = 0;
     int64_t last_launches = 0;
     int64_t dev_bytes = 0;
+    // polls of the TMA sweeps' pipeline waits (0: the kernels' default)
+    unsigned wait_limit = 0;
     // kernel timing
     bool timing = false;
     std::vector<cudaEvent_t> ev_pool;

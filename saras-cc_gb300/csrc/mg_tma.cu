@@ -14,8 +14,10 @@
 // is that of k_rbgs_v8 (mg_fast.cu), so results are bit-identical.
 //
 // Every wait on an mbarrier is bounded; a wait that runs out sets an error
-// word the host reads with the residual (norm_out[7]), waits (bounded) for
-// the copies it issued and returns.
+// word the host reads with the residual (norm_out[7]); the block then stops
+// issuing copies, waits (with the default bound) for the loads and stores it
+// issued and returns.  The host may lower the pipeline waits' bound
+// (saras_mg_set_wait_limit) to exercise that path.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -53,9 +55,26 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
         : "memory");
     return done != 0;
 }
-// bounded wait; false when the limit ran out
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-    for (unsigned n = 0; n < TMA_WAIT_LIMIT; n++)
+__device__ __forceinline__ bool mbar_test_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(sa(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+// bounded wait of at most `limit` polls (the first a non-blocking test, the
+// others potentially blocking tries); false when the limit ran out.  The
+// pipeline's waits take the handle's limit (TMA_WAIT_LIMIT unless the host
+// set another); the waits that drain a block's own copies before it exits
+// always take TMA_WAIT_LIMIT, so that no copy is in flight when the block's
+// shared memory is released
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, unsigned limit = TMA_WAIT_LIMIT) {
+    if (mbar_test_wait(bar, parity)) return true;
+    for (unsigned n = 1; n < limit; n++)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
@@ -133,7 +152,7 @@ __global__ void __launch_bounds__(TMA_WS_THREADS) k_rbgs_tma(const __grid_consta
                                                              const __grid_constant__ CUtensorMap rld,
                                                              const float *__restrict__ eg, Lay L, Tab3<float> t,
                                                              Bnd b, int colour, float w, float omc, int tj,
-                                                             int chunk, int *err) {
+                                                             int chunk, int *err, unsigned wlim) {
     pdl_enter();
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ int s_fail;
@@ -171,7 +190,7 @@ __global__ void __launch_bounds__(TMA_WS_THREADS) k_rbgs_tma(const __grid_consta
             for (; p <= i1; p++) {
                 const int q = slot_of(p);
                 if (p - first >= TMA_SLOTS && !s_fail) {
-                    if (!mbar_wait(&empty[q], (uint32_t)(((p - first) / TMA_SLOTS - 1) & 1))) {
+                    if (!mbar_wait(&empty[q], (uint32_t)(((p - first) / TMA_SLOTS - 1) & 1), wlim)) {
                         s_fail = 1;
                         atomicExch(err, 1);
                     }
@@ -215,7 +234,7 @@ __global__ void __launch_bounds__(TMA_WS_THREADS) k_rbgs_tma(const __grid_consta
     }
     auto wait_full = [&](int p) {
         if (s_fail) return false;
-        if (!mbar_wait(&full[slot_of(p)], par_of(p))) {
+        if (!mbar_wait(&full[slot_of(p)], par_of(p), wlim)) {
             s_fail = 1;
             atomicExch(err, 1);
             return false;
@@ -432,7 +451,7 @@ __global__ void __launch_bounds__(fu_threads<RS>(), 1)
     k_rbgs_fused(const __grid_constant__ CUtensorMap esrc, const __grid_constant__ CUtensorMap esrc2,
                  const __grid_constant__ CUtensorMap edst, const __grid_constant__ CUtensorMap rld,
                  const __grid_constant__ CUtensorMap rld1, Lay L, Tab3<float> t, Bnd b, float w, float omc, int tj,
-                 int chunk, int *err) {
+                 int chunk, int *err, unsigned wlim) {
     constexpr int NT = fu_nt<RS>();
     pdl_enter();
     extern __shared__ __align__(128) unsigned char smem[];
@@ -478,7 +497,7 @@ __global__ void __launch_bounds__(fu_threads<RS>(), 1)
             bool fail = false;
             for (int P = P0; P <= i1 + 1 && !fail; P++) {
                 const int u = P - P0, s = u % FU_ESLOTS;
-                if (u >= FU_ESLOTS && !mbar_wait(&eempty[s], (uint32_t)((u / FU_ESLOTS - 1) & 1))) {
+                if (u >= FU_ESLOTS && !mbar_wait(&eempty[s], (uint32_t)((u / FU_ESLOTS - 1) & 1), wlim)) {
                     fail = true;
                     break;
                 }
@@ -491,7 +510,7 @@ __global__ void __launch_bounds__(fu_threads<RS>(), 1)
                 const int Q = P - 1;
                 if (Q < Q0 || Q > i1) continue;
                 const int v = Q - Q0, sr = v % FU_RSLOTS;
-                if (v >= FU_RSLOTS && !mbar_wait(&rempty[sr], (uint32_t)((v / FU_RSLOTS - 1) & 1))) {
+                if (v >= FU_RSLOTS && !mbar_wait(&rempty[sr], (uint32_t)((v / FU_RSLOTS - 1) & 1), wlim)) {
                     fail = true;
                     break;
                 }
@@ -552,14 +571,14 @@ __global__ void __launch_bounds__(fu_threads<RS>(), 1)
     auto rptr = [&](int p) { return rs + ((p - Q0) % FU_RSLOTS) * r_slot; };
     auto wait_e = [&](int p) {
         const int u = p - P0;
-        if (!s_fail && !mbar_wait(&efull[u % FU_ESLOTS], (uint32_t)((u / FU_ESLOTS) & 1))) {
+        if (!s_fail && !mbar_wait(&efull[u % FU_ESLOTS], (uint32_t)((u / FU_ESLOTS) & 1), wlim)) {
             s_fail = 1;
             atomicExch(err, 1);
         }
     };
     auto wait_r = [&](int p) {
         const int u = p - Q0;
-        if (!s_fail && !mbar_wait(&rfull[u % FU_RSLOTS], (uint32_t)((u / FU_RSLOTS) & 1))) {
+        if (!s_fail && !mbar_wait(&rfull[u % FU_RSLOTS], (uint32_t)((u / FU_RSLOTS) & 1), wlim)) {
             s_fail = 1;
             atomicExch(err, 1);
         }
@@ -793,6 +812,9 @@ void tma_plan(saras_mg *h, Level &v) {
     v.tma.ok = 1;
 }
 
+// Polls of the pipeline waits: the handle's limit, or TMA_WAIT_LIMIT.
+unsigned tma_wait_limit(const saras_mg *h) { return h->wait_limit > 0 ? h->wait_limit : TMA_WAIT_LIMIT; }
+
 // One colour sweep through the TMA path; false when the level has none.
 bool tma_colour(saras_mg *h, cudaStream_t s, Level &v, int colour) {
     if (!v.tma.ok) return false;
@@ -803,7 +825,7 @@ bool tma_colour(saras_mg *h, cudaStream_t s, Level &v, int colour) {
     int *err = reinterpret_cast<int *>(h->norm_out + 7);
     launch_pdl(k_rbgs_tma, grid, dim3(TMA_WS_THREADS), tma_smem(v.tma.tj, L.n2), s, v.tma.eld, v.tma.est, v.tma.rld,
                (const float *)v.e32, L, t, b, colour, (float)h->prm.sor_param, (float)(1.0 - h->prm.sor_param),
-               v.tma.tj, v.tma.chunk, err);
+               v.tma.tj, v.tma.chunk, err, tma_wait_limit(h));
     return true;
 }
 
@@ -818,7 +840,7 @@ bool tma_fused(saras_mg *h, cudaStream_t s, Level &v, bool to_b) {
     const dim3 block((unsigned)(v.rs ? fu_threads<true>() : fu_threads<false>()));
     launch_pdl(v.rs ? k_rbgs_fused<true> : k_rbgs_fused<false>, grid, block, fused_smem(m.ftj, L.n2), s,
                to_b ? m.fa : m.fb, to_b ? m.fa2 : m.fb2, to_b ? m.fb : m.fa, m.fr, m.fr1, L, sweep_tab(v), sweep_bnd(h),
-               (float)h->prm.sor_param, (float)(1.0 - h->prm.sor_param), m.ftj, m.fchunk, err);
+               (float)h->prm.sor_param, (float)(1.0 - h->prm.sor_param), m.ftj, m.fchunk, err, tma_wait_limit(h));
     return true;
 }
 

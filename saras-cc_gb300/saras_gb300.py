@@ -191,6 +191,8 @@ def load():
     lib.saras_mg_last_launches.restype = i64
     lib.saras_mg_last_vcycles.argtypes = [vp]
     lib.saras_mg_last_vcycles.restype = i64
+    lib.saras_mg_set_wait_limit.argtypes = [vp, i64]
+    lib.saras_mg_set_wait_limit.restype = C.c_int
     lib.saras_measure_fp64_rate.argtypes = [vp, dp, dp]
     lib.saras_measure_fp64_rate.restype = C.c_int
     lib.saras_grid_metrics.argtypes = [C.POINTER(GridDesc), i32, i32, i32, dp, dp, dp, C.POINTER(i32)]
@@ -353,6 +355,10 @@ class Multigrid:
 
     def last_launches(self) -> int:
         return self.lib.saras_mg_last_launches(self.h)
+
+    def set_wait_limit(self, polls: int):
+        """Bound of the TMA sweeps' mbarrier waits in polls (0: default)."""
+        check(self.lib.saras_mg_set_wait_limit(self.h, polls), "set_wait_limit")
 
     def last_vcycles(self) -> int:
         """V-cycles of the last solve (MIXED: FP32 V-cycles of all outer

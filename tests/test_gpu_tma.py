@@ -97,3 +97,38 @@ def test_tma_mixed_solve_matches_oracle(name, gk, mgk):
     assert r.history[-1] < 1e-12
     a, b = demean(core(mix, g)), demean(core(orc, g))
     assert np.abs(a - b).max() <= 1e-9 * np.abs(b).max()
+
+
+@pytest.mark.parametrize("gk", [
+    # colour sweeps through the TMA ring (2M cells)
+    dict(n=(128, 128, 128), mesh="UUD", beta=(1, 1, 1.2), domain="NNN"),
+    # the fused iteration on the row-split layout (4M cells, 2/2 smoothing)
+    dict(n=(128, 128, 256), length=(1.0, 1.0, 2.0), mesh="UUD", beta=(1, 1, 1.2), domain="NNN"),
+], ids=["tma_colour_128c", "fused_128x128x256"])
+def test_bounded_wait_runs_out_and_handle_recovers(gk):
+    """A bound of one poll on the TMA sweeps' mbarrier waits makes a wait run
+    out in the first V-cycle of a normal MIXED solve: the kernel records the
+    error, waits (with the default bound) for the copies it issued and
+    returns, and the solve reports TIMEOUT.  With the default bound restored,
+    the next solve on the same handle is bit for bit the solve of a fresh
+    handle."""
+    g = S.grid_desc(**gk)
+    rhs = random_rhs(g, 41)
+    prm = S.mg_params(precision=S.PREC_MIXED, vc_count=100, vc_tolerance=1e-10, mg_tolerance=1e-6, pre_smooth=2,
+                      post_smooth=2, inner_cycles=-16)
+    mg = S.Multigrid(g, prm)
+    mg.set_wait_limit(1)
+    lhs = S.padded_field(g)
+    with pytest.raises(S.SarasError) as e:
+        mg.mg_solve(lhs, rhs)
+    assert e.value.status == S.TIMEOUT
+    mg.set_wait_limit(0)
+    again = S.padded_field(g)
+    assert mg.mg_solve(again, rhs) == S.OK
+    hist = mg.history.copy()
+    mg.close()
+    fresh = S.Multigrid(g, prm)
+    ref = S.padded_field(g)
+    assert fresh.mg_solve(ref, rhs) == S.OK
+    assert np.array_equal(again, ref) and np.array_equal(hist, fresh.history)
+    fresh.close()
