@@ -383,12 +383,19 @@ __device__ __forceinline__ void fu_strip(float *row, const float *xmr, const flo
 // same row at m .. m+3 shifted by one (left of it for o = 0, right for
 // o = 1), with the row's wrap or wall mirror at its ends.  strip4's
 // arithmetic, cell for cell, on four cells of one colour.
-template <int o>
+// The strip's neighbour outside its four z positions (left for o = 0, right
+// for o = 1): `zo` indexes it in the row when it is a cell of the row (an
+// interior neighbour or a periodic wrap), otherwise zmode is 1 (Neumann
+// wall: the strip's own end cell) or 2 (Dirichlet wall: minus it).  The
+// thread's strip position is fixed, so zo and zmode are set once per kernel.
+// W1: the SOR parameter is 1, and (1 - w) u + w s/(2d) is s/(2d) (w s = s
+// exactly; 0 u + v = v for finite u), so the multiply and the final FMA are
+// skipped with the same values.
+template <int o, bool W1>
 __device__ __forceinline__ void fu_strip_rs(float *row, const float *xmr, const float *xpr, const float *rrow, int n2,
-                                            int H, int own, int m, bool xlo, bool xhi, bool ylo, bool yhi,
-                                            const Bnd &b, float cmx, float cpx, float dx, float cmy, float cpy,
-                                            float dy, const float (&zc)[3][4], float w, float omc) {
-    const int oth = H - own;
+                                            int own, int oth, int m, int zo, int zmode, bool xlo, bool xhi, bool ylo,
+                                            bool yhi, const Bnd &b, float cmx, float cpx, float dx, float cmy,
+                                            float cpy, float dy, const float (&zc)[3][4], float w, float omc) {
     const float4 cur4 = lds4(row + own + m);
     // neighbour rows always exist in the slots; mirrors replace them on walls
     float4 xm4 = lds4(xmr + oth + m), xp4 = lds4(xpr + oth + m);
@@ -405,26 +412,15 @@ __device__ __forceinline__ void fu_strip_rs(float *row, const float *xmr, const 
     const float xm[4] = {xm4.x, xm4.y, xm4.z, xm4.w}, xp[4] = {xp4.x, xp4.y, xp4.z, xp4.w};
     const float ym[4] = {ym4.x, ym4.y, ym4.z, ym4.w}, yp[4] = {yp4.x, yp4.y, yp4.z, yp4.w};
     const float f[4] = {f4.x, f4.y, f4.z, f4.w};
+    const float zl = row[zo];
+    const float end = o == 1 ? c[3] : c[0];
+    const float outside = zmode == 0 ? zl : (zmode == 1 ? end : -end);
     float zm[4], zp[4];
     if (o == 1) {
-        float right;
-        if (m + 4 < H)
-            right = row[oth + m + 4];
-        else if (b.per[2])
-            right = row[oth];
-        else
-            right = b.sg_hi[2] > 0 ? c[3] : -c[3];
         zm[0] = a4.x; zm[1] = a4.y; zm[2] = a4.z; zm[3] = a4.w;
-        zp[0] = a4.y; zp[1] = a4.z; zp[2] = a4.w; zp[3] = right;
+        zp[0] = a4.y; zp[1] = a4.z; zp[2] = a4.w; zp[3] = outside;
     } else {
-        float left;
-        if (m > 0)
-            left = row[oth + m - 1];
-        else if (b.per[2])
-            left = row[oth + H - 1];
-        else
-            left = b.sg_lo[2] > 0 ? c[0] : -c[0];
-        zm[0] = left; zm[1] = a4.x; zm[2] = a4.y; zm[3] = a4.z;
+        zm[0] = outside; zm[1] = a4.x; zm[2] = a4.y; zm[3] = a4.z;
         zp[0] = a4.x; zp[1] = a4.y; zp[2] = a4.z; zp[3] = a4.w;
     }
     float u[4];
@@ -439,14 +435,14 @@ __device__ __forceinline__ void fu_strip_rs(float *row, const float *xmr, const 
         sm = sm - f[q];
         float d = dx + zc[2][q];
         d += dy;
-        u[q] = fmat(omc, c[q], sweep_div(w * sm, d + d));
+        u[q] = W1 ? sweep_div(sm, d + d) : fmat(omc, c[q], sweep_div(w * sm, d + d));
     }
     *reinterpret_cast<float4 *>(row + own + m) = make_float4(u[0], u[1], u[2], u[3]);
 }
 
 // esrc / esrc2: source e with boxes of tj rows and of two rows; edst:
 // destination e, tj rows; rld / rld1: r with tj rows and one row.
-template <bool RS>
+template <bool RS, bool W1>
 __global__ void __launch_bounds__(fu_threads<RS>(), 1)
     k_rbgs_fused(const __grid_constant__ CUtensorMap esrc, const __grid_constant__ CUtensorMap esrc2,
                  const __grid_constant__ CUtensorMap edst, const __grid_constant__ CUtensorMap rld,
@@ -554,10 +550,6 @@ __global__ void __launch_bounds__(fu_threads<RS>(), 1)
             zc[oo][1][c] = t.cp[2][k];
             zc[oo][2][c] = t.dg[2][k];
         }
-    const int li = k0 > 0 ? k0 - 1 : (b.per[2] ? n2 - 1 : k0);
-    const bool lneg = k0 == 0 && !b.per[2] && b.sg_lo[2] < 0;
-    const int ri = k0 + 4 < n2 ? k0 + 4 : (b.per[2] ? 0 : k0 + 3);
-    const bool rneg = k0 + 4 >= n2 && !b.per[2] && b.sg_hi[2] < 0;
     const int ny = tj + 2;
     for (int x = ct; x < ny; x += NT) {
         const int j = j0 - 1 + x;
@@ -583,44 +575,9 @@ __global__ void __launch_bounds__(fu_threads<RS>(), 1)
             atomicExch(err, 1);
         }
     };
-    const bool px = b.per[0] != 0, py = b.per[1] != 0;
-    wait_e(P0);
-    wait_e(P0 + 1);
-    // every consumer thread runs every step and barrier, failed or not
-    for (int q = i0 - 1; q <= i1; q++) {
-        wait_e(q + 1);
-        wait_r(q);
-        if (px || (q >= 0 && q < n0)) {
-            // R(q)
-            const int qi = px ? wrap(q, n0) : q;
-            float *pc = eptr(q);
-            const float *pm = eptr(q - 1), *pp = eptr(q + 1), *rr = rptr(q);
-            const float cmx = t.cm[0][qi], cpx = t.cp[0][qi], dx = t.dg[0][qi];
-            const bool xlo = !px && qi == 0, xhi = !px && qi == n0 - 1;
-            for (int x = ro; x < ny; x += rstep) {
-                const int j = j0 - 1 + x;
-                if (!py && (j < 0 || j >= n1)) continue;
-                const int jw = py ? wrap(j, n1) : j;
-                const int off = (x + 1) * n2;
-                if (RS) {
-                    // red: own half 0, k = 2m + parity
-                    const bool ylo = !py && jw == 0, yhi = !py && jw == n1 - 1;
-                    if (((qi + jw) & 1) == 0)
-                        fu_strip_rs<0>(pc + off, pm + off, pp + off, rr + x * n2, n2, H, 0, k0, xlo, xhi, ylo, yhi,
-                                       b, cmx, cpx, dx, sy[x], sy[ny + x], sy[2 * ny + x], zc[0], w, omc);
-                    else
-                        fu_strip_rs<1>(pc + off, pm + off, pp + off, rr + x * n2, n2, H, 0, k0, xlo, xhi, ylo, yhi,
-                                       b, cmx, cpx, dx, sy[x], sy[ny + x], sy[2 * ny + x], zc[1], w, omc);
-                } else {
-                    fu_strip(pc + off, pm + off, pp + off, rr + x * n2, n2, k0, xlo, xhi, !py && jw == 0,
-                             !py && jw == n1 - 1, b, (qi + jw) & 1, li, ri, lneg, rneg, cmx, cpx, dx, sy[x],
-                             sy[ny + x], sy[2 * ny + x], zc[0], w, omc);
-                }
-            }
-        }
-        // this thread's writes (R(q), K(q-2)) before the async proxy reads them
-        fence_async_smem();
-        consumer_sync<NT>();
+    // the TMA store of plane q-2 and the slot releases, once the consumers
+    // have met after R(q)
+    auto store_release = [&](int q) {
         if (ct == 0 && !s_fail) {
             if (q - 2 >= i0) {
                 tma_store3(&edst, eptr(q - 2) + 2 * n2, KOFF, j0 + 1, q - 1);
@@ -632,28 +589,154 @@ __global__ void __launch_bounds__(fu_threads<RS>(), 1)
             }
             if (q - 2 >= Q0) mbar_arrive(&rempty[(q - 2 - Q0) % FU_RSLOTS]);
         }
-        const int p = q - 1;
-        if (p >= i0) {
-            // K(p)
-            float *pc = eptr(p);
-            const float *pm = eptr(p - 1), *pp = eptr(p + 1), *rr = rptr(p);
-            const float cmx = t.cm[0][p], cpx = t.cp[0][p], dx = t.dg[0][p];
-            const bool xlo = !px && p == 0, xhi = !px && p == n0 - 1;
-            for (int x = ro; x < tj; x += rstep) {
-                const int j = j0 + x;
-                const int off = (x + 2) * n2;
-                if (RS) {
-                    // black: own half H, k = 2m + 1 - parity
-                    const bool ylo = !py && j == 0, yhi = !py && j == n1 - 1;
-                    if (((p + j) & 1) == 1)
-                        fu_strip_rs<0>(pc + off, pm + off, pp + off, rr + (x + 1) * n2, n2, H, H, k0, xlo, xhi, ylo,
-                                       yhi, b, cmx, cpx, dx, sy[x + 1], sy[ny + x + 1], sy[2 * ny + x + 1], zc[0], w,
-                                       omc);
+    };
+    const bool px = b.per[0] != 0, py = b.per[1] != 0;
+    wait_e(P0);
+    wait_e(P0 + 1);
+    if constexpr (RS) {
+        // Row-split layout: every thread visits at most two rows of R (tile
+        // rows and the halo row each side) and two of K per plane, the same
+        // rows on every plane, so their offsets, wall flags, y coefficients
+        // and row parities are formed once; so are the strip's z neighbours
+        // outside it (zo: for R, whose own half is the red one, and for K).
+        // Slot indices advance by one per plane instead of being recomputed.
+        int r_off[2], r_jp[2];
+        bool r_ok[2], r_lo[2], r_hi[2];
+        float r_cm[2], r_cp[2], r_dg[2];
+        int k_off[2], k_jp[2];
+        bool k_ok[2], k_lo[2], k_hi[2];
+        float k_cm[2], k_cp[2], k_dg[2];
+#pragma unroll
+        for (int v = 0; v < 2; v++) {
+            const int x = ro + v * rstep;
+            const int j = j0 - 1 + x;
+            r_ok[v] = x < ny && (py || (j >= 0 && j < n1));
+            const int jw = r_ok[v] ? (py ? wrap(j, n1) : j) : 0;
+            const int xs = r_ok[v] ? x : 0;
+            r_off[v] = xs;
+            r_jp[v] = jw & 1;
+            r_lo[v] = !py && jw == 0;
+            r_hi[v] = !py && jw == n1 - 1;
+            r_cm[v] = sy[xs];
+            r_cp[v] = sy[ny + xs];
+            r_dg[v] = sy[2 * ny + xs];
+            const int xk = ro + v * rstep;
+            k_ok[v] = xk < tj;
+            const int xks = k_ok[v] ? xk : 0;
+            const int jk = j0 + xks;
+            k_off[v] = xks;
+            k_jp[v] = jk & 1;
+            k_lo[v] = !py && jk == 0;
+            k_hi[v] = !py && jk == n1 - 1;
+            k_cm[v] = sy[xks + 1];
+            k_cp[v] = sy[ny + xks + 1];
+            k_dg[v] = sy[2 * ny + xks + 1];
+        }
+        // z neighbours outside the strip: o = 0 the left one, o = 1 the right
+        // one, in the other half (R: own 0, other H; K: own H, other 0)
+        const int zmode0 = k0 > 0 || b.per[2] ? 0 : (b.sg_lo[2] > 0 ? 1 : 2);
+        const int zmode1 = k0 + 4 < H || b.per[2] ? 0 : (b.sg_hi[2] > 0 ? 1 : 2);
+        const int zl_oth = k0 > 0 ? k0 - 1 : H - 1, zr_oth = k0 + 4 < H ? k0 + 4 : 0;
+        const int zoR0 = zmode0 == 0 ? H + zl_oth : k0, zoR1 = zmode1 == 0 ? H + zr_oth : k0;
+        const int zoK0 = zmode0 == 0 ? zl_oth : H + k0, zoK1 = zmode1 == 0 ? zr_oth : H + k0;
+        int se = (i0 - 1 - P0) % FU_ESLOTS;  // slot of e plane q
+        int sr = 0;                          // slot of r plane q (q - Q0 = 0 at the start)
+        for (int q = i0 - 1; q <= i1; q++) {
+            wait_e(q + 1);
+            wait_r(q);
+            const int sm1 = se == 0 ? FU_ESLOTS - 1 : se - 1, sp1 = se == FU_ESLOTS - 1 ? 0 : se + 1;
+            const int sm2 = sm1 == 0 ? FU_ESLOTS - 1 : sm1 - 1, srm1 = sr == 0 ? FU_RSLOTS - 1 : sr - 1;
+            if (px || (q >= 0 && q < n0)) {
+                // R(q): the red half of the tile rows and the halo rows
+                const int qi = px ? wrap(q, n0) : q;
+                float *pc = es + se * e_slot;
+                const float *pm = es + sm1 * e_slot, *pp = es + sp1 * e_slot, *rr = rs + sr * r_slot;
+                const float cmx = t.cm[0][qi], cpx = t.cp[0][qi], dx = t.dg[0][qi];
+                const bool xlo = !px && qi == 0, xhi = !px && qi == n0 - 1;
+#pragma unroll
+                for (int v = 0; v < 2; v++) {
+                    if (!r_ok[v]) continue;
+                    const int off = (r_off[v] + 1) * n2;
+                    const float *rrow = rr + r_off[v] * n2;
+                    if (((qi + r_jp[v]) & 1) == 0)
+                        fu_strip_rs<0, W1>(pc + off, pm + off, pp + off, rrow, n2, 0, H, k0, zoR0, zmode0, xlo, xhi,
+                                           r_lo[v], r_hi[v], b, cmx, cpx, dx, r_cm[v], r_cp[v], r_dg[v], zc[0], w,
+                                           omc);
                     else
-                        fu_strip_rs<1>(pc + off, pm + off, pp + off, rr + (x + 1) * n2, n2, H, H, k0, xlo, xhi, ylo,
-                                       yhi, b, cmx, cpx, dx, sy[x + 1], sy[ny + x + 1], sy[2 * ny + x + 1], zc[1], w,
-                                       omc);
-                } else {
+                        fu_strip_rs<1, W1>(pc + off, pm + off, pp + off, rrow, n2, 0, H, k0, zoR1, zmode1, xlo, xhi,
+                                           r_lo[v], r_hi[v], b, cmx, cpx, dx, r_cm[v], r_cp[v], r_dg[v], zc[1], w,
+                                           omc);
+                }
+            }
+            // this thread's writes (R(q), K(q-2)) before the async proxy reads them
+            fence_async_smem();
+            consumer_sync<NT>();
+            store_release(q);
+            const int p = q - 1;
+            if (p >= i0) {
+                // K(p): the black half of the tile rows
+                float *pc = es + sm1 * e_slot;
+                const float *pm = es + sm2 * e_slot, *pp = es + se * e_slot, *rr = rs + srm1 * r_slot;
+                const float cmx = t.cm[0][p], cpx = t.cp[0][p], dx = t.dg[0][p];
+                const bool xlo = !px && p == 0, xhi = !px && p == n0 - 1;
+#pragma unroll
+                for (int v = 0; v < 2; v++) {
+                    if (!k_ok[v]) continue;
+                    const int off = (k_off[v] + 2) * n2;
+                    const float *rrow = rr + (k_off[v] + 1) * n2;
+                    if (((p + k_jp[v]) & 1) == 1)
+                        fu_strip_rs<0, W1>(pc + off, pm + off, pp + off, rrow, n2, H, 0, k0, zoK0, zmode0, xlo, xhi,
+                                           k_lo[v], k_hi[v], b, cmx, cpx, dx, k_cm[v], k_cp[v], k_dg[v], zc[0], w,
+                                           omc);
+                    else
+                        fu_strip_rs<1, W1>(pc + off, pm + off, pp + off, rrow, n2, H, 0, k0, zoK1, zmode1, xlo, xhi,
+                                           k_lo[v], k_hi[v], b, cmx, cpx, dx, k_cm[v], k_cp[v], k_dg[v], zc[1], w,
+                                           omc);
+                }
+            }
+            se = sp1;
+            sr = sr == FU_RSLOTS - 1 ? 0 : sr + 1;
+        }
+    } else {
+        const int li = k0 > 0 ? k0 - 1 : (b.per[2] ? n2 - 1 : k0);
+        const bool lneg = k0 == 0 && !b.per[2] && b.sg_lo[2] < 0;
+        const int ri = k0 + 4 < n2 ? k0 + 4 : (b.per[2] ? 0 : k0 + 3);
+        const bool rneg = k0 + 4 >= n2 && !b.per[2] && b.sg_hi[2] < 0;
+        // every consumer thread runs every step and barrier, failed or not
+        for (int q = i0 - 1; q <= i1; q++) {
+            wait_e(q + 1);
+            wait_r(q);
+            if (px || (q >= 0 && q < n0)) {
+                // R(q)
+                const int qi = px ? wrap(q, n0) : q;
+                float *pc = eptr(q);
+                const float *pm = eptr(q - 1), *pp = eptr(q + 1), *rr = rptr(q);
+                const float cmx = t.cm[0][qi], cpx = t.cp[0][qi], dx = t.dg[0][qi];
+                const bool xlo = !px && qi == 0, xhi = !px && qi == n0 - 1;
+                for (int x = ro; x < ny; x += rstep) {
+                    const int j = j0 - 1 + x;
+                    if (!py && (j < 0 || j >= n1)) continue;
+                    const int jw = py ? wrap(j, n1) : j;
+                    const int off = (x + 1) * n2;
+                    fu_strip(pc + off, pm + off, pp + off, rr + x * n2, n2, k0, xlo, xhi, !py && jw == 0,
+                             !py && jw == n1 - 1, b, (qi + jw) & 1, li, ri, lneg, rneg, cmx, cpx, dx, sy[x],
+                             sy[ny + x], sy[2 * ny + x], zc[0], w, omc);
+                }
+            }
+            // this thread's writes (R(q), K(q-2)) before the async proxy reads them
+            fence_async_smem();
+            consumer_sync<NT>();
+            store_release(q);
+            const int p = q - 1;
+            if (p >= i0) {
+                // K(p)
+                float *pc = eptr(p);
+                const float *pm = eptr(p - 1), *pp = eptr(p + 1), *rr = rptr(p);
+                const float cmx = t.cm[0][p], cpx = t.cp[0][p], dx = t.dg[0][p];
+                const bool xlo = !px && p == 0, xhi = !px && p == n0 - 1;
+                for (int x = ro; x < tj; x += rstep) {
+                    const int j = j0 + x;
+                    const int off = (x + 2) * n2;
                     fu_strip(pc + off, pm + off, pp + off, rr + (x + 1) * n2, n2, k0, xlo, xhi, !py && j == 0,
                              !py && j == n1 - 1, b, (1 + p + j) & 1, li, ri, lneg, rneg, cmx, cpx, dx, sy[x + 1],
                              sy[ny + x + 1], sy[2 * ny + x + 1], zc[0], w, omc);
@@ -734,18 +817,26 @@ void fused_plan(Level &v, int sms) {
         !encode3(&m.fb, v.e32b, L, tj) || !encode3(&m.fb2, v.e32b, L, 2) || !encode3(&m.fr, v.r32, L, tj) ||
         !encode3(&m.fr1, v.r32, L, 1))
         return;
-    if (cudaFuncSetAttribute(k_rbgs_fused<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess ||
-        cudaFuncSetAttribute(k_rbgs_fused<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess) {
+    if (cudaFuncSetAttribute(k_rbgs_fused<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(k_rbgs_fused<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(k_rbgs_fused<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) !=
+            cudaSuccess) {
         cudaGetLastError();
         return;
     }
     // the block must fit an SM (registers and shared memory) or the level
     // keeps the colour sweeps
     int per_sm = 0, per_sm_rs = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rbgs_fused<false>, fu_threads<false>(),
+    int per_sm_w1 = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rbgs_fused<false, false>, fu_threads<false>(),
                                                       fused_smem(tj, L.n2)) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_rs, k_rbgs_fused<true>, fu_threads<true>(),
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_rs, k_rbgs_fused<true, false>, fu_threads<true>(),
                                                       fused_smem(tj, L.n2)) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_w1, k_rbgs_fused<true, true>, fu_threads<true>(),
+                                                      fused_smem(tj, L.n2)) != cudaSuccess ||
+        per_sm_w1 < 1 ||
         per_sm < 1 || per_sm_rs < 1) {
         cudaGetLastError();
         return;
@@ -771,6 +862,8 @@ bool fused_sweep_fits(const Lay &L, bool d3) {
         fu_nt<true>() % (L.n2 / 8) != 0)
         return false;
     const int tj = FU_TILE / L.n2;
+    // the row-split consumers visit at most two rows of each colour phase
+    if (tj + 2 > 2 * (fu_nt<true>() / (L.n2 / 8))) return false;
     return L.n1 % tj == 0 && L.n0 >= 16 && (int64_t)L.n0 * L.n1 * L.n2 >= FU_MIN_CELLS;
 }
 
@@ -838,7 +931,10 @@ bool tma_fused(saras_mg *h, cudaStream_t s, Level &v, bool to_b) {
     const dim3 grid((unsigned)(L.n1 / m.ftj), (unsigned)((L.n0 + m.fchunk - 1) / m.fchunk));
     int *err = reinterpret_cast<int *>(h->norm_out + 7);
     const dim3 block((unsigned)(v.rs ? fu_threads<true>() : fu_threads<false>()));
-    launch_pdl(v.rs ? k_rbgs_fused<true> : k_rbgs_fused<false>, grid, block, fused_smem(m.ftj, L.n2), s,
+    // the row-split kernel skips the SOR blend when the parameter is 1
+    const bool w1 = h->prm.sor_param == 1.0;
+    launch_pdl(v.rs ? (w1 ? k_rbgs_fused<true, true> : k_rbgs_fused<true, false>) : k_rbgs_fused<false, false>, grid,
+               block, fused_smem(m.ftj, L.n2), s,
                to_b ? m.fa : m.fb, to_b ? m.fa2 : m.fb2, to_b ? m.fb : m.fa, m.fr, m.fr1, L, sweep_tab(v), sweep_bnd(h),
                (float)h->prm.sor_param, (float)(1.0 - h->prm.sor_param), m.ftj, m.fchunk, err, tma_wait_limit(h));
     return true;
