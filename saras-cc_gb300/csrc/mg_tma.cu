@@ -337,7 +337,11 @@ __host__ __device__ constexpr int fu_threads() {
 constexpr int FU_ESLOTS = 6, FU_RSLOTS = 4;
 constexpr int FU_TILE = 4096;
 constexpr int64_t FU_MIN_CELLS = int64_t(1) << 22;
-constexpr size_t FU_HEAD = 1024;  // mbarriers and the tile's y coefficients
+// head of the dynamic shared memory: mbarriers, the tile's y coefficients
+// (from byte 256) and the chunk's x coefficients (from byte 1024, at most
+// FU_SX_MAX planes)
+constexpr size_t FU_HEAD = 4096;
+constexpr int FU_SX_MAX = 256;
 
 template <int NT>
 __device__ __forceinline__ void consumer_sync() {
@@ -456,7 +460,8 @@ __global__ void __launch_bounds__(fu_threads<RS>(), 1)
     const int e_slot = (tj + 4) * n2, r_slot = (tj + 2) * n2;
     uint64_t *efull = reinterpret_cast<uint64_t *>(smem), *eempty = efull + FU_ESLOTS;
     uint64_t *rfull = eempty + FU_ESLOTS, *rempty = rfull + FU_RSLOTS;
-    float *sy = reinterpret_cast<float *>(smem + 256);  // cm, cp, dg of y for rows j0-1 .. j0+tj
+    float *sy = reinterpret_cast<float *>(smem + 256);   // cm, cp, dg of y for rows j0-1 .. j0+tj
+    float *sx = reinterpret_cast<float *>(smem + 1024);  // cm, cp, dg of x for planes i0-1 .. i1
     float *es = reinterpret_cast<float *>(smem + FU_HEAD);
     float *rs = es + FU_ESLOTS * e_slot;
     const int j0 = (int)blockIdx.x * tj;
@@ -558,6 +563,16 @@ __global__ void __launch_bounds__(fu_threads<RS>(), 1)
         sy[ny + x] = t.cp[1][jw];
         sy[2 * ny + x] = t.dg[1][jw];
     }
+    // the x coefficients of every plane the chunk's steps visit, so that no
+    // step waits on a global load after its ring wait
+    const int nx = i1 - i0 + 2;
+    for (int x = ct; x < nx; x += NT) {
+        const int q = i0 - 1 + x;
+        const int qw = b.per[0] ? wrap(q, n0) : min(max(q, 0), n0 - 1);
+        sx[x] = t.cm[0][qw];
+        sx[nx + x] = t.cp[0][qw];
+        sx[2 * nx + x] = t.dg[0][qw];
+    }
     consumer_sync<NT>();
     auto eptr = [&](int p) { return es + ((p - P0) % FU_ESLOTS) * e_slot; };
     auto rptr = [&](int p) { return rs + ((p - Q0) % FU_RSLOTS) * r_slot; };
@@ -651,7 +666,8 @@ __global__ void __launch_bounds__(fu_threads<RS>(), 1)
                 const int qi = px ? wrap(q, n0) : q;
                 float *pc = es + se * e_slot;
                 const float *pm = es + sm1 * e_slot, *pp = es + sp1 * e_slot, *rr = rs + sr * r_slot;
-                const float cmx = t.cm[0][qi], cpx = t.cp[0][qi], dx = t.dg[0][qi];
+                const int xq = q - (i0 - 1);
+                const float cmx = sx[xq], cpx = sx[nx + xq], dx = sx[2 * nx + xq];
                 const bool xlo = !px && qi == 0, xhi = !px && qi == n0 - 1;
 #pragma unroll
                 for (int v = 0; v < 2; v++) {
@@ -677,7 +693,8 @@ __global__ void __launch_bounds__(fu_threads<RS>(), 1)
                 // K(p): the black half of the tile rows
                 float *pc = es + sm1 * e_slot;
                 const float *pm = es + sm2 * e_slot, *pp = es + se * e_slot, *rr = rs + srm1 * r_slot;
-                const float cmx = t.cm[0][p], cpx = t.cp[0][p], dx = t.dg[0][p];
+                const int xp_ = p - (i0 - 1);
+                const float cmx = sx[xp_], cpx = sx[nx + xp_], dx = sx[2 * nx + xp_];
                 const bool xlo = !px && p == 0, xhi = !px && p == n0 - 1;
 #pragma unroll
                 for (int v = 0; v < 2; v++) {
@@ -711,7 +728,8 @@ __global__ void __launch_bounds__(fu_threads<RS>(), 1)
                 const int qi = px ? wrap(q, n0) : q;
                 float *pc = eptr(q);
                 const float *pm = eptr(q - 1), *pp = eptr(q + 1), *rr = rptr(q);
-                const float cmx = t.cm[0][qi], cpx = t.cp[0][qi], dx = t.dg[0][qi];
+                const int xq = q - (i0 - 1);
+                const float cmx = sx[xq], cpx = sx[nx + xq], dx = sx[2 * nx + xq];
                 const bool xlo = !px && qi == 0, xhi = !px && qi == n0 - 1;
                 for (int x = ro; x < ny; x += rstep) {
                     const int j = j0 - 1 + x;
@@ -732,7 +750,8 @@ __global__ void __launch_bounds__(fu_threads<RS>(), 1)
                 // K(p)
                 float *pc = eptr(p);
                 const float *pm = eptr(p - 1), *pp = eptr(p + 1), *rr = rptr(p);
-                const float cmx = t.cm[0][p], cpx = t.cp[0][p], dx = t.dg[0][p];
+                const int xp_ = p - (i0 - 1);
+                const float cmx = sx[xp_], cpx = sx[nx + xp_], dx = sx[2 * nx + xp_];
                 const bool xlo = !px && p == 0, xhi = !px && p == n0 - 1;
                 for (int x = ro; x < tj; x += rstep) {
                     const int j = j0 + x;
@@ -844,7 +863,8 @@ void fused_plan(Level &v, int sms) {
     per_sm = std::min(per_sm, per_sm_rs);
     // one wave: the chunks of every tile column fill the resident blocks
     const int nch = std::max(1, per_sm * sms / (L.n1 / tj));
-    const int chunk = std::max(8, (L.n0 + nch - 1) / nch);
+    // at most FU_SX_MAX planes of x coefficients per block (chunk + 2)
+    const int chunk = std::min(FU_SX_MAX - 2, std::max(8, (L.n0 + nch - 1) / nch));
     m.ftj = tj;
     m.fchunk = chunk;
     m.fok = 1;
