@@ -420,6 +420,13 @@ def run_gb300(args):
             serving["poisson_only"] = {k: p[k] for k in ("requests", "completed", "statuses", "throughput_req_per_s",
                                                          "p50_ms", "p99_ms", "mean_ms", "makespan_s",
                                                          "model_hbm_frac")}
+        # the engine's capacity: the first 500 Poisson requests of the same
+        # draws all arriving at once (at 200/s the stream is arrival-bound,
+        # which caps its HBM fraction near 0.07 whatever the engine does)
+        c = run_serving(S, args, 0.0, n=500, rate=1e9)
+        serving["capacity"] = {k: c[k] for k in ("requests", "completed", "statuses", "throughput_req_per_s",
+                                                 "makespan_s", "cell_cycles_per_s", "model_hbm_GBps",
+                                                 "model_hbm_frac", "max_active", "engine_seconds")}
     # CPU baseline: the oracle's full FP64 solve of the same workload once
     # (about 20 s on 16 Grace cores, inside the 10-30 s sample bound); its
     # solution and history are the parity reference of the three GPU forms
@@ -600,11 +607,12 @@ def serve_stream(S, n, rate, seed=7, step_frac=0.0):
     return arrivals, kinds, steps, reqs
 
 
-def run_serving(S, args, step_frac=None):
+def run_serving(S, args, step_frac=None, n=None, rate=None):
     """Continuous-batching stream through the serving engine (host API,
     host buffers): latency = completion seen by the host minus the request's
     scheduled arrival."""
-    n, rate = args.serve_requests, args.serve_rate
+    n = n or args.serve_requests
+    rate = rate or args.serve_rate
     if step_frac is None:
         step_frac = args.serve_step_frac
     arrivals, kinds, steps, reqs = serve_stream(S, n, rate, step_frac=step_frac)
