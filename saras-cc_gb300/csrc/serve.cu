@@ -22,13 +22,18 @@
 // single-problem MIXED solve (mg_fast.cu) with the engine's parameters.
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <cstdio>
 #include <cstring>
 #include <deque>
 #include <map>
+#include <memory>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "mg_fast.cuh"
@@ -466,8 +471,92 @@ struct ServeDone {
     double latency;
 };
 
+// Host copies of request boxes between the caller's pageable memory and the
+// pinned staging ring, split across a few persistent worker threads: one
+// host thread copies about 10 GB/s, a fraction of what the copy engines move,
+// and a stream of requests arriving together spends its admissions and
+// retirements in these copies.  copy() is called by the engine's thread
+// alone and returns when every chunk is done.
+class CopyPool {
+  public:
+    explicit CopyPool(int workers) {
+        for (int w = 0; w < workers; w++) th_.emplace_back([this] { run(); });
+    }
+    ~CopyPool() {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        for (auto &t : th_) t.join();
+    }
+    void copy(void *dst, const void *src, size_t bytes) {
+        constexpr size_t MIN_SPLIT = (size_t)2 << 20;
+        if (th_.empty() || bytes < MIN_SPLIT) {
+            std::memcpy(dst, src, bytes);
+            return;
+        }
+        const size_t parts = th_.size() + 1;
+        size_t chunk = (bytes + parts - 1) / parts;
+        chunk = (chunk + 4095) / 4096 * 4096;
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            dst_ = static_cast<char *>(dst);
+            src_ = static_cast<const char *>(src);
+            bytes_ = bytes;
+            chunk_ = chunk;
+            nchunks_ = (int)((bytes + chunk - 1) / chunk);
+            next_.store(0);
+            left_.store(nchunks_);
+            gen_++;
+        }
+        cv_.notify_all();
+        work();
+        std::unique_lock<std::mutex> lk(mu_);
+        done_cv_.wait(lk, [this] { return left_.load() == 0; });
+    }
+
+  private:
+    // takes chunks of the current job until none is left
+    void work() {
+        for (;;) {
+            const int c = next_.fetch_add(1);
+            if (c >= nchunks_) return;
+            const size_t lo = (size_t)c * chunk_, n = std::min(chunk_, bytes_ - lo);
+            std::memcpy(dst_ + lo, src_ + lo, n);
+            if (left_.fetch_sub(1) == 1) {
+                std::lock_guard<std::mutex> lk(mu_);
+                done_cv_.notify_all();
+            }
+        }
+    }
+    void run() {
+        uint64_t seen = 0;
+        for (;;) {
+            {
+                std::unique_lock<std::mutex> lk(mu_);
+                cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
+                if (stop_) return;
+                seen = gen_;
+            }
+            work();
+        }
+    }
+    std::vector<std::thread> th_;
+    std::mutex mu_;
+    std::condition_variable cv_, done_cv_;
+    char *dst_ = nullptr;
+    const char *src_ = nullptr;
+    size_t bytes_ = 0, chunk_ = 0;
+    int nchunks_ = 0;
+    std::atomic<int> next_{0}, left_{0};
+    uint64_t gen_ = 0;
+    bool stop_ = false;
+};
+
 struct saras_serve {
     saras_serve_params prm{};
+    std::unique_ptr<CopyPool> copies;  // host copies of request boxes (made with the pinned ring)
     cudaStream_t stream = nullptr;   // batched iterations, time-step work
     cudaStream_t adm = nullptr;      // Poisson admissions and retirements
     cudaStream_t stp = nullptr;      // time-step requests (integrators and their hierarchies)
@@ -863,10 +952,8 @@ void pin_wait(saras_serve *h, size_t lo, size_t hi) {
     }
 }
 
-// Host box -> device staging box on the admission stream: through the
-// pinned ring (a host memcpy, then an asynchronous DMA) when it fits,
-// otherwise straight from the caller's pageable memory.
-saras_status upload_box(saras_serve *h, double *dev, const double *host, size_t bytes) {
+// The pinned staging ring and the copy threads, made on first use.
+saras_status ensure_pin(saras_serve *h) {
     if (!h->pin && h->pin_cap == 0) {
         if (cudaMallocHost((void **)&h->pin, PIN_BYTES) == cudaSuccess) {
             h->pin_cap = PIN_BYTES;
@@ -876,6 +963,18 @@ saras_status upload_box(saras_serve *h, double *dev, const double *host, size_t 
             h->pin_cap = 1;  // do not retry
         }
     }
+    if (!h->copies) {
+        const unsigned hw = std::thread::hardware_concurrency();
+        h->copies.reset(new CopyPool((int)std::min(7u, std::max(1u, hw / 2) - 1)));
+    }
+    return SARAS_OK;
+}
+
+// Host box -> device staging box on the admission stream: through the
+// pinned ring (a host copy by the copy threads, then an asynchronous DMA)
+// when it fits, otherwise straight from the caller's pageable memory.
+saras_status upload_box(saras_serve *h, double *dev, const double *host, size_t bytes) {
+    SARAS_TRY(ensure_pin(h));
     const size_t need = (bytes + 255) / 256 * 256;
     if (!h->pin || need > h->pin_cap) {
         SARAS_CUDA(cudaMemcpyAsync(dev, host, bytes, cudaMemcpyHostToDevice, h->adm));
@@ -884,7 +983,7 @@ saras_status upload_box(saras_serve *h, double *dev, const double *host, size_t 
     size_t lo = h->pin_head;
     if (lo + need > h->pin_cap) lo = 0;
     pin_wait(h, lo, lo + need);
-    std::memcpy(h->pin + lo, host, bytes);
+    h->copies->copy(h->pin + lo, host, bytes);
     SARAS_CUDA(cudaMemcpyAsync(dev, h->pin + lo, bytes, cudaMemcpyHostToDevice, h->adm));
     cudaEvent_t ev = nullptr;
     if (!h->ev_pool.empty()) {
@@ -1130,9 +1229,23 @@ saras_status retire(saras_serve *h, size_t idx, int32_t status) {
             SARAS_CUDA(cudaMemcpyAsync(h->d_box, c.out - b.origin, (size_t)b.elems * sizeof(double),
                                        cudaMemcpyHostToDevice, m->stream));
         mg_store_lhs(m, h->d_box + b.origin, b.st);
-        SARAS_CUDA(cudaMemcpyAsync(c.out - b.origin, h->d_box, (size_t)b.elems * sizeof(double),
-                                   cudaMemcpyDeviceToHost, m->stream));
-        SARAS_CUDA(cudaStreamSynchronize(m->stream));
+        const size_t bytes = (size_t)b.elems * sizeof(double), need = (bytes + 255) / 256 * 256;
+        SARAS_TRY(ensure_pin(h));
+        if (h->pin && need <= h->pin_cap) {
+            // through the pinned ring: a DMA at full speed, then the copy
+            // threads into the caller's box; the ring part is free again
+            // when this returns
+            size_t lo = h->pin_head;
+            if (lo + need > h->pin_cap) lo = 0;
+            pin_wait(h, lo, lo + need);
+            SARAS_CUDA(cudaMemcpyAsync(h->pin + lo, h->d_box, bytes, cudaMemcpyDeviceToHost, m->stream));
+            SARAS_CUDA(cudaStreamSynchronize(m->stream));
+            h->copies->copy(c.out - b.origin, h->pin + lo, bytes);
+            h->pin_head = lo + need;
+        } else {
+            SARAS_CUDA(cudaMemcpyAsync(c.out - b.origin, h->d_box, bytes, cudaMemcpyDeviceToHost, m->stream));
+            SARAS_CUDA(cudaStreamSynchronize(m->stream));
+        }
         h->done.push_back(ServeDone{c.id, c.res, c.cycles, status,
                                     std::chrono::duration<double>(Clock::now() - c.t_submit).count()});
         h->retired++;
