@@ -573,15 +573,30 @@ int saras_mg::maxCount() const {
 
 namespace {
 
+// Device array of `count` elements: a 256-byte aligned piece of the
+// handle's arena while saras_mg_create carves it (one cudaMalloc per
+// hierarchy instead of about thirty: each cudaMalloc may wait for the whole
+// device, which a serving engine creating hierarchies beside a running batch
+// feels), otherwise its own allocation.
 template <class T>
 saras_status dalloc(saras_mg *h, T **p, int64_t count) {
     const size_t bytes = (size_t)std::max<int64_t>(count, 1) * sizeof(T);
+    if (h->carving && h->arena) {
+        const size_t off = (h->arena_used + 255) / 256 * 256;
+        if (off + bytes <= h->arena_cap) {
+            *p = reinterpret_cast<T *>(h->arena + off);
+            h->arena_used = off + bytes;
+            return SARAS_OK;
+        }
+    }
     cudaError_t e = cudaMalloc((void **)p, bytes);
     if (e != cudaSuccess) {
         cudaGetLastError();
+        *p = nullptr;
         set_error("cudaMalloc of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
         return e == cudaErrorMemoryAllocation ? SARAS_OOM : SARAS_CUDA_ERR;
     }
+    h->allocs.push_back((void *)*p);
     h->dev_bytes += (int64_t)bytes;
     return SARAS_OK;
 }
@@ -742,27 +757,11 @@ saras_status check_params(const saras_mg_params &p) {
 }
 
 void free_all(saras_mg *h) {
-    for (Level &v : h->lv) {
-        cudaFree(v.lhs);
-        cudaFree(v.rhs);
-        cudaFree(v.tmp);
-        cudaFree(v.smd);
-        cudaFree(v.e32);
-        cudaFree(v.e32b);
-        cudaFree(v.r32);
-        cudaFree(v.tab);
-        cudaFree(v.tab32);
-        cudaFree(v.inv_diag);
-        cudaFree(v.inv_diag32);
-        cudaFree(v.dd);
-    }
-    cudaFree(h->walls);
-    cudaFree(h->norm_part);
-    cudaFree(h->norm_out);
-    cudaFree(h->coarse_sweeps);
-    cudaFree(h->stage_lhs);
-    cudaFree(h->stage_rhs);
-    cudaFree(h->mix_scalar);
+    // every device array came from dalloc: pieces of the arena or listed
+    for (void *q : h->allocs) cudaFree(q);
+    h->allocs.clear();
+    if (h->arena) cudaFree(h->arena);
+    h->arena = nullptr;
     if (h->norm_host) cudaFreeHost(h->norm_host);
     if (h->tab_stage) cudaFreeHost(h->tab_stage);
     if (h->graph) cudaGraphExecDestroy(h->graph);
@@ -836,6 +835,22 @@ saras_status create(const saras_grid_desc *gd, const saras_mg_params *prm, void 
         set_error("the MIXED form needs at least two levels");
         return SARAS_BAD_ARG;
     }
+    {
+        // one allocation for the hierarchy: the bytes the per-level rule
+        // gives plus the alignment of every piece
+        const int64_t est = mg_estimate_bytes(gd, prm);
+        if (est > 0) {
+            const size_t cap = (size_t)est + (size_t)256 * (16 * (size_t)h->nl + 32);
+            if (cudaMalloc((void **)&h->arena, cap) == cudaSuccess) {
+                h->arena_cap = cap;
+                h->dev_bytes += (int64_t)cap;
+                h->carving = true;
+            } else {
+                cudaGetLastError();
+                h->arena = nullptr;
+            }
+        }
+    }
     for (int l = 0; l < h->nl; l++) {
         Level &v = h->lv[(size_t)l];
         const AxisLevel *a = h->grid.lv[(size_t)l].data();
@@ -873,6 +888,7 @@ saras_status create(const saras_grid_desc *gd, const saras_mg_params *prm, void 
     SARAS_TRY(dalloc(h, &h->norm_out, 8));
     SARAS_TRY(dalloc(h, &h->coarse_sweeps, 4));
     SARAS_TRY(dalloc(h, &h->mix_scalar, 16));
+    h->carving = false;  // later allocations (the host entry point's boxes) are their own
     SARAS_CUDA(cudaMemsetAsync(h->coarse_sweeps, 0, 4 * sizeof(int), h->stream));
     SARAS_CUDA(cudaMemsetAsync(h->norm_out, 0, 8 * sizeof(double), h->stream));
     SARAS_CUDA(cudaMallocHost((void **)&h->norm_host, 8 * sizeof(double)));

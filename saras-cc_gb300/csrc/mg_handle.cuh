@@ -118,6 +118,13 @@ struct saras_mg {
     int64_t launches_cycle = 0;
     int64_t last_launches = 0;
     int64_t dev_bytes = 0;
+    // device memory: the hierarchy made by saras_mg_create is carved out of
+    // one allocation (arena); allocations made later, or that do not fit it,
+    // are listed in allocs
+    char *arena = nullptr;
+    size_t arena_cap = 0, arena_used = 0;
+    bool carving = false;
+    std::vector<void *> allocs;
     // polls of the TMA sweeps' pipeline waits (0: the kernels' default)
     unsigned wait_limit = 0;
     // kernel timing
