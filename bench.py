@@ -625,7 +625,11 @@ def run_serving(S, args, step_frac=None, n=None, rate=None):
     else:
         chosen = eng.autotune(tune, cycles=2)
     done, outs = {}, {}
+    # a time-step request's fields exist when it arrives, like a Poisson
+    # request's right-hand side: made before the clock starts
+    step_fields = {q: rbc_fields(S, reqs[q][0], 1000 + q) for q in range(n) if steps[q]}
     nxt = 0
+    drv = {"submit": 0.0, "engine_step": 0.0, "poll": 0.0, "idle_sleep": 0.0}
     t0 = time.perf_counter()
     deadline = args.serve_timeout
     while len(done) < n:
@@ -635,14 +639,17 @@ def run_serving(S, args, step_frac=None, n=None, rate=None):
         while nxt < n and arrivals[nxt] <= now:
             g, rhs = reqs[nxt]
             if steps[nxt]:
-                outs[nxt] = rbc_fields(S, g, 1000 + nxt)
+                outs[nxt] = step_fields.pop(nxt)
                 eng.submit_step(nxt, g, step_prm, outs[nxt])
             else:
                 outs[nxt] = S.padded_field(g)
                 eng.submit(nxt, g, rhs, outs[nxt])
             nxt += 1
+        t1 = time.perf_counter()
+        drv["submit"] += t1 - t0 - now
         a, p = eng.step()
         t = time.perf_counter() - t0
+        drv["engine_step"] += t + t0 - t1
         for d in eng.poll():
             q = d["id"]
             d["latency_s"] = t - arrivals[q]
@@ -650,8 +657,11 @@ def run_serving(S, args, step_frac=None, n=None, rate=None):
             done[q] = d
             outs.pop(q, None)
             reqs[q] = None
+        t2 = time.perf_counter()
+        drv["poll"] += t2 - t0 - t
         if a == 0 and p == 0 and nxt < n and len(done) == nxt:
             time.sleep(max(0.0, arrivals[nxt] - (time.perf_counter() - t0)))
+            drv["idle_sleep"] += time.perf_counter() - t2
     st = eng.stats()
     eng.close()
     lat = np.array([d["latency_s"] for d in done.values()]) * 1e3
@@ -702,7 +712,8 @@ def run_serving(S, args, step_frac=None, n=None, rate=None):
         "model_hbm_frac": model_bytes / makespan / 1e9 / hbm if done else None,
         "model_bytes_per_cell_cycle": SERVE_BYTES_PER_CELL,
         "engine_seconds": {"batched_iterations": st["t_batch_s"], "admissions": st["t_admit_s"],
-                           "retirements": st["t_retire_s"], "time_step_host_phases": st["t_steps_s"]},
+                           "retirements": st["t_retire_s"], "time_step_worker": st["t_steps_s"]},
+        "driver_seconds": drv,
         "max_active": st["max_active"], "batched_cycles": st["batched_cycles"], "gpu_launches": st["launches"],
         "device_bytes_resident_peak": st["bytes_allocated"],
         "schedule": {"cells_per_item": chosen.cells_per_item, "threads": chosen.threads,

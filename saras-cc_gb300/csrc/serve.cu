@@ -29,6 +29,7 @@
 #include <cstdio>
 #include <cstring>
 #include <deque>
+#include <functional>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -554,6 +555,116 @@ class CopyPool {
     bool stop_ = false;
 };
 
+// Time-step work off the engine's thread.  Between its pressure solves a
+// time-step request runs its right-hand sides, its Crank-Nicolson sweeps
+// (each sweep's residual read on the host and compared with the tolerance,
+// as the reference's solveVx loop does) and its correction.  On the
+// engine's thread that work held up every batched iteration; here one
+// worker thread runs it on the time-step stream while the engine goes on
+// launching batches, and hands each case back with an event that the next
+// batch waits on before the case's pressure solve joins it.
+enum { STEP_ADMIT = 0, STEP_ADVANCE = 1 };
+
+struct StepJob {
+    ServeCase c;
+    int kind = STEP_ADMIT;
+    int32_t solve_status = SARAS_OK;  // STEP_ADVANCE: how the sub-stage's pressure solve ended
+    bool retarget = false;            // STEP_ADMIT: a pooled integrator, to re-point at the request's grid
+};
+
+struct StepOut {
+    ServeCase c;
+    int32_t status = SARAS_OK;  // the request's outcome, when it leaves
+    bool left = false;          // the request leaves the engine (done or failed)
+    bool destroy = false;       // its integrator could not be re-pointed: free it
+    cudaEvent_t ev = nullptr;   // the case's work on the time-step stream (when it rejoins)
+    double secs = 0.0;          // wall time of the job
+    std::string err;            // the worker's error message on failure
+};
+
+class StepWorker {
+  public:
+    using Fn = std::function<StepOut(StepJob &)>;
+    StepWorker(int dev, Fn fn) : fn_(std::move(fn)) {
+        th_ = std::thread([this, dev] { run(dev); });
+    }
+    ~StepWorker() { stop(); }
+    void submit(StepJob j) {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            jobs_.push_back(std::move(j));
+            held_++;
+        }
+        cv_.notify_all();
+    }
+    // Finished jobs; when none is ready and work is held, waits up to wait_s
+    // seconds for one.
+    std::vector<StepOut> take(double wait_s) {
+        std::unique_lock<std::mutex> lk(mu_);
+        if (outs_.empty() && held_ > 0 && wait_s > 0.0)
+            done_cv_.wait_for(lk, std::chrono::duration<double>(wait_s), [this] { return !outs_.empty(); });
+        std::vector<StepOut> r(std::make_move_iterator(outs_.begin()), std::make_move_iterator(outs_.end()));
+        outs_.clear();
+        held_ -= (int)r.size();
+        return r;
+    }
+    // Requests the worker holds: queued, running, or finished and not taken.
+    int held() {
+        std::lock_guard<std::mutex> lk(mu_);
+        return held_;
+    }
+    // Ends the thread after the job it is running; returns the cases of the
+    // jobs it did not run and of the results nobody took.
+    std::vector<ServeCase> stop() {
+        std::vector<ServeCase> left;
+        if (!th_.joinable()) return left;
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        th_.join();
+        for (StepJob &j : jobs_) left.push_back(j.c);
+        for (StepOut &o : outs_) {
+            if (o.ev) cudaEventDestroy(o.ev);
+            left.push_back(o.c);
+        }
+        jobs_.clear();
+        outs_.clear();
+        held_ = 0;
+        return left;
+    }
+
+  private:
+    void run(int dev) {
+        cudaSetDevice(dev);
+        for (;;) {
+            StepJob j;
+            {
+                std::unique_lock<std::mutex> lk(mu_);
+                cv_.wait(lk, [this] { return stop_ || !jobs_.empty(); });
+                if (stop_) return;
+                j = std::move(jobs_.front());
+                jobs_.pop_front();
+            }
+            StepOut o = fn_(j);
+            {
+                std::lock_guard<std::mutex> lk(mu_);
+                outs_.push_back(std::move(o));
+            }
+            done_cv_.notify_all();
+        }
+    }
+    Fn fn_;
+    std::thread th_;
+    std::mutex mu_;
+    std::condition_variable cv_, done_cv_;
+    std::deque<StepJob> jobs_;
+    std::deque<StepOut> outs_;
+    int held_ = 0;
+    bool stop_ = false;
+};
+
 struct saras_serve {
     saras_serve_params prm{};
     std::unique_ptr<CopyPool> copies;  // host copies of request boxes (made with the pinned ring)
@@ -561,8 +672,12 @@ struct saras_serve {
     cudaStream_t adm = nullptr;      // Poisson admissions and retirements
     cudaStream_t stp = nullptr;      // time-step requests (integrators and their hierarchies)
     cudaEvent_t ev_adm = nullptr;    // admission work the next batch waits for
-    cudaEvent_t ev_stp = nullptr;    // time-step work the next batch waits for
+    cudaEvent_t ev_stp = nullptr;    // time-step work the next batch waits for (autotuning)
+    std::unique_ptr<StepWorker> steps;  // time-step work, made with the first time-step request
+    std::vector<cudaEvent_t> join_ev;   // cases back from the worker: the next batch waits for their work
+    int dev = 0;
     std::vector<ServeCase> incoming; // admitted while a batch ran; join the next one
+    std::deque<std::pair<ServeCase, int32_t>> finishing;  // finished by the last batch, retired during the next
     // pinned staging ring for admission uploads (copies from pageable memory
     // would wait for the admission stream, and so for the running batch)
     char *pin = nullptr;
@@ -849,8 +964,18 @@ saras_status graph_for(saras_serve *h, int depth, cudaGraphExec_t *out) {
 saras_status launch_batched(saras_serve *h, int *depth_out) {
     SARAS_CUDA(cudaEventRecord(h->ev_adm, h->adm));
     SARAS_CUDA(cudaStreamWaitEvent(h->stream, h->ev_adm, 0));
-    SARAS_CUDA(cudaEventRecord(h->ev_stp, h->stp));
-    SARAS_CUDA(cudaStreamWaitEvent(h->stream, h->ev_stp, 0));
+    // time-step cases back from the worker: the work that set up their
+    // pressure solves (the worker may meanwhile run other cases' work on the
+    // time-step stream, which the batch does not wait for)
+    for (cudaEvent_t e : h->join_ev) {
+        const cudaError_t r = cudaStreamWaitEvent(h->stream, e, 0);
+        cudaEventDestroy(e);
+        if (r != cudaSuccess) {
+            h->join_ev.clear();
+            return cuda_fail(r, "cudaStreamWaitEvent", __FILE__, __LINE__);
+        }
+    }
+    h->join_ev.clear();
     if (h->dirty) SARAS_TRY(upload_tables(h));
     cudaGraphExec_t g;
     const int depth = active_depth(h);
@@ -933,7 +1058,9 @@ saras_status stage_box(saras_serve *h, int64_t elems) {
 }
 
 // Nothing resident: a request that does not fit now never will.
-bool idle(const saras_serve *h) { return h->active.empty() && h->incoming.empty(); }
+bool idle(saras_serve *h) {
+    return h->active.empty() && h->incoming.empty() && h->finishing.empty() && (!h->steps || h->steps->held() == 0);
+}
 
 constexpr size_t PIN_BYTES = (size_t)256 << 20;
 
@@ -1028,88 +1155,38 @@ void drop_step(saras_serve *h, ServeCase &c, int32_t status) {
 
 enum AdmitStep { ADMIT_DONE = 0, ADMIT_WAIT = 1 };
 
-// Admission of a time-step request: its integrator (fields and hierarchy)
-// inside the HBM budget, the caller's fields uploaded, the first sub-stage
-// up to its pressure solve, which then joins the batch.
-AdmitStep admit_step(saras_serve *h, ServeCase &c, std::vector<ServeCase> &dst) {
-    const saras_rk3_params rp = step_params(h, c.rprm);
-    saras_rk3 *rk = nullptr;
+// The worker's side of a time-step request, on the worker thread.  It
+// touches the case's integrator and hierarchy, its slot's entry of d_fden
+// and the time-step stream, nothing the engine's thread uses meanwhile.
+//   STEP_ADMIT: re-point a pooled integrator at the request's grid, upload
+//     the caller's fields, run the first sub-stage up to its pressure solve.
+//   STEP_ADVANCE (the sub-stage's pressure solve has left the batch): finish
+//     the solve, the sub-stage's correction, then either the next sub-stage
+//     up to its pressure solve or the download of the fields.
+// A case that goes on carries an event on the time-step stream after the
+// work that set up its next pressure solve.
+StepOut step_work(saras_serve *h, StepJob &j) {
+    const auto t0 = Clock::now();
+    StepOut o;
+    o.c = j.c;
+    ServeCase &c = o.c;
     saras_status s = SARAS_OK;
-    auto pit = h->step_pool.find(c.shape);
-    if (pit != h->step_pool.end() && !pit->second.empty()) {
-        rk = pit->second.back();
-        pit->second.pop_back();
-        s = rk3_retarget(rk, &c.grid, &rp);
-        if (s != SARAS_OK) {
-            h->bytes_alloc -= rk3_device_bytes(rk) + rk3_multigrid(rk)->dev_bytes;
-            saras_rk3_destroy(rk);
-            h->done.push_back(ServeDone{c.id, 0.0, 0, (int32_t)s, since(c)});
-            return ADMIT_DONE;
+    bool rejoin = false;
+    if (j.kind == STEP_ADMIT) {
+        if (j.retarget) {
+            const saras_rk3_params rp = step_params(h, c.rprm);
+            s = rk3_retarget(c.rk, &c.grid, &rp);
+            o.destroy = s != SARAS_OK;
         }
-    } else {
-        const int64_t est = rk3_estimate_bytes(&c.grid, &rp);
-        if (h->bytes_alloc + est > h->prm.hbm_budget_bytes) evict_pooled(h, est);
-        if (h->bytes_alloc + est > h->prm.hbm_budget_bytes) {
-            if (!idle(h)) return ADMIT_WAIT;
-            set_error("request %lld needs about %lld bytes, above the HBM budget", (long long)c.id,
-                      (long long)est);
-            h->done.push_back(ServeDone{c.id, 0.0, 0, SARAS_BUDGET, since(c)});
-            return ADMIT_DONE;
-        }
-        s = saras_rk3_create(&c.grid, &rp, h->stp, &rk);
-        if (s != SARAS_OK) {
-            h->done.push_back(ServeDone{c.id, 0.0, 0, (int32_t)s, since(c)});
-            return ADMIT_DONE;
-        }
-        rk3_multigrid(rk)->no_rowsplit = true;
-        rk3_multigrid(rk)->lv[0].rs = 0;
-        h->bytes_alloc += rk3_device_bytes(rk) + rk3_multigrid(rk)->dev_bytes;
-    }
-    c.rk = rk;
-    c.mg = rk3_multigrid(rk);
-    const std::array<int, NREG> items = case_items(h, c.mg);
-    if (!fits(h, items)) {
-        h->step_pool[c.shape].push_back(rk);
-        c.rk = nullptr;
-        c.mg = nullptr;
-        if (!idle(h)) return ADMIT_WAIT;
-        set_error("request %lld has more work items than the tables hold", (long long)c.id);
-        h->done.push_back(ServeDone{c.id, 0.0, 0, SARAS_BUDGET, since(c)});
-        return ADMIT_DONE;
-    }
-    const Box b = box_of(c.grid);
-    s = saras_rk3_upload(rk, c.fields[0], c.fields[1], c.fields[2], c.fields[3], c.fields[4], c.fields[5], b.st);
-    if (s == SARAS_OK) s = rk3_stage_begin(rk, 0);
-    if (s != SARAS_OK) {
-        drop_step(h, c, s);
-        return ADMIT_DONE;
-    }
-    c.items = items;
-    c.slot = h->free_slots.back();
-    h->free_slots.pop_back();
-    c.stage = 0;
-    if (start_solve(h, c) != SARAS_OK) {
-        h->free_slots.push_back(c.slot);
-        drop_step(h, c, SARAS_CUDA_ERR);
-        return ADMIT_DONE;
-    }
-    for (int r = 0; r < NREG; r++) h->used[r] += items[r];
-    dst.push_back(c);
-    h->admitted++;
-    h->dirty = true;
-    return ADMIT_DONE;
-}
-
-// A time-step case whose pressure solve of this sub-stage has retired:
-// finish the solve, the sub-stage's correction, then either the next
-// sub-stage up to its pressure solve (the case stays in the batch with the
-// same hierarchy and tables) or the download of the fields.  Returns true
-// when the case left the batch.
-bool advance_step(saras_serve *h, size_t idx, int32_t solve_status) {
-    ServeCase &c = h->active[idx];
-    c.total_cycles += c.cycles;
-    saras_status s = SARAS_OK;
-    if (solve_status == SARAS_NAN) {
+        const Box b = box_of(c.grid);
+        if (s == SARAS_OK)
+            s = saras_rk3_upload(c.rk, c.fields[0], c.fields[1], c.fields[2], c.fields[3], c.fields[4], c.fields[5],
+                                 b.st);
+        c.stage = 0;
+        if (s == SARAS_OK) s = rk3_stage_begin(c.rk, 0);
+        if (s == SARAS_OK) s = start_solve(h, c);
+        rejoin = s == SARAS_OK;
+    } else if (j.solve_status == SARAS_NAN) {
         s = SARAS_NAN;
     } else {
         // a pressure solve that stopped at its V-Cycle Count above the
@@ -1122,21 +1199,115 @@ bool advance_step(saras_serve *h, size_t idx, int32_t solve_status) {
             c.stage++;
             s = rk3_stage_begin(c.rk, c.stage);
             if (s == SARAS_OK) s = start_solve(h, c);
-            if (s == SARAS_OK) return false;
+            rejoin = s == SARAS_OK;
         } else if (s == SARAS_OK) {
             const Box b = box_of(c.grid);
             s = saras_rk3_download(c.rk, c.fields[0], c.fields[1], c.fields[2], c.fields[3], c.fields[4],
                                    c.fields[5], b.st);
-            if (s == SARAS_OK) s = (saras_status)c.step_status;
         }
     }
-    ServeCase done = c;
-    h->free_slots.push_back(c.slot);
-    for (int r = 0; r < NREG; r++) h->used[r] -= c.items[r];
-    h->active.erase(h->active.begin() + (long)idx);
-    h->dirty = true;
-    drop_step(h, done, s);
-    return true;
+    if (rejoin) {
+        cudaError_t e = cudaEventCreateWithFlags(&o.ev, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventRecord(o.ev, c.mg->stream);
+        if (e != cudaSuccess) {
+            s = cuda_fail(e, "cudaEventRecord", __FILE__, __LINE__);
+            if (o.ev) cudaEventDestroy(o.ev);
+            o.ev = nullptr;
+            rejoin = false;
+        }
+    }
+    o.left = !rejoin;
+    o.status = s;
+    if (s != SARAS_OK) o.err = saras_last_error();
+    o.secs = std::chrono::duration<double>(Clock::now() - t0).count();
+    return o;
+}
+
+// Admission of a time-step request: its integrator (fields and hierarchy)
+// inside the HBM budget, a slot and its work items.  The worker then
+// uploads the caller's fields and runs the first sub-stage up to its
+// pressure solve, which joins the batch when the worker hands the case back.
+AdmitStep admit_step(saras_serve *h, ServeCase &c) {
+    const saras_rk3_params rp = step_params(h, c.rprm);
+    saras_rk3 *rk = nullptr;
+    bool pooled = false;
+    auto pit = h->step_pool.find(c.shape);
+    if (pit != h->step_pool.end() && !pit->second.empty()) {
+        rk = pit->second.back();
+        pit->second.pop_back();
+        pooled = true;
+    } else {
+        const int64_t est = rk3_estimate_bytes(&c.grid, &rp);
+        if (h->bytes_alloc + est > h->prm.hbm_budget_bytes) evict_pooled(h, est);
+        if (h->bytes_alloc + est > h->prm.hbm_budget_bytes) {
+            if (!idle(h)) return ADMIT_WAIT;
+            set_error("request %lld needs about %lld bytes, above the HBM budget", (long long)c.id,
+                      (long long)est);
+            h->done.push_back(ServeDone{c.id, 0.0, 0, SARAS_BUDGET, since(c)});
+            return ADMIT_DONE;
+        }
+        const saras_status s = saras_rk3_create(&c.grid, &rp, h->stp, &rk);
+        if (s != SARAS_OK) {
+            h->done.push_back(ServeDone{c.id, 0.0, 0, (int32_t)s, since(c)});
+            return ADMIT_DONE;
+        }
+        rk3_multigrid(rk)->no_rowsplit = true;
+        rk3_multigrid(rk)->lv[0].rs = 0;
+        h->bytes_alloc += rk3_device_bytes(rk) + rk3_multigrid(rk)->dev_bytes;
+    }
+    c.rk = rk;
+    c.mg = rk3_multigrid(rk);
+    // a pooled integrator has the request's shape, so its items are the
+    // request's before it is re-pointed
+    const std::array<int, NREG> items = case_items(h, c.mg);
+    if (!fits(h, items)) {
+        h->step_pool[c.shape].push_back(rk);
+        c.rk = nullptr;
+        c.mg = nullptr;
+        if (!idle(h)) return ADMIT_WAIT;
+        set_error("request %lld has more work items than the tables hold", (long long)c.id);
+        h->done.push_back(ServeDone{c.id, 0.0, 0, SARAS_BUDGET, since(c)});
+        return ADMIT_DONE;
+    }
+    if (!h->steps) h->steps.reset(new StepWorker(h->dev, [h](StepJob &j) { return step_work(h, j); }));
+    c.items = items;
+    c.slot = h->free_slots.back();
+    h->free_slots.pop_back();
+    for (int r = 0; r < NREG; r++) h->used[r] += items[r];
+    StepJob j;
+    j.c = c;
+    j.kind = STEP_ADMIT;
+    j.retarget = pooled;
+    h->steps->submit(std::move(j));
+    h->admitted++;
+    return ADMIT_DONE;
+}
+
+// Cases the worker has finished with: back into the batch (the next batch
+// waits for their work on the time-step stream) or out of the engine.
+// Called between batches only, when the active list is not in use.
+void collect_steps(saras_serve *h, double wait_s) {
+    if (!h->steps) return;
+    for (StepOut &o : h->steps->take(wait_s)) {
+        h->t_steps += o.secs;
+        ServeCase &c = o.c;
+        if (!o.left) {
+            h->join_ev.push_back(o.ev);
+            h->active.push_back(c);
+            h->dirty = true;
+            continue;
+        }
+        if (o.status != SARAS_OK && !o.err.empty()) set_error("%s", o.err.c_str());
+        h->free_slots.push_back(c.slot);
+        for (int r = 0; r < NREG; r++) h->used[r] -= c.items[r];
+        if (o.destroy) {
+            h->bytes_alloc -= rk3_device_bytes(c.rk) + rk3_multigrid(c.rk)->dev_bytes;
+            saras_rk3_destroy(c.rk);
+            c.rk = nullptr;
+            c.mg = nullptr;
+        }
+        drop_step(h, c, o.status);
+    }
 }
 
 // Admits pending requests in order while slots, the item tables and the HBM
@@ -1146,7 +1317,7 @@ saras_status admit(saras_serve *h, std::vector<ServeCase> &dst) {
     while (!h->pending.empty() && !h->free_slots.empty()) {
         ServeCase &c = h->pending.front();
         if (c.rk == nullptr && c.fields[0]) {
-            const AdmitStep a = admit_step(h, c, dst);
+            const AdmitStep a = admit_step(h, c);
             if (a == ADMIT_WAIT) break;
             h->pending.pop_front();
             continue;
@@ -1211,14 +1382,14 @@ saras_status admit(saras_serve *h, std::vector<ServeCase> &dst) {
         h->admitted++;
         h->dirty = true;
     }
-    h->max_active = std::max(h->max_active, (int)(h->active.size() + h->incoming.size()));
+    h->max_active = std::max(h->max_active, (int)(h->active.size() + h->incoming.size() + h->finishing.size()) +
+                                                (h->steps ? h->steps->held() : 0));
     return SARAS_OK;
 }
 
-// Retires active case idx: null-space projection, ghost layer, copy out,
-// hierarchy back to its pool.
-saras_status retire(saras_serve *h, size_t idx, int32_t status) {
-    ServeCase c = h->active[idx];
+// Retires a case that has left the batch: null-space projection, ghost
+// layer, copy out, hierarchy back to its pool, slot and items free.
+saras_status retire_case(saras_serve *h, const ServeCase &c, int32_t status) {
     saras_mg *m = c.mg;
     if (!c.internal) {
         mixed_finish(m, m->stream);
@@ -1253,9 +1424,28 @@ saras_status retire(saras_serve *h, size_t idx, int32_t status) {
     h->pool[c.shape].push_back(m);
     h->free_slots.push_back(c.slot);
     for (int r = 0; r < NREG; r++) h->used[r] -= c.items[r];
+    return SARAS_OK;
+}
+
+// Retires active case idx at once.
+saras_status retire(saras_serve *h, size_t idx, int32_t status) {
+    const ServeCase c = h->active[idx];
     h->active.erase(h->active.begin() + (long)idx);
     h->dirty = true;
-    return SARAS_OK;
+    return retire_case(h, c, status);
+}
+
+// Retires the cases the last batch finished.  Their copies out run on the
+// admission stream and the host while the next batch runs.
+saras_status flush_finishing(saras_serve *h) {
+    const auto t0 = Clock::now();
+    saras_status st = SARAS_OK;
+    while (!h->finishing.empty() && st == SARAS_OK) {
+        st = retire_case(h, h->finishing.front().first, h->finishing.front().second);
+        h->finishing.pop_front();
+    }
+    h->t_retire += std::chrono::duration<double>(Clock::now() - t0).count();
+    return st;
 }
 
 saras_status enqueue(saras_serve *h, int64_t id, const saras_grid_desc *grid, const double *rhs, double *lhs,
@@ -1330,6 +1520,7 @@ saras_status saras_serve_create(const saras_serve_params *prm, saras_serve **out
     if (prm->threads) h->threads = prm->threads;
     if (prm->blocks_per_sm) h->bps = prm->blocks_per_sm;
     cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, dev);
+    h->dev = dev;
     h->lev_cap = prm->max_cases * DMAX;
     plan_regions(h);
     bool ok = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) == cudaSuccess;
@@ -1414,9 +1605,13 @@ saras_status saras_serve_submit_step(saras_serve *h, int64_t id, const saras_gri
 saras_status saras_serve_step(saras_serve *h, int32_t *active, int32_t *pending) {
     if (!h) return SARAS_BAD_ARG;
     auto secs = [](Clock::time_point a, Clock::time_point b) { return std::chrono::duration<double>(b - a).count(); };
+    collect_steps(h, 0.0);
     auto t0 = Clock::now();
     if (h->active.empty()) {
-        // nothing to overlap with: admit straight into the batch
+        // nothing to overlap with: retire what the last batch finished and
+        // admit straight into the batch
+        SARAS_TRY(flush_finishing(h));
+        t0 = Clock::now();
         SARAS_TRY(admit(h, h->active));
         h->dirty = h->dirty || !h->active.empty();
     }
@@ -1428,6 +1623,8 @@ saras_status saras_serve_step(saras_serve *h, int32_t *active, int32_t *pending)
         // batch, so the iterations of every request keep their arithmetic
         int depth = 0;
         SARAS_TRY(launch_batched(h, &depth));
+        // meanwhile the cases the previous batch finished leave
+        SARAS_TRY(flush_finishing(h));
         t0 = Clock::now();
         SARAS_TRY(admit(h, h->incoming));
         t1 = Clock::now();
@@ -1445,15 +1642,23 @@ saras_status saras_serve_step(saras_serve *h, int32_t *active, int32_t *pending)
             if (bad || c.res < c.tol || c.cycles >= c.cap) {
                 const int32_t st = bad ? SARAS_NAN : (c.res < c.tol ? SARAS_OK : SARAS_NOT_CONVERGED);
                 if (c.rk) {
-                    const auto a0 = Clock::now();
-                    const bool left = advance_step(h, q, st);
-                    h->t_steps += secs(a0, Clock::now());
-                    if (!left) q++;
+                    // the sub-stage's end (and the next one's start) runs on
+                    // the worker while the next batch runs; the case keeps
+                    // its slot and items
+                    c.total_cycles += c.cycles;
+                    StepJob j;
+                    j.c = c;
+                    j.kind = STEP_ADVANCE;
+                    j.solve_status = st;
+                    h->active.erase(h->active.begin() + (long)q);
+                    h->dirty = true;
+                    h->steps->submit(std::move(j));
                     continue;
                 }
-                const auto r0 = Clock::now();
-                SARAS_TRY(retire(h, q, st));
-                h->t_retire += secs(r0, Clock::now());
+                // out of the next batch's tables; retired while it runs
+                h->finishing.emplace_back(c, st);
+                h->active.erase(h->active.begin() + (long)q);
+                h->dirty = true;
                 continue;
             }
             q++;
@@ -1463,8 +1668,15 @@ saras_status saras_serve_step(saras_serve *h, int32_t *active, int32_t *pending)
             h->incoming.clear();
             h->dirty = true;
         }
+    } else if (h->steps && h->steps->held() > 0) {
+        // nothing to batch until the worker hands a case back: wait for one
+        // (briefly, so that the caller can submit meanwhile)
+        collect_steps(h, 0.002);
     }
-    if (active) *active = (int32_t)h->active.size();
+    // no batch follows to overlap the copies out with
+    if (h->active.empty()) SARAS_TRY(flush_finishing(h));
+    const int held = h->steps ? h->steps->held() : 0;
+    if (active) *active = (int32_t)(h->active.size() + h->incoming.size() + h->finishing.size() + held);
     if (pending) *pending = (int32_t)h->pending.size();
     return SARAS_OK;
 }
@@ -1493,7 +1705,7 @@ saras_status saras_serve_autotune(saras_serve *h, const saras_grid_desc *grids, 
         set_error("invalid autotune arguments");
         return SARAS_BAD_ARG;
     }
-    if (!h->active.empty() || !h->pending.empty()) {
+    if (!idle(h) || !h->pending.empty()) {
         set_error("autotune needs an idle engine");
         return SARAS_BAD_ARG;
     }
@@ -1580,7 +1792,8 @@ saras_status saras_serve_get_stats(const saras_serve *h, saras_serve_stats *out)
     out->launches = h->launches;
     out->admitted = h->admitted;
     out->retired = h->retired;
-    out->active = (int32_t)h->active.size();
+    out->active = (int32_t)(h->active.size() + h->incoming.size() + h->finishing.size() +
+                            (h->steps ? h->steps->held() : 0));
     out->pending = (int32_t)h->pending.size();
     int pooled = 0;
     for (const auto &kv : h->pool) pooled += (int)kv.second.size();
@@ -1596,11 +1809,22 @@ saras_status saras_serve_get_stats(const saras_serve *h, saras_serve_stats *out)
 
 saras_status saras_serve_destroy(saras_serve *h) {
     if (!h) return SARAS_OK;
+    if (h->steps) {
+        // the job the worker is running ends first; the cases it still
+        // holds go with their integrators
+        for (ServeCase &c : h->steps->stop())
+            if (c.rk) saras_rk3_destroy(c.rk);
+        h->steps.reset();
+    }
+    for (cudaEvent_t e : h->join_ev) cudaEventDestroy(e);
+    h->join_ev.clear();
     if (h->stream) cudaStreamSynchronize(h->stream);
     if (h->adm) cudaStreamSynchronize(h->adm);
     if (h->stp) cudaStreamSynchronize(h->stp);
     for (ServeCase &c : h->incoming) h->active.push_back(c);
     h->incoming.clear();
+    for (auto &f : h->finishing) h->active.push_back(f.first);
+    h->finishing.clear();
     for (ServeCase &c : h->active) {
         if (c.rk)
             saras_rk3_destroy(c.rk);  // owns its hierarchy
