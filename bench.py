@@ -814,9 +814,14 @@ def c4_block(S, torch, n=256, steps=100, beta=1.3):
     (the CPU restatement does the same)."""
     g = S.grid_desc(n=(n, n, n), mesh="UUD", beta=(1.0, 1.0, beta), domain="PPN")
     out = {"workload": f"RK3 Rayleigh-Benard {n}^3, Ra 1e7, Pr 1, z tanh beta {beta}, PPN, dt 1e-4, CN tol 1e-6, "
-                       f"MG 3/6 tol 1e-6 coarsest 1e-2, {steps} steps after one warm-up step"}
-    for name, prec in (("fp64", S.PREC_FP64), ("mixed", S.PREC_MIXED)):
+                       f"MG 3/6 tol 1e-6 coarsest 1e-2, {steps} steps after one warm-up step; FP64 and MIXED "
+                       "pressure solves with the separately rounded time-step stencils, and MIXED with the FAST "
+                       "stencils"}
+    finals = {}
+    for name, prec, form in (("fp64", S.PREC_FP64, S.STENCIL_EXACT), ("mixed", S.PREC_MIXED, S.STENCIL_EXACT),
+                             ("mixed_fast", S.PREC_MIXED, S.STENCIL_FAST)):
         p = rbc_step_params(S, prec)
+        p.stencil_form = form
         f = rbc_fields(S, g, 4)
         rk = S.RK3(g, p)
         rk.upload(f["vx"], f["vy"], f["vz"], f["p"], f["t"], f["pp"])
@@ -833,7 +838,18 @@ def c4_block(S, torch, n=256, steps=100, beta=1.3):
         out[f"{name}_cn_iters_per_step"] = cni / steps
         out[f"{name}_max_w"] = float(np.abs(f["vz"][1:-1, 1:-1, 1:-1]).max())
         out[f"{name}_t_mean"] = float(f["t"][1:-1, 1:-1, 1:-1].mean())
+        finals[name] = f
     out["speedup_mixed_vs_fp64"] = out["fp64_ms_per_step"] / out["mixed_ms_per_step"]
+    out["speedup_mixed_fast_vs_fp64"] = out["fp64_ms_per_step"] / out["mixed_fast_ms_per_step"]
+    # largest difference of each field after the run, relative to the
+    # field's largest magnitude: the FAST time-step stencils against the
+    # separately rounded ones (both with the MIXED pressure solve), beside the
+    # MIXED pressure solve against the FP64 one (both separately rounded)
+    def rel(a, b):
+        return {k: float(np.abs(a[k] - b[k]).max() / max(np.abs(b[k]).max(), 1e-300))
+                for k in ("vx", "vy", "vz", "p", "t")}
+    out["mixed_fast_vs_mixed_rel_diff"] = rel(finals["mixed_fast"], finals["mixed"])
+    out["mixed_vs_fp64_rel_diff"] = rel(finals["mixed"], finals["fp64"])
     return out
 
 

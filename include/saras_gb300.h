@@ -189,6 +189,9 @@ typedef struct saras_field_bc {
     double  value[6];
 } saras_field_bc;
 
+#define SARAS_STENCIL_EXACT 0
+#define SARAS_STENCIL_FAST  1
+
 typedef struct saras_rk3_params {
     double  nu, kappa;      /* from timestep::timestep (see saras_rbc_coefficients) */
     double  dt;             /* "Time-Step" */
@@ -207,7 +210,13 @@ typedef struct saras_rk3_params {
     /* "Integration Scheme": 2 (or 0) low-storage RK3, lsRK3_d3/_d2;
      * 1 Euler/Crank-Nicolson, eulerCN_d3/_d2 (scalar_d3.cc:156-163) */
     int32_t integration;
-    int32_t pad_;
+    /* SARAS_STENCIL_EXACT (0): every value of the right-hand sides and the
+     * Crank-Nicolson sweeps in the reference's order with separately
+     * rounded FP64 operations (bit parity).  SARAS_STENCIL_FAST (1): the same
+     * stencils with folded coefficients, fused multiply-adds and products
+     * with reciprocals of the stencil constants; equal to the exact form to
+     * rounding, not bit for bit. */
+    int32_t stencil_form;
 } saras_rk3_params;
 /* The Differentiation Scheme follows the grid descriptor's pad: pad 1 is
  * dScheme 1 (second order), pad 2 is dScheme 2 (fourth order in the interior,

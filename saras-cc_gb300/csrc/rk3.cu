@@ -38,6 +38,7 @@ using namespace saras;
 namespace {
 
 constexpr int BX = 128;
+constexpr int RK_TABLES = 11;  // per-axis metric tables of a handle (RkTab)
 
 // Field layout: core plus `p` ghost layers on x and z and `py` on y (1 for
 // the planar case, grid.cc:91-95).  Element (i,j,k) sits at (i+p)*s0 +
@@ -77,6 +78,10 @@ struct RkTab {
     const double *dh[3];          // x(i+1) - x(i): the upwind Peclet length
     const double *dv[3];          // dXi / xi_x: cell extent (tseries volumes and areas)
     const double *xc[3];          // cell-centre coordinate x(i)
+    // the FAST stencil form's folded coefficients
+    const double *k1[3];   // xi_x / (2 dXi): first derivative, second order
+    const double *k2a[3];  // xixx / (2 dXi): the first-derivative part of the second derivative
+    const double *k2b[3];  // xix2 / dXi^2: its second-difference part
 };
 struct RkScal {
     double ih[3], ih2d[3];  // derivative: 1/dXi, pow(1/dXi, 2)
@@ -279,38 +284,167 @@ __device__ __forceinline__ void rhs_cell(const Fields &f, const FLay &L, const R
     nl_out = n;
 }
 
+// ---- the FAST stencil form ----
+// The same right-hand sides and Crank-Nicolson sweeps with the reference's
+// operation order relaxed, for runs that do not need bit parity: the
+// metric products folded into per-index tables (k1, k2a, k2b), the compiler
+// free to contract a product into the add that follows (FMA), divisions by
+// the stencils' constants taken as products with their reciprocals, and the
+// Peclet test |u| dh / D < limit taken as |u| dh < limit D.  Values agree
+// with the separately rounded form to rounding; they are not bit-identical
+// to it.
+
+// calcDerivative1: (F+ - F-) xi_x / (2 dXi); dScheme 2 interior
+// (8 (F+ - F-) - (F+2 - F-2)) xi_x / (12 dXi).
+template <int DS, class LY>
+__device__ __forceinline__ double f_d1(const double *F, const LY &L, const RkTab &T, int a, int idx, int64_t c) {
+    const int64_t st = axis_stride(L, a);
+    const double df = F[c + st] - F[c - st];
+    const double k = T.k1[a][idx];
+    if (DS == 1 || idx == 0 || idx == axis_ext(L, a) - 1) return df * k;
+    return (8.0 * df - (F[c + 2 * st] - F[c - 2 * st])) * (k * (1.0 / 6.0));
+}
+
+// calcDerivative2: xixx d/dXi + xix2 d2/dXi2 with the same stencils as d2.
+template <int DS>
+__device__ __forceinline__ double f_d2(const double *F, const FLay &L, const RkTab &T, int a, int idx, int64_t c) {
+    const int64_t st = axis_stride(L, a);
+    const double fp = F[c + st], fm = F[c - st], f0 = F[c];
+    const double ka = T.k2a[a][idx], kb = T.k2b[a][idx];
+    if (DS == 1 || idx == 0 || idx == L.ext(a) - 1) return (fp - fm) * ka + ((fp + fm) - 2.0 * f0) * kb;
+    const double fp2 = F[c + 2 * st], fm2 = F[c - 2 * st];
+    const double c1 = 8.0 * (fp - fm) - (fp2 - fm2);
+    const double c2 = 16.0 * (fp + fm) - 30.0 * f0 - (fp2 + fm2);
+    return c1 * (ka * (1.0 / 6.0)) + c2 * (kb * (1.0 / 12.0));
+}
+
+// Morinishi's term (mterm): (Va xi dF + xi d(Va F)) / (4 dXi), or with the
+// fourth-order differences / (24 dXi).
+template <int DS>
+__device__ __forceinline__ double f_mterm(const double *F, const double *Va, const FLay &L, const RkTab &T,
+                                          const RkScal &S, int a, int idx, int64_t c) {
+    const int64_t st = axis_stride(L, a);
+    const double x = T.xi_x[a][idx];
+    const int last = (a == 2 ? L.n1 : L.ext(a)) - 1;
+    if (DS == 2 && idx != 0 && idx != last) {
+        const double f2 = F[c + 2 * st], f1 = F[c + st], g1 = F[c - st], g2 = F[c - 2 * st];
+        const double sf = ((8.0 * f1 - f2) - 8.0 * g1) + g2;
+        const double sv = ((8.0 * (Va[c + st] * f1) - Va[c + 2 * st] * f2) - 8.0 * (Va[c - st] * g1)) +
+                          Va[c - 2 * st] * g2;
+        return (Va[c] * sf + sv) * (x * S.i2d[a] * (1.0 / 12.0));
+    }
+    const double fp = F[c + st], fm = F[c - st];
+    return (Va[c] * (fp - fm) + (Va[c + st] * fp - Va[c - st] * fm)) * (x * S.i2d[a] * 0.5);
+}
+
+// The hybrid upwind term (uterm).
+template <int DS>
+__device__ __forceinline__ double f_uterm(const double *F, const double *Va, const FLay &L, const RkTab &T,
+                                          const RkScal &S, double dcoef, int a, int idx, int64_t c) {
+    const int64_t st = axis_stride(L, a);
+    const double u = Va[c];
+    const double uk = u * T.xi_x[a][idx] * S.i2d[a];
+    const double f0 = F[c], fp = F[c + st], fm = F[c - st];
+    if (DS == 2 && (idx == 0 || idx == L.ext(a) - 1)) return uk * (fp - fm);
+    const bool central = fabs(u) * T.dh[a][idx] < S.pe_limit * dcoef;
+    if (DS == 1) {
+        if (central) return uk * (fp - fm);
+        if (u > 0) return uk * ((S.ub * f0 - S.ua * fm) - S.uc * fp);
+        return uk * ((S.ua * fp - S.ub * f0) + S.uc * fm);
+    }
+    const double fp2 = F[c + 2 * st], fm2 = F[c - 2 * st];
+    if (central) return uk * (((8.0 * fp - fp2) - 8.0 * fm) + fm2) * (1.0 / 6.0);
+    if (u > 0) return uk * (((S.ua * fm2 - S.ub * fm) + S.uc * f0) - S.ud * fp);
+    return uk * (((S.ub * fp - S.ua * fp2) - S.uc * f0) + S.ud * fm);
+}
+
+template <int DS>
+__device__ __forceinline__ double f_nterm(int nls, const double *F, const double *Va, const FLay &L,
+                                          const RkTab &T, const RkScal &S, double dcoef, int a, int idx,
+                                          int64_t c) {
+    if (nls == 3) return f_mterm<DS>(F, Va, L, T, S, a, idx, c);
+    if (nls == 2) return f_uterm<DS>(F, Va, L, T, S, dcoef, a, idx, c);
+    return Va[c] * f_d1<DS>(F, L, T, a, idx, c);
+}
+
+// rhs_cell's sums in the FAST form.
 template <bool D3, bool SC, int DS>
+__device__ __forceinline__ void f_rhs_cell(const Fields &f, const FLay &L, const RkTab &T, const RkScal &S,
+                                           const Stage &sg, int comp, int i, int j, int k, int64_t c,
+                                           double &rhs_out, double &nl_out) {
+    const int id[3] = {i, j, k};
+    const bool vel = comp < 3;
+    const double *F = vel ? f.V[comp] : f.T;
+    const double dcoef = vel ? S.dc_v : S.dc_t;
+    double dif = f_d2<DS>(F, L, T, 0, i, c) + f_d2<DS>(F, L, T, 2, k, c);
+    if (D3) dif += f_d2<DS>(F, L, T, 1, j, c);
+    double n = f_nterm<DS>(sg.nls, F, f.V[0], L, T, S, dcoef, 0, i, c) +
+               f_nterm<DS>(sg.nls, F, f.V[2], L, T, S, dcoef, 2, k, c);
+    if (D3) n += f_nterm<DS>(sg.nls, F, f.V[1], L, T, S, dcoef, 1, j, c);
+    double t = 0.0;  // forcing minus the pressure gradient
+    if (vel) {
+        t = -f_d1<DS>(f.P, L, T, comp, id[comp], c);
+        if (SC) t -= sg.g[comp] * f.T[c];
+    }
+    const double a = vel ? sg.anu : sg.akap;
+    if (sg.euler) {
+        rhs_out = (a * dif - n + t) * sg.dt + F[c];
+        nl_out = 0.0;
+        return;
+    }
+    double r = a * dif + sg.ab * t - sg.gam * n;
+    if (sg.rk > 0) r += sg.zeta * (vel ? f.nl[comp][c] : f.nlT[c]);
+    rhs_out = r * sg.dt + F[c];
+    nl_out = -n;
+}
+
+template <bool D3, bool SC, int DS, bool FAST>
 __global__ void k_rhs(Fields f, FLay L, RkTab T, RkScal S, Stage sg) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = D3 ? (int)blockIdx.y : 0;
     const int i = blockIdx.z;
     if (k >= L.n2) return;
     const int64_t c = L.at(i, j, k);
-    for (int comp = 0; comp < 3; comp++) {
+    for (int comp = 0; comp < (SC ? 4 : 3); comp++) {
         if (!D3 && comp == 1) continue;
         double r, n;
-        rhs_cell<D3, SC, DS>(f, L, T, S, sg, comp, i, j, k, c, r, n);
-        f.nse[comp][c] = r;
-        if (!sg.euler) f.nl[comp][c] = n;
-    }
-    if (SC) {
-        double r, n;
-        rhs_cell<D3, SC, DS>(f, L, T, S, sg, 3, i, j, k, c, r, n);
-        f.tmpR[c] = r;
-        if (!sg.euler) f.nlT[c] = n;
+        if (FAST)
+            f_rhs_cell<D3, SC, DS>(f, L, T, S, sg, comp, i, j, k, c, r, n);
+        else
+            rhs_cell<D3, SC, DS>(f, L, T, S, sg, comp, i, j, k, c, r, n);
+        if (comp < 3) {
+            f.nse[comp][c] = r;
+            if (!sg.euler) f.nl[comp][c] = n;
+        } else {
+            f.tmpR[c] = r;
+            if (!sg.euler) f.nlT[c] = n;
+        }
     }
 }
 
 // One Jacobi sweep of (1 - beta*dt*coef*L) u = rhs (predictors.cc:65-91).
-template <bool D3>
+// bdc = beta*dt*coef (the FAST form's folded factor).
+template <bool D3, bool FAST>
 __global__ void k_cn_jacobi(const double *__restrict__ F, const double *__restrict__ R, double *__restrict__ out,
-                            FLay L, RkTab T, double dt, double coef, double beta, double den_fac) {
+                            FLay L, RkTab T, double dt, double coef, double beta, double den_fac, double bdc) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = D3 ? (int)blockIdx.y : 0;
     const int i = blockIdx.z;
     if (k >= L.n2) return;
     const int64_t c = L.at(i, j, k);
     const double xp = F[c + L.s0], xm = F[c - L.s0], zp = F[c + 1], zm = F[c - 1];
+    if (FAST) {
+        double s = T.a2[0][i] * (xp + xm) + T.a1[0][i] * (xp - xm);
+        s += T.a2[2][k] * (zp + zm) + T.a1[2][k] * (zp - zm);
+        double d3 = T.a2[0][i] + T.a2[2][k];
+        if (D3) {
+            const double yp = F[c + L.s1], ym = F[c - L.s1];
+            s += T.a2[1][j] * (yp + ym) + T.a1[1][j] * (yp - ym);
+            d3 += T.a2[1][j];
+        }
+        out[c] = (s * bdc + R[c]) / (den_fac * d3 + 1.0);
+        return;
+    }
     double s = radd(rmul(T.a2[0][i], radd(xp, xm)), rmul(T.a1[0][i], rsub(xp, xm)));
     double d3 = T.a2[0][i];
     if (D3) {
@@ -336,7 +470,7 @@ __device__ __forceinline__ double warp_max(double v) {
 
 // max |u - beta*dt*coef*L u - rhs| over the core (predictors.cc:96-131),
 // per-block partials.
-template <bool D3>
+template <bool D3, bool FAST>
 __global__ void k_cn_resid(const double *__restrict__ F, const double *__restrict__ R, FLay L, RkTab T, RkScal S,
                            double bdc, double *__restrict__ part) {
     double m = 0.0;
@@ -344,6 +478,19 @@ __global__ void k_cn_resid(const double *__restrict__ F, const double *__restric
         const int64_t c = L.at(i, j, k);
         const double u = F[c], u2 = rmul(2.0, u);
         const double xp = F[c + L.s0], xm = F[c - L.s0], zp = F[c + 1], zm = F[c - 1];
+        if (FAST) {
+            // the a2 / a1 tables are xix2 / dXi^2 and xixx / (2 dXi)
+            double s = T.a2[0][i] * ((xp + xm) - u2) + T.a1[0][i] * (xp - xm);
+            s += T.a2[2][k] * ((zp + zm) - u2) + T.a1[2][k] * (zp - zm);
+            if (D3) {
+                const double yp = F[c + L.s1], ym = F[c - L.s1];
+                s += T.a2[1][j] * ((yp + ym) - u2) + T.a1[1][j] * (yp - ym);
+            }
+            const double t = fabs((u - bdc * s) - R[c]);
+            if (t > m) m = t;
+            if (!isfinite(t)) m = CUDART_INF;
+            return;
+        }
         double s = radd(rmul(rmul(T.xix2[0][i], radd(rsub(xp, u2), xm)), S.ih2t[0]),
                         rmul(rmul(T.xixx[0][i], rsub(xp, xm)), S.i2ht[0]));
         if (D3) {
@@ -680,18 +827,19 @@ saras_status cn_solve(saras_rk3 *h, cudaStream_t s, int comp, const double *rhs,
     const FBC &B = h->bc[comp < 3 ? comp : 4];
     int iterCount = 0;
     for (;;) {
-        if (h->d3)
-            k_cn_jacobi<true><<<cgrid(L, true, bx), bx, 0, s>>>(*cur, rhs, *alt, L, h->tabs, dt, coef, beta, den_fac);
-        else
-            k_cn_jacobi<false><<<cgrid(L, false, bx), bx, 0, s>>>(*cur, rhs, *alt, L, h->tabs, dt, coef, beta,
-                                                                   den_fac);
+        using JK = void (*)(const double *, const double *, double *, FLay, RkTab, double, double, double, double,
+                            double);
+        using RK = void (*)(const double *, const double *, FLay, RkTab, RkScal, double, double *);
+        static const JK jk[2][2] = {{k_cn_jacobi<false, false>, k_cn_jacobi<false, true>},
+                                    {k_cn_jacobi<true, false>, k_cn_jacobi<true, true>}};
+        static const RK rk[2][2] = {{k_cn_resid<false, false>, k_cn_resid<false, true>},
+                                    {k_cn_resid<true, false>, k_cn_resid<true, true>}};
+        const int d3 = h->d3 ? 1 : 0, fast = h->prm.stencil_form == SARAS_STENCIL_FAST ? 1 : 0;
+        jk[d3][fast]<<<cgrid(L, h->d3, bx), bx, 0, s>>>(*cur, rhs, *alt, L, h->tabs, dt, coef, beta, den_fac, bdc);
         h->launches++;
         std::swap(*cur, *alt);
         impose(h, s, *cur, B, true);
-        if (h->d3)
-            k_cn_resid<true><<<h->nblocks, 256, 0, s>>>(*cur, rhs, L, h->tabs, h->scal, bdc, h->part);
-        else
-            k_cn_resid<false><<<h->nblocks, 256, 0, s>>>(*cur, rhs, L, h->tabs, h->scal, bdc, h->part);
+        rk[d3][fast]<<<h->nblocks, 256, 0, s>>>(*cur, rhs, L, h->tabs, h->scal, bdc, h->part);
         k_max_final<<<1, 32, 0, s>>>(h->part, h->nblocks, h->red);
         h->launches += 2;
         SARAS_CUDA(cudaMemcpyAsync(h->red_host, h->red, sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -713,12 +861,19 @@ saras_status cn_solve(saras_rk3 *h, cudaStream_t s, int comp, const double *rhs,
 
 using RhsKernel = void (*)(Fields, FLay, RkTab, RkScal, Stage);
 
-RhsKernel rhs_kernel(bool d3, bool sc, int ds) {
+template <bool FAST>
+RhsKernel rhs_kernel_of(bool d3, bool sc, int ds) {
     // (dimension, scalar, differentiation scheme) -> kernel
     static const RhsKernel ks[2][2][2] = {
-        {{k_rhs<false, false, 1>, k_rhs<false, false, 2>}, {k_rhs<false, true, 1>, k_rhs<false, true, 2>}},
-        {{k_rhs<true, false, 1>, k_rhs<true, false, 2>}, {k_rhs<true, true, 1>, k_rhs<true, true, 2>}}};
+        {{k_rhs<false, false, 1, FAST>, k_rhs<false, false, 2, FAST>},
+         {k_rhs<false, true, 1, FAST>, k_rhs<false, true, 2, FAST>}},
+        {{k_rhs<true, false, 1, FAST>, k_rhs<true, false, 2, FAST>},
+         {k_rhs<true, true, 1, FAST>, k_rhs<true, true, 2, FAST>}}};
     return ks[d3 ? 1 : 0][sc ? 1 : 0][ds == 2 ? 1 : 0];
+}
+
+RhsKernel rhs_kernel(bool d3, bool sc, int ds, bool fast) {
+    return fast ? rhs_kernel_of<true>(d3, sc, ds) : rhs_kernel_of<false>(d3, sc, ds);
 }
 
 void launch_rhs(saras_rk3 *h, const Stage &sg) {
@@ -733,7 +888,9 @@ void launch_rhs(saras_rk3 *h, const Stage &sg) {
     f.tmpR = h->tmpR;
     f.nlT = h->nlT;
     const int bx = bxfor(h->L.n2);
-    rhs_kernel(h->d3, h->sc, h->ds)<<<cgrid(h->L, h->d3, bx), bx, 0, h->stream>>>(f, h->L, h->tabs, h->scal, sg);
+    rhs_kernel(h->d3, h->sc, h->ds, h->prm.stencil_form == SARAS_STENCIL_FAST)<<<cgrid(h->L, h->d3, bx), bx, 0,
+                                                                                   h->stream>>>(f, h->L, h->tabs,
+                                                                                                h->scal, sg);
     h->launches++;
 }
 
@@ -957,7 +1114,8 @@ saras_status check_params(const saras_grid_desc *gd, const saras_rk3_params *p) 
         return SARAS_BAD_ARG;
     }
     if (p->nl_scheme < 1 || p->nl_scheme > 3 || p->integration < 0 || p->integration > 2 || !(p->dt > 0.0) ||
-        !(p->nu >= 0.0) || !(p->kappa >= 0.0) || p->max_iterations < 0) {
+        !(p->nu >= 0.0) || !(p->kappa >= 0.0) || p->max_iterations < 0 ||
+        (p->stencil_form != SARAS_STENCIL_EXACT && p->stencil_form != SARAS_STENCIL_FAST)) {
         set_error("invalid time-step parameters");
         return SARAS_BAD_ARG;
     }
@@ -974,8 +1132,9 @@ saras_status rk3_configure(saras_rk3 *h, const saras_grid_desc *gd, const saras_
     h->sc = p->with_scalar != 0;
     h->ds = gd->pad;
     const HostGrid &g = h->grid;
-    // metric tables: xi_x, xixx, xix2, a2, a1, dh, dv, xc per axis over the core
-    constexpr int NT = 8;
+    // metric tables: xi_x, xixx, xix2, a2, a1, dh, dv, xc per axis over the
+    // core, and the FAST form's k1, k2a, k2b
+    constexpr int NT = RK_TABLES;
     const int n[3] = {h->L.n0, h->L.n1, h->L.n2};
     const int64_t tot = NT * (int64_t)(n[0] + n[1] + n[2]);
     std::vector<double> host((size_t)tot, 0.0);
@@ -999,6 +1158,9 @@ saras_status rk3_configure(saras_rk3 *h, const saras_grid_desc *gd, const saras_
         h->tabs.dh[d] = dst[5];
         h->tabs.dv[d] = dst[6];
         h->tabs.xc[d] = dst[7];
+        h->tabs.k1[d] = dst[8];
+        h->tabs.k2a[d] = dst[9];
+        h->tabs.k2b[d] = dst[10];
         for (int i = 0; i < n[d]; i++) {
             const size_t q = (size_t)(i + p0);
             const double v[NT] = {g.fxi_x[d][q],
@@ -1008,7 +1170,10 @@ saras_status rk3_configure(saras_rk3 *h, const saras_grid_desc *gd, const saras_
                                   h->scal.i2ht[d] * g.fxixx[d][q],
                                   g.fx[d][q + 1] - g.fx[d][q],
                                   g.dxi[d] / g.fxi_x[d][q],
-                                  g.fx[d][q]};
+                                  g.fx[d][q],
+                                  g.fxi_x[d][q] * (0.5 * ih),
+                                  g.fxixx[d][q] * (0.5 * ih),
+                                  g.fxix2[d][q] * h->scal.ih2d[d]};
             for (int qq = 0; qq < NT; qq++) host[(size_t)(off + (int64_t)qq * n[d] + i)] = v[qq];
         }
         off += NT * (int64_t)n[d];
@@ -1066,7 +1231,7 @@ saras_status rk3_create(const saras_grid_desc *gd, const saras_rk3_params *p, vo
     h->nfields = (int)h->allocs.size();
     for (double *q : h->allocs) SARAS_CUDA(cudaMemsetAsync(q, 0, (size_t)sz * sizeof(double), h->stream));
     const int n[3] = {h->L.n0, h->L.n1, h->L.n2};
-    SARAS_TRY(rk_alloc(h, &h->tab, 8 * (int64_t)(n[0] + n[1] + n[2])));
+    SARAS_TRY(rk_alloc(h, &h->tab, RK_TABLES * (int64_t)(n[0] + n[1] + n[2])));
     SARAS_TRY(rk3_configure(h, gd, p));
     const int64_t cells = (int64_t)n[0] * n[1] * n[2];
     h->nblocks = (int)std::max<int64_t>(1, std::min<int64_t>(1216, (cells + 255) / 256));

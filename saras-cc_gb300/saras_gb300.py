@@ -33,6 +33,8 @@ STATUS_NAMES = ["OK", "NOT_CONVERGED", "BAD_ARG", "OOM", "BUDGET", "TIMEOUT", "C
 MESH = {"U": 0, "S": 1, "D": 2}
 BC_NEUMANN, BC_DIRICHLET, BC_DIRICHLET_TEST = 0, 1, 2
 PREC_FP64_EXACT, PREC_FP64, PREC_MIXED = 0, 1, 2
+# time-step stencils: separately rounded in the reference's order, or FAST
+STENCIL_EXACT, STENCIL_FAST = 0, 1
 FBC_DIRICHLET, FBC_NEUMANN = 0, 1
 
 
@@ -61,7 +63,7 @@ class Rk3Params(C.Structure):
                 ("g_terms", C.c_double * 3), ("with_scalar", C.c_int32), ("nl_scheme", C.c_int32),
                 ("bc_vx", FieldBC), ("bc_vy", FieldBC), ("bc_vz", FieldBC), ("bc_t", FieldBC),
                 ("bc_p", FieldBC), ("mg", MgParams), ("pe_limit", C.c_double), ("up_param", C.c_double),
-                ("integration", C.c_int32), ("pad_", C.c_int32)]
+                ("integration", C.c_int32), ("stencil_form", C.c_int32)]
 
 
 class RunParams(C.Structure):
