@@ -274,9 +274,13 @@ class multigrid_d2 : public poisson {
 // lsRK3_d3 runs the low-storage RK3 (lsRK3_d3.cc:190-305), eulerCN_d3 the
 // Euler/Crank-Nicolson step (eulerCN_d3.cc:178-268); the differentiation and
 // non-linear schemes, "Peclet Limit" and "Central Bias" come from the parser.
+// stencil_form SARAS_STENCIL_FAST takes the time-step stencils with fused
+// multiply-adds (equal to the reference's arithmetic to rounding).
 class timeIntegrator {
   public:
-    timeIntegrator(const grid &mesh, const double &dt, int integration, int mg_precision) : mesh(mesh) {
+    timeIntegrator(const grid &mesh, const double &dt, int integration, int mg_precision,
+                   int stencil_form = SARAS_STENCIL_EXACT)
+        : mesh(mesh) {
         const parser &p = mesh.inputParams;
         saras_rk3_params r{};
         double fb = 1.0;
@@ -290,6 +294,7 @@ class timeIntegrator {
         r.pe_limit = p.peLimit;
         r.up_param = p.upParam;
         r.integration = integration;
+        r.stencil_form = stencil_form;
         for (int f = 0; f < 6; f++) {
             r.bc_vx.type[f] = r.bc_vy.type[f] = r.bc_vz.type[f] = SARAS_FBC_DIRICHLET;
             r.bc_p.type[f] = SARAS_FBC_NEUMANN;
@@ -328,14 +333,16 @@ class timeIntegrator {
 
 class lsRK3_d3 : public timeIntegrator {
   public:
-    lsRK3_d3(const grid &mesh, const double &dt, int mg_precision = SARAS_PREC_FP64_EXACT)
-        : timeIntegrator(mesh, dt, 2, mg_precision) {}
+    lsRK3_d3(const grid &mesh, const double &dt, int mg_precision = SARAS_PREC_FP64_EXACT,
+             int stencil_form = SARAS_STENCIL_EXACT)
+        : timeIntegrator(mesh, dt, 2, mg_precision, stencil_form) {}
 };
 
 class eulerCN_d3 : public timeIntegrator {
   public:
-    eulerCN_d3(const grid &mesh, const double &dt, int mg_precision = SARAS_PREC_FP64_EXACT)
-        : timeIntegrator(mesh, dt, 1, mg_precision) {}
+    eulerCN_d3(const grid &mesh, const double &dt, int mg_precision = SARAS_PREC_FP64_EXACT,
+               int stencil_form = SARAS_STENCIL_EXACT)
+        : timeIntegrator(mesh, dt, 1, mg_precision, stencil_form) {}
 };
 
 // lsRK3_d2 / eulerCN_d2: the same classes over a planar grid
