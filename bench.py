@@ -841,13 +841,20 @@ def c4_block(S, torch, n=256, steps=100, beta=1.3):
         finals[name] = f
     out["speedup_mixed_vs_fp64"] = out["fp64_ms_per_step"] / out["mixed_ms_per_step"]
     out["speedup_mixed_fast_vs_fp64"] = out["fp64_ms_per_step"] / out["mixed_fast_ms_per_step"]
-    # largest difference of each field after the run, relative to the
+    # largest difference of each field's core after the run, relative to the
     # field's largest magnitude: the FAST time-step stencils against the
     # separately rounded ones (both with the MIXED pressure solve), beside the
-    # MIXED pressure solve against the FP64 one (both separately rounded)
+    # MIXED pressure solve against the FP64 one (both separately rounded).
+    # The pressure is compared without its mean: the all-Neumann pressure
+    # problem leaves a constant that the forms fix differently.
     def rel(a, b):
-        return {k: float(np.abs(a[k] - b[k]).max() / max(np.abs(b[k]).max(), 1e-300))
-                for k in ("vx", "vy", "vz", "p", "t")}
+        out = {}
+        for k in ("vx", "vy", "vz", "p", "t"):
+            x, y = a[k][1:-1, 1:-1, 1:-1], b[k][1:-1, 1:-1, 1:-1]
+            if k == "p":
+                x, y = x - x.mean(), y - y.mean()
+            out[k] = float(np.abs(x - y).max() / max(np.abs(y).max(), 1e-300))
+        return out
     out["mixed_fast_vs_mixed_rel_diff"] = rel(finals["mixed_fast"], finals["mixed"])
     out["mixed_vs_fp64_rel_diff"] = rel(finals["mixed"], finals["fp64"])
     return out
