@@ -1260,7 +1260,9 @@ void residual_restrict(saras_mg *h, cudaStream_t s, int l, bool mixed) {
             // FP32: two coarse cells per thread
             const int pairs = Lc.n2 / 2, bx2 = std::min(pairs, 64), by2 = h->d3 ? std::max(1, 256 / bx2) : 1;
             const dim3 g2(cdiv(pairs, bx2), h->d3 ? cdiv(Lc.n1, by2) : 1u, (unsigned)Lc.n0);
-            if (h->d3)
+            if (h->d3 && tma_resid_restrict(h, s, f, c, tab32(f), wt32(c), z32)) {
+                // the large levels: planes through the TMA pipeline, the same bits
+            } else if (h->d3)
                 launch_pdl(f.rs ? k_resid_restrict4<true, true> : k_resid_restrict4<true, false>, g2, dim3(bx2, by2),
                            0, s, f.e32, f.r32, f.lay, tab32(f), b, wt32(c), c.r32, Lc, z32);
             else

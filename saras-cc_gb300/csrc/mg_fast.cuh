@@ -26,11 +26,18 @@ double kernel_bytes(const saras_mg *h, int kclass);
 void rhs_norm(saras_mg *h, cudaStream_t s);       // max|f| (or sums) of the solve, once
 void coarsest_fast(saras_mg *h, cudaStream_t s, Level &c);
 
+template <class T>
+struct Tab3;  // mg_stencil.cuh
+template <class T>
+struct WTab;
+
 // mg_tma.cu: TMA-staged FP32 colour sweep of the large 3-D levels
 void tma_plan(saras_mg *h, Level &v);
 bool tma_colour(saras_mg *h, cudaStream_t s, Level &v, int colour);
 bool tma_fused(saras_mg *h, cudaStream_t s, Level &v, bool to_b);
 bool fused_sweep_fits(const Lay &L, bool d3);
+bool tma_resid_restrict(saras_mg *h, cudaStream_t s, Level &f, Level &c, const Tab3<float> &t,
+                        const WTab<float> &w, float *z32);
 bool pair_sweep_fits(const Lay &L, bool d3);  // mg_fast.cu: levels of k_rbgs_pair
 
 // mg.cu: handle reuse by the serving engine

@@ -21,6 +21,8 @@ struct TmaPlan {
     int tj = 0, chunk = 0, ok = 0;
     CUtensorMap fa, fa2, fb, fb2, fr, fr1;
     int ftj = 0, fchunk = 0, fok = 0;
+    CUtensorMap rre, rre1, rrr;  // the TMA residual-restriction's e (tile, one row) and r
+    int rtj = 0, rchunk = 0, rok = 0;
 };
 
 // Per-level device state.  FP64 arrays serve the FP64_EXACT and FP64 forms

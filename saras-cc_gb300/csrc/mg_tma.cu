@@ -774,6 +774,277 @@ __global__ void __launch_bounds__(fu_threads<RS>(), 1)
     }
 }
 
+// ---- residual and restriction through the same kind of pipeline ----
+//
+// k_resid_restrict4's work on the large 3-D levels of the MIXED form, with
+// the fine planes streamed through shared memory.  A block owns a tile of tj
+// fine rows (tj/2 coarse rows) by the whole row and an even chunk of fine
+// planes.  A producer lane loads e planes (the tile and one halo row on each
+// side) and r planes (the tile) into rings of slots.  Each consumer thread
+// owns two coarse cells of one coarse row: on fine plane p it forms the
+// residuals of their eight children in that plane (two fine rows of four
+// cells, resid_row4's arithmetic on the slots) and their weighted sums over
+// k and j (restrict2's), and on the odd plane it combines the two planes'
+// sums and stores the coarse cells.  Each consumer warp releases a plane's
+// slots once its step no longer reads them; warps never wait for one
+// another.  The same bits as k_resid_restrict4, the row-split layout
+// included (a fine row of parity pr holds the cells of colour pr first).
+constexpr int RR_ESLOTS = 4, RR_RSLOTS = 3;
+constexpr int RR_WARPS = 8;
+constexpr int RR_THREADS = 32 * (RR_WARPS + 1);
+constexpr int RR_TILE = 2048;  // fine cells of a tile plane: tj = RR_TILE / n_z rows, 2 coarse cells a thread
+constexpr int RR_SX_MAX = 64;  // fine planes of a chunk at most (their x coefficients are staged)
+// head of the dynamic shared memory: mbarriers, then the chunk's x
+// coefficients (from byte 256) and the coarse planes' x weights
+constexpr size_t RR_HEAD = 2048;
+
+template <bool RS>
+__global__ void __launch_bounds__(RR_THREADS, 3) k_resid_restrict_tma(
+    const __grid_constant__ CUtensorMap eld, const __grid_constant__ CUtensorMap eld1,
+    const __grid_constant__ CUtensorMap rld, Lay Lf, Tab3<float> t, Bnd b, WTab<float> w, float *__restrict__ rc,
+    Lay Lc, float *__restrict__ ezero, int tj, int chunk, int *err, unsigned wlim) {
+    pdl_enter();
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ int s_fail;
+    const int n0 = Lf.n0, n1 = Lf.n1, n2 = Lf.n2;
+    const int e_slot = (tj + 2) * n2, r_slot = tj * n2;
+    uint64_t *efull = reinterpret_cast<uint64_t *>(smem), *eempty = efull + RR_ESLOTS;
+    uint64_t *rfull = eempty + RR_ESLOTS, *rempty = rfull + RR_RSLOTS;
+    float *sx = reinterpret_cast<float *>(smem + 256);  // cm, cp, dg of x for planes i0 .. i1-1
+    float *sw = sx + 3 * RR_SX_MAX;                     // w0, w1 of x for coarse planes i0/2 ..
+    float *es = reinterpret_cast<float *>(smem + RR_HEAD);
+    float *rs = es + RR_ESLOTS * e_slot;
+    const int j0 = (int)blockIdx.x * tj;
+    const int i0 = (int)blockIdx.y * chunk;  // even
+    const int i1 = min(n0, i0 + chunk);
+    if (i0 >= i1) return;
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < RR_ESLOTS; q++) {
+            mbar_init(&efull[q], 1);
+            mbar_init(&eempty[q], RR_WARPS);
+        }
+        for (int q = 0; q < RR_RSLOTS; q++) {
+            mbar_init(&rfull[q], 1);
+            mbar_init(&rempty[q], RR_WARPS);
+        }
+        mbar_init_fence();
+        s_fail = 0;
+    }
+    // the chunk's x coefficients and weights
+    const int nx = i1 - i0;
+    for (int x = threadIdx.x; x < nx; x += blockDim.x) {
+        sx[x] = t.cm[0][i0 + x];
+        sx[RR_SX_MAX + x] = t.cp[0][i0 + x];
+        sx[2 * RR_SX_MAX + x] = t.dg[0][i0 + x];
+        if ((x & 1) == 0) {
+            sw[x >> 1] = w.w0[0][(i0 + x) >> 1];
+            sw[RR_SX_MAX / 2 + (x >> 1)] = w.w1[0][(i0 + x) >> 1];
+        }
+    }
+    __syncthreads();
+    // e planes i0-1 .. i1 (plane P in slot (P - P0) % RR_ESLOTS) and r planes
+    // i0 .. i1-1 (plane Q in slot (Q - i0) % RR_RSLOTS); periodic axes wrap
+    // the halo planes and rows, at walls they are the ghost layer and never
+    // read (mirrors replace them)
+    const int P0 = i0 - 1;
+    auto pco = [&](int q) { return (b.per[0] ? wrap(q, n0) : q) + 1; };
+    auto rco = [&](int j) { return (b.per[1] ? wrap(j, n1) : j) + 1; };
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp == 0) {
+        if (lane == 0) {
+            const uint32_t eb = (uint32_t)(e_slot * sizeof(float)), rb = (uint32_t)(r_slot * sizeof(float));
+            int ne = 0, nr = 0;
+            bool fail = false;
+            for (int P = P0; P <= i1 && !fail; P++) {
+                const int u = P - P0, se = u % RR_ESLOTS;
+                if (u >= RR_ESLOTS && !mbar_wait(&eempty[se], (uint32_t)((u / RR_ESLOTS - 1) & 1), wlim)) {
+                    fail = true;
+                    break;
+                }
+                mbar_expect_tx(&efull[se], eb);
+                float *d = es + se * e_slot;
+                tma_load3(d, &eld1, &efull[se], KOFF, rco(j0 - 1), pco(P));
+                tma_load3(d + n2, &eld, &efull[se], KOFF, j0 + 1, pco(P));
+                tma_load3(d + (tj + 1) * n2, &eld1, &efull[se], KOFF, rco(j0 + tj), pco(P));
+                ne++;
+                const int Q = P - 1;  // r of plane Q goes with e of plane Q + 1
+                if (Q < i0 || Q >= i1) continue;
+                const int v = Q - i0, sr = v % RR_RSLOTS;
+                if (v >= RR_RSLOTS && !mbar_wait(&rempty[sr], (uint32_t)((v / RR_RSLOTS - 1) & 1), wlim)) {
+                    fail = true;
+                    break;
+                }
+                mbar_expect_tx(&rfull[sr], rb);
+                tma_load3(rs + sr * r_slot, &rld, &rfull[sr], KOFF, j0 + 1, pco(Q));
+                nr++;
+            }
+            if (fail) {
+                s_fail = 1;
+                atomicExch(err, 1);
+            }
+            // nothing may be in flight when the block exits
+            for (int x = max(0, ne - RR_ESLOTS); x < ne; x++)
+                mbar_wait(&efull[x % RR_ESLOTS], (uint32_t)((x / RR_ESLOTS) & 1));
+            for (int x = max(0, nr - RR_RSLOTS); x < nr; x++)
+                mbar_wait(&rfull[x % RR_RSLOTS], (uint32_t)((x / RR_RSLOTS) & 1));
+        }
+        return;
+    }
+    // ---- consumers: two coarse cells (kc0, kc0 + 1) of coarse row cj ----
+    const int ct = threadIdx.x - 32;
+    const int cpr = n2 >> 2;  // threads per coarse row
+    const int cjl = ct / cpr, kc0 = 2 * (ct % cpr), k0 = 2 * kc0;
+    const int jc = (j0 >> 1) + cjl;
+    const bool px = b.per[0] != 0, py = b.per[1] != 0;
+    const int H = n2 >> 1, h2 = k0 >> 1;
+    // per fine row bb: local row, wall flags, y coefficients, parity offset
+    int jl[2];
+    bool ylo[2], yhi[2];
+    float cmy[2], cpy[2], dgy[2];
+#pragma unroll
+    for (int bb = 0; bb < 2; bb++) {
+        jl[bb] = 2 * cjl + bb;
+        const int j = j0 + jl[bb];
+        ylo[bb] = !py && j == 0;
+        yhi[bb] = !py && j == n1 - 1;
+        cmy[bb] = t.cm[1][j];
+        cpy[bb] = t.cp[1][j];
+        dgy[bb] = t.dg[1][j];
+    }
+    float cmz[4], cpz[4], dgz[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        cmz[q] = t.cm[2][k0 + q];
+        cpz[q] = t.cp[2][k0 + q];
+        dgz[q] = t.dg[2][k0 + q];
+    }
+    const float w0z[2] = {w.w0[2][kc0], w.w0[2][kc0 + 1]}, w1z[2] = {w.w1[2][kc0], w.w1[2][kc0 + 1]};
+    const float w0y = w.w0[1][jc], w1y = w.w1[1][jc];
+    auto wait_e = [&](int p) {
+        const int u = p - P0;
+        if (!s_fail && !mbar_wait(&efull[u % RR_ESLOTS], (uint32_t)((u / RR_ESLOTS) & 1), wlim)) {
+            s_fail = 1;
+            atomicExch(err, 1);
+        }
+    };
+    auto wait_r = [&](int p) {
+        const int u = p - i0;
+        if (!s_fail && !mbar_wait(&rfull[u % RR_RSLOTS], (uint32_t)((u / RR_RSLOTS) & 1), wlim)) {
+            s_fail = 1;
+            atomicExch(err, 1);
+        }
+    };
+    // four cells k0 .. k0+3 of a row of parity par (RS: its two halves)
+    auto ld = [&](const float *row, int par, float (&o)[4]) {
+        if (!RS) {
+            const float4 v = lds4(row + k0);
+            o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+            return;
+        }
+        const float2 a = *reinterpret_cast<const float2 *>(row + h2);
+        const float2 c = *reinterpret_cast<const float2 *>(row + H + h2);
+        if (par == 0) {
+            o[0] = a.x; o[1] = c.x; o[2] = a.y; o[3] = c.y;
+        } else {
+            o[0] = c.x; o[1] = a.x; o[2] = c.y; o[3] = a.y;
+        }
+    };
+    wait_e(P0);
+    wait_e(P0 + 1);
+    float sy0[2] = {0.f, 0.f};
+    for (int p = i0; p < i1; p++) {
+        wait_e(p + 1);
+        wait_r(p);
+        const int ue = p - P0;
+        const float *pc = es + (ue % RR_ESLOTS) * e_slot;
+        const float *pm = es + ((ue + RR_ESLOTS - 1) % RR_ESLOTS) * e_slot;
+        const float *pp = es + ((ue + 1) % RR_ESLOTS) * e_slot;
+        const float *rr = rs + ((p - i0) % RR_RSLOTS) * r_slot;
+        const int xq = p - i0;
+        const float cmx = sx[xq], cpx = sx[RR_SX_MAX + xq], dgx = sx[2 * RR_SX_MAX + xq];
+        const bool xlo = !px && p == 0, xhi = !px && p == n0 - 1;
+        float sz[2][2];
+#pragma unroll
+        for (int bb = 0; bb < 2; bb++) {
+            const int j = j0 + jl[bb];
+            const int pr = (p + j) & 1;
+            const int off = (jl[bb] + 1) * n2;
+            const float *row = pc + off;
+            float cur[4], xm[4], xp[4], ym[4], yp[4], fr[4];
+            ld(row, pr, cur);
+            if (xlo) {
+#pragma unroll
+                for (int q = 0; q < 4; q++) xm[q] = b.sg_lo[0] > 0 ? cur[q] : -cur[q];
+            } else {
+                ld(pm + off, 1 - pr, xm);
+            }
+            if (xhi) {
+#pragma unroll
+                for (int q = 0; q < 4; q++) xp[q] = b.sg_hi[0] > 0 ? cur[q] : -cur[q];
+            } else {
+                ld(pp + off, 1 - pr, xp);
+            }
+            if (ylo[bb]) {
+#pragma unroll
+                for (int q = 0; q < 4; q++) ym[q] = b.sg_lo[1] > 0 ? cur[q] : -cur[q];
+            } else {
+                ld(row - n2, 1 - pr, ym);
+            }
+            if (yhi[bb]) {
+#pragma unroll
+                for (int q = 0; q < 4; q++) yp[q] = b.sg_hi[1] > 0 ? cur[q] : -cur[q];
+            } else {
+                ld(row + n2, 1 - pr, yp);
+            }
+            ld(rr + jl[bb] * n2, pr, fr);
+            // position of cell k of this row
+            auto at_k = [&](int k) { return RS ? (k >> 1) + ((pr + k) & 1) * H : k; };
+            const float left =
+                k0 > 0 ? row[at_k(k0 - 1)] : (b.per[2] ? row[at_k(n2 - 1)] : (b.sg_lo[2] > 0 ? cur[0] : -cur[0]));
+            const float right = k0 + 4 < n2 ? row[at_k(k0 + 4)]
+                                            : (b.per[2] ? row[at_k(0)] : (b.sg_hi[2] > 0 ? cur[3] : -cur[3]));
+            float r[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const float zm = q > 0 ? cur[q - 1] : left;
+                const float zp = q < 3 ? cur[q + 1] : right;
+                float sm = cmx * xm[q];
+                sm = fmat(cpx, xp[q], sm);
+                sm = fmat(cmy[bb], ym[q], sm);
+                sm = fmat(cpy[bb], yp[q], sm);
+                sm = fmat(cmz[q], zm, sm);
+                sm = fmat(cpz[q], zp, sm);
+                float d = dgx + dgz[q];
+                d += dgy[bb];
+                d = d + d;
+                r[q] = fr[q] - fmat(-d, cur[q], sm);
+            }
+#pragma unroll
+            for (int q = 0; q < 2; q++) sz[bb][q] = fmat(w1z[q], r[2 * q + 1], w0z[q] * r[2 * q]);
+        }
+        // this warp no longer reads e(p-1) and r(p)
+        __syncwarp();
+        if (lane == 0) {
+            mbar_arrive(&eempty[(ue + RR_ESLOTS - 1) % RR_ESLOTS]);
+            mbar_arrive(&rempty[(p - i0) % RR_RSLOTS]);
+        }
+        float sy[2];
+#pragma unroll
+        for (int q = 0; q < 2; q++) sy[q] = fmat(w1y, sz[1][q], w0y * sz[0][q]);
+        if (((p - i0) & 1) == 0) {
+            sy0[0] = sy[0];
+            sy0[1] = sy[1];
+        } else if (!s_fail) {
+            const int ic = p >> 1;
+            const float w0x = sw[xq >> 1], w1x = sw[RR_SX_MAX / 2 + (xq >> 1)];
+            const int64_t q = Lc.at(ic, jc, kc0);
+            *reinterpret_cast<float2 *>(rc + q) = make_float2(fmat(w1x, sy[0], w0x * sy0[0]),
+                                                               fmat(w1x, sy[1], w0x * sy0[1]));
+            if (ezero) *reinterpret_cast<float2 *>(ezero + q) = make_float2(0.f, 0.f);
+        }
+    }
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
     static bool tried = false;
@@ -870,6 +1141,45 @@ void fused_plan(Level &v, int sms) {
     m.fok = 1;
 }
 
+size_t rr_smem(int tj, int n2) {
+    return RR_HEAD + ((size_t)RR_ESLOTS * (tj + 2) + (size_t)RR_RSLOTS * tj) * n2 * sizeof(float);
+}
+
+// The TMA residual-restriction's plan for a fine level: tile rows, an even
+// plane chunk (all blocks resident in one wave) and three tensor maps.
+void rr_plan(Level &v, int sms) {
+    const Lay &L = v.lay;
+    const int tj = RR_TILE / L.n2;
+    TmaPlan &m = v.tma;
+    const size_t smem = rr_smem(tj, L.n2);
+    if (smem > 200 * 1024 || !encode3(&m.rre, v.e32, L, tj) || !encode3(&m.rre1, v.e32, L, 1) ||
+        !encode3(&m.rrr, v.r32, L, tj))
+        return;
+    if (cudaFuncSetAttribute(k_resid_restrict_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(k_resid_restrict_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    int per_sm = 0, per_sm_rs = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_resid_restrict_tma<false>, RR_THREADS, smem) !=
+            cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_rs, k_resid_restrict_tma<true>, RR_THREADS, smem) !=
+            cudaSuccess ||
+        per_sm < 1 || per_sm_rs < 1) {
+        cudaGetLastError();
+        return;
+    }
+    per_sm = std::min(per_sm, per_sm_rs);
+    const int nch = std::max(1, per_sm * sms / (L.n1 / tj));
+    int chunk = (L.n0 + nch - 1) / nch;
+    chunk = std::min(RR_SX_MAX, std::max(2, chunk + (chunk & 1)));
+    m.rtj = tj;
+    m.rchunk = chunk;
+    m.rok = 1;
+}
+
 }  // namespace
 
 // Levels that take the fused red-black iteration (and hold a second e
@@ -887,6 +1197,18 @@ bool fused_sweep_fits(const Lay &L, bool d3) {
     return L.n1 % tj == 0 && L.n0 >= 16 && (int64_t)L.n0 * L.n1 * L.n2 >= FU_MIN_CELLS;
 }
 
+// Levels that take the TMA residual-restriction: 3-D, at least
+// FU_MIN_CELLS cells, rows of 128 or 256 cells, even extents, tiles of
+// RR_TILE cells that divide the level's rows.
+bool rr_fits(const Lay &L, bool d3) {
+    if (!d3 || L.n2 < 128 || L.n2 > 256 || RR_TILE % L.n2 != 0) return false;
+    const int tj = RR_TILE / L.n2;
+    // one consumer thread per pair of coarse cells of the tile's coarse rows
+    if ((tj / 2) * (L.n2 / 4) != 32 * RR_WARPS) return false;
+    return (tj & 1) == 0 && L.n1 % tj == 0 && (L.n0 & 1) == 0 && L.n0 >= 4 &&
+           (int64_t)L.n0 * L.n1 * L.n2 >= FU_MIN_CELLS;
+}
+
 // Plans the TMA sweeps of one level: the fused iteration's (levels with a
 // second e buffer) and the colour sweep's tile rows, plane chunk and three
 // tensor maps (e with halo rows, e without, r).  Levels that do not qualify
@@ -900,6 +1222,8 @@ void tma_plan(saras_mg *h, Level &v) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (v.e32b && fused_sweep_fits(L, h->d3)) fused_plan(v, sms);
+    v.tma.rok = 0;
+    if (rr_fits(L, h->d3)) rr_plan(v, sms);
     // rows of 32..256 cells (a power of two); tiles of 2048 cells shared by
     // the consumer warps row-wise
     if (L.n2 < 32 || L.n2 > 256 || 1024 % L.n2 != 0 || (int64_t)L.n0 * L.n1 * L.n2 < (1 << 20)) return;
@@ -944,6 +1268,22 @@ bool tma_colour(saras_mg *h, cudaStream_t s, Level &v, int colour) {
 
 // One red-black iteration through the fused kernel, e32 -> e32b (to_b) or
 // e32b -> e32; false when the level has no fused plan.
+// The FP32 residual of fine level f restricted into coarse level c (not the
+// coarsest) through the TMA pipeline, the coarse error cleared when z32 is
+// given; false when the level has no plan.
+bool tma_resid_restrict(saras_mg *h, cudaStream_t s, Level &f, Level &c, const Tab3<float> &t,
+                        const WTab<float> &w, float *z32) {
+    if (!f.tma.rok) return false;
+    const Lay &L = f.lay;
+    const TmaPlan &m = f.tma;
+    const dim3 grid((unsigned)(L.n1 / m.rtj), (unsigned)((L.n0 + m.rchunk - 1) / m.rchunk));
+    int *err = reinterpret_cast<int *>(h->norm_out + 7);
+    launch_pdl(f.rs ? k_resid_restrict_tma<true> : k_resid_restrict_tma<false>, grid, dim3(RR_THREADS),
+               rr_smem(m.rtj, L.n2), s, m.rre, m.rre1, m.rrr, L, t, sweep_bnd(h), w, c.r32, c.lay, z32, m.rtj,
+               m.rchunk, err, tma_wait_limit(h));
+    return true;
+}
+
 bool tma_fused(saras_mg *h, cudaStream_t s, Level &v, bool to_b) {
     if (!v.tma.fok) return false;
     const Lay &L = v.lay;
