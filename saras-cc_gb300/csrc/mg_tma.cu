@@ -789,7 +789,7 @@ __global__ void __launch_bounds__(fu_threads<RS>(), 1)
 // slots once its step no longer reads them; warps never wait for one
 // another.  The same bits as k_resid_restrict4, the row-split layout
 // included (a fine row of parity pr holds the cells of colour pr first).
-constexpr int RR_ESLOTS = 4, RR_RSLOTS = 3;
+constexpr int RR_ESLOTS = 5, RR_RSLOTS = 4;
 constexpr int RR_WARPS = 8;
 constexpr int RR_THREADS = 32 * (RR_WARPS + 1);
 constexpr int RR_TILE = 2048;  // fine cells of a tile plane: tj = RR_TILE / n_z rows, 2 coarse cells a thread
@@ -799,7 +799,7 @@ constexpr int RR_SX_MAX = 64;  // fine planes of a chunk at most (their x coeffi
 constexpr size_t RR_HEAD = 2048;
 
 template <bool RS>
-__global__ void __launch_bounds__(RR_THREADS, 3) k_resid_restrict_tma(
+__global__ void __launch_bounds__(RR_THREADS, 2) k_resid_restrict_tma(
     const __grid_constant__ CUtensorMap eld, const __grid_constant__ CUtensorMap eld1,
     const __grid_constant__ CUtensorMap rld, Lay Lf, Tab3<float> t, Bnd b, WTab<float> w, float *__restrict__ rc,
     Lay Lc, float *__restrict__ ezero, int tj, int chunk, int *err, unsigned wlim) {
