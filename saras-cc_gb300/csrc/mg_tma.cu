@@ -22,6 +22,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "mg_fast.cuh"
 #include "mg_stencil.cuh"
@@ -920,85 +921,88 @@ __global__ void __launch_bounds__(RR_THREADS, 2) k_resid_restrict_tma(
     }
     const float w0z[2] = {w.w0[2][kc0], w.w0[2][kc0 + 1]}, w1z[2] = {w.w1[2][kc0], w.w1[2][kc0 + 1]};
     const float w0y = w.w0[1][jc], w1y = w.w1[1][jc];
-    auto wait_e = [&](int p) {
-        const int u = p - P0;
-        if (!s_fail && !mbar_wait(&efull[u % RR_ESLOTS], (uint32_t)((u / RR_ESLOTS) & 1), wlim)) {
+    // ring positions, advanced by one per plane: the slot and fill parity
+    // of the e plane the step reads as its centre and of the r plane
+    int se = 1, ne_ph = 0;  // e(i0) is fill 1 of slot 1 (e(i0-1) fill 0 of slot 0)
+    int sr = 0, nr_ph = 0;  // r(i0) is fill 0 of slot 0
+    auto wait_slot = [&](uint64_t *bar, int phase) {
+        if (!s_fail && !mbar_wait(bar, (uint32_t)(phase & 1), wlim)) {
             s_fail = 1;
             atomicExch(err, 1);
         }
     };
-    auto wait_r = [&](int p) {
-        const int u = p - i0;
-        if (!s_fail && !mbar_wait(&rfull[u % RR_RSLOTS], (uint32_t)((u / RR_RSLOTS) & 1), wlim)) {
-            s_fail = 1;
-            atomicExch(err, 1);
-        }
-    };
-    // four cells k0 .. k0+3 of a row of parity par (RS: its two halves)
-    auto ld = [&](const float *row, int par, float (&o)[4]) {
-        if (!RS) {
+    // four cells k0 .. k0+3 of a row of parity PAR (RS: its two halves)
+    auto ld = [&](const float *row, auto par_c, float (&o)[4]) {
+        if constexpr (!RS) {
             const float4 v = lds4(row + k0);
             o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
-            return;
-        }
-        const float2 a = *reinterpret_cast<const float2 *>(row + h2);
-        const float2 c = *reinterpret_cast<const float2 *>(row + H + h2);
-        if (par == 0) {
-            o[0] = a.x; o[1] = c.x; o[2] = a.y; o[3] = c.y;
         } else {
-            o[0] = c.x; o[1] = a.x; o[2] = c.y; o[3] = a.y;
+            const float2 a = *reinterpret_cast<const float2 *>(row + h2);
+            const float2 c = *reinterpret_cast<const float2 *>(row + H + h2);
+            if constexpr (decltype(par_c)::value == 0) {
+                o[0] = a.x; o[1] = c.x; o[2] = a.y; o[3] = c.y;
+            } else {
+                o[0] = c.x; o[1] = a.x; o[2] = c.y; o[3] = a.y;
+            }
         }
     };
-    wait_e(P0);
-    wait_e(P0 + 1);
+    // e(i0 - 1) and e(i0) before the first step
+    wait_slot(&efull[0], 0);
+    wait_slot(&efull[1], 0);
     float sy0[2] = {0.f, 0.f};
-    for (int p = i0; p < i1; p++) {
-        wait_e(p + 1);
-        wait_r(p);
-        const int ue = p - P0;
-        const float *pc = es + (ue % RR_ESLOTS) * e_slot;
-        const float *pm = es + ((ue + RR_ESLOTS - 1) % RR_ESLOTS) * e_slot;
-        const float *pp = es + ((ue + 1) % RR_ESLOTS) * e_slot;
-        const float *rr = rs + ((p - i0) % RR_RSLOTS) * r_slot;
+    // One fine plane p of parity A (the child index along x of its coarse
+    // plane): the residuals of the eight children in it, their weighted sums
+    // over k and j, and on A = 1 the coarse cells.  Fine row j of the tile has
+    // the parity of bb (j0 is even), so the row's colour parity is A ^ bb.
+    auto step = [&](int p, auto a_c) {
+        constexpr int A = decltype(a_c)::value;
+        const int sp = se == RR_ESLOTS - 1 ? 0 : se + 1, sm1 = se == 0 ? RR_ESLOTS - 1 : se - 1;
+        // e(p+1) is the fill after the centre's: the next slot, the same
+        // phase unless the ring wrapped
+        wait_slot(&efull[sp], sp == 0 ? ne_ph + 1 : ne_ph);
+        wait_slot(&rfull[sr], nr_ph);
+        const float *pc = es + se * e_slot, *pm = es + sm1 * e_slot, *pp = es + sp * e_slot;
+        const float *rr = rs + sr * r_slot;
         const int xq = p - i0;
         const float cmx = sx[xq], cpx = sx[RR_SX_MAX + xq], dgx = sx[2 * RR_SX_MAX + xq];
         const bool xlo = !px && p == 0, xhi = !px && p == n0 - 1;
         float sz[2][2];
-#pragma unroll
-        for (int bb = 0; bb < 2; bb++) {
-            const int j = j0 + jl[bb];
-            const int pr = (p + j) & 1;
-            const int off = (jl[bb] + 1) * n2;
+        auto row_sums = [&](auto bb_c) {
+            constexpr int BB = decltype(bb_c)::value;
+            constexpr int PR = A ^ BB;
+            const std::integral_constant<int, PR> own{};
+            const std::integral_constant<int, 1 - PR> oth{};
+            const int off = (jl[BB] + 1) * n2;
             const float *row = pc + off;
             float cur[4], xm[4], xp[4], ym[4], yp[4], fr[4];
-            ld(row, pr, cur);
+            ld(row, own, cur);
             if (xlo) {
 #pragma unroll
                 for (int q = 0; q < 4; q++) xm[q] = b.sg_lo[0] > 0 ? cur[q] : -cur[q];
             } else {
-                ld(pm + off, 1 - pr, xm);
+                ld(pm + off, oth, xm);
             }
             if (xhi) {
 #pragma unroll
                 for (int q = 0; q < 4; q++) xp[q] = b.sg_hi[0] > 0 ? cur[q] : -cur[q];
             } else {
-                ld(pp + off, 1 - pr, xp);
+                ld(pp + off, oth, xp);
             }
-            if (ylo[bb]) {
+            if (ylo[BB]) {
 #pragma unroll
                 for (int q = 0; q < 4; q++) ym[q] = b.sg_lo[1] > 0 ? cur[q] : -cur[q];
             } else {
-                ld(row - n2, 1 - pr, ym);
+                ld(row - n2, oth, ym);
             }
-            if (yhi[bb]) {
+            if (yhi[BB]) {
 #pragma unroll
                 for (int q = 0; q < 4; q++) yp[q] = b.sg_hi[1] > 0 ? cur[q] : -cur[q];
             } else {
-                ld(row + n2, 1 - pr, yp);
+                ld(row + n2, oth, yp);
             }
-            ld(rr + jl[bb] * n2, pr, fr);
+            ld(rr + jl[BB] * n2, own, fr);
             // position of cell k of this row
-            auto at_k = [&](int k) { return RS ? (k >> 1) + ((pr + k) & 1) * H : k; };
+            auto at_k = [&](int k) { return RS ? (k >> 1) + ((PR + k) & 1) * H : k; };
             const float left =
                 k0 > 0 ? row[at_k(k0 - 1)] : (b.per[2] ? row[at_k(n2 - 1)] : (b.sg_lo[2] > 0 ? cur[0] : -cur[0]));
             const float right = k0 + 4 < n2 ? row[at_k(k0 + 4)]
@@ -1010,38 +1014,51 @@ __global__ void __launch_bounds__(RR_THREADS, 2) k_resid_restrict_tma(
                 const float zp = q < 3 ? cur[q + 1] : right;
                 float sm = cmx * xm[q];
                 sm = fmat(cpx, xp[q], sm);
-                sm = fmat(cmy[bb], ym[q], sm);
-                sm = fmat(cpy[bb], yp[q], sm);
+                sm = fmat(cmy[BB], ym[q], sm);
+                sm = fmat(cpy[BB], yp[q], sm);
                 sm = fmat(cmz[q], zm, sm);
                 sm = fmat(cpz[q], zp, sm);
                 float d = dgx + dgz[q];
-                d += dgy[bb];
+                d += dgy[BB];
                 d = d + d;
                 r[q] = fr[q] - fmat(-d, cur[q], sm);
             }
 #pragma unroll
-            for (int q = 0; q < 2; q++) sz[bb][q] = fmat(w1z[q], r[2 * q + 1], w0z[q] * r[2 * q]);
-        }
+            for (int q = 0; q < 2; q++) sz[BB][q] = fmat(w1z[q], r[2 * q + 1], w0z[q] * r[2 * q]);
+        };
+        row_sums(std::integral_constant<int, 0>{});
+        row_sums(std::integral_constant<int, 1>{});
         // this warp no longer reads e(p-1) and r(p)
         __syncwarp();
         if (lane == 0) {
-            mbar_arrive(&eempty[(ue + RR_ESLOTS - 1) % RR_ESLOTS]);
-            mbar_arrive(&rempty[(p - i0) % RR_RSLOTS]);
+            mbar_arrive(&eempty[sm1]);
+            mbar_arrive(&rempty[sr]);
         }
+        se = sp;
+        if (sp == 0) ne_ph++;
+        sr = sr == RR_RSLOTS - 1 ? 0 : sr + 1;
+        if (sr == 0) nr_ph++;
         float sy[2];
 #pragma unroll
         for (int q = 0; q < 2; q++) sy[q] = fmat(w1y, sz[1][q], w0y * sz[0][q]);
-        if (((p - i0) & 1) == 0) {
+        if constexpr (A == 0) {
             sy0[0] = sy[0];
             sy0[1] = sy[1];
-        } else if (!s_fail) {
-            const int ic = p >> 1;
-            const float w0x = sw[xq >> 1], w1x = sw[RR_SX_MAX / 2 + (xq >> 1)];
-            const int64_t q = Lc.at(ic, jc, kc0);
-            *reinterpret_cast<float2 *>(rc + q) = make_float2(fmat(w1x, sy[0], w0x * sy0[0]),
-                                                               fmat(w1x, sy[1], w0x * sy0[1]));
-            if (ezero) *reinterpret_cast<float2 *>(ezero + q) = make_float2(0.f, 0.f);
+        } else {
+            if (!s_fail) {
+                const int ic = p >> 1;
+                const float w0x = sw[xq >> 1], w1x = sw[RR_SX_MAX / 2 + (xq >> 1)];
+                const int64_t q = Lc.at(ic, jc, kc0);
+                *reinterpret_cast<float2 *>(rc + q) =
+                    make_float2(fmat(w1x, sy[0], w0x * sy0[0]), fmat(w1x, sy[1], w0x * sy0[1]));
+                if (ezero) *reinterpret_cast<float2 *>(ezero + q) = make_float2(0.f, 0.f);
+            }
         }
+    };
+    // chunks are even and start on even planes
+    for (int p = i0; p < i1; p += 2) {
+        step(p, std::integral_constant<int, 0>{});
+        step(p + 1, std::integral_constant<int, 1>{});
     }
 }
 
