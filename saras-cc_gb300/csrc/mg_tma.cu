@@ -795,6 +795,7 @@ constexpr int RR_WARPS = 8;
 constexpr int RR_THREADS = 32 * (RR_WARPS + 1);
 constexpr int RR_TILE = 2048;  // fine cells of a tile plane: tj = RR_TILE / n_z rows, 2 coarse cells a thread
 constexpr int RR_SX_MAX = 64;  // fine planes of a chunk at most (their x coefficients are staged)
+constexpr int64_t RR_MIN_CELLS = int64_t(1) << 20;
 // head of the dynamic shared memory: mbarriers, then the chunk's x
 // coefficients (from byte 256) and the coarse planes' x weights
 constexpr size_t RR_HEAD = 2048;
@@ -1172,9 +1173,10 @@ void rr_plan(Level &v, int sms) {
     if (smem > 200 * 1024 || !encode3(&m.rre, v.e32, L, tj) || !encode3(&m.rre1, v.e32, L, 1) ||
         !encode3(&m.rrr, v.r32, L, tj))
         return;
-    if (cudaFuncSetAttribute(k_resid_restrict_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+    // one attribute for every level and handle: the largest ring any plan may use
+    if (cudaFuncSetAttribute(k_resid_restrict_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) !=
             cudaSuccess ||
-        cudaFuncSetAttribute(k_resid_restrict_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaFuncSetAttribute(k_resid_restrict_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) !=
             cudaSuccess) {
         cudaGetLastError();
         return;
@@ -1215,7 +1217,7 @@ bool fused_sweep_fits(const Lay &L, bool d3) {
 }
 
 // Levels that take the TMA residual-restriction: 3-D, at least
-// FU_MIN_CELLS cells, rows of 128 or 256 cells, even extents, tiles of
+// RR_MIN_CELLS cells, rows of 128 or 256 cells, even extents, tiles of
 // RR_TILE cells that divide the level's rows.
 bool rr_fits(const Lay &L, bool d3) {
     if (!d3 || L.n2 < 128 || L.n2 > 256 || RR_TILE % L.n2 != 0) return false;
@@ -1223,7 +1225,7 @@ bool rr_fits(const Lay &L, bool d3) {
     // one consumer thread per pair of coarse cells of the tile's coarse rows
     if ((tj / 2) * (L.n2 / 4) != 32 * RR_WARPS) return false;
     return (tj & 1) == 0 && L.n1 % tj == 0 && (L.n0 & 1) == 0 && L.n0 >= 4 &&
-           (int64_t)L.n0 * L.n1 * L.n2 >= FU_MIN_CELLS;
+           (int64_t)L.n0 * L.n1 * L.n2 >= RR_MIN_CELLS;
 }
 
 // Plans the TMA sweeps of one level: the fused iteration's (levels with a

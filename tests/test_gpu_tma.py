@@ -132,3 +132,25 @@ def test_bounded_wait_runs_out_and_handle_recovers(gk):
     assert fresh.mg_solve(ref, rhs) == S.OK
     assert np.array_equal(again, ref) and np.array_equal(hist, fresh.history)
     fresh.close()
+
+
+def test_handles_with_different_rings_interleave():
+    """Handles whose large levels use TMA rings of different sizes (rows of
+    256 and of 128 cells) solve interleaved: a plan made for one handle
+    leaves the other's launches valid, and each solve repeats its bits."""
+    ga = S.grid_desc(n=(128, 128, 256), length=(1.0, 1.0, 2.0), mesh="UUD", beta=(1, 1, 1.2), domain="NNN")
+    gb = S.grid_desc(n=(128, 128, 128), mesh="UUD", beta=(1, 1, 1.2), domain="NNN")
+    prm = S.mg_params(precision=S.PREC_MIXED, vc_count=100, vc_tolerance=1e-8, mg_tolerance=1e-6, pre_smooth=2,
+                      post_smooth=2, inner_cycles=-16)
+    ra, rb = random_rhs(ga, 51), random_rhs(gb, 52)
+    a = S.Multigrid(ga, prm)
+    first = S.padded_field(ga)
+    assert a.mg_solve(first, ra) == S.OK
+    b = S.Multigrid(gb, prm)
+    ub = S.padded_field(gb)
+    assert b.mg_solve(ub, rb) == S.OK
+    again = S.padded_field(ga)
+    assert a.mg_solve(again, ra) == S.OK
+    assert np.array_equal(first, again)
+    a.close()
+    b.close()
