@@ -267,10 +267,9 @@ def rel_err(a, b, singular=True):
 
 # FP64 instructions (add, multiply, fused multiply-add: one each) per cell
 # one colour launch of the FP64 form's finest sweep updates (k_rbgs_v8 with
-# the stored omega/D: one multiply and five fused multiply-adds for the
-# neighbour sum, the subtraction of f, then (1 - omega) u + (omega/D) s as a
-# multiply and a fused multiply-add)
-FP64_SWEEP_OPS_PER_CELL = 9
+# the stored omega/D and SOR parameter 1: six fused multiply-adds for the
+# neighbour sum minus f, then one multiply by omega/D)
+FP64_SWEEP_OPS_PER_CELL = 7
 
 
 def run_gb300(args):

@@ -67,7 +67,7 @@ __global__ void k_rbgs32(float *e, const float *__restrict__ r, Lay L, Tab3<floa
 // vectors, so many loads are in flight per thread, and only the four cells of
 // the sweep's colour are stored.  Used when n_z is a multiple of 8; the core
 // of every row starts on a 32-byte boundary (Lay).
-template <class T, bool D3, bool WD>
+template <class T, bool D3, bool WD, bool W1 = false>
 __global__ void k_rbgs_v8(T *u, const T *__restrict__ f, const T *__restrict__ wd, Lay L, Tab3<T> t, Bnd b,
                           int colour, T w, T omc) {
     pdl_enter();
@@ -75,7 +75,7 @@ __global__ void k_rbgs_v8(T *u, const T *__restrict__ f, const T *__restrict__ w
     const int j = D3 ? (int)(blockIdx.y * blockDim.y + threadIdx.y) : 0;
     const int i = blockIdx.z;
     if (k0 >= L.n2 || j >= L.n1) return;
-    rbgs_strip8<T, D3, WD>(u, f, wd, L, t, b, colour, w, omc, i, j, k0);
+    rbgs_strip8<T, D3, WD, W1>(u, f, wd, L, t, b, colour, w, omc, i, j, k0);
 }
 
 // Fused residual and restriction: one thread per coarse cell forms the
@@ -955,10 +955,14 @@ void colour_v8(saras_mg *h, cudaStream_t s, Level &v, T *u, const T *f, const T 
     const dim3 blk(bx, by);
     const dim3 g(cdiv(strips, bx), h->d3 ? cdiv(L.n1, by) : 1u, (unsigned)L.n0);
     const Bnd b = bnd(h);
+    // the stored-omega/D form skips the (1 - omega) u term when it is zero
+    const bool w1 = WD && h->prm.sor_param == 1.0;
     if (h->d3)
-        launch_pdl(k_rbgs_v8<T, true, WD>, g, blk, 0, s, u, f, wd, L, tb, b, colour, w, omc);
+        launch_pdl(w1 ? k_rbgs_v8<T, true, WD, true> : k_rbgs_v8<T, true, WD>, g, blk, 0, s, u, f, wd, L, tb, b,
+                   colour, w, omc);
     else
-        launch_pdl(k_rbgs_v8<T, false, WD>, g, blk, 0, s, u, f, wd, L, tb, b, colour, w, omc);
+        launch_pdl(w1 ? k_rbgs_v8<T, false, WD, true> : k_rbgs_v8<T, false, WD>, g, blk, 0, s, u, f, wd, L, tb, b,
+                   colour, w, omc);
 }
 
 void colour64(saras_mg *h, cudaStream_t s, int l, int colour) {

@@ -194,7 +194,12 @@ __device__ __forceinline__ void mirror8(const T (&cur)[8], int sg, T (&o)[8]) {
     for (int q = 0; q < 8; q++) o[q] = sg > 0 ? cur[q] : -cur[q];
 }
 
-template <class T, bool D3, bool WD, int T0>
+// WD (the FP64 form, omega/D stored per cell): f enters the neighbour sum's
+// chain as its first addend, and with W1 (SOR parameter 1) the (1 - omega) u
+// term, zero, is not formed: seven FP64 operations per cell instead of nine,
+// equal to the longer form to rounding.  Without WD (the FP32 sweeps, whose
+// bits the served and single solves share) the chain is unchanged.
+template <class T, bool D3, bool WD, int T0, bool W1 = false>
 __device__ __forceinline__ void strip_update(T *u, const T (&cur)[8], const T (&xm)[8], const T (&xp)[8],
                                              const T (&ym)[8], const T (&yp)[8], const T (&fr)[8], const T (&wv)[8],
                                              T left, T right, const Tab3<T> &t, int i, int j, int k0, int64_t c0, T w,
@@ -211,7 +216,7 @@ __device__ __forceinline__ void strip_update(T *u, const T (&cur)[8], const T (&
         const int k = k0 + q;
         const T zm = q > 0 ? cur[q - 1] : left;
         const T zp = q < 7 ? cur[q + 1] : right;
-        T sm = cmx * xm[q];
+        T sm = WD ? fmat(cmx, xm[q], -fr[q]) : cmx * xm[q];
         sm = fmat(cpx, xp[q], sm);
         if (D3) {
             sm = fmat(cmy, ym[q], sm);
@@ -219,10 +224,10 @@ __device__ __forceinline__ void strip_update(T *u, const T (&cur)[8], const T (&
         }
         sm = fmat(t.cm[2][k], zm, sm);
         sm = fmat(t.cp[2][k], zp, sm);
-        sm = sm - fr[q];
+        if (!WD) sm = sm - fr[q];
         T v;
         if (WD) {
-            v = fmat(sm, wv[q], omc * cur[q]);
+            v = W1 ? sm * wv[q] : fmat(sm, wv[q], omc * cur[q]);
         } else {
             T d = dx + t.dg[2][k];
             if (D3) d += dy;
@@ -263,7 +268,7 @@ __device__ __forceinline__ void ld4<double>(const double *__restrict__ p, double
 // One colour of the RBGS sweep on the 8-cell strip (i, j, k0 .. k0+7): the
 // strip and its neighbour rows as vectors, boundary ghosts folded in, only
 // the sweep's colour cells stored.
-template <class T, bool D3, bool WD>
+template <class T, bool D3, bool WD, bool W1 = false>
 __device__ __forceinline__ void rbgs_strip8(T *u, const T *__restrict__ f, const T *__restrict__ wd, const Lay &L,
                                             const Tab3<T> &t, const Bnd &b, int colour, T w, T omc, int i, int j,
                                             int k0) {
@@ -291,9 +296,9 @@ __device__ __forceinline__ void rbgs_strip8(T *u, const T *__restrict__ f, const
     const T right = k0 + 8 < L.n2 ? u[c0 + 8]
                                   : (b.per[2] ? u[c0 + 8 - L.n2] : (b.sg_hi[2] > 0 ? cur[7] : -cur[7]));
     if (((colour + i + j + k0) & 1) == 0)
-        strip_update<T, D3, WD, 0>(u, cur, xm, xp, ym, yp, fr, wv, left, right, t, i, j, k0, c0, w, omc);
+        strip_update<T, D3, WD, 0, W1>(u, cur, xm, xp, ym, yp, fr, wv, left, right, t, i, j, k0, c0, w, omc);
     else
-        strip_update<T, D3, WD, 1>(u, cur, xm, xp, ym, yp, fr, wv, left, right, t, i, j, k0, c0, w, omc);
+        strip_update<T, D3, WD, 1, W1>(u, cur, xm, xp, ym, yp, fr, wv, left, right, t, i, j, k0, c0, w, omc);
 }
 
 // Residuals of eight consecutive fine cells of one row (k_resid_restrict's
