@@ -78,6 +78,75 @@ __global__ void k_rbgs_v8(T *u, const T *__restrict__ f, const T *__restrict__ w
     rbgs_strip8<T, D3, WD, W1>(u, f, wd, L, t, b, colour, w, omc, i, j, k0);
 }
 
+// The FP64 form's colour sweep (omega/D stored per cell) on 4-cell strips:
+// strip_update's WD arithmetic cell for cell, with half of k_rbgs_v8's
+// registers per thread (8-cell FP64 strips take 128), so that twice the
+// warps hide the loads' latency.
+template <bool D3, bool W1>
+__global__ void __launch_bounds__(128, 8) k_rbgs_v4wd(double *u, const double *__restrict__ f,
+                                                   const double *__restrict__ wd, Lay L, Tab3<double> t, Bnd b,
+                                                   int colour, double omc) {
+    pdl_enter();
+    const int k0 = 4 * (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = D3 ? (int)(blockIdx.y * blockDim.y + threadIdx.y) : 0;
+    const int i = blockIdx.z;
+    if (k0 >= L.n2 || j >= L.n1) return;
+    const int64_t c0 = L.at(i, j, k0);
+    double cur[4], xm[4], xp[4], ym[4], yp[4], fr[4], wv[4];
+    auto ldu = [](const double *q, double (&o)[4]) {
+        const double2 a = *reinterpret_cast<const double2 *>(q);
+        const double2 c = *reinterpret_cast<const double2 *>(q + 2);
+        o[0] = a.x; o[1] = a.y; o[2] = c.x; o[3] = c.y;
+    };
+    auto mirror = [](const double (&c)[4], int sg, double (&o)[4]) {
+#pragma unroll
+        for (int q = 0; q < 4; q++) o[q] = sg > 0 ? c[q] : -c[q];
+    };
+    ldu(u + c0, cur);
+    if (i > 0) ldu(u + c0 - L.s0, xm);
+    else if (b.per[0]) ldu(u + c0 + (int64_t)(L.n0 - 1) * L.s0, xm);
+    else mirror(cur, b.sg_lo[0], xm);
+    if (i < L.n0 - 1) ldu(u + c0 + L.s0, xp);
+    else if (b.per[0]) ldu(u + c0 - (int64_t)(L.n0 - 1) * L.s0, xp);
+    else mirror(cur, b.sg_hi[0], xp);
+    if (D3) {
+        if (j > 0) ldu(u + c0 - L.s1, ym);
+        else if (b.per[1]) ldu(u + c0 + (int64_t)(L.n1 - 1) * L.s1, ym);
+        else mirror(cur, b.sg_lo[1], ym);
+        if (j < L.n1 - 1) ldu(u + c0 + L.s1, yp);
+        else if (b.per[1]) ldu(u + c0 - (int64_t)(L.n1 - 1) * L.s1, yp);
+        else mirror(cur, b.sg_hi[1], yp);
+    }
+    ld4(f + c0, fr);
+    ld4(wd + c0, wv);
+    const double left = k0 > 0 ? u[c0 - 1] : (b.per[2] ? u[c0 + L.n2 - 1] : (b.sg_lo[2] > 0 ? cur[0] : -cur[0]));
+    const double right =
+        k0 + 4 < L.n2 ? u[c0 + 4] : (b.per[2] ? u[c0 + 4 - L.n2] : (b.sg_hi[2] > 0 ? cur[3] : -cur[3]));
+    const double cmx = t.cm[0][i], cpx = t.cp[0][i];
+    double cmy = 0.0, cpy = 0.0;
+    if (D3) {
+        cmy = t.cm[1][j];
+        cpy = t.cp[1][j];
+    }
+    const int t0 = (colour + i + j + k0) & 1;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        if ((q & 1) != t0) continue;
+        const int k = k0 + q;
+        const double zm = q > 0 ? cur[q - 1] : left;
+        const double zp = q < 3 ? cur[q + 1] : right;
+        double sm = fmat(cmx, xm[q], -fr[q]);
+        sm = fmat(cpx, xp[q], sm);
+        if (D3) {
+            sm = fmat(cmy, ym[q], sm);
+            sm = fmat(cpy, yp[q], sm);
+        }
+        sm = fmat(t.cm[2][k], zm, sm);
+        sm = fmat(t.cp[2][k], zp, sm);
+        u[c0 + q] = W1 ? sm * wv[q] : fmat(sm, wv[q], omc * cur[q]);
+    }
+}
+
 // Fused residual and restriction: one thread per coarse cell forms the
 // residuals of its 2x2x2 children and their weighted sum (the coarsen
 // weights v_abc / vTot of poisson_d3.cc:494-508, factorised per axis).
@@ -968,6 +1037,22 @@ void colour_v8(saras_mg *h, cudaStream_t s, Level &v, T *u, const T *f, const T 
 void colour64(saras_mg *h, cudaStream_t s, int l, int colour) {
     Level &v = h->lv[(size_t)l];
     const Lay &L = v.lay;
+    if (L.n2 % 4 == 0 && L.n2 >= 16 && (int64_t)L.n0 * L.n1 * L.n2 >= (int64_t(1) << 20)) {
+        // the large levels: 4-cell strips, twice the resident warps
+        kbegin(h, s, l == 0 ? KC_SMOOTH0 : -1);
+        const int strips = L.n2 / 4, bx = std::min(strips, 64), by = h->d3 ? std::max(1, 128 / bx) : 1;
+        const dim3 g(cdiv(strips, bx), h->d3 ? cdiv(L.n1, by) : 1u, (unsigned)L.n0);
+        const bool w1 = h->prm.sor_param == 1.0;
+        const double omc = 1.0 - h->prm.sor_param;
+        if (h->d3)
+            launch_pdl(w1 ? k_rbgs_v4wd<true, true> : k_rbgs_v4wd<true, false>, g, dim3(bx, by), 0, s, v.lhs,
+                       (const double *)v.rhs, (const double *)v.inv_diag, L, tab64(v), bnd(h), colour, omc);
+        else
+            launch_pdl(w1 ? k_rbgs_v4wd<false, true> : k_rbgs_v4wd<false, false>, g, dim3(bx, by), 0, s, v.lhs,
+                       (const double *)v.rhs, (const double *)v.inv_diag, L, tab64(v), bnd(h), colour, omc);
+        kend(h, s, l == 0 ? KC_SMOOTH0 : -1);
+        return;
+    }
     if (v8_ok(L)) {
         kbegin(h, s, l == 0 ? KC_SMOOTH0 : -1);
         colour_v8<double, true>(h, s, v, v.lhs, v.rhs, v.inv_diag, tab64(v), colour, 0.0, 1.0 - h->prm.sor_param);
