@@ -232,6 +232,27 @@ __global__ void __launch_bounds__(256, 3) k_resid_restrict4(const float *__restr
     if (ezero) *reinterpret_cast<float2 *>(ezero + q) = make_float2(0.f, 0.f);  // the coarse error starts from zero
 }
 
+// The FP64 form's fused residual and restriction with the stored diagonal,
+// two coarse cells along k per thread: k_resid_restrict8's arithmetic
+// (restrict2 forms the same residuals and sums) at fewer registers.
+template <bool D3>
+__global__ void __launch_bounds__(128, 6) k_resid_restrict4d(const double *__restrict__ u,
+                                                          const double *__restrict__ f, Lay Lf, Tab3<double> t,
+                                                          Bnd b, WTab<double> w, double *__restrict__ rc, Lay Lc,
+                                                          const double *__restrict__ dd,
+                                                          double *__restrict__ ezero) {
+    pdl_enter();
+    const int kc0 = 2 * (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = D3 ? (int)(blockIdx.y * blockDim.y + threadIdx.y) : 0;
+    const int i = blockIdx.z;
+    if (kc0 >= Lc.n2 || j >= Lc.n1) return;
+    double out[2];
+    restrict2<double, D3>(u, f, Lf, t, b, w, dd, i, j, kc0, out);
+    const int64_t q = Lc.at(i, j, kc0);
+    *reinterpret_cast<double2 *>(rc + q) = make_double2(out[0], out[1]);
+    if (ezero) *reinterpret_cast<double2 *>(ezero + q) = make_double2(0.0, 0.0);
+}
+
 // Injection prolongation and correction in place: fine += coarse(i/2,..).
 template <class TF, class TC>
 __global__ void k_prolong_add(TF *__restrict__ f, const TC *__restrict__ c, Lay Lf, Lay Lc, int d3) {
@@ -1338,7 +1359,13 @@ void residual_restrict(saras_mg *h, cudaStream_t s, int l, bool mixed) {
         const int strips = Lc.n2 / 4, bx4 = std::min(strips, 32), by = h->d3 ? std::max(1, 128 / bx4) : 1;
         const dim3 g4(cdiv(strips, bx4), h->d3 ? cdiv(Lc.n1, by) : 1u, (unsigned)Lc.n0);
         const dim3 blk(bx4, by);
-        if (!mixed) {
+        if (!mixed && h->d3 && (int64_t)Lc.n0 * Lc.n1 * Lc.n2 >= (int64_t(1) << 17)) {
+            // the large levels: two coarse cells per thread
+            const int pairs = Lc.n2 / 2, bx2 = std::min(pairs, 64), by2 = std::max(1, 128 / bx2);
+            const dim3 g2(cdiv(pairs, bx2), cdiv(Lc.n1, by2), (unsigned)Lc.n0);
+            launch_pdl(k_resid_restrict4d<true>, g2, dim3(bx2, by2), 0, s, (const double *)f.lhs,
+                       (const double *)f.rhs, f.lay, tab64(f), b, wt64(c), c.rhs, Lc, (const double *)f.dd, z64);
+        } else if (!mixed) {
             if (h->d3)
                 launch_pdl(k_resid_restrict8<double, true>, g4, blk, 0, s, f.lhs, f.rhs, f.lay, tab64(f), b, wt64(c),
                            c.rhs, Lc, f.dd, z64);
