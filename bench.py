@@ -641,7 +641,9 @@ def run_serving(S, args, step_frac=None, n=None, rate=None):
                 outs[nxt] = step_fields.pop(nxt)
                 eng.submit_step(nxt, g, step_prm, outs[nxt])
             else:
-                outs[nxt] = S.padded_field(g)
+                # the caller's output box: a Poisson request solves from zero
+                # and writes the whole pad-1 box, so it need not be cleared
+                outs[nxt] = np.empty(S.padded_shape(g))
                 eng.submit(nxt, g, rhs, outs[nxt])
             nxt += 1
         t1 = time.perf_counter()

@@ -1091,8 +1091,10 @@ saras_status ensure_pin(saras_serve *h) {
         }
     }
     if (!h->copies) {
+        // every host core but the engine's thread and the step worker's
+        // (the pool runs only while the engine's thread waits for a copy)
         const unsigned hw = std::thread::hardware_concurrency();
-        h->copies.reset(new CopyPool((int)std::min(7u, std::max(1u, hw / 2) - 1)));
+        h->copies.reset(new CopyPool((int)std::min(30u, hw > 3 ? hw - 3 : 1u)));
     }
     return SARAS_OK;
 }

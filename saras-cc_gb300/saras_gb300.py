@@ -139,12 +139,17 @@ def field_bc(types, values) -> FieldBC:
     return b
 
 
-def padded_field(grid: GridDesc, dtype=np.float64) -> np.ndarray:
-    """Zero field with the reference's plainsf shape (core + pad on each side)."""
+def padded_shape(grid: GridDesc) -> tuple:
+    """The reference's plainsf shape of a field (core + pad on each side)."""
     p = grid.pad
     ny = 1 if grid.dims == 2 else grid.n[1]
     py = 1 if grid.dims == 2 else p
-    return np.zeros((grid.n[0] + 2 * p, ny + 2 * py, grid.n[2] + 2 * p), dtype=dtype)
+    return (grid.n[0] + 2 * p, ny + 2 * py, grid.n[2] + 2 * p)
+
+
+def padded_field(grid: GridDesc, dtype=np.float64) -> np.ndarray:
+    """Zero field with the reference's plainsf shape (core + pad on each side)."""
+    return np.zeros(padded_shape(grid), dtype=dtype)
 
 
 def field_origin(a: np.ndarray, grid: GridDesc):
@@ -537,8 +542,9 @@ class Serve:
         self._keep = {}
 
     def submit(self, rid: int, grid: GridDesc, rhs: np.ndarray, lhs: np.ndarray):
+        shape = padded_shape(grid)
         for a in (rhs, lhs):
-            if a.dtype != np.float64 or not a.flags.c_contiguous or a.shape != padded_field(grid).shape:
+            if a.dtype != np.float64 or not a.flags.c_contiguous or a.shape != shape:
                 raise ValueError("request fields must be C-contiguous float64 padded boxes of the grid")
         check(self.lib.saras_serve_submit(self.h, rid, C.byref(grid), C.c_void_p(rhs.ctypes.data),
                                           C.c_void_p(lhs.ctypes.data)), "saras_serve_submit")
@@ -547,7 +553,7 @@ class Serve:
     def submit_step(self, rid: int, grid: GridDesc, params: Rk3Params, fields: dict):
         """One time step of `fields` (vx, vy, vz, p, t, pp padded boxes,
         updated in place when the request is polled)."""
-        shape = padded_field(grid).shape
+        shape = padded_shape(grid)
         ptrs = []
         for k in ("vx", "vy", "vz", "p", "t", "pp"):
             a = fields.get(k)
