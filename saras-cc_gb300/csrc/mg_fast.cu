@@ -1613,6 +1613,7 @@ saras_status fast_setup(saras_mg *h) {
     {
         Level &v0 = h->lv[0];
         v0.rs = !h->no_rowsplit && h->prm.precision == SARAS_PREC_MIXED && h->d3 && v0.tma.fok &&
+                        fused_rowsplit_fits(v0.lay, h->d3) &&
                         h->prm.pre_smooth % 2 == 0 && h->prm.post_smooth % 2 == 0
                     ? 1
                     : 0;

@@ -36,6 +36,7 @@ void tma_plan(saras_mg *h, Level &v);
 bool tma_colour(saras_mg *h, cudaStream_t s, Level &v, int colour);
 bool tma_fused(saras_mg *h, cudaStream_t s, Level &v, bool to_b);
 bool fused_sweep_fits(const Lay &L, bool d3);
+bool fused_rowsplit_fits(const Lay &L, bool d3);
 bool tma_resid_restrict(saras_mg *h, cudaStream_t s, Level &f, Level &c, const Tab3<float> &t,
                         const WTab<float> &w, float *z32);
 bool pair_sweep_fits(const Lay &L, bool d3);  // mg_fast.cu: levels of k_rbgs_pair

@@ -92,6 +92,37 @@ __device__ __forceinline__ void tma_store3(const CUtensorMap *map, const void *s
                  "r"(x), "r"(y), "r"(z), "r"(sa(src))
                  : "memory");
 }
+__device__ __forceinline__ void tma_load4(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y, int z,
+                                          int w) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+        "%5}], [%6];" ::"r"(sa(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(w), "r"(sa(bar))
+        : "memory");
+}
+__device__ __forceinline__ void tma_store4(const CUtensorMap *map, const void *src, int x, int y, int z, int w) {
+    asm volatile("cp.async.bulk.tensor.4d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3, %4}], [%5];" ::"l"(
+                     reinterpret_cast<uint64_t>(map)),
+                 "r"(x), "r"(y), "r"(z), "r"(w), "r"(sa(src))
+                 : "memory");
+}
+// Whole rows of a level between global and shared memory: rows of up to 256
+// cells through a 3-D map (x = KOFF, the core's first cell); rows of 512
+// (split) through a 4-D map that views each row's core as two halves of 256
+// cells, box 256 x 2 x rows, which lands as rows of 512 contiguous cells.
+// y and z are the row and plane coordinates (ghost layer at 0).
+__device__ __forceinline__ void tma_rows(void *dst, const CUtensorMap *map, uint64_t *bar, int split, int y, int z) {
+    if (split)
+        tma_load4(dst, map, bar, 0, 0, y, z);
+    else
+        tma_load3(dst, map, bar, KOFF, y, z);
+}
+__device__ __forceinline__ void tma_rows_store(const CUtensorMap *map, const void *src, int split, int y, int z) {
+    if (split)
+        tma_store4(map, src, 0, 0, y, z);
+    else
+        tma_store3(map, src, KOFF, y, z);
+}
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait_read1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
@@ -338,11 +369,17 @@ __host__ __device__ constexpr int fu_threads() {
 constexpr int FU_ESLOTS = 6, FU_RSLOTS = 4;
 constexpr int FU_TILE = 4096;
 constexpr int64_t FU_MIN_CELLS = int64_t(1) << 22;
+// tile rows: FU_TILE cells, or four rows of 512 cells (the rings of 8-row
+// tiles would not fit the shared memory)
+__host__ __device__ constexpr int fu_tile_rows(int n2) { return n2 == 512 ? 4 : FU_TILE / n2; }
 // head of the dynamic shared memory: mbarriers, the tile's y coefficients
-// (from byte 256) and the chunk's x coefficients (from byte 1024, at most
-// FU_SX_MAX planes)
-constexpr size_t FU_HEAD = 4096;
-constexpr int FU_SX_MAX = 256;
+// (from byte 256) and the chunk's x coefficients (from byte 1024, chunk + 2
+// planes of three), rounded up to 1 KB and at least 4 KB
+__host__ __device__ constexpr size_t fu_head(int chunk) {
+    return ((1024 + 12 * (size_t)(chunk + 2) + 1023) / 1024 * 1024) > 4096
+               ? (1024 + 12 * (size_t)(chunk + 2) + 1023) / 1024 * 1024
+               : 4096;
+}
 
 template <int NT>
 __device__ __forceinline__ void consumer_sync() {
@@ -452,7 +489,7 @@ __global__ void __launch_bounds__(fu_threads<RS>(), 1)
     k_rbgs_fused(const __grid_constant__ CUtensorMap esrc, const __grid_constant__ CUtensorMap esrc2,
                  const __grid_constant__ CUtensorMap edst, const __grid_constant__ CUtensorMap rld,
                  const __grid_constant__ CUtensorMap rld1, Lay L, Tab3<float> t, Bnd b, float w, float omc, int tj,
-                 int chunk, int *err, unsigned wlim) {
+                 int chunk, int *err, unsigned wlim, int split) {
     constexpr int NT = fu_nt<RS>();
     pdl_enter();
     extern __shared__ __align__(128) unsigned char smem[];
@@ -463,7 +500,7 @@ __global__ void __launch_bounds__(fu_threads<RS>(), 1)
     uint64_t *rfull = eempty + FU_ESLOTS, *rempty = rfull + FU_RSLOTS;
     float *sy = reinterpret_cast<float *>(smem + 256);   // cm, cp, dg of y for rows j0-1 .. j0+tj
     float *sx = reinterpret_cast<float *>(smem + 1024);  // cm, cp, dg of x for planes i0-1 .. i1
-    float *es = reinterpret_cast<float *>(smem + FU_HEAD);
+    float *es = reinterpret_cast<float *>(smem + fu_head(chunk));
     float *rs = es + FU_ESLOTS * e_slot;
     const int j0 = (int)blockIdx.x * tj;
     const int i0 = (int)blockIdx.y * chunk;
@@ -505,9 +542,9 @@ __global__ void __launch_bounds__(fu_threads<RS>(), 1)
                 }
                 mbar_expect_tx(&efull[s], eb);
                 float *d = es + s * e_slot;
-                tma_load3(d, &esrc2, &efull[s], KOFF, rco(j0 - 2), pco(P));
-                tma_load3(d + 2 * n2, &esrc, &efull[s], KOFF, j0 + 1, pco(P));
-                tma_load3(d + (tj + 2) * n2, &esrc2, &efull[s], KOFF, rco(j0 + tj), pco(P));
+                tma_rows(d, &esrc2, &efull[s], split, rco(j0 - 2), pco(P));
+                tma_rows(d + 2 * n2, &esrc, &efull[s], split, j0 + 1, pco(P));
+                tma_rows(d + (tj + 2) * n2, &esrc2, &efull[s], split, rco(j0 + tj), pco(P));
                 ne++;
                 const int Q = P - 1;
                 if (Q < Q0 || Q > i1) continue;
@@ -518,9 +555,9 @@ __global__ void __launch_bounds__(fu_threads<RS>(), 1)
                 }
                 mbar_expect_tx(&rfull[sr], rb);
                 float *d2 = rs + sr * r_slot;
-                tma_load3(d2, &rld1, &rfull[sr], KOFF, rco(j0 - 1), pco(Q));
-                tma_load3(d2 + n2, &rld, &rfull[sr], KOFF, j0 + 1, pco(Q));
-                tma_load3(d2 + (tj + 1) * n2, &rld1, &rfull[sr], KOFF, rco(j0 + tj), pco(Q));
+                tma_rows(d2, &rld1, &rfull[sr], split, rco(j0 - 1), pco(Q));
+                tma_rows(d2 + n2, &rld, &rfull[sr], split, j0 + 1, pco(Q));
+                tma_rows(d2 + (tj + 1) * n2, &rld1, &rfull[sr], split, rco(j0 + tj), pco(Q));
                 nr++;
             }
             if (fail) {
@@ -596,7 +633,7 @@ __global__ void __launch_bounds__(fu_threads<RS>(), 1)
     auto store_release = [&](int q) {
         if (ct == 0 && !s_fail) {
             if (q - 2 >= i0) {
-                tma_store3(&edst, eptr(q - 2) + 2 * n2, KOFF, j0 + 1, q - 1);
+                tma_rows_store(&edst, eptr(q - 2) + 2 * n2, split, j0 + 1, q - 1);
                 bulk_commit();
             }
             if (q - 3 >= P0) {
@@ -768,7 +805,7 @@ __global__ void __launch_bounds__(fu_threads<RS>(), 1)
     consumer_sync<NT>();
     if (ct == 0) {
         if (!s_fail) {
-            tma_store3(&edst, eptr(i1 - 1) + 2 * n2, KOFF, j0 + 1, i1);
+            tma_rows_store(&edst, eptr(i1 - 1) + 2 * n2, split, j0 + 1, i1);
             bulk_commit();
         }
         bulk_wait_all();
@@ -804,7 +841,7 @@ template <bool RS>
 __global__ void __launch_bounds__(RR_THREADS, 2) k_resid_restrict_tma(
     const __grid_constant__ CUtensorMap eld, const __grid_constant__ CUtensorMap eld1,
     const __grid_constant__ CUtensorMap rld, Lay Lf, Tab3<float> t, Bnd b, WTab<float> w, float *__restrict__ rc,
-    Lay Lc, float *__restrict__ ezero, int tj, int chunk, int *err, unsigned wlim) {
+    Lay Lc, float *__restrict__ ezero, int tj, int chunk, int *err, unsigned wlim, int split) {
     pdl_enter();
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ int s_fail;
@@ -865,9 +902,9 @@ __global__ void __launch_bounds__(RR_THREADS, 2) k_resid_restrict_tma(
                 }
                 mbar_expect_tx(&efull[se], eb);
                 float *d = es + se * e_slot;
-                tma_load3(d, &eld1, &efull[se], KOFF, rco(j0 - 1), pco(P));
-                tma_load3(d + n2, &eld, &efull[se], KOFF, j0 + 1, pco(P));
-                tma_load3(d + (tj + 1) * n2, &eld1, &efull[se], KOFF, rco(j0 + tj), pco(P));
+                tma_rows(d, &eld1, &efull[se], split, rco(j0 - 1), pco(P));
+                tma_rows(d + n2, &eld, &efull[se], split, j0 + 1, pco(P));
+                tma_rows(d + (tj + 1) * n2, &eld1, &efull[se], split, rco(j0 + tj), pco(P));
                 ne++;
                 const int Q = P - 1;  // r of plane Q goes with e of plane Q + 1
                 if (Q < i0 || Q >= i1) continue;
@@ -877,7 +914,7 @@ __global__ void __launch_bounds__(RR_THREADS, 2) k_resid_restrict_tma(
                     break;
                 }
                 mbar_expect_tx(&rfull[sr], rb);
-                tma_load3(rs + sr * r_slot, &rld, &rfull[sr], KOFF, j0 + 1, pco(Q));
+                tma_rows(rs + sr * r_slot, &rld, &rfull[sr], split, j0 + 1, pco(Q));
                 nr++;
             }
             if (fail) {
@@ -1092,12 +1129,31 @@ bool encode3(CUtensorMap *m, const float *base, const Lay &L, int rows) {
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// Rows of `rows` of a level for tma_rows: encode3's map for rows of up to
+// 256 cells; for rows of 512, a 4-D map of the core viewed as two halves of
+// 256 cells (its base is the first core cell, 16-byte aligned: rows start
+// their core at KOFF on a 32-byte boundary, and a half is 1 KB).
+bool encode_rows(CUtensorMap *m, const float *base, const Lay &L, int rows) {
+    if (L.n2 <= 256) return encode3(m, base, L, rows);
+    if (L.n2 != 512) return false;
+    auto fn = encode_fn();
+    if (!fn) return false;
+    const cuuint64_t dim[4] = {256, 2, (cuuint64_t)L.n1 + 2, (cuuint64_t)L.n0 + 2};
+    const cuuint64_t stride[3] = {256 * sizeof(float), (cuuint64_t)L.s1 * sizeof(float),
+                                  (cuuint64_t)L.s0 * sizeof(float)};
+    const cuuint32_t box[4] = {256, 2, (cuuint32_t)rows, 1};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float *>(base + KOFF), dim, stride, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 size_t tma_smem(int tj, int n2) {
     return (size_t)TMA_SLOTS * ((size_t)(tj + 2) * n2 + (size_t)tj * n2) * sizeof(float) + 2 * TMA_SLOTS * 8;
 }
 
-size_t fused_smem(int tj, int n2) {
-    return FU_HEAD + ((size_t)FU_ESLOTS * (tj + 4) + (size_t)FU_RSLOTS * (tj + 2)) * n2 * sizeof(float);
+size_t fused_smem(int tj, int n2, int chunk) {
+    return fu_head(chunk) + ((size_t)FU_ESLOTS * (tj + 4) + (size_t)FU_RSLOTS * (tj + 2)) * n2 * sizeof(float);
 }
 
 Tab3<float> sweep_tab(const Level &v) {
@@ -1119,11 +1175,10 @@ Bnd sweep_bnd(const saras_mg *h) {
 // in one wave) and the six tensor maps.
 void fused_plan(Level &v, int sms) {
     const Lay &L = v.lay;
-    const int tj = FU_TILE / L.n2;
+    const int tj = fu_tile_rows(L.n2);
     TmaPlan &m = v.tma;
-    if (fused_smem(tj, L.n2) > 200 * 1024 || !encode3(&m.fa, v.e32, L, tj) || !encode3(&m.fa2, v.e32, L, 2) ||
-        !encode3(&m.fb, v.e32b, L, tj) || !encode3(&m.fb2, v.e32b, L, 2) || !encode3(&m.fr, v.r32, L, tj) ||
-        !encode3(&m.fr1, v.r32, L, 1))
+    if (!encode_rows(&m.fa, v.e32, L, tj) || !encode_rows(&m.fa2, v.e32, L, 2) || !encode_rows(&m.fb, v.e32b, L, tj) ||
+        !encode_rows(&m.fb2, v.e32b, L, 2) || !encode_rows(&m.fr, v.r32, L, tj) || !encode_rows(&m.fr1, v.r32, L, 1))
         return;
     if (cudaFuncSetAttribute(k_rbgs_fused<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) !=
             cudaSuccess ||
@@ -1135,25 +1190,27 @@ void fused_plan(Level &v, int sms) {
         return;
     }
     // the block must fit an SM (registers and shared memory) or the level
-    // keeps the colour sweeps
+    // keeps the colour sweeps; the occupancy is taken at the smallest head
+    const size_t smem0 = fused_smem(tj, L.n2, 0);
     int per_sm = 0, per_sm_rs = 0;
     int per_sm_w1 = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rbgs_fused<false, false>, fu_threads<false>(),
-                                                      fused_smem(tj, L.n2)) != cudaSuccess ||
+    if (smem0 > 200 * 1024 ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rbgs_fused<false, false>, fu_threads<false>(),
+                                                      smem0) != cudaSuccess ||
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_rs, k_rbgs_fused<true, false>, fu_threads<true>(),
-                                                      fused_smem(tj, L.n2)) != cudaSuccess ||
+                                                      smem0) != cudaSuccess ||
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_w1, k_rbgs_fused<true, true>, fu_threads<true>(),
-                                                      fused_smem(tj, L.n2)) != cudaSuccess ||
-        per_sm_w1 < 1 ||
-        per_sm < 1 || per_sm_rs < 1) {
+                                                      smem0) != cudaSuccess ||
+        per_sm_w1 < 1 || per_sm < 1 || per_sm_rs < 1) {
         cudaGetLastError();
         return;
     }
     per_sm = std::min(per_sm, per_sm_rs);
     // one wave: the chunks of every tile column fill the resident blocks
     const int nch = std::max(1, per_sm * sms / (L.n1 / tj));
-    // at most FU_SX_MAX planes of x coefficients per block (chunk + 2)
-    const int chunk = std::min(FU_SX_MAX - 2, std::max(8, (L.n0 + nch - 1) / nch));
+    const int chunk = std::max(8, (L.n0 + nch - 1) / nch);
+    // the chunk's x coefficients sit in the head: the ring must still fit
+    if (fused_smem(tj, L.n2, chunk) > 200 * 1024) return;
     m.ftj = tj;
     m.fchunk = chunk;
     m.fok = 1;
@@ -1170,8 +1227,8 @@ void rr_plan(Level &v, int sms) {
     const int tj = RR_TILE / L.n2;
     TmaPlan &m = v.tma;
     const size_t smem = rr_smem(tj, L.n2);
-    if (smem > 200 * 1024 || !encode3(&m.rre, v.e32, L, tj) || !encode3(&m.rre1, v.e32, L, 1) ||
-        !encode3(&m.rrr, v.r32, L, tj))
+    if (smem > 200 * 1024 || !encode_rows(&m.rre, v.e32, L, tj) || !encode_rows(&m.rre1, v.e32, L, 1) ||
+        !encode_rows(&m.rrr, v.r32, L, tj))
         return;
     // one attribute for every level and handle: the largest ring any plan may use
     if (cudaFuncSetAttribute(k_resid_restrict_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) !=
@@ -1202,25 +1259,32 @@ void rr_plan(Level &v, int sms) {
 }  // namespace
 
 // Levels that take the fused red-black iteration (and hold a second e
-// buffer for it): 3-D, rows of 128 or 256 cells, FU_TILE-cell tiles that
-// divide the level's rows, at least FU_MIN_CELLS cells.
+// buffer for it): 3-D, rows of 128, 256 or 512 cells, tiles of
+// fu_tile_rows rows that divide the level's rows, at least FU_MIN_CELLS
+// cells.
 bool fused_sweep_fits(const Lay &L, bool d3) {
     // every consumer thread owns one strip of each row it visits: strips of
-    // four cells of the row (plain layout) or of a row half (row-split)
-    if (!d3 || L.n2 < 128 || L.n2 > 256 || FU_TILE % L.n2 != 0 || fu_nt<false>() % (L.n2 / 4) != 0 ||
-        fu_nt<true>() % (L.n2 / 8) != 0)
+    // four cells of the row (plain layout)
+    if (!d3 || (L.n2 != 512 && (L.n2 < 128 || L.n2 > 256 || FU_TILE % L.n2 != 0)) ||
+        fu_nt<false>() % (L.n2 / 4) != 0)
         return false;
-    const int tj = FU_TILE / L.n2;
-    // the row-split consumers visit at most two rows of each colour phase
-    if (tj + 2 > 2 * (fu_nt<true>() / (L.n2 / 8))) return false;
+    const int tj = fu_tile_rows(L.n2);
     return L.n1 % tj == 0 && L.n0 >= 16 && (int64_t)L.n0 * L.n1 * L.n2 >= FU_MIN_CELLS;
+}
+
+// The row-split layout's fused iteration (strips of a row half): rows of up
+// to 256 cells.
+bool fused_rowsplit_fits(const Lay &L, bool d3) {
+    if (!fused_sweep_fits(L, d3) || L.n2 > 256 || fu_nt<true>() % (L.n2 / 8) != 0) return false;
+    // the row-split consumers visit at most two rows of each colour phase
+    return fu_tile_rows(L.n2) + 2 <= 2 * (fu_nt<true>() / (L.n2 / 8));
 }
 
 // Levels that take the TMA residual-restriction: 3-D, at least
 // RR_MIN_CELLS cells, rows of 128 or 256 cells, even extents, tiles of
 // RR_TILE cells that divide the level's rows.
 bool rr_fits(const Lay &L, bool d3) {
-    if (!d3 || L.n2 < 128 || L.n2 > 256 || RR_TILE % L.n2 != 0) return false;
+    if (!d3 || L.n2 < 128 || (L.n2 > 256 && L.n2 != 512) || RR_TILE % L.n2 != 0) return false;
     const int tj = RR_TILE / L.n2;
     // one consumer thread per pair of coarse cells of the tile's coarse rows
     if ((tj / 2) * (L.n2 / 4) != 32 * RR_WARPS) return false;
@@ -1299,7 +1363,7 @@ bool tma_resid_restrict(saras_mg *h, cudaStream_t s, Level &f, Level &c, const T
     int *err = reinterpret_cast<int *>(h->norm_out + 7);
     launch_pdl(f.rs ? k_resid_restrict_tma<true> : k_resid_restrict_tma<false>, grid, dim3(RR_THREADS),
                rr_smem(m.rtj, L.n2), s, m.rre, m.rre1, m.rrr, L, t, sweep_bnd(h), w, c.r32, c.lay, z32, m.rtj,
-               m.rchunk, err, tma_wait_limit(h));
+               m.rchunk, err, tma_wait_limit(h), L.n2 > 256 ? 1 : 0);
     return true;
 }
 
@@ -1313,9 +1377,10 @@ bool tma_fused(saras_mg *h, cudaStream_t s, Level &v, bool to_b) {
     // the row-split kernel skips the SOR blend when the parameter is 1
     const bool w1 = h->prm.sor_param == 1.0;
     launch_pdl(v.rs ? (w1 ? k_rbgs_fused<true, true> : k_rbgs_fused<true, false>) : k_rbgs_fused<false, false>, grid,
-               block, fused_smem(m.ftj, L.n2), s,
+               block, fused_smem(m.ftj, L.n2, m.fchunk), s,
                to_b ? m.fa : m.fb, to_b ? m.fa2 : m.fb2, to_b ? m.fb : m.fa, m.fr, m.fr1, L, sweep_tab(v), sweep_bnd(h),
-               (float)h->prm.sor_param, (float)(1.0 - h->prm.sor_param), m.ftj, m.fchunk, err, tma_wait_limit(h));
+               (float)h->prm.sor_param, (float)(1.0 - h->prm.sor_param), m.ftj, m.fchunk, err, tma_wait_limit(h),
+               L.n2 > 256 ? 1 : 0);
     return true;
 }
 

@@ -41,6 +41,13 @@ GRIDS = [
     # red cells, then its black cells) for the fused iteration
     ("rowsplit_128x128x256_ppp_2x2", dict(n=(128, 128, 256), length=(1.0, 1.0, 2.0), mesh="UUU", domain="PPP"),
      dict(mg_tolerance=1e-9, pre_smooth=2, post_smooth=2)),
+    # rows of 512 cells: the fused iteration and the residual-restriction
+    # load and store rows as two 256-cell halves (4-D tensor maps) on 4-row
+    # tiles; the plain layout whatever the smoothing counts
+    ("fused_64x128x512_uud", dict(n=(64, 128, 512), length=(0.125, 0.25, 1.0), mesh="UUD", beta=(1, 1, 1.2),
+                                  domain="NNN"), MG),
+    ("fused_64x128x512_ppp_2x2", dict(n=(64, 128, 512), length=(0.125, 0.25, 1.0), mesh="UUU", domain="PPP"),
+     dict(mg_tolerance=1e-9, pre_smooth=2, post_smooth=2)),
 ]
 DDD = dict(n=(128, 128, 256), length=(1.0, 1.0, 2.0), mesh="DDD", beta=(1.05, 1.05, 1.1), domain="NNN")
 
