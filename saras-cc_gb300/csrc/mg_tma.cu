@@ -132,7 +132,7 @@ __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.a
 // The colour cells of one 4-cell strip: k_rbgs_v8's strip_update (WD off),
 // cell for cell.  Lanes of a warp own consecutive strips, so each quarter
 // warp reads 128 contiguous bytes of shared memory per vector load.
-template <int T0>
+template <int T0, bool W1 = false>
 __device__ __forceinline__ void strip4(float *u, const float4 cur, const float4 xm, const float4 xp,
                                        const float4 ym, const float4 yp, const float4 fr, float left, float right,
                                        float cmx, float cpx, float dx, float cmy, float cpy, float dy,
@@ -154,7 +154,8 @@ __device__ __forceinline__ void strip4(float *u, const float4 cur, const float4 
         sm = sm - f[q];
         float d = dx + zc[2][q];
         d += dy;
-        u[q] = fmat(omc, c[q], sweep_div(w * sm, d + d));
+        // W1: the SOR parameter is 1 and the blend returns s/(2d) unchanged
+        u[q] = W1 ? sweep_div(sm, d + d) : fmat(omc, c[q], sweep_div(w * sm, d + d));
     }
 }
 
@@ -390,11 +391,11 @@ __device__ __forceinline__ int wrap(int a, int n) { return ((a % n) + n) % n; }
 // Colour cells of the strip at row[k0 .. k0+3] (a tile row of e in shared
 // memory); xmr / xpr: the same row on the planes below and above, rrow: the
 // row of r.  Mirrors at non-periodic walls as k_rbgs_tma forms them.
+template <int PAR, bool W1>
 __device__ __forceinline__ void fu_strip(float *row, const float *xmr, const float *xpr, const float *rrow, int n2,
-                                         int k0, bool xlo, bool xhi, bool ylo, bool yhi, const Bnd &b, int par,
-                                         int li, int ri, bool lneg, bool rneg, float cmx, float cpx, float dx,
-                                         float cmy, float cpy, float dy, const float (&zc)[3][4], float w,
-                                         float omc) {
+                                         int k0, bool xlo, bool xhi, bool ylo, bool yhi, const Bnd &b, int li, int ri,
+                                         bool lneg, bool rneg, float cmx, float cpx, float dx, float cmy, float cpy,
+                                         float dy, const float (&zc)[3][4], float w, float omc) {
     const float4 cur = lds4(row + k0);
     // the neighbour rows always exist in the slots (halo rows, ghost or
     // out-of-range planes), so they are loaded unconditionally and replaced
@@ -410,10 +411,7 @@ __device__ __forceinline__ void fu_strip(float *row, const float *xmr, const flo
     const float lv = row[li], rv = row[ri];
     const float left = lneg ? -lv : lv, right = rneg ? -rv : rv;
     float o[4] = {cur.x, cur.y, cur.z, cur.w};
-    if (par == 0)
-        strip4<0>(o, cur, xm, xp, ym, yp, fr, left, right, cmx, cpx, dx, cmy, cpy, dy, zc, w, omc);
-    else
-        strip4<1>(o, cur, xm, xp, ym, yp, fr, left, right, cmx, cpx, dx, cmy, cpy, dy, zc, w, omc);
+    strip4<PAR, W1>(o, cur, xm, xp, ym, yp, fr, left, right, cmx, cpx, dx, cmy, cpy, dy, zc, w, omc);
     *reinterpret_cast<float4 *>(row + k0) = make_float4(o[0], o[1], o[2], o[3]);
 }
 
@@ -757,26 +755,69 @@ __global__ void __launch_bounds__(fu_threads<RS>(), 1)
         const bool lneg = k0 == 0 && !b.per[2] && b.sg_lo[2] < 0;
         const int ri = k0 + 4 < n2 ? k0 + 4 : (b.per[2] ? 0 : k0 + 3);
         const bool rneg = k0 + 4 >= n2 && !b.per[2] && b.sg_hi[2] < 0;
+        // A thread visits the same rows on every plane (at most FU_PROWS of
+        // each colour phase), so their offsets, wall flags, y coefficients
+        // and row parities are formed once, and the ring slots advance by
+        // one per plane.
+        constexpr int FU_PROWS = 3;
+        int r_off[FU_PROWS], r_jp[FU_PROWS];
+        bool r_ok[FU_PROWS], r_lo[FU_PROWS], r_hi[FU_PROWS];
+        float r_cm[FU_PROWS], r_cp[FU_PROWS], r_dg[FU_PROWS];
+        int k_off[FU_PROWS], k_jp[FU_PROWS];
+        bool k_ok[FU_PROWS], k_lo[FU_PROWS], k_hi[FU_PROWS];
+        float k_cm[FU_PROWS], k_cp[FU_PROWS], k_dg[FU_PROWS];
+#pragma unroll
+        for (int v = 0; v < FU_PROWS; v++) {
+            const int x = ro + v * rstep;
+            const int j = j0 - 1 + x;
+            r_ok[v] = x < ny && (py || (j >= 0 && j < n1));
+            const int jw = r_ok[v] ? (py ? wrap(j, n1) : j) : 0;
+            const int xs = r_ok[v] ? x : 0;
+            r_off[v] = xs;
+            r_jp[v] = jw & 1;
+            r_lo[v] = !py && jw == 0;
+            r_hi[v] = !py && jw == n1 - 1;
+            r_cm[v] = sy[xs];
+            r_cp[v] = sy[ny + xs];
+            r_dg[v] = sy[2 * ny + xs];
+            k_ok[v] = x < tj;
+            const int xk = k_ok[v] ? x : 0;
+            const int jk = j0 + xk;
+            k_off[v] = xk;
+            k_jp[v] = jk & 1;
+            k_lo[v] = !py && jk == 0;
+            k_hi[v] = !py && jk == n1 - 1;
+            k_cm[v] = sy[xk + 1];
+            k_cp[v] = sy[ny + xk + 1];
+            k_dg[v] = sy[2 * ny + xk + 1];
+        }
+        int se = (i0 - 1 - P0) % FU_ESLOTS;  // slot of e plane q
+        int sr = 0;                          // slot of r plane q
+        int qi = px ? wrap(i0 - 1, n0) : i0 - 1;  // plane q in the level
         // every consumer thread runs every step and barrier, failed or not
         for (int q = i0 - 1; q <= i1; q++) {
             wait_e(q + 1);
             wait_r(q);
+            const int sm1 = se == 0 ? FU_ESLOTS - 1 : se - 1, sp1 = se == FU_ESLOTS - 1 ? 0 : se + 1;
+            const int sm2 = sm1 == 0 ? FU_ESLOTS - 1 : sm1 - 1, srm1 = sr == 0 ? FU_RSLOTS - 1 : sr - 1;
             if (px || (q >= 0 && q < n0)) {
-                // R(q)
-                const int qi = px ? wrap(q, n0) : q;
-                float *pc = eptr(q);
-                const float *pm = eptr(q - 1), *pp = eptr(q + 1), *rr = rptr(q);
+                // R(q): the first colour on the tile rows and the halo rows
+                float *pc = es + se * e_slot;
+                const float *pm = es + sm1 * e_slot, *pp = es + sp1 * e_slot, *rr = rs + sr * r_slot;
                 const int xq = q - (i0 - 1);
                 const float cmx = sx[xq], cpx = sx[nx + xq], dx = sx[2 * nx + xq];
                 const bool xlo = !px && qi == 0, xhi = !px && qi == n0 - 1;
-                for (int x = ro; x < ny; x += rstep) {
-                    const int j = j0 - 1 + x;
-                    if (!py && (j < 0 || j >= n1)) continue;
-                    const int jw = py ? wrap(j, n1) : j;
-                    const int off = (x + 1) * n2;
-                    fu_strip(pc + off, pm + off, pp + off, rr + x * n2, n2, k0, xlo, xhi, !py && jw == 0,
-                             !py && jw == n1 - 1, b, (qi + jw) & 1, li, ri, lneg, rneg, cmx, cpx, dx, sy[x],
-                             sy[ny + x], sy[2 * ny + x], zc[0], w, omc);
+#pragma unroll
+                for (int v = 0; v < FU_PROWS; v++) {
+                    if (!r_ok[v]) continue;
+                    const int off = (r_off[v] + 1) * n2;
+                    const float *rrow = rr + r_off[v] * n2;
+                    if (((qi + r_jp[v]) & 1) == 0)
+                        fu_strip<0, W1>(pc + off, pm + off, pp + off, rrow, n2, k0, xlo, xhi, r_lo[v], r_hi[v], b,
+                                        li, ri, lneg, rneg, cmx, cpx, dx, r_cm[v], r_cp[v], r_dg[v], zc[0], w, omc);
+                    else
+                        fu_strip<1, W1>(pc + off, pm + off, pp + off, rrow, n2, k0, xlo, xhi, r_lo[v], r_hi[v], b,
+                                        li, ri, lneg, rneg, cmx, cpx, dx, r_cm[v], r_cp[v], r_dg[v], zc[0], w, omc);
                 }
             }
             // this thread's writes (R(q), K(q-2)) before the async proxy reads them
@@ -785,20 +826,28 @@ __global__ void __launch_bounds__(fu_threads<RS>(), 1)
             store_release(q);
             const int p = q - 1;
             if (p >= i0) {
-                // K(p)
-                float *pc = eptr(p);
-                const float *pm = eptr(p - 1), *pp = eptr(p + 1), *rr = rptr(p);
+                // K(p): the second colour on the tile rows
+                float *pc = es + sm1 * e_slot;
+                const float *pm = es + sm2 * e_slot, *pp = es + se * e_slot, *rr = rs + srm1 * r_slot;
                 const int xp_ = p - (i0 - 1);
                 const float cmx = sx[xp_], cpx = sx[nx + xp_], dx = sx[2 * nx + xp_];
                 const bool xlo = !px && p == 0, xhi = !px && p == n0 - 1;
-                for (int x = ro; x < tj; x += rstep) {
-                    const int j = j0 + x;
-                    const int off = (x + 2) * n2;
-                    fu_strip(pc + off, pm + off, pp + off, rr + (x + 1) * n2, n2, k0, xlo, xhi, !py && j == 0,
-                             !py && j == n1 - 1, b, (1 + p + j) & 1, li, ri, lneg, rneg, cmx, cpx, dx, sy[x + 1],
-                             sy[ny + x + 1], sy[2 * ny + x + 1], zc[0], w, omc);
+#pragma unroll
+                for (int v = 0; v < FU_PROWS; v++) {
+                    if (!k_ok[v]) continue;
+                    const int off = (k_off[v] + 2) * n2;
+                    const float *rrow = rr + (k_off[v] + 1) * n2;
+                    if (((1 + p + k_jp[v]) & 1) == 0)
+                        fu_strip<0, W1>(pc + off, pm + off, pp + off, rrow, n2, k0, xlo, xhi, k_lo[v], k_hi[v], b,
+                                        li, ri, lneg, rneg, cmx, cpx, dx, k_cm[v], k_cp[v], k_dg[v], zc[0], w, omc);
+                    else
+                        fu_strip<1, W1>(pc + off, pm + off, pp + off, rrow, n2, k0, xlo, xhi, k_lo[v], k_hi[v], b,
+                                        li, ri, lneg, rneg, cmx, cpx, dx, k_cm[v], k_cp[v], k_dg[v], zc[0], w, omc);
                 }
             }
+            se = sp1;
+            sr = sr == FU_RSLOTS - 1 ? 0 : sr + 1;
+            qi = px ? (qi == n0 - 1 ? 0 : qi + 1) : qi + 1;
         }
     }
     fence_async_smem();
@@ -1182,6 +1231,8 @@ void fused_plan(Level &v, int sms) {
         return;
     if (cudaFuncSetAttribute(k_rbgs_fused<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) !=
             cudaSuccess ||
+        cudaFuncSetAttribute(k_rbgs_fused<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) !=
+            cudaSuccess ||
         cudaFuncSetAttribute(k_rbgs_fused<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) !=
             cudaSuccess ||
         cudaFuncSetAttribute(k_rbgs_fused<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) !=
@@ -1193,15 +1244,17 @@ void fused_plan(Level &v, int sms) {
     // keeps the colour sweeps; the occupancy is taken at the smallest head
     const size_t smem0 = fused_smem(tj, L.n2, 0);
     int per_sm = 0, per_sm_rs = 0;
-    int per_sm_w1 = 0;
+    int per_sm_w1 = 0, per_sm_pw1 = 0;
     if (smem0 > 200 * 1024 ||
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rbgs_fused<false, false>, fu_threads<false>(),
+                                                      smem0) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_pw1, k_rbgs_fused<false, true>, fu_threads<false>(),
                                                       smem0) != cudaSuccess ||
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_rs, k_rbgs_fused<true, false>, fu_threads<true>(),
                                                       smem0) != cudaSuccess ||
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_w1, k_rbgs_fused<true, true>, fu_threads<true>(),
                                                       smem0) != cudaSuccess ||
-        per_sm_w1 < 1 || per_sm < 1 || per_sm_rs < 1) {
+        per_sm_w1 < 1 || per_sm_pw1 < 1 || per_sm < 1 || per_sm_rs < 1) {
         cudaGetLastError();
         return;
     }
@@ -1269,6 +1322,8 @@ bool fused_sweep_fits(const Lay &L, bool d3) {
         fu_nt<false>() % (L.n2 / 4) != 0)
         return false;
     const int tj = fu_tile_rows(L.n2);
+    // the plain consumers visit at most three rows of each colour phase
+    if (tj + 2 > 3 * (fu_nt<false>() / (L.n2 / 4))) return false;
     return L.n1 % tj == 0 && L.n0 >= 16 && (int64_t)L.n0 * L.n1 * L.n2 >= FU_MIN_CELLS;
 }
 
@@ -1374,9 +1429,11 @@ bool tma_fused(saras_mg *h, cudaStream_t s, Level &v, bool to_b) {
     const dim3 grid((unsigned)(L.n1 / m.ftj), (unsigned)((L.n0 + m.fchunk - 1) / m.fchunk));
     int *err = reinterpret_cast<int *>(h->norm_out + 7);
     const dim3 block((unsigned)(v.rs ? fu_threads<true>() : fu_threads<false>()));
-    // the row-split kernel skips the SOR blend when the parameter is 1
+    // the kernels skip the SOR blend when the parameter is 1
     const bool w1 = h->prm.sor_param == 1.0;
-    launch_pdl(v.rs ? (w1 ? k_rbgs_fused<true, true> : k_rbgs_fused<true, false>) : k_rbgs_fused<false, false>, grid,
+    launch_pdl(v.rs ? (w1 ? k_rbgs_fused<true, true> : k_rbgs_fused<true, false>)
+                    : (w1 ? k_rbgs_fused<false, true> : k_rbgs_fused<false, false>),
+               grid,
                block, fused_smem(m.ftj, L.n2, m.fchunk), s,
                to_b ? m.fa : m.fb, to_b ? m.fa2 : m.fb2, to_b ? m.fb : m.fa, m.fr, m.fr1, L, sweep_tab(v), sweep_bnd(h),
                (float)h->prm.sor_param, (float)(1.0 - h->prm.sor_param), m.ftj, m.fchunk, err, tma_wait_limit(h),
