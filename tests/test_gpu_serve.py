@@ -203,3 +203,21 @@ def test_bad_arguments():
     with pytest.raises(S.SarasError):  # autotune wants an idle engine
         eng.autotune([g])
     eng.close()
+
+
+def test_cycle_cap_reports_not_converged(alone):
+    """A request that reaches the engine's outer-iteration cap above its
+    tolerance returns NOT_CONVERGED with its residual; the others in the
+    same batch finish as they would alone."""
+    reqs = {q: _request(gk, 10 + q) for q, gk in enumerate(CASES[:2])}
+    done, _ = _serve(reqs, params=_params(max_cycles=1))
+    for q in range(2):
+        assert done[q]["status"] == S.NOT_CONVERGED and done[q]["cycles"] == 1
+        assert done[q]["residual"] > TOL
+    # with room for every outer iteration the same requests converge, bit for
+    # bit as alone
+    reqs = {q: _request(gk, 10 + q) for q, gk in enumerate(CASES[:2])}
+    done, _ = _serve(reqs)
+    for q in range(2):
+        assert done[q]["status"] == S.OK
+        assert np.array_equal(reqs[q][2], alone[q][0])

@@ -145,3 +145,24 @@ def test_pooled_integrator_gives_same_results(alone):
     eng.close()
     for k in f0:
         assert np.array_equal(f0[k], alone[0][k]), k
+
+
+def test_failing_step_request_leaves_the_mix():
+    """A time-step request whose temperature holds a NaN fails in its first
+    Crank-Nicolson sweep, on the engine's step worker: it is polled with
+    status NAN, and a Poisson request served beside it keeps its alone
+    result."""
+    pois_alone = _serve([], [0])[1]
+    g, prm, f = _step_request(0)
+    f["t"][3, 3, 3] = np.nan
+    eng = S.Serve(S.serve_params(**ENGINE))
+    eng.submit_step(100, g, prm, f)
+    gp = S.grid_desc(**POISSON[0])
+    rhs, lhs = random_rhs(gp, 40), S.padded_field(gp)
+    eng.submit(0, gp, rhs, lhs)
+    done = {d["id"]: d for d in eng.run()}
+    st = eng.stats()
+    eng.close()
+    assert done[100]["status"] == S.NAN
+    assert done[0]["status"] == S.OK and np.array_equal(lhs, pois_alone[0])
+    assert st["active"] == 0 and st["retired"] == 2
