@@ -888,9 +888,8 @@ void launch_rhs(saras_rk3 *h, const Stage &sg) {
     f.tmpR = h->tmpR;
     f.nlT = h->nlT;
     const int bx = bxfor(h->L.n2);
-    rhs_kernel(h->d3, h->sc, h->ds, h->prm.stencil_form == SARAS_STENCIL_FAST)<<<cgrid(h->L, h->d3, bx), bx, 0,
-                                                                                   h->stream>>>(f, h->L, h->tabs,
-                                                                                                h->scal, sg);
+    const RhsKernel k = rhs_kernel(h->d3, h->sc, h->ds, h->prm.stencil_form == SARAS_STENCIL_FAST);
+    k<<<cgrid(h->L, h->d3, bx), bx, 0, h->stream>>>(f, h->L, h->tabs, h->scal, sg);
     h->launches++;
 }
 

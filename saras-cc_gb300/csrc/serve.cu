@@ -1442,8 +1442,11 @@ saras_status retire(saras_serve *h, size_t idx, int32_t status) {
 saras_status flush_finishing(saras_serve *h) {
     const auto t0 = Clock::now();
     saras_status st = SARAS_OK;
-    while (!h->finishing.empty() && st == SARAS_OK) {
+    while (!h->finishing.empty()) {
         st = retire_case(h, h->finishing.front().first, h->finishing.front().second);
+        // a retirement that failed has not released the case (its hierarchy,
+        // slot and items are released last): it stays for destroy to free
+        if (st != SARAS_OK) break;
         h->finishing.pop_front();
     }
     h->t_retire += std::chrono::duration<double>(Clock::now() - t0).count();
