@@ -152,3 +152,131 @@ def test_emulation_catches_a_wrong_phase():
     with pytest.raises(AssertionError):
         for seed in range(20):
             emulate(0, 20, warps=2, seed=seed, wrap_bug=True)
+
+
+# ---- the fused red-black iteration's ring (k_rbgs_fused) ----
+FU_ESLOTS, FU_RSLOTS = 6, 4
+
+
+def emulate_fused(i0, i1, seed, early_release=False):
+    """k_rbgs_fused's protocol: e planes i0-2 .. i1+1 and r planes i0-1 .. i1
+    through rings of 6 and 4 slots.  The consumers move in step (a block
+    barrier per plane step q): R(q) reads e(q-1..q+1) and r(q); after the
+    barrier one thread issues the TMA store of plane q-2, waits until the
+    store issued one step earlier (plane q-3) has read its slot, and releases
+    e(q-3) and r(q-2); then K(q-1) reads e(q-2..q) and r(q-1).  A store
+    reads its slot at an arbitrary later time."""
+    rng = random.Random(seed)
+    P0, Q0 = i0 - 2, i0 - 1
+    efull = [Barrier(1) for _ in range(FU_ESLOTS)]
+    eempty = [Barrier(1) for _ in range(FU_ESLOTS)]
+    rfull = [Barrier(1) for _ in range(FU_RSLOTS)]
+    rempty = [Barrier(1) for _ in range(FU_RSLOTS)]
+    etag = [None] * FU_ESLOTS
+    rtag = [None] * FU_RSLOTS
+    in_flight = []  # loads: (kind, slot, plane)
+    stores = []  # stores not done reading: (slot, plane)
+
+    def eslot(p):
+        return (p - P0) % FU_ESLOTS
+
+    def rslot(p):
+        return (p - Q0) % FU_RSLOTS
+
+    def producer():
+        for P in range(P0, i1 + 2):
+            u = P - P0
+            s = u % FU_ESLOTS
+            if u >= FU_ESLOTS:
+                k = u // FU_ESLOTS - 1
+                while not eempty[s].passes(k & 1, k):
+                    yield
+                assert all(slot != s for slot, _ in stores), "e slot refilled while a store reads it"
+            in_flight.append(("e", s, P))
+            Q = P - 1
+            if Q0 <= Q <= i1:
+                v = Q - Q0
+                sr = v % FU_RSLOTS
+                if v >= FU_RSLOTS:
+                    k = v // FU_RSLOTS - 1
+                    while not rempty[sr].passes(k & 1, k):
+                        yield
+                in_flight.append(("r", sr, Q))
+            yield
+
+    def wait(bars, p, base, n):
+        u = p - base
+        f = u // n
+        while not bars[u % n].passes(f & 1, f):
+            yield
+
+    def consumers():
+        yield from wait(efull, P0, P0, FU_ESLOTS)
+        yield from wait(efull, P0 + 1, P0, FU_ESLOTS)
+        for q in range(i0 - 1, i1 + 1):
+            yield from wait(efull, q + 1, P0, FU_ESLOTS)
+            yield from wait(rfull, q, Q0, FU_RSLOTS)
+            # R(q)
+            assert [etag[eslot(x)] for x in (q - 1, q, q + 1)] == [q - 1, q, q + 1] and rtag[rslot(q)] == q
+            yield
+            # barrier, then the store of plane q-2 and the releases
+            if q - 2 >= i0:
+                stores.append((eslot(q - 2), q - 2))
+            if q - 3 >= P0:
+                if q - 3 >= i0 and not early_release:
+                    while any(pl == q - 3 for _, pl in stores):  # cp.async.bulk.wait_group.read 1
+                        yield
+                eempty[eslot(q - 3)].arrive()
+            if q - 2 >= Q0:
+                rempty[rslot(q - 2)].arrive()
+            # K(q-1)
+            p = q - 1
+            if p >= i0:
+                assert [etag[eslot(x)] for x in (p - 1, p, p + 1)] == [p - 1, p, p + 1] and rtag[rslot(p)] == p
+            yield
+        # the last plane's store; the block waits for every store to finish
+        stores.append((eslot(i1 - 1), i1 - 1))
+        while stores:
+            yield
+
+    tasks = [producer(), consumers()]
+    alive = list(tasks)
+    steps = 0
+    while alive or in_flight or stores:
+        steps += 1
+        assert steps < 200000, "deadlock"
+        r = rng.random()
+        if in_flight and (not alive or r < 0.3):
+            kind, s, plane = in_flight.pop(rng.randrange(len(in_flight)))
+            if kind == "e":
+                etag[s] = plane
+                efull[s].arrive()
+            else:
+                rtag[s] = plane
+                rfull[s].arrive()
+            continue
+        if stores and r < 0.5:
+            slot, plane = stores.pop(rng.randrange(len(stores)))
+            assert etag[slot] == plane, "a store read a refilled slot"
+            continue
+        if not alive:
+            continue
+        t = rng.choice(alive)
+        try:
+            next(t)
+        except StopIteration:
+            alive.remove(t)
+
+
+@pytest.mark.parametrize("chunk", [1, 2, 3, 8, 29, 64])
+def test_fused_ring_protocol(chunk):
+    for seed in range(30):
+        emulate_fused(seed % 4, seed % 4 + chunk, seed=500 * chunk + seed)
+
+
+def test_fused_emulation_catches_an_early_release():
+    """The emulation itself: releasing e(q-3) without waiting for its store
+    to have read the slot lets the producer refill it under the store."""
+    with pytest.raises(AssertionError):
+        for seed in range(200):
+            emulate_fused(0, 29, seed=seed, early_release=True)
