@@ -344,7 +344,9 @@ def run_gb300(args):
     # host thread clears the other, used by the next step (the clearing
     # overlaps the solve, after the call's host-to-device copies of about
     # 1.3 ms, so that it does not share the host memory bandwidth with them;
-    # the thread is joined before the next call).
+    # the thread is joined before the next call).  A box the GPU has not
+    # copied to or from before costs about 13 ms more on its first call on
+    # this host, so one fresh box per step would time that instead.
     h_rhs = torch.from_numpy(rhs).pin_memory()
     h_np_rhs = h_rhs.numpy()
     h_lhs = [torch.zeros_like(h_rhs).pin_memory() for _ in range(2)]
@@ -366,6 +368,7 @@ def run_gb300(args):
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     clearer = None
+    call_ms = []
     ev0.record(stream)
     for q in range(args.steps):
         if clearer is not None:
@@ -374,7 +377,9 @@ def run_gb300(args):
         if q >= 1 and q + 1 < args.steps:
             clearer = threading.Thread(target=clear_after, args=(h_np_lhs[(q + 1) % 2], 0.01))
             clearer.start()
+        t_call = time.perf_counter()
         mix.mg_solve(h_np_lhs[q % 2], h_np_rhs)
+        call_ms.append((time.perf_counter() - t_call) * 1e3)
     ev1.record(stream)
     torch.cuda.synchronize()
     if clearer is not None:
@@ -481,6 +486,9 @@ def run_gb300(args):
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": 2 * field_bytes,
                 "d2h_bytes_per_step": field_bytes},
         "e2e_copies_ms": {k: v[1] for k, v in copy_stats.items()},
+        # wall time of each timed call (the rest of `e2e` is host time
+        # between calls)
+        "e2e_call_ms": {"min": min(call_ms), "median": float(np.median(call_ms)), "max": max(call_ms)},
         "e2e_copy_GBps": {k: v[0] * v[2] / v[1] / 1e6 if v[1] > 0 else None for k, v in copy_stats.items()},
         "gpu_launches": int(launches) * args.steps,
         "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": hbm,
