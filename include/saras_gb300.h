@@ -384,11 +384,11 @@ saras_status saras_serve_destroy(saras_serve *h);
  * device work.  It is for callers that cannot allocate at solve time:
  * cudaMalloc/cudaFree synchronise the whole device, a caching allocator may
  * already hold the free HBM, and a time step must not fail half-way for want
- * of memory.  The first call on a device does the set-up (it looks up the
- * scratch's address with that device current); make that first call before
- * any stream capture.  The looked-up address is kept for the life of the
- * process, so the entry point must not be used again on a device after
- * cudaDeviceReset.  Nothing in the scratch has to start at zero.  The call
+ * of memory.  Every call looks up the scratch's address on the current
+ * device, so the entry point stays usable after a cudaDeviceReset; the first
+ * lookup on a device loads the library's module there, so make the first
+ * call before any stream capture.  Nothing in the scratch has to start at
+ * zero.  The call
  * returns once its work on `stream` has finished (it synchronises the
  * stream), so a later call on any stream finds the scratch free.  Every call
  * on a device uses the same scratch, so calls that overlap in time (from

@@ -6,7 +6,6 @@
 // a time step must not fail half-way for want of memory.  The scratch is a
 // static __device__ array of SARAS_STATIC_SCRATCH_BYTES; grids whose
 // hierarchy does not fit are rejected before any device work.
-#include <mutex>
 
 #include "mg_fast.cuh"
 
@@ -20,10 +19,6 @@ namespace {
 
 constexpr size_t kScratchBytes = SARAS_STATIC_SCRATCH_BYTES;
 static __device__ __align__(256) double g_scratch[kScratchBytes / sizeof(double)];
-
-constexpr int kMaxDevices = 64;
-char *g_scratch_ptr[kMaxDevices] = {};  // device address of g_scratch, per device
-std::mutex g_setup;
 
 }  // namespace
 
@@ -42,22 +37,12 @@ extern "C" saras_status saras_mg_solve_static(const saras_grid_desc *grid, const
         saras::set_error("no CUDA device");
         return SARAS_NO_DEVICE;
     }
-    if (dev < 0 || dev >= kMaxDevices) {
-        saras::set_error("device ordinal %d above the static-scratch table", dev);
-        return SARAS_BAD_ARG;
-    }
-    char *base = nullptr;
-    {
-        // set-up, once per device, with that device current
-        std::lock_guard<std::mutex> lock(g_setup);
-        if (!g_scratch_ptr[dev]) {
-            void *p = nullptr;
-            e = cudaGetSymbolAddress(&p, g_scratch);
-            if (e != cudaSuccess) return saras::cuda_fail(e, "cudaGetSymbolAddress", __FILE__, __LINE__);
-            g_scratch_ptr[dev] = static_cast<char *>(p);
-        }
-        base = g_scratch_ptr[dev];
-    }
-    return saras::mg_solve_in_scratch(grid, prm, (cudaStream_t)stream, base, kScratchBytes, lhs, rhs, strides,
-                                      res_hist, hist_cap, n_cycles);
+    // the array's device address on the current device, looked up on every
+    // call (a cudaDeviceReset loads the module again at another address;
+    // the lookup costs microseconds against a solve)
+    void *base = nullptr;
+    e = cudaGetSymbolAddress(&base, g_scratch);
+    if (e != cudaSuccess) return saras::cuda_fail(e, "cudaGetSymbolAddress", __FILE__, __LINE__);
+    return saras::mg_solve_in_scratch(grid, prm, (cudaStream_t)stream, static_cast<char *>(base), kScratchBytes,
+                                      lhs, rhs, strides, res_hist, hist_cap, n_cycles);
 }
