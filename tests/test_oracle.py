@@ -8,8 +8,11 @@ analytic solution must fall at second order (poisson.cc:132-176),
 (2) the 2D manufactured solution cos(2 pi x) cos(2 pi z) -> -f/(8 pi^2),
 (3) the tanh-grid formulas of grid::createTanHypGrid evaluated independently
 in numpy (grid.cc:442-463), and (4) the V-cycle depths setVCDepth gives
-(grid.cc:678-742), and (5) committed fixtures of small solves
-(tests/golden/, made by tests/golden/make_golden.py).
+(grid.cc:678-742), (5) committed fixtures of small solves
+(tests/golden/, made by tests/golden/make_golden.py), and (6) 3-D
+manufactured solutions on the benchmark meshes (z tanh-stretched with
+Neumann walls; stretched on every axis with Dirichlet z walls), recovered at
+second order.
 """
 import json
 import math
@@ -152,6 +155,56 @@ def test_2d_cos_manufactured_second_order():
         ex = -f / (8 * np.pi ** 2)
         errs.append(np.abs((u - u.mean()) - (ex - ex.mean())).max())
     assert 3.5 < errs[0] / errs[1] < 4.5, errs
+
+
+def _manufactured_3d(n, mesh, beta, domain, bc_kind, exact, lap):
+    """Solves A u = lap(exact) at the cell centres of a 3-D grid; returns the
+    deviation from `exact` over the core (the constant removed where the
+    operator is singular)."""
+    g = S.grid_desc(n=(n, n, n), mesh=mesh, beta=beta, domain=domain)
+    xs = [O.field_metrics(g, d)[0] for d in range(3)]
+    x, y, z = xs[0][:, None, None], xs[1][None, :, None], xs[2][None, None, :]
+    ex = exact(x, y, z)
+    core = (slice(1, -1),) * 3
+    rhs = S.padded_field(g)
+    singular = all(k == 0 for k in bc_kind)
+    f = lap(x, y, z)[core]
+    # an all-Neumann operator wants a compatible right-hand side (its
+    # component along the discrete left null vector removed)
+    rhs[core] = O.project_compatible(g, f) if singular else f
+    lhs = S.padded_field(g)
+    prm = S.mg_params(vc_count=200, vc_tolerance=1e-10, pre_smooth=3, post_smooth=6, mg_tolerance=1e-12,
+                      bc_kind=bc_kind)
+    r = O.mg_solve(g, prm, lhs, rhs)
+    assert r.status == 0 and r.cycles < 40
+    d = (lhs - ex)[core]
+    return np.abs(d - d.mean()).max() if singular else np.abs(d).max()
+
+
+def test_benchmark_mesh_manufactured_second_order():
+    """The operator of the 256^3 benchmark's mesh (z tanh-stretched, beta 1.3,
+    Neumann walls) converges to the Laplacian: cos(pi x) cos(pi y) cos(pi z)
+    is recovered with a deviation falling by 4 per halving of h."""
+    pi = math.pi
+    errs = [_manufactured_3d(n, "UUD", (1, 1, 1.3), "NNN", [0] * 6,
+                             lambda x, y, z: np.cos(pi * x) * np.cos(pi * y) * np.cos(pi * z),
+                             lambda x, y, z: -3 * pi ** 2 * np.cos(pi * x) * np.cos(pi * y) * np.cos(pi * z))
+            for n in (16, 32, 64)]
+    for a, b in zip(errs, errs[1:]):
+        assert 3.7 < a / b < 4.3, errs
+
+
+def test_dirichlet_stretched_mesh_manufactured_second_order():
+    """The 512^3 configuration's mesh (tanh-stretched on every axis, beta 1.2,
+    periodic x and y, homogeneous Dirichlet walls in z through the boundary
+    selector): cos(2 pi x) cos(2 pi y) sin(pi z) at second order."""
+    pi = math.pi
+    errs = [_manufactured_3d(n, "DDD", (1.2, 1.2, 1.2), "PPN", [0, 0, 0, 0, 1, 1],
+                             lambda x, y, z: np.cos(2 * pi * x) * np.cos(2 * pi * y) * np.sin(pi * z),
+                             lambda x, y, z: -9 * pi ** 2 * np.cos(2 * pi * x) * np.cos(2 * pi * y) * np.sin(pi * z))
+            for n in (16, 32, 64)]
+    for a, b in zip(errs, errs[1:]):
+        assert 3.5 < a / b < 4.3, errs
 
 
 def test_oracle_thread_count_invariant():
