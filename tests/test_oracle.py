@@ -7,7 +7,7 @@ and analytic r^2/6 Dirichlet walls on a 'DDD' grid, whose deviation from the
 analytic solution must fall at second order (poisson.cc:132-176),
 (2) the 2D manufactured solution cos(2 pi x) cos(2 pi z) -> -f/(8 pi^2),
 (3) the tanh-grid formulas of grid::createTanHypGrid evaluated independently
-in numpy (grid.cc:442-463), and (4) the V-cycle depths setVCDepth gives
+in numpy (grid.cc:442-463), (4) the V-cycle depths setVCDepth gives
 (grid.cc:678-742), (5) committed fixtures of small solves
 (tests/golden/, made by tests/golden/make_golden.py), and (6) 3-D
 manufactured solutions on the benchmark meshes (z tanh-stretched with
