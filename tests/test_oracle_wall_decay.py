@@ -20,6 +20,10 @@ nu = 1e-2, kappa = 2e-2, Fb = 1:
 * dScheme 2 on the uniform mesh: second order too (its first and last core
   cells take the second-order forms), with about half dScheme 1's
   deviation; max |w| stays below 1e-6;
+* a moving top wall (u = 1 there, the lid of the reference's lid-driven
+  cavity): u = z + sin(pi z) exp(-nu pi^2 t) is exact, and so is the linear
+  Couette profile on the grid, so the deviation equals the fixed wall's to
+  rounding, and the top ghost is 2 - u at the last core cell;
 * tanh-stretched mesh (double-sided, beta 1.3): the reference places the
   ghost coordinates and metrics by copying from the other end of the axis
   (grid.cc:467-477), so the left ghost sits at -z_1 and carries the right
@@ -110,3 +114,37 @@ def test_wall_decay_dscheme2():
             assert 3.5 < a / b < 4.5, errs
     assert runs[1][0] < 0.6 * wall_decay(32)[0]
     assert max(r[2] for r in runs) < 1e-6
+
+
+def couette(nz, lid, pad=1):
+    """u = lid * z + sin(pi z) under walls at rest below and moving at `lid`
+    above, no scalar; returns the deviation from the exact decay and u."""
+    g = S.grid_desc(n=(4, 4, nz), domain="PPN", pad=pad)
+    p = params()
+    p.nu, p.dt = NU, DT
+    p.bc_vx = S.field_bc([S.FBC_DIRICHLET] * 6, [0.0] * 5 + [lid])
+    p.bc_vy = p.bc_vz = S.field_bc([S.FBC_DIRICHLET] * 6, [0.0] * 6)
+    p.bc_p = S.field_bc([S.FBC_NEUMANN] * 6, [0.0] * 6)
+    p.mg = S.mg_params(vc_count=30, vc_tolerance=1e-10, pre_smooth=3, post_smooth=6, mg_tolerance=1e-10)
+    f = {k: S.padded_field(g) for k in ("vx", "vy", "vz", "p", "t", "pp")}
+    z = O.field_metrics(g, 2)[0][None, None, :]
+    f["vx"][...] = lid * z + np.sin(math.pi * z)
+    r = O.rk3_run(g, p, f["vx"], f["vy"], f["vz"], f["p"], f["t"], f["pp"], STEPS)
+    assert r.status == 0
+    exact = lid * z + np.sin(math.pi * z) * math.exp(-NU * math.pi ** 2 * STEPS * DT)
+    core = (slice(pad, -pad),) * 3
+    return np.abs(f["vx"] - exact)[core].max(), f["vx"]
+
+
+@pytest.mark.parametrize("pad", [1, 2])
+def test_moving_wall(pad):
+    errs = []
+    for nz in (16, 32):
+        e1, u = couette(nz, 1.0, pad)
+        e0, _ = couette(nz, 0.0, pad)
+        assert abs(e1 - e0) < 1e-12, (e1, e0)
+        errs.append(e1)
+        if pad == 1:
+            assert np.abs(u[:, :, -1] + u[:, :, -2] - 2.0).max() < 1e-14
+            assert np.abs(u[:, :, 0] + u[:, :, 1]).max() < 1e-14
+    assert 3.5 < errs[0] / errs[1] < 4.5, errs
