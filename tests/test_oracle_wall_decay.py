@@ -24,6 +24,9 @@ nu = 1e-2, kappa = 2e-2, Fb = 1:
   cavity): u = z + sin(pi z) exp(-nu pi^2 t) is exact, and so is the linear
   Couette profile on the grid, so the deviation equals the fixed wall's to
   rounding, and the top ghost is 2 - u at the last core cell;
+* a prescribed heat flux (Neumann temperature walls with value dT/dz = -1,
+  neumann.cc): T = 1 - z is a steady state, kept to rounding on a uniform
+  mesh with either pad, with the ghosts on the same line;
 * tanh-stretched mesh (double-sided, beta 1.3): the reference places the
   ghost coordinates and metrics by copying from the other end of the axis
   (grid.cc:467-477), so the left ghost sits at -z_1 and carries the right
@@ -148,3 +151,32 @@ def test_moving_wall(pad):
             assert np.abs(u[:, :, -1] + u[:, :, -2] - 2.0).max() < 1e-14
             assert np.abs(u[:, :, 0] + u[:, :, 1]).max() < 1e-14
     assert 3.5 < errs[0] / errs[1] < 4.5, errs
+
+
+@pytest.mark.parametrize("pad", [1, 2])
+def test_heat_flux_walls_keep_linear_profile(pad):
+    n = 16
+    g = S.grid_desc(n=(4, 4, n), domain="PPN", pad=pad)
+    p = params()
+    p.nu, p.kappa, p.dt = NU, KAPPA, DT
+    p.with_scalar = 1
+    p.bc_vx = p.bc_vy = p.bc_vz = S.field_bc([S.FBC_DIRICHLET] * 6, [0.0] * 6)
+    p.bc_t = S.field_bc([S.FBC_NEUMANN] * 6, [0.0] * 4 + [-1.0, -1.0])
+    p.bc_p = S.field_bc([S.FBC_NEUMANN] * 6, [0.0] * 6)
+    p.mg = S.mg_params(vc_count=30, vc_tolerance=1e-10, pre_smooth=3, post_smooth=6, mg_tolerance=1e-10)
+    f = {k: S.padded_field(g) for k in ("vx", "vy", "vz", "p", "t", "pp")}
+    z = O.field_metrics(g, 2)[0][None, None, :]
+    f["t"][...] = 1.0 - z
+    r = O.rk3_run(g, p, f["vx"], f["vy"], f["vz"], f["p"], f["t"], f["pp"], 10)
+    assert r.status == 0
+    core = (slice(pad, -pad),) * 3
+    assert np.abs(f["t"] - (1.0 - z))[core].max() < 1e-13
+    if pad == 1:
+        # the ghosts continue the line: 1 + h/2 below, -h/2 above
+        assert np.abs(f["t"][:, :, 0] - (1.0 + 0.5 / n)).max() < 1e-13
+        assert np.abs(f["t"][:, :, -1] + 0.5 / n).max() < 1e-13
+    # a flux of the wrong sign on one wall moves the profile
+    p.bc_t = S.field_bc([S.FBC_NEUMANN] * 6, [0.0] * 4 + [-1.0, 1.0])
+    f["t"][...] = 1.0 - z
+    O.rk3_run(g, p, f["vx"], f["vy"], f["vz"], f["p"], f["t"], f["pp"], 10)
+    assert np.abs(f["t"] - (1.0 - z))[core].max() > 1e-4
