@@ -21,7 +21,8 @@ show in the pressure at 64 cells):
   order);
 * the hybrid upwind form agrees with the central form to rounding where the
   cell Peclet number u h / nu is below the limit (64 cells: 1.56 < 2), and is
-  far worse above it (16 cells: 6.25), where it is first order;
+  far worse above it (16 cells: 6.25), where its deviation falls at first
+  order (16 to 32 cells, both above the limit);
 * the 3-D step of a y-independent field repeats the planar step;
 * dScheme 2: the reference uses its second-order forms on the first and last
   core cell of an axis whatever the axis's periodicity (derivative.cc:83-87
@@ -126,6 +127,10 @@ def test_taylor_green_hybrid_upwind_follows_peclet_limit():
     c16 = taylor_green(16, nl_scheme=1)[0]
     u16 = taylor_green(16, nl_scheme=2)[0]
     assert u16 > 5 * c16
+    # above the limit at 16 and 32 cells (Peclet 6.25 and 3.1) the upwind
+    # term is first order: the deviation halves with h
+    u32 = taylor_green(32, nl_scheme=2)[0]
+    assert 1.8 < u16 / u32 < 2.5, (u16, u32)
 
 
 def test_taylor_green_3d_repeats_planar():
