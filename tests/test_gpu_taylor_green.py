@@ -35,6 +35,6 @@ def test_taylor_green_bitwise(n, integration, nl_scheme):
     # the periodic ghosts of the x-z plane too
     for k in ("vx", "vz", "p", "pp"):
         assert np.array_equal(gpu[k][:, 1, :], orc[k][:, 1, :]), ("ghosts", k)
-    eu, ew, _ = deviations(gpu, n)
+    eu, ew, _ = deviations(gpu, g)
     if n == 64:
         assert eu < 2e-5 and ew < 2e-5

@@ -24,6 +24,8 @@ show in the pressure at 64 cells):
   far worse above it (16 cells: 6.25), where its deviation falls at first
   order (16 to 32 cells, both above the limit);
 * the 3-D step of a y-independent field repeats the planar step;
+* with both periodic axes tanh-stretched the velocity still converges at
+  second order;
 * dScheme 2: the reference uses its second-order forms on the first and last
   core cell of an axis whatever the axis's periodicity (derivative.cc:83-87
   and 108-113: xfr and xlr name the first and last rank).  On a periodic axis
@@ -46,35 +48,37 @@ K = 2 * math.pi
 VC_COUNT = 60
 
 
-def setup(n, integration=2, nl_scheme=1, pad=1, planar=True, sub=1):
+def setup(n, integration=2, nl_scheme=1, pad=1, planar=True, sub=1, mesh="UUU", beta=1.0):
     """Grid, parameters and the Taylor-Green start.  `sub` divides the time
-    step (the caller multiplies the step count)."""
+    step (the caller multiplies the step count); `mesh` and `beta` stretch
+    the x and z axes."""
+    b = (beta, 1.0, beta)
     if planar:
-        g = S.grid_desc(n=(n, 1, n), domain="PNP", dims=2, pad=pad)
+        g = S.grid_desc(n=(n, 1, n), mesh=mesh, beta=b, domain="PNP", dims=2, pad=pad)
     else:
-        g = S.grid_desc(n=(n, 4, n), domain="PPP", pad=pad)
+        g = S.grid_desc(n=(n, 4, n), mesh=mesh, beta=b, domain="PPP", pad=pad)
     prm = params(nl_scheme=nl_scheme, integration=integration)
     prm.nu, prm.dt = NU, DT / sub
     per = S.field_bc([S.FBC_NEUMANN] * 6, [0.0] * 6)
     prm.bc_vx = prm.bc_vy = prm.bc_vz = prm.bc_p = prm.bc_t = per
     prm.mg = S.mg_params(vc_count=VC_COUNT, vc_tolerance=1e-10, pre_smooth=3, post_smooth=6, mg_tolerance=1e-12)
     f = {k: S.padded_field(g) for k in ("vx", "vy", "vz", "p", "t", "pp")}
-    x, z = centres(f, n, pad)
+    x, z = centres(g)
     f["vx"][...] = np.sin(K * x) * np.cos(K * z)
     f["vz"][...] = -np.cos(K * x) * np.sin(K * z)
     return g, prm, f
 
 
-def centres(f, n, pad):
-    shape = f["vx"].shape
-    return (((np.arange(shape[0]) - pad + 0.5) / n)[:, None, None],
-            ((np.arange(shape[2]) - pad + 0.5) / n)[None, None, :])
+def centres(g):
+    """Cell-centre coordinates along x and z, ghosts included."""
+    return O.field_metrics(g, 0)[0][:, None, None], O.field_metrics(g, 2)[0][None, None, :]
 
 
-def deviations(f, n, pad=1, planar=True):
+def deviations(f, g, planar=True):
     """Deviations of u, w and p (p up to its mean) from the exact solution at
     t = STEPS * DT over the core."""
-    x, z = centres(f, n, pad)
+    pad = g.pad
+    x, z = centres(g)
     t = STEPS * DT
     du = math.exp(-2 * NU * K * K * t)
     dp = math.exp(-4 * NU * K * K * t)
@@ -87,13 +91,13 @@ def deviations(f, n, pad=1, planar=True):
     return eu, ew, ep
 
 
-def taylor_green(n, integration=2, nl_scheme=1, pad=1, planar=True, sub=1):
+def taylor_green(n, integration=2, nl_scheme=1, pad=1, planar=True, sub=1, mesh="UUU", beta=1.0):
     """Runs the oracle from the Taylor-Green start to t = STEPS * DT; returns
     the deviations of u, w and p, the fields and the V-cycle count."""
-    g, prm, f = setup(n, integration, nl_scheme, pad, planar, sub)
+    g, prm, f = setup(n, integration, nl_scheme, pad, planar, sub, mesh, beta)
     r = O.rk3_run(g, prm, f["vx"], f["vy"], f["vz"], f["p"], f["t"], f["pp"], STEPS * sub)
     assert r.status == 0
-    eu, ew, ep = deviations(f, n, pad, planar)
+    eu, ew, ep = deviations(f, g, planar)
     return eu, ew, ep, f, r.mg_cycles
 
 
@@ -131,6 +135,20 @@ def test_taylor_green_hybrid_upwind_follows_peclet_limit():
     # term is first order: the deviation halves with h
     u32 = taylor_green(32, nl_scheme=2)[0]
     assert 1.8 < u16 / u32 < 2.5, (u16, u32)
+
+
+def test_taylor_green_stretched_periodic_axes():
+    """Both periodic axes tanh-stretched (double-sided, beta 1.2), as the
+    512^3 configuration's are: the velocity's deviation still falls at
+    second order.  The stretched divergence is not orthogonal to the
+    operator's left null vector, so the pressure solves stop at the V-cycle
+    count there."""
+    runs = [taylor_green(n, mesh="DUD", beta=1.2) for n in (16, 32, 64)]
+    for q in (0, 1):
+        errs = [r[q] for r in runs]
+        for a, b in zip(errs, errs[1:]):
+            assert 3.5 < a / b < 4.5, errs
+    assert runs[-1][0] < 2e-3
 
 
 def test_taylor_green_3d_repeats_planar():
