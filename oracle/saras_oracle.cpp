@@ -22,11 +22,16 @@
  * This restatement is pinned against the reference's own known answer -- the
  * TEST_POISSON manufactured solution of tests/mgTest (p = r^2/6 in 3D,
  * r^2/4 in 2D) -- against the analytic tanh-grid formulas and against the
- * level counts of setVCDepth.  The Blitz++ stencil operators central12n and
- * central22n (lib/field/derivative.cc:104-318) come from a third-party
- * library that is absent here (version unpinned); they are restated from
- * their published definitions, (F[+1]-F[-1])*0.5 and (F[-1]-2F)+F[+1], and
- * parity at that boundary is unpinned.
+ * level counts of setVCDepth.  Exact solutions of the equations pin it to
+ * discretisation order: manufactured Poisson solutions on stretched meshes,
+ * the Taylor-Green vortex of lib/initial/taylorGreen.cc, and sine modes
+ * decaying between no-slip, moving and heat-flux walls.  The Blitz++
+ * stencil operators central12n, central22n, central14n and central24n
+ * (lib/field/derivative.cc:104-318) come from a third-party library that is
+ * absent here (version unpinned); they are restated from their published
+ * definitions, (F[+1]-F[-1])*0.5, (F[-1]-2F)+F[+1] and the fourth-order
+ * pair over /12, and parity at that boundary is unpinned: their formulas are
+ * held by polynomial exactness, their rounding order is this restatement's.
  */
 #include "../include/saras_gb300.h"
 
