@@ -15,7 +15,14 @@ int main(int argc, char **argv) {
         std::fprintf(stderr, "usage: %s parameters.yaml [--parse-only]\n", argv[0]);
         return 2;
     }
-    saras_shim::parser p(argv[1]);
+    saras_shim::parser p;
+    try {
+        p = saras_shim::parser(argv[1]);
+    } catch (const std::exception &e) {
+        // the reference prints the same ERROR line and ends the job
+        std::printf("%s\n", e.what());
+        return 3;
+    }
     saras_shim::grid g(p);
     std::printf("grid %dx%dx%d mesh %s domain %s levels %d vcCount %d tol %.1e pre/post %d/%d\n", p.Nx, p.Ny, p.Nz,
                 p.meshType.c_str(), p.domainType.c_str(), saras_reference_levels(&g.desc), p.vcCount, p.vcTolerance,

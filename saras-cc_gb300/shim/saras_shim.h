@@ -5,7 +5,8 @@
 // parameters.yaml (the reference's key names), a `grid`, `plainsf` fields
 // indexed from -pad, and calls multigrid_d3::mgSolve(outLHS, inpRHS) or
 // lsRK3_d3::timeAdvance(V, P, T).  The classes mirror, for the hot path only:
-//   parser          lib/io/parser.h (keys read at parser.cc:69-284)
+//   parser          lib/io/parser.h (keys read at parser.cc:69-284, checks of
+//                   parser.cc:299-411 thrown as std::invalid_argument)
 //   grid            lib/grid/grid.h (sizes, pads, periodicity)
 //   plainsf         lib/field/plainsf.h (F(i,j,k) from -pad, row-major, k fastest)
 //   multigrid_d3/_d2 lib/poisson/poisson.h:148-205
@@ -18,6 +19,8 @@
 #include <cmath>
 #include <cstdint>
 #include <fstream>
+#include <iostream>
+#include <limits>
 #include <map>
 #include <sstream>
 #include <stdexcept>
@@ -44,6 +47,7 @@ class parser {
     // Solver
     int dScheme = 1, nlScheme = 1, iScheme = 2;
     double cnTolerance = 1e-6, tStp = 1e-3;
+    double tMax = std::numeric_limits<double>::infinity();  // "Final Time"; unchecked when absent
     double peLimit = 2.0, upParam = 0.8;
     // Multigrid
     int vcCount = 20, preSmooth = 3, postSmooth = 6, resType = 0;
@@ -77,9 +81,35 @@ class parser {
             kv[section + "/" + key] = val;
         }
         read();
+        checkData();
     }
 
     std::map<std::string, std::string> kv;
+
+    // parser::checkData (parser.cc:299-411), the checks that concern this
+    // path, with the reference's messages.  The reference prints an ERROR
+    // and ends the MPI job; a library cannot end its caller's process, so
+    // the message is thrown as std::invalid_argument instead.  A WARNING is
+    // printed and the value adjusted, as in the reference.
+    void checkData() {
+        auto fail = [](const std::string &m) { throw std::invalid_argument("ERROR: " + m + ". Aborting"); };
+        if (Nx < 2) fail("Insufficient number of points along X axis");
+        if (planar) {
+            if (Ny != 1) {
+                std::cout << "WARNING: The number of points along Y is greater than 1 although solver has been "
+                             "compiled with PLANAR flag. Resetting Y Size to 1"
+                          << std::endl;
+                Ny = 1;
+            }
+        } else if (Ny == 1) {
+            fail("Insufficient number of points along Y axis");
+        }
+        if (Nz < 2) fail("Insufficient number of points along Z axis");
+        if (domainType.length() != 3) fail("Domain type string is not correct");
+        if (meshType.length() != 3) fail("Mesh type string is not correct");
+        if (tStp > tMax) fail("Time step is larger than the maximum duration assigned for simulation");
+        if (resType > 2) fail("The specified value for printing error at end of V-Cycles is not defined");
+    }
 
   private:
     static std::string unq(std::string s) {
@@ -125,6 +155,7 @@ class parser {
         upParam = num("Solver/Central Bias", upParam);
         cnTolerance = num("Solver/Solve Tolerance", cnTolerance);
         tStp = num("Solver/Time-Step", tStp);
+        tMax = num("Solver/Final Time", tMax);
         vcCount = (int)num("Multigrid/V-Cycle Count", vcCount);
         vcTolerance = num("Multigrid/Residual Tolerance", vcTolerance);
         solveFlag = flag("Multigrid/Solve Coarsest", solveFlag);

@@ -25,6 +25,39 @@ def test_shim_compiles_and_parses(tmp_path):
     assert "grid 32x32x32 mesh UUU domain NNN levels 4 vcCount 60 tol 1.0e-10 pre/post 2/2" in out
 
 
+REJECTED = [
+    ('"X Size": 32', '"X Size": 1', "ERROR: Insufficient number of points along X axis. Aborting"),
+    ('"Y Size": 32', '"Y Size": 1', "ERROR: Insufficient number of points along Y axis. Aborting"),
+    ('"Z Size": 32', '"Z Size": 1', "ERROR: Insufficient number of points along Z axis. Aborting"),
+    ('"Domain Type": "NNN"', '"Domain Type": "NN"', "ERROR: Domain type string is not correct. Aborting"),
+    ('"Mesh Type": "UUU"', '"Mesh Type": "UUUU"', "ERROR: Mesh type string is not correct. Aborting"),
+    ('"Solve Tolerance": 1.0e-10', '"Solve Tolerance": 1.0e-10\n    "Time-Step": 0.1\n    "Final Time": 0.01',
+     "ERROR: Time step is larger than the maximum duration assigned for simulation. Aborting"),
+    ('"Residual Type": 0', '"Residual Type": 3',
+     "ERROR: The specified value for printing error at end of V-Cycles is not defined. Aborting"),
+]
+
+
+def test_shim_rejects_what_the_reference_rejects(tmp_path):
+    """parser::checkData (parser.cc:299-411): each input the reference
+    aborts on is rejected with its message (exit status 3 from the example,
+    which catches the exception), before any device work."""
+    exe = _build(tmp_path)
+    base = (ROOT / "tests" / "golden" / "mg_params.yaml").read_text()
+    for old, new, msg in REJECTED:
+        assert old in base, old
+        y = tmp_path / "bad.yaml"
+        y.write_text(base.replace(old, new, 1))
+        r = subprocess.run([str(exe), str(y), "--parse-only"], capture_output=True, text=True)
+        assert r.returncode == 3 and msg in r.stdout, (new, r.returncode, r.stdout, r.stderr)
+    # a time step within the final time passes
+    y = tmp_path / "ok.yaml"
+    y.write_text(base.replace('"Solve Tolerance": 1.0e-10', '"Solve Tolerance": 1.0e-10\n    "Time-Step": 0.01\n'
+                              '    "Final Time": 1.0', 1))
+    r = subprocess.run([str(exe), str(y), "--parse-only"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout
+
+
 @pytest.mark.gpu
 def test_shim_mgsolve(tmp_path):
     exe = _build(tmp_path)
