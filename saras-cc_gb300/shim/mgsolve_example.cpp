@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 
 #include "saras_shim.h"
 
@@ -16,14 +17,16 @@ int main(int argc, char **argv) {
         return 2;
     }
     saras_shim::parser p;
+    std::unique_ptr<saras_shim::grid> gp;
     try {
         p = saras_shim::parser(argv[1]);
+        gp.reset(new saras_shim::grid(p));
     } catch (const std::exception &e) {
         // the reference prints the same ERROR line and ends the job
         std::printf("%s\n", e.what());
         return 3;
     }
-    saras_shim::grid g(p);
+    const saras_shim::grid &g = *gp;
     std::printf("grid %dx%dx%d mesh %s domain %s levels %d vcCount %d tol %.1e pre/post %d/%d\n", p.Nx, p.Ny, p.Nz,
                 p.meshType.c_str(), p.domainType.c_str(), saras_reference_levels(&g.desc), p.vcCount, p.vcTolerance,
                 p.preSmooth, p.postSmooth);

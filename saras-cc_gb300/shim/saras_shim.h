@@ -16,6 +16,7 @@
 // "key": value form of the reference's parameters files.
 #pragma once
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <fstream>
@@ -183,7 +184,14 @@ class grid {
     saras_grid_desc desc{};
 
     explicit grid(const parser &p) : inputParams(p) {
-        pad = p.dScheme == 2 ? 2 : 1;  // grid.cc:69-77
+        // the pad from the differentiation scheme (grid.cc:69-77)
+        if (p.dScheme == 1) {
+            pad = 1;
+        } else if (p.dScheme == 2) {
+            pad = 2;
+        } else {
+            throw std::invalid_argument("Undefined finite differencing scheme in YAML file. ABORTING");
+        }
         dims = p.planar ? 2 : 3;
         desc.dims = dims;
         desc.n[0] = p.Nx;
@@ -200,6 +208,43 @@ class grid {
         desc.periodic[1] = p.yPer;
         desc.periodic[2] = p.zPer;
         desc.pad = pad;
+        // grid::checkAnisotropy runs when an axis is stretched (grid.cc:117-142)
+        bool stretched = false;
+        for (int d = 0; d < 3; d++) stretched = stretched || (desc.mesh_type[d] != 0 && (dims == 3 || d != 1));
+        if (stretched) {
+            const double ar = anisotropy();
+            if (ar > 7.0)
+                std::cout << "\nWARNING: Grid anisotropy exceeds limits. Finite-difference calculations will be "
+                             "inaccurate"
+                          << std::endl;
+            else
+                std::cout << "\nMaximum grid anisotropy is " << ar << std::endl;
+        }
+    }
+
+    // grid::checkAnisotropy (grid.cc:756-804): the largest ratio of two
+    // widths of a cell, over the core cells and the ghost layer (widths
+    // between consecutive centres -1..N along each axis); 0 when the host
+    // metrics cannot be formed (no V-cycle hierarchy for these sizes).
+    double anisotropy() const {
+        double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+        for (int d = 0; d < 3; d++) {
+            if (dims == 2 && d == 1) continue;
+            std::vector<double> x((size_t)desc.n[d] + 2);
+            int32_t n = 0;
+            if (saras_grid_metrics(&desc, 0, 0, d, x.data(), nullptr, nullptr, &n) != SARAS_OK) return 0.0;
+            lo[d] = std::numeric_limits<double>::infinity();
+            for (int i = 0; i <= n; i++) {
+                const double w = std::fabs(x[(size_t)i + 1] - x[(size_t)i]);
+                lo[d] = std::min(lo[d], w);
+                hi[d] = std::max(hi[d], w);
+            }
+        }
+        double ar = 0.0;
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++)
+                if (a != b && hi[a] > 0.0 && lo[b] > 0.0) ar = std::max(ar, hi[a] / lo[b]);
+        return ar;
     }
 };
 

@@ -35,6 +35,9 @@ REJECTED = [
      "ERROR: Time step is larger than the maximum duration assigned for simulation. Aborting"),
     ('"Residual Type": 0', '"Residual Type": 3',
      "ERROR: The specified value for printing error at end of V-Cycles is not defined. Aborting"),
+    # grid::grid (grid.cc:69-77)
+    ('"Differentiation Scheme": 1', '"Differentiation Scheme": 3',
+     "Undefined finite differencing scheme in YAML file. ABORTING"),
 ]
 
 
@@ -56,6 +59,36 @@ def test_shim_rejects_what_the_reference_rejects(tmp_path):
                               '    "Final Time": 1.0', 1))
     r = subprocess.run([str(exe), str(y), "--parse-only"], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout
+
+
+def test_shim_grid_anisotropy(tmp_path):
+    """grid::checkAnisotropy (grid.cc:756-804) runs when an axis is
+    stretched: it reports the largest ratio of two cell widths (centres -1..N
+    along each axis), with a WARNING above 7."""
+    import sys
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import numpy as np
+    import pyoracle as O
+    import saras_gb300 as S
+    exe = _build(tmp_path)
+    base = (ROOT / "tests" / "golden" / "mg_params.yaml").read_text()
+    r = subprocess.run([str(exe), str(ROOT / "tests" / "golden" / "mg_params.yaml"), "--parse-only"],
+                       capture_output=True, text=True, check=True)
+    assert "anisotropy" not in r.stdout  # uniform: no check, as in the reference
+    for beta, warn in ((1.3, False), (3.0, True)):
+        y = tmp_path / "stretched.yaml"
+        y.write_text(base.replace('"Mesh Type": "UUU"', '"Mesh Type": "UUD"').replace('"Z Beta": 1.0',
+                                                                                     f'"Z Beta": {beta}'))
+        out = subprocess.run([str(exe), str(y), "--parse-only"], capture_output=True, text=True,
+                             check=True).stdout
+        if warn:
+            assert "WARNING: Grid anisotropy exceeds limits. Finite-difference calculations will be inaccurate" in out
+            continue
+        g = S.grid_desc(n=(32, 32, 32), mesh="UUD", beta=(1, 1, beta), domain="NNN")
+        w = [np.abs(np.diff(O.field_metrics(g, d)[0])) for d in range(3)]
+        ar = max(w[a].max() / w[b].min() for a in range(3) for b in range(3) if a != b)
+        got = float(out.split("Maximum grid anisotropy is")[1].split()[0])
+        assert abs(got - ar) <= 1e-5 * ar, (got, ar)
 
 
 @pytest.mark.gpu
