@@ -141,6 +141,33 @@ def test_mgtest_second_order():
     assert errs[-1] < 1.1e-5
 
 
+def test_mgtest_planar():
+    """tests/mgTest in a PLANAR build (poisson.cc:139-147): RHS 1, analytic
+    ((x-1/2)^2 + (z-1/2)^2)/4 on the TEST_POISSON Dirichlet walls.  The
+    deviation falls at second order on the tanh mesh; on a uniform mesh,
+    where the five-point stencil is exact for the quadratic, it is h^2/16:
+    the mirrored wall ghost's error alone."""
+    for mesh in ("DUD", "UUU"):
+        errs = []
+        for n in (32, 64, 128):
+            g = S.grid_desc(n=(n, 1, n), mesh=mesh, beta=(1, 1, 1), domain="NNN", dims=2)
+            prm = S.mg_params(vc_count=20, vc_tolerance=1e-6, pre_smooth=5, post_smooth=5, mg_tolerance=1e-6,
+                              test_poisson=1, bc_kind=[2] * 6)
+            rhs = S.padded_field(g)
+            rhs[1:-1, 1, 1:-1] = 1.0
+            lhs = S.padded_field(g)
+            r = O.mg_solve(g, prm, lhs, rhs)
+            assert r.status == 0 and r.history[-1] < 1e-10
+            x = O.grid_metrics(g, 0, 0)[0][1:-1]
+            z = O.grid_metrics(g, 0, 2)[0][1:-1]
+            pa = ((x[:, None] - 0.5) ** 2 + (z[None, :] - 0.5) ** 2) / 4
+            errs.append(np.abs(pa - lhs[1:-1, 1, 1:-1]).max())
+            if mesh == "UUU":
+                assert abs(errs[-1] - 1.0 / (16 * n * n)) < 1e-8 / (n * n), (n, errs[-1])
+        for a, b in zip(errs, errs[1:]):
+            assert 3.9 < a / b < 4.1, (mesh, errs)
+
+
 def test_2d_cos_manufactured_second_order():
     errs = []
     for n in (64, 128):
