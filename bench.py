@@ -227,9 +227,11 @@ class BoxClearer:
             self.go.clear()
             if self.box is None:
                 return
-            time.sleep(self.delay_s)
-            self.box.fill(0.0)
-            self.idle.set()
+            try:
+                time.sleep(self.delay_s)
+                self.box.fill(0.0)
+            finally:
+                self.idle.set()
 
     def clear(self, box):
         self.idle.wait()
