@@ -215,6 +215,7 @@ class BoxClearer:
     def __init__(self, delay_s):
         self.delay_s = delay_s
         self.box = None
+        self.error = None
         self.go = threading.Event()
         self.idle = threading.Event()
         self.idle.set()
@@ -230,6 +231,8 @@ class BoxClearer:
             try:
                 time.sleep(self.delay_s)
                 self.box.fill(0.0)
+            except Exception as e:  # the thread stays alive; close() raises it
+                self.error = e
             finally:
                 self.idle.set()
 
@@ -247,6 +250,8 @@ class BoxClearer:
         self.box = None
         self.go.set()
         self.thread.join()
+        if self.error is not None:
+            raise self.error
 
 
 def time_solves(mg, lhs_d, rhs_d, st, off, steps, torch, stream):
